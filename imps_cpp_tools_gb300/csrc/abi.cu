@@ -1,0 +1,942 @@
+// C ABI of imps_gb300: contexts, sector tables, compiled contraction plans, the
+// reference-facing functors and the device Krylov solvers.
+#include <cuda_runtime.h>
+
+#include <algorithm>
+#include <cmath>
+#include <cstdio>
+#include <cstring>
+#include <new>
+#include <vector>
+
+#include "../../include/imps_gb300.h"
+#include "imps_internal.h"
+#include "imps_krylov.h"
+#include "imps_tc.h"
+
+using namespace imps;
+
+struct imps_ctx {
+  int device = 0;
+  cudaStream_t own = nullptr;
+  cudaStream_t stream = nullptr;
+  KrylovWs ws;
+  double* dscal = nullptr;  // 64 device scalars
+  int* dflag = nullptr;     // 16 device flags
+  char* arena = nullptr;
+  size_t arena_bytes = 0;
+};
+
+struct imps_layout {
+  Layout L;
+};
+
+struct imps_plan {
+  imps_ctx* ctx = nullptr;
+  Plan P;
+  double* stage_in = nullptr;
+  double* stage_out = nullptr;
+  double* stage_aux[2] = {nullptr, nullptr};
+  // in-layout tables (TM plans): block offsets / dims for traces
+  int64_t* d_boff = nullptr;
+  int32_t* d_bdim = nullptr;
+  int nb_in = 0;
+  Layout in_layout;
+  // gradient plan segments
+  int64_t* d_soff = nullptr;
+  int64_t* d_slen = nullptr;
+  int nseg = 0;
+  int64_t count_elems = 0;
+  int prec = IMPS_PREC_FP64;
+  TcPlan* tc = nullptr;
+};
+
+namespace {
+
+#define CK(x)                                                        \
+  do {                                                               \
+    cudaError_t e_ = (x);                                            \
+    if (e_ != cudaSuccess) {                                         \
+      fprintf(stderr, "imps_gb300: %s at %s:%d\n", cudaGetErrorString(e_), __FILE__, __LINE__); \
+      return e_ == cudaErrorMemoryAllocation ? IMPS_ERR_OOM : IMPS_ERR_CUDA;                   \
+    }                                                                \
+  } while (0)
+
+#define RC(x)              \
+  do {                     \
+    int r_ = (x);          \
+    if (r_ < 0) return r_; \
+  } while (0)
+
+std::vector<HNnz> make_h(int nnz, const int32_t* r, const int32_t* c, const double* v) {
+  std::vector<HNnz> h;
+  for (int i = 0; i < nnz; ++i) h.push_back({r[i], c[i], v[i]});
+  return h;
+}
+
+int upload_stage(Stage& S) {
+  // tile size: 32x32 unless that leaves the GPU underfilled (152 SMs)
+  int64_t n32 = 0;
+  for (const OutBlock& o : S.outs) n32 += (int64_t)((o.M + 31) / 32) * ((o.N + 31) / 32);
+  finalize_tiles(S, n32 < 2 * 152 ? 16 : 32, n32 < 2 * 152 ? 16 : 32);
+  if (!S.tiles.empty()) {
+    CK(cudaMalloc(&S.d_tiles, S.tiles.size() * sizeof(Tile)));
+    CK(cudaMemcpy(S.d_tiles, S.tiles.data(), S.tiles.size() * sizeof(Tile), cudaMemcpyHostToDevice));
+  }
+  if (!S.terms.empty()) {
+    CK(cudaMalloc(&S.d_terms, S.terms.size() * sizeof(Term)));
+    CK(cudaMemcpy(S.d_terms, S.terms.data(), S.terms.size() * sizeof(Term), cudaMemcpyHostToDevice));
+  }
+  return IMPS_OK;
+}
+
+int finish_plan(imps_ctx* ctx, Plan& P, imps_plan** out) {
+  imps_plan* p = new (std::nothrow) imps_plan();
+  if (!p) return IMPS_ERR_OOM;
+  p->ctx = ctx;
+  p->P = std::move(P);
+  if (ctx->device < 0) {  // host-only context: tables are built, nothing is uploaded
+    for (Stage& S : p->P.prep) finalize_tiles(S, 32, 32);
+    for (Stage& S : p->P.stages) finalize_tiles(S, 32, 32);
+    *out = p;
+    return IMPS_OK;
+  }
+  for (Slot& s : p->P.slots) {
+    if (s.kind == SLOT_INTERNAL && s.nelem > 0) {
+      cudaError_t e = cudaMalloc(&s.dptr, s.nelem * sizeof(double));
+      if (e != cudaSuccess) { imps_plan_destroy(p); return IMPS_ERR_OOM; }
+      cudaMemsetAsync(s.dptr, 0, s.nelem * sizeof(double), ctx->stream);
+    }
+  }
+  for (Stage& S : p->P.prep) { int r = upload_stage(S); if (r) { imps_plan_destroy(p); return r; } }
+  for (Stage& S : p->P.stages) { int r = upload_stage(S); if (r) { imps_plan_destroy(p); return r; } }
+  *out = p;
+  return IMPS_OK;
+}
+
+int run_stages(imps_plan* p, std::vector<Stage>& stages) {
+  if (p->ctx->device < 0) return IMPS_ERR_NO_DEVICE;
+  imps_dslots sl{};
+  for (size_t i = 0; i < p->P.slots.size() && i < (size_t)kMaxSlots; ++i) sl.p[i] = p->P.slots[i].dptr;
+  for (size_t i = 0; i < p->P.slots.size(); ++i)
+    if (!p->P.slots[i].dptr && p->P.slots[i].nelem > 0) return IMPS_ERR_BAD_ARG;  // unbound slot
+  for (Stage& S : stages) {
+    if (p->prec == IMPS_PREC_BF16X6 && p->tc) {
+      RC(tc_run_stage(p->tc, S, sl, p->ctx->stream));
+    } else {
+      RC(imps_launch_grouped_f64(S.d_tiles, (int)S.tiles.size(), S.d_terms, sl, S.tile_m, p->ctx->stream));
+    }
+  }
+  return IMPS_OK;
+}
+
+// ---- arena (per-context scratch, grows; never shrinks) ----
+int arena_reserve(imps_ctx* c, size_t bytes) {
+  if (bytes <= c->arena_bytes) return IMPS_OK;
+  if (c->arena) { cudaStreamSynchronize(c->stream); cudaFree(c->arena); c->arena = nullptr; c->arena_bytes = 0; }
+  size_t nb = std::max(bytes, (size_t)1 << 20);
+  CK(cudaMalloc(&c->arena, nb));
+  c->arena_bytes = nb;
+  return IMPS_OK;
+}
+
+struct Bump {
+  char* base;
+  size_t used = 0;
+  double* take(size_t n) {
+    double* p = (double*)(base + used);
+    used += ((n * sizeof(double) + 255) / 256) * 256;
+    return p;
+  }
+};
+
+size_t round256(size_t b) { return ((b + 255) / 256) * 256; }
+
+int stage_host(imps_plan* p, double** buf, int64_t n) {
+  if (!*buf) CK(cudaMalloc(buf, std::max<int64_t>(n, 1) * sizeof(double)));
+  return IMPS_OK;
+}
+
+// apply the plan's operator: IN -> OUT with device pointers
+int apply_dev(imps_plan* p, const double* in, double* out) {
+  p->P.slots[p->P.n_in].dptr = const_cast<double*>(in);
+  p->P.slots[p->P.n_out].dptr = out;
+  return run_stages(p, p->P.stages);
+}
+
+// ---- small dense symmetric eigensolver on the host (cyclic Jacobi), n <= kMaxCols ----
+void jacobi_eig(int n, std::vector<double> A, std::vector<double>& w, std::vector<double>& V) {
+  V.assign(n * n, 0.0);
+  for (int i = 0; i < n; ++i) V[i * n + i] = 1.0;
+  for (int sweep = 0; sweep < 100; ++sweep) {
+    double off = 0.0, tot = 0.0;
+    for (int i = 0; i < n; ++i)
+      for (int j = 0; j < n; ++j) {
+        tot += A[i * n + j] * A[i * n + j];
+        if (i != j) off += A[i * n + j] * A[i * n + j];
+      }
+    if (off <= 1e-34 * tot || off == 0.0) break;
+    for (int p = 0; p < n - 1; ++p)
+      for (int q = p + 1; q < n; ++q) {
+        const double apq = A[p * n + q];
+        if (apq == 0.0) continue;
+        const double app = A[p * n + p], aqq = A[q * n + q];
+        const double theta = (aqq - app) / (2.0 * apq);
+        const double t = (theta >= 0 ? 1.0 : -1.0) / (std::fabs(theta) + std::sqrt(theta * theta + 1.0));
+        const double c = 1.0 / std::sqrt(t * t + 1.0), s = t * c;
+        for (int k = 0; k < n; ++k) {  // rows p,q
+          const double akp = A[k * n + p], akq = A[k * n + q];
+          A[k * n + p] = c * akp - s * akq;
+          A[k * n + q] = s * akp + c * akq;
+        }
+        for (int k = 0; k < n; ++k) {  // cols p,q
+          const double apk = A[p * n + k], aqk = A[q * n + k];
+          A[p * n + k] = c * apk - s * aqk;
+          A[q * n + k] = s * apk + c * aqk;
+        }
+        for (int k = 0; k < n; ++k) {
+          const double vkp = V[k * n + p], vkq = V[k * n + q];
+          V[k * n + p] = c * vkp - s * vkq;
+          V[k * n + q] = s * vkp + c * vkq;
+        }
+      }
+  }
+  w.resize(n);
+  for (int i = 0; i < n; ++i) w[i] = A[i * n + i];
+}
+
+}  // namespace
+
+// =====================================================================================
+extern "C" {
+
+const char* imps_status_string(int s) {
+  switch (s) {
+    case IMPS_OK: return "ok";
+    case IMPS_WARN_NOT_CONVERGED: return "not converged";
+    case IMPS_ERR_BAD_ARG: return "bad argument";
+    case IMPS_ERR_BAD_TABLE: return "inconsistent sector table";
+    case IMPS_ERR_CUDA: return "CUDA error";
+    case IMPS_ERR_NAN: return "NaN/Inf detected";
+    case IMPS_ERR_TIMEOUT: return "timeout";
+    case IMPS_ERR_NO_DEVICE: return "no CUDA device";
+    case IMPS_ERR_OOM: return "out of device memory";
+    case IMPS_ERR_UNSUPPORTED: return "unsupported";
+    default: return "unknown status";
+  }
+}
+
+int imps_version(void) { return 100; }
+
+int imps_ctx_create(int device, imps_ctx** out) {
+  if (!out) return IMPS_ERR_BAD_ARG;
+  if (device == -1) {  // host-only context: sector tables and plans, no execution
+    imps_ctx* c = new (std::nothrow) imps_ctx();
+    if (!c) return IMPS_ERR_OOM;
+    c->device = -1;
+    *out = c;
+    return IMPS_OK;
+  }
+  int n = 0;
+  if (cudaGetDeviceCount(&n) != cudaSuccess || n <= device || device < 0) return IMPS_ERR_NO_DEVICE;
+  CK(cudaSetDevice(device));
+  imps_ctx* c = new (std::nothrow) imps_ctx();
+  if (!c) return IMPS_ERR_OOM;
+  c->device = device;
+  CK(cudaStreamCreateWithFlags(&c->own, cudaStreamNonBlocking));
+  c->stream = c->own;
+  CK(cudaMalloc(&c->ws.partials, kr_partials_elems() * sizeof(double)));
+  CK(cudaMalloc(&c->ws.counter, 256));
+  CK(cudaMemset(c->ws.counter, 0, 256));
+  CK(cudaMalloc(&c->dscal, 64 * sizeof(double)));
+  CK(cudaMemset(c->dscal, 0, 64 * sizeof(double)));
+  CK(cudaMalloc(&c->dflag, 16 * sizeof(int)));
+  CK(cudaMemset(c->dflag, 0, 16 * sizeof(int)));
+  *out = c;
+  return IMPS_OK;
+}
+
+int imps_ctx_destroy(imps_ctx* c) {
+  if (!c) return IMPS_OK;
+  if (c->device < 0) { delete c; return IMPS_OK; }
+  cudaStreamSynchronize(c->stream);
+  cudaFree(c->ws.partials);
+  cudaFree(c->ws.counter);
+  cudaFree(c->dscal);
+  cudaFree(c->dflag);
+  if (c->arena) cudaFree(c->arena);
+  if (c->own) cudaStreamDestroy(c->own);
+  delete c;
+  return IMPS_OK;
+}
+
+int imps_ctx_set_stream(imps_ctx* c, void* s) {
+  if (!c) return IMPS_ERR_BAD_ARG;
+  c->stream = s ? (cudaStream_t)s : c->own;
+  return IMPS_OK;
+}
+
+int imps_ctx_synchronize(imps_ctx* c) {
+  if (!c) return IMPS_ERR_BAD_ARG;
+  if (c->device < 0) return IMPS_OK;
+  CK(cudaStreamSynchronize(c->stream));
+  return IMPS_OK;
+}
+
+// ---- layouts ----
+int imps_layout_create(int nsym, int nblocks, const int32_t* qin, const int32_t* qout,
+                       const int32_t* rows, const int32_t* cols, const int32_t* group,
+                       imps_layout** out) {
+  if (!out || (nblocks > 0 && (!qin || !qout || !rows || !cols))) return IMPS_ERR_BAD_ARG;
+  imps_layout* L = new (std::nothrow) imps_layout();
+  if (!L) return IMPS_ERR_OOM;
+  int r = layout_build(L->L, nsym, nblocks, qin, qout, rows, cols, group);
+  if (r) { delete L; return r; }
+  *out = L;
+  return IMPS_OK;
+}
+
+int imps_layout_destroy(imps_layout* L) { delete L; return IMPS_OK; }
+int64_t imps_layout_nelem(const imps_layout* L) { return L ? L->L.nelem : -1; }
+int imps_layout_nblocks(const imps_layout* L) { return L ? (int)L->L.blocks.size() : -1; }
+int imps_layout_nsym(const imps_layout* L) { return L ? L->L.nsym : -1; }
+
+int imps_layout_get(const imps_layout* L, int32_t* qin, int32_t* qout, int32_t* rows, int32_t* cols,
+                    int32_t* group, int64_t* off) {
+  if (!L) return IMPS_ERR_BAD_ARG;
+  const int ns = L->L.nsym;
+  for (size_t b = 0; b < L->L.blocks.size(); ++b) {
+    const Block& B = L->L.blocks[b];
+    for (int k = 0; k < ns; ++k) {
+      if (qin) qin[b * ns + k] = B.qin[k];
+      if (qout) qout[b * ns + k] = B.qout[k];
+    }
+    if (rows) rows[b] = B.rows;
+    if (cols) cols[b] = B.cols;
+    if (group) group[b] = B.group;
+    if (off) off[b] = B.off;
+  }
+  return IMPS_OK;
+}
+
+int imps_layout_bond(const imps_layout* A, int side, imps_layout** out) {
+  if (!A || !out) return IMPS_ERR_BAD_ARG;
+  imps_layout* L = new (std::nothrow) imps_layout();
+  if (!L) return IMPS_ERR_OOM;
+  L->L = layout_bond(A->L, side);
+  *out = L;
+  return IMPS_OK;
+}
+
+// ---- plans ----
+int imps_plan_hac(imps_ctx* ctx, const imps_layout* AC, const imps_layout* EHL, const imps_layout* EHR,
+                  const imps_layout* HL, const imps_layout* HR, int d, imps_plan** out) {
+  if (!ctx || !AC || !EHL || !EHR || !HL || !HR || !out || d <= 0) return IMPS_ERR_BAD_ARG;
+  Plan P;
+  RC(build_hac(P, AC->L, EHL->L, EHR->L, HL->L, HR->L, d));
+  RC(finish_plan(ctx, P, out));
+  (*out)->in_layout = AC->L;
+  return IMPS_OK;
+}
+
+int imps_plan_hc(imps_ctx* ctx, const imps_layout* C, const imps_layout* EHL, const imps_layout* EHR,
+                 const imps_layout* AL, const imps_layout* AR, int d, int nnz, const int32_t* hrow,
+                 const int32_t* hcol, const double* hval, imps_plan** out) {
+  if (!ctx || !C || !EHL || !EHR || !AL || !AR || !out || d <= 0 || nnz < 0) return IMPS_ERR_BAD_ARG;
+  Plan P;
+  RC(build_hc(P, C->L, EHL->L, EHR->L, AL->L, AR->L, d, make_h(nnz, hrow, hcol, hval)));
+  RC(finish_plan(ctx, P, out));
+  (*out)->in_layout = C->L;
+  return IMPS_OK;
+}
+
+int imps_plan_tm(imps_ctx* ctx, int nsites, const imps_layout* const* A, int dir, const imps_layout* in,
+                 const imps_layout* outl, imps_plan** out) {
+  if (!ctx || !A || !in || !outl || !out || nsites < 1 || (dir != 0 && dir != 1)) return IMPS_ERR_BAD_ARG;
+  std::vector<const Layout*> As;
+  for (int k = 0; k < nsites; ++k) {
+    if (!A[k]) return IMPS_ERR_BAD_ARG;
+    As.push_back(&A[k]->L);
+  }
+  Plan P;
+  RC(build_tm(P, As, dir, in->L, outl->L));
+  RC(finish_plan(ctx, P, out));
+  imps_plan* p = *out;
+  p->in_layout = in->L;
+  // block tables of the in layout for traces / identity
+  std::vector<int64_t> bo;
+  std::vector<int32_t> bd;
+  for (const Block& b : in->L.blocks) { bo.push_back(b.off); bd.push_back(b.rows); }
+  p->nb_in = (int)bo.size();
+  if (p->nb_in && ctx->device >= 0) {
+    CK(cudaMalloc(&p->d_boff, bo.size() * sizeof(int64_t)));
+    CK(cudaMalloc(&p->d_bdim, bd.size() * sizeof(int32_t)));
+    CK(cudaMemcpy(p->d_boff, bo.data(), bo.size() * sizeof(int64_t), cudaMemcpyHostToDevice));
+    CK(cudaMemcpy(p->d_bdim, bd.data(), bd.size() * sizeof(int32_t), cudaMemcpyHostToDevice));
+  }
+  return IMPS_OK;
+}
+
+int imps_plan_redop(imps_ctx* ctx, const imps_layout* A, int d, int nnz, const int32_t* hrow,
+                    const int32_t* hcol, const double* hval, int dir, imps_plan** out) {
+  if (!ctx || !A || !out || d <= 0 || nnz < 0) return IMPS_ERR_BAD_ARG;
+  Plan P;
+  RC(build_redop(P, A->L, d, make_h(nnz, hrow, hcol, hval), dir));
+  return finish_plan(ctx, P, out);
+}
+
+int imps_plan_optm(imps_ctx* ctx, const imps_layout* A0, const imps_layout* A1, int d, int nnz,
+                   const int32_t* hrow, const int32_t* hcol, const double* hval, int dir,
+                   const imps_layout* outl, imps_plan** out) {
+  if (!ctx || !A0 || !A1 || !outl || !out || d <= 0) return IMPS_ERR_BAD_ARG;
+  Plan P;
+  RC(build_optm(P, A0->L, A1->L, d, make_h(nnz, hrow, hcol, hval), dir, outl->L));
+  return finish_plan(ctx, P, out);
+}
+
+int imps_plan_mps_bd(imps_ctx* ctx, const imps_layout* A, const imps_layout* X, int side, double alpha,
+                     imps_plan** out) {
+  if (!ctx || !A || !X || !out) return IMPS_ERR_BAD_ARG;
+  Plan P;
+  RC(build_mps_bd(P, A->L, X->L, side, alpha));
+  return finish_plan(ctx, P, out);
+}
+
+int imps_plan_grad_right(imps_ctx* ctx, const imps_layout* Y, const imps_layout* AR, imps_plan** out) {
+  if (!ctx || !Y || !AR || !out) return IMPS_ERR_BAD_ARG;
+  Plan P;
+  RC(build_grad_right(P, Y->L, AR->L));
+  RC(finish_plan(ctx, P, out));
+  imps_plan* p = *out;
+  // segments: AR blocks whose left sector has a right null space (mr_tot > ml),
+  // Nullspace(AR, r) of MPSBlockUtilities.hpp:299-321
+  std::map<Key, std::pair<int64_t, int64_t>> sec;  // qin -> (ml, mr_tot)
+  for (const Block& b : AR->L.blocks) {
+    auto& e = sec[b.qin];
+    e.first = b.rows;
+    e.second += b.cols;
+  }
+  std::vector<int64_t> so, sl;
+  int64_t count = 0;
+  for (const Block& b : AR->L.blocks) {
+    auto& e = sec[b.qin];
+    if (e.second > e.first) { so.push_back(b.off); sl.push_back((int64_t)b.rows * b.cols); }
+  }
+  for (auto& kv : sec)
+    if (kv.second.second > kv.second.first) count += kv.second.first * (kv.second.second - kv.second.first);
+  p->nseg = (int)so.size();
+  p->count_elems = count;
+  if (p->nseg && ctx->device >= 0) {
+    CK(cudaMalloc(&p->d_soff, so.size() * sizeof(int64_t)));
+    CK(cudaMalloc(&p->d_slen, sl.size() * sizeof(int64_t)));
+    CK(cudaMemcpy(p->d_soff, so.data(), so.size() * sizeof(int64_t), cudaMemcpyHostToDevice));
+    CK(cudaMemcpy(p->d_slen, sl.data(), sl.size() * sizeof(int64_t), cudaMemcpyHostToDevice));
+  }
+  return IMPS_OK;
+}
+
+int imps_plan_destroy(imps_plan* p) {
+  if (!p) return IMPS_OK;
+  if (p->ctx && p->ctx->device < 0) { delete p; return IMPS_OK; }
+  if (p->ctx) cudaStreamSynchronize(p->ctx->stream);
+  for (Slot& s : p->P.slots)
+    if (s.kind == SLOT_INTERNAL && s.dptr) cudaFree(s.dptr);
+  for (auto* v : {&p->P.prep, &p->P.stages})
+    for (Stage& S : *v) {
+      if (S.d_tiles) cudaFree(S.d_tiles);
+      if (S.d_terms) cudaFree(S.d_terms);
+    }
+  cudaFree(p->stage_in);
+  cudaFree(p->stage_out);
+  cudaFree(p->stage_aux[0]);
+  cudaFree(p->stage_aux[1]);
+  cudaFree(p->d_boff);
+  cudaFree(p->d_bdim);
+  cudaFree(p->d_soff);
+  cudaFree(p->d_slen);
+  if (p->tc) tc_destroy(p->tc);
+  delete p;
+  return IMPS_OK;
+}
+
+int imps_plan_derived_layout(const imps_plan* p, int which, imps_layout** out) {
+  if (!p || !out || which < 0 || which >= (int)p->P.derived.size()) return IMPS_ERR_BAD_ARG;
+  imps_layout* L = new (std::nothrow) imps_layout();
+  if (!L) return IMPS_ERR_OOM;
+  L->L = p->P.derived[which];
+  *out = L;
+  return IMPS_OK;
+}
+
+int imps_plan_info(const imps_plan* p, int64_t* fa, int64_t* fp, int64_t* dropped, int* nslots, int* nstages) {
+  if (!p) return IMPS_ERR_BAD_ARG;
+  if (fa) *fa = p->P.flops_apply;
+  if (fp) *fp = p->P.flops_prep;
+  if (dropped) *dropped = p->P.dropped;
+  if (nslots) *nslots = (int)p->P.slots.size();
+  if (nstages) *nstages = (int)p->P.stages.size();
+  return IMPS_OK;
+}
+
+int imps_plan_slot_info(const imps_plan* p, int slot, int* kind, int64_t* nelem) {
+  if (!p || slot < 0 || slot >= (int)p->P.slots.size()) return IMPS_ERR_BAD_ARG;
+  if (kind) *kind = p->P.slots[slot].kind;
+  if (nelem) *nelem = p->P.slots[slot].nelem;
+  return IMPS_OK;
+}
+
+int imps_plan_bind(imps_plan* p, int slot, double* ptr) {
+  if (!p || slot < 0 || slot >= (int)p->P.slots.size()) return IMPS_ERR_BAD_ARG;
+  if (p->P.slots[slot].kind != SLOT_EXTERNAL) return IMPS_ERR_BAD_ARG;
+  p->P.slots[slot].dptr = ptr;
+  return IMPS_OK;
+}
+
+int imps_plan_prepare(imps_plan* p) {
+  if (!p) return IMPS_ERR_BAD_ARG;
+  RC(run_stages(p, p->P.prep));
+  if (p->tc) RC(tc_invalidate(p->tc));
+  return IMPS_OK;
+}
+
+int imps_plan_run(imps_plan* p) {
+  if (!p) return IMPS_ERR_BAD_ARG;
+  return run_stages(p, p->P.stages);
+}
+
+int imps_plan_table(const imps_plan* p, int prep, int stage, int64_t* n_outs, int64_t* n_terms,
+                    int32_t* out_tag, int32_t* out_t0, int32_t* out_t1, int32_t* term_aslot,
+                    int64_t* term_aoff, int32_t* term_bslot, int64_t* term_boff, int32_t* term_k,
+                    double* term_alpha) {
+  if (!p) return IMPS_ERR_BAD_ARG;
+  const std::vector<Stage>& v = prep ? p->P.prep : p->P.stages;
+  if (stage < 0 || stage >= (int)v.size()) return IMPS_ERR_BAD_ARG;
+  const Stage& S = v[stage];
+  if (n_outs) *n_outs = (int64_t)S.outs.size();
+  if (n_terms) *n_terms = (int64_t)S.terms.size();
+  for (size_t i = 0; i < S.outs.size(); ++i) {
+    if (out_tag) out_tag[i] = S.outs[i].tag;
+    if (out_t0) out_t0[i] = S.outs[i].t0;
+    if (out_t1) out_t1[i] = S.outs[i].t1;
+  }
+  for (size_t i = 0; i < S.terms.size(); ++i) {
+    const Term& t = S.terms[i];
+    if (term_aslot) term_aslot[i] = t.a_slot;
+    if (term_aoff) term_aoff[i] = t.a_off;
+    if (term_bslot) term_bslot[i] = t.b_slot;
+    if (term_boff) term_boff[i] = t.b_off;
+    if (term_k) term_k[i] = t.k;
+    if (term_alpha) term_alpha[i] = t.alpha;
+  }
+  return IMPS_OK;
+}
+
+int imps_plan_set_precision(imps_plan* p, int prec) {
+  if (!p) return IMPS_ERR_BAD_ARG;
+  if (prec == IMPS_PREC_FP64) { p->prec = prec; return IMPS_OK; }
+  if (prec != IMPS_PREC_BF16X6) return IMPS_ERR_BAD_ARG;
+  if (!p->tc) RC(tc_create(&p->tc, p->P, p->ctx->stream));
+  p->prec = prec;
+  return IMPS_OK;
+}
+
+// ---- functors ----
+static int apply_mem(imps_plan* p, const double* in, double* out, int mem) {
+  if (!p || !in || !out) return IMPS_ERR_BAD_ARG;
+  const int64_t nin = p->P.slots[p->P.n_in].nelem, nout = p->P.slots[p->P.n_out].nelem;
+  cudaStream_t st = p->ctx->stream;
+  if (mem == IMPS_MEM_DEVICE) return apply_dev(p, in, out);
+  RC(stage_host(p, &p->stage_in, nin));
+  RC(stage_host(p, &p->stage_out, nout));
+  CK(cudaMemcpyAsync(p->stage_in, in, nin * sizeof(double), cudaMemcpyHostToDevice, st));
+  RC(apply_dev(p, p->stage_in, p->stage_out));
+  CK(cudaMemcpyAsync(out, p->stage_out, nout * sizeof(double), cudaMemcpyDeviceToHost, st));
+  CK(cudaStreamSynchronize(st));
+  return IMPS_OK;
+}
+
+int imps_hac_apply(imps_plan* p, const double* in, double* out, int mem) {
+  if (!p || p->P.kind != PLAN_HAC) return IMPS_ERR_BAD_ARG;
+  return apply_mem(p, in, out, mem);
+}
+
+int imps_hc_apply(imps_plan* p, const double* in, double* out, int mem) {
+  if (!p || p->P.kind != PLAN_HC) return IMPS_ERR_BAD_ARG;
+  return apply_mem(p, in, out, mem);
+}
+
+int imps_tm_apply(imps_plan* p, const double* in, double* out, int mem) {
+  if (!p || p->P.kind != PLAN_TM) return IMPS_ERR_BAD_ARG;
+  return apply_mem(p, in, out, mem);
+}
+
+// device-side InvEfun_proj: y = x - T(x) + tr(x*rho_in) * rho_out (tmp: n doubles)
+static int proj_apply_dev(imps_plan* p, const double* x, const double* rho_in, const double* rho_out,
+                          double* y, double* tmp, double* dtr) {
+  imps_ctx* c = p->ctx;
+  const int64_t n = p->P.slots[0].nelem;
+  RC(kr_trace_prod(c->ws, x, rho_in, p->d_boff, p->d_bdim, p->nb_in, dtr, c->stream));
+  RC(apply_dev(p, x, tmp));
+  RC(kr_proj_epilogue(x, tmp, dtr, rho_out, y, n, c->stream));
+  return IMPS_OK;
+}
+
+int imps_tm_proj_apply(imps_plan* p, const double* in, const double* rho_in, const double* rho_out,
+                       double* out, int mem) {
+  if (!p || p->P.kind != PLAN_TM || !in || !rho_in || !rho_out || !out) return IMPS_ERR_BAD_ARG;
+  imps_ctx* c = p->ctx;
+  const int64_t n = p->P.slots[0].nelem;
+  if (p->P.slots[1].nelem != n) return IMPS_ERR_BAD_ARG;
+  RC(arena_reserve(c, round256(n * 8) * 5));
+  Bump bp{c->arena};
+  double* tmp = bp.take(n);
+  if (mem == IMPS_MEM_DEVICE) return proj_apply_dev(p, in, rho_in, rho_out, out, tmp, c->dscal);
+  double* x = bp.take(n);
+  double* ri = bp.take(n);
+  double* ro = bp.take(n);
+  double* y = bp.take(n);
+  CK(cudaMemcpyAsync(x, in, n * 8, cudaMemcpyHostToDevice, c->stream));
+  CK(cudaMemcpyAsync(ri, rho_in, n * 8, cudaMemcpyHostToDevice, c->stream));
+  CK(cudaMemcpyAsync(ro, rho_out, n * 8, cudaMemcpyHostToDevice, c->stream));
+  RC(proj_apply_dev(p, x, ri, ro, y, tmp, c->dscal));
+  CK(cudaMemcpyAsync(out, y, n * 8, cudaMemcpyDeviceToHost, c->stream));
+  CK(cudaStreamSynchronize(c->stream));
+  return IMPS_OK;
+}
+
+int imps_dot(imps_ctx* c, const double* x, const double* y, int64_t n, double* result) {
+  if (!c || !x || !y || !result) return IMPS_ERR_BAD_ARG;
+  RC(kr_multidot(c->ws, x, n, 1, y, n, c->dscal, 0, nullptr, c->stream));
+  CK(cudaMemcpyAsync(result, c->dscal, 8, cudaMemcpyDeviceToHost, c->stream));
+  CK(cudaStreamSynchronize(c->stream));
+  return IMPS_OK;
+}
+
+// ---- Lanczos: eigs_rs(nev=1, "SA") ----
+int imps_eigs_rs(imps_plan* p, double* x, int mem, double tol, int ncv, int maxit, double* eval,
+                 int* n_applies) {
+  if (!p || !x || (p->P.kind != PLAN_HAC && p->P.kind != PLAN_HC)) return IMPS_ERR_BAD_ARG;
+  imps_ctx* c = p->ctx;
+  cudaStream_t st = c->stream;
+  const int64_t n = p->P.slots[p->P.n_in].nelem;
+  if (n < 2) return IMPS_ERR_BAD_ARG;
+  int m = ncv > 0 ? ncv : 20;  // eigs.cpp:4, 390: max(std_ncv, 2*nev) capped at N
+  if (m > n) m = (int)n;
+  if (m > kMaxCols - 2) m = kMaxCols - 2;
+  if (m < 2) m = 2;
+  if (maxit <= 0) maxit = (int)std::min<int64_t>(n, 100000);
+  const int ld = m + 1;
+  RC(arena_reserve(c, round256(n * 8) * (m + 4) + round256((size_t)ld * ld * 8) + 4096));
+  Bump bp{c->arena};
+  double* V = bp.take((size_t)n * (m + 1));
+  double* w = bp.take(n);
+  double* xr = bp.take(n);
+  double* Hd = bp.take((size_t)ld * ld);
+  double* tmp = bp.take(ld);
+  double* nrm = c->dscal + 8;
+  int* bflag = c->dflag;
+  CK(cudaMemsetAsync(bflag, 0, sizeof(int), st));
+  if (mem == IMPS_MEM_HOST) CK(cudaMemcpyAsync(xr, x, n * 8, cudaMemcpyHostToDevice, st));
+  else CK(cudaMemcpyAsync(xr, x, n * 8, cudaMemcpyDeviceToDevice, st));
+  RC(kr_multidot(c->ws, xr, n, 1, xr, n, tmp, 0, nrm, st));
+  RC(kr_scale_inv(xr, nrm, V, n, bflag, st));
+
+  std::vector<double> H((size_t)ld * ld, 0.0);  // host projected matrix, column-major
+  std::vector<double> col(ld);
+  std::vector<double> evals, evecs, y;
+  int jstart = 0, applies = 0, status = IMPS_WARN_NOT_CONVERGED;
+  double theta = 0.0;
+  const int chk = 4;
+  bool done = false;
+  while (!done) {
+    int jlast = -1;
+    for (int j = jstart; j < m; ++j) {
+      double* vj = V + (size_t)j * n;
+      double* hc = Hd + (size_t)j * ld;
+      RC(apply_dev(p, vj, w));
+      ++applies;
+      RC(kr_multidot(c->ws, V, n, j + 1, w, n, hc, 0, nullptr, st));
+      RC(kr_gemv_sub(V, n, j + 1, hc, w, n, st));
+      RC(kr_multidot(c->ws, V, n, j + 1, w, n, tmp, 0, nullptr, st));
+      RC(kr_gemv_sub(V, n, j + 1, tmp, w, n, st));
+      RC(kr_axpby(1.0, tmp, 1.0, hc, j + 1, st));
+      RC(kr_multidot(c->ws, w, n, 1, w, n, tmp, 0, hc + j + 1, st));
+      RC(kr_scale_inv(w, hc + j + 1, V + (size_t)(j + 1) * n, n, bflag, st));
+      jlast = j;
+      const bool check = ((j + 1 - jstart) % chk == 0) || j == m - 1 || applies >= maxit;
+      if (!check) continue;
+      // pull the new columns and solve the small projected problem
+      CK(cudaMemcpyAsync(H.data() + (size_t)jstart * ld, Hd + (size_t)jstart * ld,
+                         (size_t)(j + 1 - jstart) * ld * 8, cudaMemcpyDeviceToHost, st));
+      int hbreak = 0;
+      CK(cudaMemcpyAsync(&hbreak, bflag, sizeof(int), cudaMemcpyDeviceToHost, st));
+      CK(cudaStreamSynchronize(st));
+      const int k = j + 1;
+      std::vector<double> A((size_t)k * k);
+      for (int r = 0; r < k; ++r)
+        for (int q = 0; q < k; ++q)
+          A[r * k + q] = 0.5 * (H[r + (size_t)q * ld] + H[q + (size_t)r * ld]);
+      jacobi_eig(k, A, evals, evecs);
+      int imin = 0;
+      for (int i = 1; i < k; ++i) if (evals[i] < evals[imin]) imin = i;
+      theta = evals[imin];
+      y.assign(k, 0.0);
+      for (int r = 0; r < k; ++r) y[r] = evecs[r * k + imin];
+      const double beta = H[(j + 1) + (size_t)j * ld];
+      const double res = std::fabs(beta * y[k - 1]);
+      if (!std::isfinite(theta)) return IMPS_ERR_NAN;
+      if (res <= tol * std::max(std::fabs(theta), 1e-300) || hbreak) {
+        status = IMPS_OK;
+        done = true;
+        break;
+      }
+      if (applies >= maxit) { done = true; break; }
+    }
+    // Ritz vector x = V[:, 0..k-1] y
+    const int k = jlast + 1;
+    CK(cudaMemcpyAsync(tmp, y.data(), k * 8, cudaMemcpyHostToDevice, st));
+    RC(kr_gemv(V, n, k, tmp, xr, n, st));
+    if (done) break;
+    // thick restart with (Ritz vector, residual direction)
+    const double beta = H[(size_t)m + (size_t)(m - 1) * ld];
+    const double coup = beta * y[m - 1];
+    CK(cudaMemcpyAsync(V, xr, n * 8, cudaMemcpyDeviceToDevice, st));
+    CK(cudaMemcpyAsync(V + n, V + (size_t)m * n, n * 8, cudaMemcpyDeviceToDevice, st));
+    std::fill(H.begin(), H.end(), 0.0);
+    H[0] = theta;
+    H[1] = coup;            // H(1,0)
+    H[(size_t)ld] = coup;   // H(0,1) (filled again by the device for column 1)
+    CK(cudaStreamSynchronize(st));
+    jstart = 1;
+  }
+  // normalise
+  RC(kr_multidot(c->ws, xr, n, 1, xr, n, tmp, 0, nrm, st));
+  if (mem == IMPS_MEM_HOST) {
+    RC(kr_scale_inv(xr, nrm, w, n, bflag, st));
+    CK(cudaMemcpyAsync(x, w, n * 8, cudaMemcpyDeviceToHost, st));
+  } else {
+    RC(kr_scale_inv(xr, nrm, x, n, bflag, st));
+  }
+  CK(cudaStreamSynchronize(st));
+  if (eval) *eval = theta;
+  if (n_applies) *n_applies = applies;
+  return status;
+}
+
+// ---- GMRES core on the projected operator A(v) = v - T(v) + tr(v*rho_in)*rho_out ----
+static int gmres_proj(imps_plan* p, const double* b, double* y, const double* rho_in,
+                      const double* rho_out, double tol, int maxit, int krylov, int* iters,
+                      double* relres, Bump& bp) {
+  imps_ctx* c = p->ctx;
+  cudaStream_t st = c->stream;
+  const int64_t n = p->P.slots[0].nelem;
+  int m = krylov > 0 ? krylov : 40;
+  if (m > kMaxCols - 2) m = kMaxCols - 2;
+  if (m > n) m = (int)n;
+  const int ld = m + 1;
+  double* V = bp.take((size_t)n * (m + 1));
+  double* w = bp.take(n);
+  double* t = bp.take(n);
+  double* Hc = bp.take(ld);
+  double* tmp = bp.take(ld);
+  double* cs = bp.take(ld);
+  double* sn = bp.take(ld);
+  double* gam = bp.take(ld);
+  double* R = bp.take((size_t)ld * ld);
+  double* ys = bp.take(ld);
+  double* dsc = c->dscal;  // 0: trace, 1: |r|, 2: |b|, 3: resid
+  int* bflag = c->dflag + 1;
+  // |b|
+  RC(kr_multidot(c->ws, b, n, 1, b, n, tmp, 0, dsc + 2, st));
+  double bnorm = 0.0;
+  CK(cudaMemcpyAsync(&bnorm, dsc + 2, 8, cudaMemcpyDeviceToHost, st));
+  CK(cudaStreamSynchronize(st));
+  if (!std::isfinite(bnorm)) return IMPS_ERR_NAN;
+  int it = 0;
+  double rel = 0.0;
+  int status = IMPS_WARN_NOT_CONVERGED;
+  if (bnorm == 0.0) {
+    CK(cudaMemsetAsync(y, 0, n * 8, st));
+    if (iters) *iters = 0;
+    if (relres) *relres = 0.0;
+    return IMPS_OK;
+  }
+  std::vector<double> Rh((size_t)ld * ld), gh(ld), yh(ld);
+  for (int outer = 0; it < maxit; ++outer) {
+    // r = b - A(y)  (FP64 residual)
+    RC(proj_apply_dev(p, y, rho_in, rho_out, w, t, dsc));
+    RC(kr_axpby(1.0, b, -1.0, w, n, st));
+    RC(kr_multidot(c->ws, w, n, 1, w, n, tmp, 0, dsc + 1, st));
+    double rn = 0.0;
+    CK(cudaMemcpyAsync(&rn, dsc + 1, 8, cudaMemcpyDeviceToHost, st));
+    CK(cudaStreamSynchronize(st));
+    if (!std::isfinite(rn)) return IMPS_ERR_NAN;
+    rel = rn / bnorm;
+    if (rn < tol * bnorm) { status = IMPS_OK; break; }
+    CK(cudaMemsetAsync(bflag, 0, sizeof(int), st));
+    RC(kr_scale_inv(w, dsc + 1, V, n, bflag, st));
+    CK(cudaMemsetAsync(gam, 0, ld * 8, st));
+    CK(cudaMemcpyAsync(gam, dsc + 1, 8, cudaMemcpyDeviceToDevice, st));
+    int kdim = 0;
+    for (int j = 0; j < m && it < maxit; ++j) {
+      double* vj = V + (size_t)j * n;
+      RC(proj_apply_dev(p, vj, rho_in, rho_out, w, t, dsc));
+      ++it;
+      RC(kr_multidot(c->ws, V, n, j + 1, w, n, Hc, 0, nullptr, st));
+      RC(kr_gemv_sub(V, n, j + 1, Hc, w, n, st));
+      RC(kr_multidot(c->ws, V, n, j + 1, w, n, tmp, 0, nullptr, st));
+      RC(kr_gemv_sub(V, n, j + 1, tmp, w, n, st));
+      RC(kr_axpby(1.0, tmp, 1.0, Hc, j + 1, st));
+      RC(kr_multidot(c->ws, w, n, 1, w, n, tmp, 0, Hc + j + 1, st));
+      RC(kr_scale_inv(w, Hc + j + 1, V + (size_t)(j + 1) * n, n, nullptr, st));
+      RC(kr_givens(Hc, j, cs, sn, gam, R, ld, dsc + 3, bflag, st));
+      kdim = j + 1;
+      if ((j + 1) % 4 == 0 || j == m - 1 || it >= maxit) {
+        double res = 0.0;
+        int brk = 0;
+        CK(cudaMemcpyAsync(&res, dsc + 3, 8, cudaMemcpyDeviceToHost, st));
+        CK(cudaMemcpyAsync(&brk, bflag, sizeof(int), cudaMemcpyDeviceToHost, st));
+        CK(cudaStreamSynchronize(st));
+        if (!std::isfinite(res)) return IMPS_ERR_NAN;
+        if (brk) { kdim = j; break; }  // invariant subspace
+        if (res < tol * bnorm) break;
+      }
+    }
+    // y += V[:, :kdim] * R^{-1} gamma
+    if (kdim > 0) {
+      CK(cudaMemcpyAsync(Rh.data(), R, (size_t)ld * kdim * 8, cudaMemcpyDeviceToHost, st));
+      CK(cudaMemcpyAsync(gh.data(), gam, kdim * 8, cudaMemcpyDeviceToHost, st));
+      CK(cudaStreamSynchronize(st));
+      for (int i = kdim - 1; i >= 0; --i) {
+        double s = gh[i];
+        for (int q = i + 1; q < kdim; ++q) s -= Rh[i + (size_t)q * ld] * yh[q];
+        yh[i] = s / Rh[i + (size_t)i * ld];
+      }
+      CK(cudaMemcpyAsync(ys, yh.data(), kdim * 8, cudaMemcpyHostToDevice, st));
+      RC(kr_gemv(V, n, kdim, ys, t, n, st));
+      RC(kr_axpby(1.0, t, 1.0, y, n, st));
+    }
+  }
+  if (status != IMPS_OK) {
+    // final explicit residual
+    RC(proj_apply_dev(p, y, rho_in, rho_out, w, t, dsc));
+    RC(kr_axpby(1.0, b, -1.0, w, n, st));
+    RC(kr_multidot(c->ws, w, n, 1, w, n, tmp, 0, dsc + 1, st));
+    double rn = 0.0;
+    CK(cudaMemcpyAsync(&rn, dsc + 1, 8, cudaMemcpyDeviceToHost, st));
+    CK(cudaStreamSynchronize(st));
+    rel = rn / bnorm;
+    if (rn < tol * bnorm) status = IMPS_OK;
+  }
+  if (iters) *iters = it;
+  if (relres) *relres = rel;
+  return status;
+}
+
+int imps_invert_e_proj(imps_plan* p, const double* x, const double* L, const double* R, int dir,
+                       double* y, int mem, double tol, int maxit, int krylov, int* iters, double* relres) {
+  if (!p || p->P.kind != PLAN_TM || !x || !L || !R || !y || (dir != 0 && dir != 1)) return IMPS_ERR_BAD_ARG;
+  imps_ctx* c = p->ctx;
+  cudaStream_t st = c->stream;
+  const int64_t n = p->P.slots[0].nelem;
+  if (p->P.slots[1].nelem != n) return IMPS_ERR_BAD_ARG;
+  int m = krylov > 0 ? std::min(krylov, kMaxCols - 2) : 40;
+  if (maxit <= 0) maxit = (int)std::min<int64_t>(n, 100000);
+  RC(arena_reserve(c, round256(n * 8) * (m + 12) + round256((size_t)(m + 1) * (m + 1) * 8) + 16 * 4096));
+  Bump bp{c->arena};
+  double *dx = (double*)x, *dL = (double*)L, *dR = (double*)R, *dy = y;
+  if (mem == IMPS_MEM_HOST) {
+    dx = bp.take(n); dL = bp.take(n); dR = bp.take(n); dy = bp.take(n);
+    CK(cudaMemcpyAsync(dx, x, n * 8, cudaMemcpyHostToDevice, st));
+    CK(cudaMemcpyAsync(dL, L, n * 8, cudaMemcpyHostToDevice, st));
+    CK(cudaMemcpyAsync(dR, R, n * 8, cudaMemcpyHostToDevice, st));
+    CK(cudaMemcpyAsync(dy, y, n * 8, cudaMemcpyHostToDevice, st));
+  }
+  // rho_in / rho_out: dir l -> (R, L), dir r -> (L, R)  (InvEBlockFunctions.hpp:239-257)
+  const double* rin = dir == 0 ? dR : dL;
+  const double* rout = dir == 0 ? dL : dR;
+  // b = x - tr(x*rho_in) * rho_out
+  double* b = bp.take(n);
+  RC(kr_trace_prod(c->ws, dx, rin, p->d_boff, p->d_bdim, p->nb_in, c->dscal + 4, st));
+  CK(cudaMemsetAsync(b, 0, n * 8, st));
+  RC(kr_proj_epilogue(dx, b, c->dscal + 4, rout, b, n, st));  // b = x + s*rho_out - 0
+  // flip sign of the projector part: b = x - s*rho_out  ->  compute b2 = 2x - b
+  RC(kr_axpby(2.0, dx, -1.0, b, n, st));
+  int rc = gmres_proj(p, b, dy, rin, rout, tol, maxit, m, iters, relres, bp);
+  if (rc < 0) return rc;
+  if (mem == IMPS_MEM_HOST) {
+    CK(cudaMemcpyAsync(y, dy, n * 8, cudaMemcpyDeviceToHost, st));
+    CK(cudaStreamSynchronize(st));
+  }
+  return rc;
+}
+
+__global__ void imps_set_identity_kernel(double* X, const int64_t* boff, const int32_t* bdim, int nb) {
+  const int b = blockIdx.x;
+  if (b >= nb) return;
+  const int m = bdim[b];
+  double* x = X + boff[b];
+  for (int64_t e = threadIdx.x; e < (int64_t)m * m; e += blockDim.x) x[e] = (e % (m + 1) == 0) ? 1.0 : 0.0;
+}
+
+int imps_tm_dominant(imps_plan* p, const double* x0, double* V, int mem, double tol, int maxit,
+                     double* eval, int* iters) {
+  if (!p || p->P.kind != PLAN_TM || !V) return IMPS_ERR_BAD_ARG;
+  imps_ctx* c = p->ctx;
+  cudaStream_t st = c->stream;
+  const int64_t n = p->P.slots[0].nelem;
+  if (p->P.slots[1].nelem != n) return IMPS_ERR_BAD_ARG;
+  const int m = 40;
+  if (maxit <= 0) maxit = (int)std::min<int64_t>(n, 100000);
+  RC(arena_reserve(c, round256(n * 8) * (m + 14) + round256((size_t)(m + 1) * (m + 1) * 8) + 16 * 4096));
+  Bump bp{c->arena};
+  double* eye = bp.take(n);
+  double* r0 = bp.take(n);
+  double* v = bp.take(n);
+  imps_set_identity_kernel<<<std::max(p->nb_in, 1), 256, 0, st>>>(eye, p->d_boff, p->d_bdim, p->nb_in);
+  if (x0) {
+    CK(cudaMemcpyAsync(r0, x0, n * 8, mem == IMPS_MEM_HOST ? cudaMemcpyHostToDevice : cudaMemcpyDeviceToDevice, st));
+  } else {
+    CK(cudaMemcpyAsync(r0, eye, n * 8, cudaMemcpyDeviceToDevice, st));
+  }
+  // normalise the seed to unit trace: r0 /= tr(r0)
+  RC(kr_trace_prod(c->ws, r0, eye, p->d_boff, p->d_bdim, p->nb_in, c->dscal + 5, st));
+  RC(kr_scale_inv(r0, c->dscal + 5, r0, n, nullptr, st));
+  CK(cudaMemcpyAsync(v, r0, n * 8, cudaMemcpyDeviceToDevice, st));
+  // (1 - T + |r0)(1|) v = r0
+  int rc = gmres_proj(p, r0, v, eye, r0, tol, maxit, m, iters, nullptr, bp);
+  if (rc < 0) return rc;
+  // normalise by the trace (EigsBlockFunctions.hpp:162) and estimate the eigenvalue
+  RC(kr_trace_prod(c->ws, v, eye, p->d_boff, p->d_bdim, p->nb_in, c->dscal + 5, st));
+  RC(kr_scale_inv(v, c->dscal + 5, v, n, nullptr, st));
+  double* tv = bp.take(n);
+  RC(apply_dev(p, v, tv));
+  RC(kr_trace_prod(c->ws, tv, eye, p->d_boff, p->d_bdim, p->nb_in, c->dscal + 6, st));
+  double lam = 0.0;
+  CK(cudaMemcpyAsync(&lam, c->dscal + 6, 8, cudaMemcpyDeviceToHost, st));
+  if (mem == IMPS_MEM_HOST) CK(cudaMemcpyAsync(V, v, n * 8, cudaMemcpyDeviceToHost, st));
+  else CK(cudaMemcpyAsync(V, v, n * 8, cudaMemcpyDeviceToDevice, st));
+  CK(cudaStreamSynchronize(st));
+  if (eval) *eval = lam;
+  return rc;
+}
+
+int imps_grad_norm_right(imps_plan* p, double* F) {
+  if (!p || p->P.kind != PLAN_GRAD || !F) return IMPS_ERR_BAD_ARG;
+  imps_ctx* c = p->ctx;
+  cudaStream_t st = c->stream;
+  Slot& Y = p->P.slots[0];
+  Slot& G = p->P.slots[2];
+  if (!Y.dptr || !G.dptr || !p->P.slots[1].dptr) return IMPS_ERR_BAD_ARG;
+  CK(cudaMemcpyAsync(G.dptr, Y.dptr, Y.nelem * 8, cudaMemcpyDeviceToDevice, st));
+  RC(run_stages(p, p->P.stages));
+  if (p->nseg == 0 || p->count_elems == 0) { *F = 0.0; return IMPS_OK; }
+  RC(kr_segsq(c->ws, G.dptr, p->d_soff, p->d_slen, p->nseg, c->dscal + 7, st));
+  double s = 0.0;
+  CK(cudaMemcpyAsync(&s, c->dscal + 7, 8, cudaMemcpyDeviceToHost, st));
+  CK(cudaStreamSynchronize(st));
+  *F = std::sqrt(s) / std::sqrt((double)p->count_elems);
+  return IMPS_OK;
+}
+
+}  // extern "C"

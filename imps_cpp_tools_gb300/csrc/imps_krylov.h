@@ -1,0 +1,36 @@
+// Krylov kernels (kernels_krylov.cu) used by the device Lanczos and GMRES drivers.
+#pragma once
+#include <cuda_runtime.h>
+
+#include <cstddef>
+#include <cstdint>
+
+namespace imps {
+
+constexpr int kMaxCols = 64;  // max Krylov basis size handled by one projection kernel
+
+struct KrylovWs {
+  double* partials = nullptr;     // kr_partials_elems() doubles
+  unsigned int* counter = nullptr;
+};
+
+size_t kr_partials_elems();
+int kr_multidot(const KrylovWs& ws, const double* V, int64_t ldv, int ncols, const double* w,
+                int64_t n, double* h, int mode, double* out_sqrt, cudaStream_t st);
+int kr_gemv_sub(const double* V, int64_t ldv, int ncols, const double* h, double* w, int64_t n,
+                cudaStream_t st);
+int kr_gemv(const double* V, int64_t ldv, int ncols, const double* h, double* y, int64_t n,
+            cudaStream_t st);
+int kr_scale_inv(const double* x, const double* nrm, double* y, int64_t n, int* flag, cudaStream_t st);
+int kr_axpby(double a, const double* x, double b, double* y, int64_t n, cudaStream_t st);
+int kr_proj_epilogue(const double* x, const double* t, const double* s, const double* rho, double* y,
+                     int64_t n, cudaStream_t st);
+int kr_trace_prod(const KrylovWs& ws, const double* X, const double* R, const int64_t* boff,
+                  const int32_t* bdim, int nb, double* out, cudaStream_t st);
+int kr_segsq(const KrylovWs& ws, const double* X, const int64_t* soff, const int64_t* slen, int ns,
+             double* out, cudaStream_t st);
+int kr_absmax(const KrylovWs& ws, const double* x, int64_t n, double* out, cudaStream_t st);
+int kr_givens(double* Hcol, int j, double* cs, double* sn, double* gamma, double* R, int ldr,
+              double* res, int* breakdown, cudaStream_t st);
+
+}  // namespace imps

@@ -1,0 +1,110 @@
+// FP64 kernels for the block-sparse hot path on sm_103a.
+//
+//  * grouped_gemm_f64: output-stationary grouped GEMM over the planner's tile/term tables.
+//    One CTA per output tile; every term of the tile is accumulated in registers and the
+//    tile is written once (deterministic, no atomics, no separate zero-fill: the first
+//    write also performs the reference's memset of `out`, VUMPS_helpers.hpp:69).
+//  * Krylov BLAS-1 (reductions without atomics: fixed-grid partials + one finishing block).
+#include <cuda_runtime.h>
+
+#include <cstdint>
+
+#include "imps_internal.h"
+#include "imps_status.h"
+
+using imps::Term;
+using imps::Tile;
+
+namespace {
+
+constexpr int TK = 16;
+
+// TMxTN tile computed by (TM/RM)*(TN/RN) threads, each holding RM x RN accumulators.
+template <int TM, int TN, int RM, int RN>
+__global__ void __launch_bounds__((TM / RM) * (TN / RN))
+grouped_gemm_f64_kernel(const Tile* __restrict__ tiles, const Term* __restrict__ terms,
+                        imps_dslots slots) {
+  constexpr int NT = (TM / RM) * (TN / RN);
+  constexpr int TX = TN / RN;  // threads along n
+  __shared__ double As[TK][TM + 1];
+  __shared__ double Bs[TK][TN + 1];
+  const Tile tl = tiles[blockIdx.x];
+  const int tid = threadIdx.x;
+  const int tx = tid % TX, ty = tid / TX;
+  double acc[RM][RN];
+#pragma unroll
+  for (int i = 0; i < RM; ++i)
+#pragma unroll
+    for (int j = 0; j < RN; ++j) acc[i][j] = 0.0;
+
+  for (int t = tl.t0; t < tl.t1; ++t) {
+    const Term tm = terms[t];
+    const double* __restrict__ A = slots.p[tm.a_slot] + tm.a_off;
+    const double* __restrict__ B = slots.p[tm.b_slot] + tm.b_off;
+    const double alpha = tm.alpha;
+    for (int k0 = 0; k0 < tm.k; k0 += TK) {
+      // A tile: rows m0..m0+TM, cols k0..k0+TK of op(A)
+      for (int e = tid; e < TM * TK; e += NT) {
+        int m, k;
+        if (tm.a_t) { k = e % TK; m = e / TK; } else { m = e % TM; k = e / TM; }
+        const int gm = tl.m0 + m, gk = k0 + k;
+        double v = 0.0;
+        if (m < tl.mt && gk < tm.k)
+          v = tm.a_t ? A[(int64_t)gm * tm.a_ld + gk] : A[gm + (int64_t)gk * tm.a_ld];
+        As[k][m] = alpha * v;
+      }
+      for (int e = tid; e < TN * TK; e += NT) {
+        int n, k;
+        if (tm.b_t) { n = e % TN; k = e / TN; } else { k = e % TK; n = e / TK; }
+        const int gn = tl.n0 + n, gk = k0 + k;
+        double v = 0.0;
+        if (n < tl.nt && gk < tm.k)
+          v = tm.b_t ? B[gn + (int64_t)gk * tm.b_ld] : B[gk + (int64_t)gn * tm.b_ld];
+        Bs[k][n] = v;
+      }
+      __syncthreads();
+      const int kmax = min(TK, tm.k - k0);
+      for (int k = 0; k < kmax; ++k) {
+        double a[RM], b[RN];
+#pragma unroll
+        for (int i = 0; i < RM; ++i) a[i] = As[k][ty + i * (TM / RM)];
+#pragma unroll
+        for (int j = 0; j < RN; ++j) b[j] = Bs[k][tx + j * TX];
+#pragma unroll
+        for (int i = 0; i < RM; ++i)
+#pragma unroll
+          for (int j = 0; j < RN; ++j) acc[i][j] = fma(a[i], b[j], acc[i][j]);
+      }
+      __syncthreads();
+    }
+  }
+  double* __restrict__ C = slots.p[tl.c_slot] + tl.c_off;
+#pragma unroll
+  for (int i = 0; i < RM; ++i) {
+    const int m = ty + i * (TM / RM);
+    if (m >= tl.mt) continue;
+#pragma unroll
+    for (int j = 0; j < RN; ++j) {
+      const int n = tx + j * TX;
+      if (n >= tl.nt) continue;
+      double* p = C + (tl.m0 + m) + (int64_t)(tl.n0 + n) * tl.c_ld;
+      *p = tl.accumulate ? *p + acc[i][j] : acc[i][j];
+    }
+  }
+}
+
+}  // namespace
+
+int imps_launch_grouped_f64(const void* d_tiles, int ntiles, const void* d_terms, imps_dslots slots,
+                            int tile_m, void* stream) {
+  if (ntiles <= 0) return IMPS_OK;
+  cudaStream_t st = (cudaStream_t)stream;
+  if (tile_m == 16) {
+    grouped_gemm_f64_kernel<16, 16, 2, 2><<<ntiles, 64, 0, st>>>((const Tile*)d_tiles,
+                                                                 (const Term*)d_terms, slots);
+  } else {
+    grouped_gemm_f64_kernel<32, 32, 2, 4><<<ntiles, 128, 0, st>>>((const Tile*)d_tiles,
+                                                                  (const Term*)d_terms, slots);
+  }
+  return cudaGetLastError() == cudaSuccess ? IMPS_OK : IMPS_ERR_CUDA;
+}

@@ -1,0 +1,338 @@
+// Krylov-space kernels (FP64 always): dot products, CGS2 projections, norms, scaling and the
+// small sequential steps of GMRES (Givens rotations) kept on the device so that an iteration
+// needs no host round trip.  Reductions use a fixed grid and a last-block finisher, so every
+// result is bitwise reproducible run to run (no floating-point atomics).
+#include <cuda_runtime.h>
+
+#include <cmath>
+#include <cstdint>
+
+#include "imps_krylov.h"
+#include "imps_status.h"
+
+namespace {
+
+constexpr int RB = 256;      // threads per reduction block
+constexpr int RGRID = 128;   // fixed reduction grid (partials buffer is RGRID * kMaxCols)
+
+__device__ __forceinline__ double warp_sum(double v) {
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) v += __shfl_down_sync(0xffffffffu, v, o);
+  return v;
+}
+
+// Block-wide sum; result valid in thread 0.
+__device__ double block_sum(double v, double* sh) {
+  v = warp_sum(v);
+  const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
+  if (lane == 0) sh[w] = v;
+  __syncthreads();
+  v = threadIdx.x < (blockDim.x >> 5) ? sh[threadIdx.x] : 0.0;
+  if (w == 0) v = warp_sum(v);
+  __syncthreads();
+  return v;
+}
+
+// h[c] = scale_c * sum_r V[r + c*ldv] * w[r], c = 0..ncols-1 (ncols <= kMaxCols).
+// mode 0: h = result; mode 1: h += result.  Also optional out_norm = sqrt(h[0]) when
+// V == w and ncols == 1 (norm use).
+__global__ void __launch_bounds__(RB) multidot_kernel(const double* __restrict__ V, int64_t ldv,
+                                                      int ncols, const double* __restrict__ w,
+                                                      int64_t n, double* __restrict__ partials,
+                                                      unsigned int* __restrict__ counter,
+                                                      double* __restrict__ h, int mode,
+                                                      double* __restrict__ out_sqrt) {
+  __shared__ double sh[32];
+  __shared__ bool last;
+  for (int c = 0; c < ncols; ++c) {
+    const double* v = V + c * ldv;
+    double acc = 0.0;
+    for (int64_t r = (int64_t)blockIdx.x * RB + threadIdx.x; r < n; r += (int64_t)gridDim.x * RB)
+      acc = fma(v[r], w[r], acc);
+    acc = block_sum(acc, sh);
+    if (threadIdx.x == 0) partials[c * RGRID + blockIdx.x] = acc;
+  }
+  __threadfence();
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    unsigned int prev = atomicAdd(counter, 1u);
+    last = (prev == gridDim.x - 1);
+  }
+  __syncthreads();
+  if (!last) return;
+  __threadfence();
+  for (int c = 0; c < ncols; ++c) {
+    double v = threadIdx.x < gridDim.x ? ((volatile double*)partials)[c * RGRID + threadIdx.x] : 0.0;
+    v = block_sum(v, sh);
+    if (threadIdx.x == 0) {
+      h[c] = mode ? h[c] + v : v;
+      if (out_sqrt && c == 0) *out_sqrt = sqrt(v);
+    }
+  }
+  if (threadIdx.x == 0) *counter = 0u;
+}
+
+// w[r] -= sum_c V[r + c*ldv] * h[c]
+__global__ void gemv_sub_kernel(const double* __restrict__ V, int64_t ldv, int ncols,
+                                const double* __restrict__ h, double* __restrict__ w, int64_t n) {
+  __shared__ double hs[imps::kMaxCols];
+  for (int c = threadIdx.x; c < ncols; c += blockDim.x) hs[c] = h[c];
+  __syncthreads();
+  for (int64_t r = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; r < n;
+       r += (int64_t)gridDim.x * blockDim.x) {
+    double acc = w[r];
+    for (int c = 0; c < ncols; ++c) acc = fma(-V[r + c * ldv], hs[c], acc);
+    w[r] = acc;
+  }
+}
+
+// y[r] = sum_c V[r + c*ldv] * h[c]
+__global__ void gemv_kernel(const double* __restrict__ V, int64_t ldv, int ncols,
+                            const double* __restrict__ h, double* __restrict__ y, int64_t n) {
+  __shared__ double hs[imps::kMaxCols];
+  for (int c = threadIdx.x; c < ncols; c += blockDim.x) hs[c] = h[c];
+  __syncthreads();
+  for (int64_t r = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; r < n;
+       r += (int64_t)gridDim.x * blockDim.x) {
+    double acc = 0.0;
+    for (int c = 0; c < ncols; ++c) acc = fma(V[r + c * ldv], hs[c], acc);
+    y[r] = acc;
+  }
+}
+
+// y = x / *nrm  (guarded: a zero norm writes zeros and raises the breakdown flag)
+__global__ void scale_inv_kernel(const double* __restrict__ x, const double* __restrict__ nrm,
+                                 double* __restrict__ y, int64_t n, int* __restrict__ flag) {
+  const double s = *nrm;
+  const bool bad = !(fabs(s) > 1e-300) || !isfinite(s);
+  if (bad && flag && blockIdx.x == 0 && threadIdx.x == 0) *flag = 1;
+  const double inv = bad ? 0.0 : 1.0 / s;
+  for (int64_t r = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; r < n;
+       r += (int64_t)gridDim.x * blockDim.x)
+    y[r] = x[r] * inv;
+}
+
+// y = a*x + b*y with host scalars
+__global__ void axpby_kernel(double a, const double* __restrict__ x, double b, double* __restrict__ y,
+                             int64_t n) {
+  for (int64_t r = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; r < n;
+       r += (int64_t)gridDim.x * blockDim.x)
+    y[r] = a * x[r] + b * y[r];
+}
+
+// y = x - t + (*s) * rho   (InvEfun_proj epilogue, InvEBlockFunctions.hpp:40-44)
+__global__ void proj_epilogue_kernel(const double* __restrict__ x, const double* __restrict__ t,
+                                     const double* __restrict__ s, const double* __restrict__ rho,
+                                     double* __restrict__ y, int64_t n) {
+  const double sc = *s;
+  for (int64_t r = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; r < n;
+       r += (int64_t)gridDim.x * blockDim.x)
+    y[r] = x[r] + sc * rho[r] - t[r];
+}
+
+// sum over blocks q of trace(X_q * R_q) = sum_{i,j} X_q[i + j m] * R_q[j + i m]
+__global__ void __launch_bounds__(RB) trace_prod_kernel(const double* __restrict__ X,
+                                                        const double* __restrict__ R,
+                                                        const int64_t* __restrict__ boff,
+                                                        const int32_t* __restrict__ bdim, int nb,
+                                                        double* __restrict__ partials,
+                                                        unsigned int* __restrict__ counter,
+                                                        double* __restrict__ out) {
+  __shared__ double sh[32];
+  __shared__ bool last;
+  double acc = 0.0;
+  // flatten (block, element) pairs with a grid-stride loop over blocks x elements
+  for (int b = 0; b < nb; ++b) {
+    const int m = bdim[b];
+    const int64_t o = boff[b];
+    const int64_t mm = (int64_t)m * m;
+    for (int64_t e = (int64_t)blockIdx.x * RB + threadIdx.x; e < mm; e += (int64_t)gridDim.x * RB) {
+      const int64_t i = e % m, j = e / m;
+      acc = fma(X[o + e], R[o + j + i * m], acc);
+    }
+  }
+  acc = block_sum(acc, sh);
+  if (threadIdx.x == 0) partials[blockIdx.x] = acc;
+  __threadfence();
+  __syncthreads();
+  if (threadIdx.x == 0) last = (atomicAdd(counter, 1u) == gridDim.x - 1);
+  __syncthreads();
+  if (!last) return;
+  __threadfence();
+  double v = threadIdx.x < gridDim.x ? ((volatile double*)partials)[threadIdx.x] : 0.0;
+  v = block_sum(v, sh);
+  if (threadIdx.x == 0) { *out = v; *counter = 0u; }
+}
+
+// sum of squares over a list of segments (off, len) -> *out (plain sum, no sqrt)
+__global__ void __launch_bounds__(RB) segsq_kernel(const double* __restrict__ X,
+                                                   const int64_t* __restrict__ soff,
+                                                   const int64_t* __restrict__ slen, int ns,
+                                                   double* __restrict__ partials,
+                                                   unsigned int* __restrict__ counter,
+                                                   double* __restrict__ out) {
+  __shared__ double sh[32];
+  __shared__ bool last;
+  double acc = 0.0;
+  for (int s = 0; s < ns; ++s) {
+    const double* x = X + soff[s];
+    for (int64_t e = (int64_t)blockIdx.x * RB + threadIdx.x; e < slen[s]; e += (int64_t)gridDim.x * RB)
+      acc = fma(x[e], x[e], acc);
+  }
+  acc = block_sum(acc, sh);
+  if (threadIdx.x == 0) partials[blockIdx.x] = acc;
+  __threadfence();
+  __syncthreads();
+  if (threadIdx.x == 0) last = (atomicAdd(counter, 1u) == gridDim.x - 1);
+  __syncthreads();
+  if (!last) return;
+  __threadfence();
+  double v = threadIdx.x < gridDim.x ? ((volatile double*)partials)[threadIdx.x] : 0.0;
+  v = block_sum(v, sh);
+  if (threadIdx.x == 0) { *out = v; *counter = 0u; }
+}
+
+// max |x| -> *out
+__global__ void __launch_bounds__(RB) absmax_kernel(const double* __restrict__ x, int64_t n,
+                                                    double* __restrict__ partials,
+                                                    unsigned int* __restrict__ counter,
+                                                    double* __restrict__ out) {
+  __shared__ double sh[RB];
+  __shared__ bool last;
+  double m = 0.0;
+  for (int64_t r = (int64_t)blockIdx.x * RB + threadIdx.x; r < n; r += (int64_t)gridDim.x * RB)
+    m = fmax(m, fabs(x[r]));
+  sh[threadIdx.x] = m;
+  __syncthreads();
+  for (int s = RB / 2; s > 0; s >>= 1) {
+    if (threadIdx.x < s) sh[threadIdx.x] = fmax(sh[threadIdx.x], sh[threadIdx.x + s]);
+    __syncthreads();
+  }
+  if (threadIdx.x == 0) partials[blockIdx.x] = sh[0];
+  __threadfence();
+  __syncthreads();
+  if (threadIdx.x == 0) last = (atomicAdd(counter, 1u) == gridDim.x - 1);
+  __syncthreads();
+  if (!last) return;
+  __threadfence();
+  sh[threadIdx.x] = threadIdx.x < gridDim.x ? ((volatile double*)partials)[threadIdx.x] : 0.0;
+  __syncthreads();
+  for (int s = RB / 2; s > 0; s >>= 1) {
+    if (threadIdx.x < s) sh[threadIdx.x] = fmax(sh[threadIdx.x], sh[threadIdx.x + s]);
+    __syncthreads();
+  }
+  if (threadIdx.x == 0) { *out = sh[0]; *counter = 0u; }
+}
+
+// One GMRES step of the reference's Givens update (IterativeSolvers.hpp:77-116), run by a
+// single thread on the device.  Hcol holds column j (j+2 entries, already orthogonalised,
+// Hcol[j+1] = |w|).  Applies rotations 0..j-1, forms rotation j, updates gamma, writes
+// |gamma[j+1]| to *res and stores the rotated column into R (column-major, ld = ldr).
+__global__ void givens_kernel(double* __restrict__ Hcol, int j, double* __restrict__ cs,
+                              double* __restrict__ sn, double* __restrict__ gamma,
+                              double* __restrict__ R, int ldr, double* __restrict__ res,
+                              int* __restrict__ breakdown) {
+  if (threadIdx.x != 0 || blockIdx.x != 0) return;
+  for (int i = 0; i < j; ++i) {
+    const double h1 = Hcol[i], h2 = Hcol[i + 1];
+    Hcol[i] = cs[i] * h1 + sn[i] * h2;
+    Hcol[i + 1] = -sn[i] * h1 + cs[i] * h2;
+  }
+  const double hjj = Hcol[j], hj1 = Hcol[j + 1];
+  const double beta = sqrt(hjj * hjj + hj1 * hj1);
+  if (!(beta >= 2e-16)) {  // flag -2 of the reference
+    *breakdown = 1;
+    *res = 0.0;
+    for (int i = 0; i <= j; ++i) R[i + (int64_t)j * ldr] = Hcol[i];
+    return;
+  }
+  const double habs = fabs(hjj);
+  const double phase = habs > 0.0 ? hjj / habs : 1.0;
+  sn[j] = phase * hj1 / beta;
+  cs[j] = habs / beta;
+  Hcol[j] = phase * beta;
+  Hcol[j + 1] = 0.0;
+  gamma[j + 1] = -sn[j] * gamma[j];
+  gamma[j] *= cs[j];
+  for (int i = 0; i <= j; ++i) R[i + (int64_t)j * ldr] = Hcol[i];
+  *res = fabs(gamma[j + 1]);
+}
+
+int grid_for(int64_t n) {
+  int64_t g = (n + 255) / 256;
+  if (g > 152 * 8) g = 152 * 8;
+  if (g < 1) g = 1;
+  return (int)g;
+}
+
+}  // namespace
+
+namespace imps {
+
+int kr_multidot(const KrylovWs& ws, const double* V, int64_t ldv, int ncols, const double* w,
+                int64_t n, double* h, int mode, double* out_sqrt, cudaStream_t st) {
+  if (ncols > kMaxCols) return IMPS_ERR_BAD_ARG;
+  int grid = (int)((n + RB - 1) / RB);
+  if (grid > RGRID) grid = RGRID;
+  if (grid < 1) grid = 1;
+  multidot_kernel<<<grid, RB, 0, st>>>(V, ldv, ncols, w, n, ws.partials, ws.counter, h, mode, out_sqrt);
+  return IMPS_OK;
+}
+
+int kr_gemv_sub(const double* V, int64_t ldv, int ncols, const double* h, double* w, int64_t n,
+                cudaStream_t st) {
+  gemv_sub_kernel<<<grid_for(n), 256, 0, st>>>(V, ldv, ncols, h, w, n);
+  return IMPS_OK;
+}
+
+int kr_gemv(const double* V, int64_t ldv, int ncols, const double* h, double* y, int64_t n,
+            cudaStream_t st) {
+  gemv_kernel<<<grid_for(n), 256, 0, st>>>(V, ldv, ncols, h, y, n);
+  return IMPS_OK;
+}
+
+int kr_scale_inv(const double* x, const double* nrm, double* y, int64_t n, int* flag, cudaStream_t st) {
+  scale_inv_kernel<<<grid_for(n), 256, 0, st>>>(x, nrm, y, n, flag);
+  return IMPS_OK;
+}
+
+int kr_axpby(double a, const double* x, double b, double* y, int64_t n, cudaStream_t st) {
+  axpby_kernel<<<grid_for(n), 256, 0, st>>>(a, x, b, y, n);
+  return IMPS_OK;
+}
+
+int kr_proj_epilogue(const double* x, const double* t, const double* s, const double* rho, double* y,
+                     int64_t n, cudaStream_t st) {
+  proj_epilogue_kernel<<<grid_for(n), 256, 0, st>>>(x, t, s, rho, y, n);
+  return IMPS_OK;
+}
+
+int kr_trace_prod(const KrylovWs& ws, const double* X, const double* R, const int64_t* boff,
+                  const int32_t* bdim, int nb, double* out, cudaStream_t st) {
+  trace_prod_kernel<<<32, RB, 0, st>>>(X, R, boff, bdim, nb, ws.partials, ws.counter, out);
+  return IMPS_OK;
+}
+
+int kr_segsq(const KrylovWs& ws, const double* X, const int64_t* soff, const int64_t* slen, int ns,
+             double* out, cudaStream_t st) {
+  segsq_kernel<<<64, RB, 0, st>>>(X, soff, slen, ns, ws.partials, ws.counter, out);
+  return IMPS_OK;
+}
+
+int kr_absmax(const KrylovWs& ws, const double* x, int64_t n, double* out, cudaStream_t st) {
+  int grid = (int)((n + RB - 1) / RB);
+  if (grid > RGRID) grid = RGRID;
+  if (grid < 1) grid = 1;
+  absmax_kernel<<<grid, RB, 0, st>>>(x, n, ws.partials, ws.counter, out);
+  return IMPS_OK;
+}
+
+int kr_givens(double* Hcol, int j, double* cs, double* sn, double* gamma, double* R, int ldr,
+              double* res, int* breakdown, cudaStream_t st) {
+  givens_kernel<<<1, 32, 0, st>>>(Hcol, j, cs, sn, gamma, R, ldr, res, breakdown);
+  return IMPS_OK;
+}
+
+size_t kr_partials_elems() { return (size_t)RGRID * kMaxCols; }
+
+}  // namespace imps

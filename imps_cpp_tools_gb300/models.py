@@ -1,0 +1,113 @@
+"""Models and charge bookkeeping of the hot path (host side, integer-exact).
+
+Restates, for the GB300 driver, the pieces of MPShelpers/src/Models.cpp and
+include/Block/ItoKey.hpp that define the inputs of the hot path: the two-site Hamiltonian h
+(as its nonzeros in armadillo SpMat iteration order), the physical-index -> charge map I2K,
+validpath and MakeDims.  Only U(1)^k charges occur in the supported models.
+"""
+from __future__ import annotations
+
+import math
+
+import numpy as np
+
+
+def _kadd(a, b):
+    return tuple(x + y for x, y in zip(a, b))
+
+
+def xxz_i2k(N=2, QN=(0,), d=2):
+    """XXZModel::GetdQ + GetI2K (Models.cpp:216-295), spin-1/2."""
+    m = QN[0]
+    if abs(m) >= N:
+        raise ValueError("|m| must be < N")
+    div = math.gcd(N - m, N + m)
+    first, second = 2 * N // div, -((N + m) // div)
+    return [(second + s * first,) for s in range(d - 1, -1, -1)]
+
+
+def fhub_i2k(N=2, QN=(2, 0)):
+    """FermiHubbardModel::GetdQ + GetI2K, (N,M) representation (Models.cpp:642-718)."""
+    n, m = QN
+    if n + m <= 0 or n + m >= 2 * N or n - m <= 0 or n - m >= 2 * N:
+        raise ValueError("QN out of range")
+    divn = math.gcd(math.gcd(N - n, 2 * N - n), n)
+    divm = math.gcd(math.gcd(N - m, N + m), m)
+    a1, a0 = N // divn, -(n // divn)
+    b1, b0 = N // divm, -((N + m) // divm)
+    return [(a0, b0 + b1), (a0 + a1, b0), (a0 + a1, b0 + 2 * b1), (a0 + 2 * a1, b0 + b1)]
+
+
+def validpath(N, I2K):
+    """ItoKey.hpp:126-165: indices j_1..j_N with sum I2K[j] = 0, first-found depth-first order."""
+    def it(n, key):
+        if n == 1:
+            for j, k in enumerate(I2K):
+                if _kadd(key, k) == I2K[0]:
+                    return [j]
+            return None
+        for j, k in enumerate(I2K):
+            p = it(n - 1, _kadd(key, k))
+            if p is not None:
+                return p + [j]
+        return None
+    p = it(N, I2K[0])
+    if p is None:
+        raise ValueError("no valid path for this I2K")
+    return p
+
+
+def make_dims(dmap0, N, I2K):
+    """ModelBase::MakeDims (Models.cpp:13-32): bond dims k = 0..N-1 from bond 0."""
+    path = validpath(N, I2K)
+    out, cur = [], dict(dmap0)
+    for k in range(N):
+        out.append(dict(cur))
+        sh = I2K[path[N - k - 1]]
+        cur = {_kadd(q, sh): m for q, m in cur.items()}
+    return out
+
+
+def xxz_h(J=1.0, Delta=1.0, hz=0.0):
+    """XYZAbstractModel::MakeOps (Models.cpp:57-93) with Jx=Jy=J, Jz=Delta (d=2)."""
+    sx = np.array([[0.0, 0.5], [0.5, 0.0]])
+    syi = np.array([[0.0, -0.5], [0.5, 0.0]])
+    sz = np.diag([0.5, -0.5])
+    one = np.eye(2)
+    return (-J * np.kron(sx, sx) + J * np.kron(syi, syi) - Delta * np.kron(sz, sz)
+            - 0.5 * hz * (np.kron(sz, one) + np.kron(one, sz)))
+
+
+def fhub_h(t=1.0, U=4.0, V=0.0, mu=0.0, hz=0.0):
+    """FermiHubbardModel::MakeOps (Models.cpp:543-572)."""
+    cup = np.zeros((4, 4)); cup[0, 2] = 1.0; cup[1, 3] = 1.0
+    cdo = np.zeros((4, 4)); cdo[0, 1] = 1.0; cdo[2, 3] = -1.0
+    nup = np.diag([0.0, 0.0, 1.0, 1.0]); ndo = np.diag([0.0, 1.0, 0.0, 1.0])
+    one = np.eye(4); F = np.diag([1.0, -1.0, -1.0, 1.0])
+    nup2, ndo2 = nup - 0.5 * one, ndo - 0.5 * one
+    nund, nupnd, nupnd2, sz = nup2 @ ndo2, nup + ndo, nup2 + ndo2, 0.5 * (nup - ndo)
+    hop = (np.kron(cup.T @ F, cup) - np.kron(cup @ F, cup.T) + np.kron(cdo.T @ F, cdo)
+           - np.kron(cdo @ F, cdo.T))
+    return (-t * hop + 0.5 * U * (np.kron(nund, one) + np.kron(one, nund)) + V * np.kron(nupnd2, nupnd2)
+            - 0.5 * mu * (np.kron(nupnd, one) + np.kron(one, nupnd))
+            - 0.5 * hz * (np.kron(sz, one) + np.kron(one, sz)))
+
+
+def h_nonzeros(h):
+    """Nonzeros (row, col, value) in armadillo SpMat iteration order (column-major)."""
+    out = []
+    for c in range(h.shape[1]):
+        for r in range(h.shape[0]):
+            if h[r, c] != 0.0:
+                out.append((r, c, float(h[r, c])))
+    return out
+
+
+def build_model(name, **params):
+    """Return (d, I2K, h) for 'xxz' (U(1), QN=[0]) or 'fhub' (U(1)xU(1), QN=[2,0], N=2)."""
+    if name == "xxz":
+        return 2, xxz_i2k(2, (0,)), xxz_h(params.get("J", 1.0), params.get("Delta", -1.0), params.get("hz", 0.0))
+    if name == "fhub":
+        return 4, fhub_i2k(2, (2, 0)), fhub_h(params.get("t", 1.0), params.get("U", 4.0), params.get("V", 0.0),
+                                              params.get("mu", 0.0), params.get("hz", 0.0))
+    raise ValueError(f"unknown model {name}")

@@ -1,0 +1,76 @@
+"""Reference-named entry points of the hot path on device buffers.
+
+Each function mirrors one reference function (named in its docstring) and runs entirely on
+the GPU through the C ABI; vectors are float64 CUDA tensors in the reference's Vectorize
+layout.  There is no CPU path: the native library is required.
+"""
+from __future__ import annotations
+
+import ctypes as C
+
+from . import _native as N
+from .blocks import _dptr
+
+
+def ApplyHAvec(plan, vin, vout):
+    """ApplyHAvec (VUMPS_helpers.hpp:55-88): vout = H_AC vin; operators bound to slots 2..5."""
+    N.call("imps_hac_apply", plan.handle, _dptr(vin), _dptr(vout), N.MEM_DEVICE)
+    return vout
+
+
+def ApplyHCvec(plan, vin, vout):
+    """ApplyHCvec (VUMPS_helpers.hpp:114-133): vout = H_C vin (call plan.prepare() after AL/AR change)."""
+    N.call("imps_hc_apply", plan.handle, _dptr(vin), _dptr(vout), N.MEM_DEVICE)
+    return vout
+
+
+def ApplyTM(plan, vin, vout):
+    """ApplyTMLeft/ApplyTMRight on a unit cell (TMBlockFunctions.hpp:557-625) via TMMultDiag."""
+    N.call("imps_tm_apply", plan.handle, _dptr(vin), _dptr(vout), N.MEM_DEVICE)
+    return vout
+
+
+def InvEfun_proj(plan, vin, rho_in, rho_out, vout):
+    """InvEfun_proj (InvEBlockFunctions.hpp:12-47): vout = vin - T(vin) + tr(vin*rho_in)*rho_out."""
+    N.call("imps_tm_proj_apply", plan.handle, _dptr(vin), _dptr(rho_in), _dptr(rho_out), _dptr(vout),
+           N.MEM_DEVICE)
+    return vout
+
+
+def eigs_rs(plan, x, tol, ncv=0, maxit=0):
+    """eigs_rs(fun, N, vals, vecs, nev=1, "SA", tol, x0) (eigs.cpp:369-494) on the device.
+
+    ``x`` holds x0 on entry and the normalised eigenvector on exit.
+    Returns (eigenvalue, number of operator applications, converged)."""
+    ev, na = C.c_double(), C.c_int()
+    st = N.call("imps_eigs_rs", plan.handle, _dptr(x), N.MEM_DEVICE, float(tol), int(ncv), int(maxit),
+                C.byref(ev), C.byref(na))
+    return ev.value, na.value, st == 0
+
+
+def InvertE_proj(plan, x, L, R, direction, y, tol, maxit=0, krylov=0):
+    """InvertE_proj (InvEBlockFunctions.hpp:201-266) for BlockDiagMat x on the unit cell of ``plan``.
+
+    ``y`` holds y0 on entry and the solution on exit.  direction: 'l' or 'r'.
+    Returns (iterations, relative residual, converged)."""
+    it, rr = C.c_int(), C.c_double()
+    d = N.DIR_LEFT if direction in ("l", 0) else N.DIR_RIGHT
+    st = N.call("imps_invert_e_proj", plan.handle, _dptr(x), _dptr(L), _dptr(R), d, _dptr(y), N.MEM_DEVICE,
+                float(tol), int(maxit), int(krylov), C.byref(it), C.byref(rr))
+    return it.value, rr.value, st == 0
+
+
+def TMDominantEig(plan, V, x0=None, tol=1e-14, maxit=0):
+    """TMDominantEig (EigsBlockFunctions.hpp:91-172) for an isometric unit cell: V <- fixed point
+    with unit trace.  Returns (eigenvalue estimate, iterations, converged)."""
+    ev, it = C.c_double(), C.c_int()
+    st = N.call("imps_tm_dominant", plan.handle, None if x0 is None else _dptr(x0), _dptr(V), N.MEM_DEVICE,
+                float(tol), int(maxit), C.byref(ev), C.byref(it))
+    return ev.value, it.value, st == 0
+
+
+def GradNormRight(plan):
+    """GradNormRight (VUMPS_helpers.hpp:145-153) from Y = H_AC(C*AR) bound to slot 0 and AR to slot 1."""
+    F = C.c_double()
+    N.call("imps_grad_norm_right", plan.handle, C.byref(F))
+    return F.value

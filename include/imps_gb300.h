@@ -1,0 +1,167 @@
+/*
+ * imps_gb300 -- C ABI of the GB300 (sm_103a) implementation of the IMPS_CPP_tools hot path:
+ * the block-sparse effective-Hamiltonian applies (H_AC, H_C), transfer-matrix applies and
+ * the Krylov solves (Lanczos eigensolve, GMRES environment solve) that drive VUMPS.
+ *
+ * Conventions
+ *  - Every function returns an int status: 0 = OK, > 0 warning, < 0 error (IMPS_* below).
+ *  - Vectors use the reference's layout unchanged: blocks concatenated in std::map key
+ *    order (s-major for MPS tensors), each block column-major (MPSBlockMat.hpp:448-465,
+ *    BlockObj.hpp:767-780, 1712), so vectors can be handed to/from ARPACK without permutation.
+ *  - A "layout" is the sector table of one block-sparse object (the reference's
+ *    GetSizesVector(), MPSBlockMat.hpp:336-347): per block (Qin, Qout, rows, cols, group),
+ *    group = physical index s for an MPS tensor, i*d+j for a RedOp grid (OperatorTypes.hpp:
+ *    160-187, row-major), 0 for BlockDiagMat/BlockMat.  Blocks must be ordered by group, then
+ *    by Qin (lexicographic), as the reference's std::map iteration yields them.
+ *  - mem = IMPS_MEM_HOST: pointers are host memory (copied through device staging);
+ *    mem = IMPS_MEM_DEVICE: pointers are device memory on the context's device.
+ *  - One context = one device + one CUDA stream; calls on one context are serialised on its
+ *    stream, no call retains a caller pointer after it returns (except imps_plan_bind).
+ */
+#ifndef IMPS_GB300_H
+#define IMPS_GB300_H
+
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define IMPS_OK 0
+#define IMPS_WARN_NOT_CONVERGED 1
+#define IMPS_ERR_BAD_ARG -1
+#define IMPS_ERR_BAD_TABLE -2
+#define IMPS_ERR_CUDA -3
+#define IMPS_ERR_NAN -4
+#define IMPS_ERR_TIMEOUT -5
+#define IMPS_ERR_NO_DEVICE -6
+#define IMPS_ERR_OOM -7
+#define IMPS_ERR_UNSUPPORTED -8
+
+#define IMPS_MEM_HOST 0
+#define IMPS_MEM_DEVICE 1
+
+#define IMPS_DIR_LEFT 0
+#define IMPS_DIR_RIGHT 1
+
+#define IMPS_PREC_FP64 0
+#define IMPS_PREC_BF16X6 1
+
+typedef struct imps_ctx imps_ctx;
+typedef struct imps_layout imps_layout;
+typedef struct imps_plan imps_plan;
+
+/* ---- library / context ------------------------------------------------------------------ */
+const char* imps_status_string(int status);
+int imps_version(void);
+int imps_ctx_create(int device, imps_ctx** out);
+int imps_ctx_destroy(imps_ctx* ctx);
+/* use an existing cudaStream_t (e.g. torch's current stream); NULL = the context's own stream */
+int imps_ctx_set_stream(imps_ctx* ctx, void* cuda_stream);
+int imps_ctx_synchronize(imps_ctx* ctx);
+
+/* ---- sector tables (replaces the std::map sector bookkeeping of BlockObj.hpp:506-600,
+ *      1360-1467 and MPSBlockMat.hpp:41-175) -------------------------------------------------- */
+int imps_layout_create(int nsym, int nblocks, const int32_t* qin, const int32_t* qout,
+                       const int32_t* rows, const int32_t* cols, const int32_t* group,
+                       imps_layout** out);
+int imps_layout_destroy(imps_layout* L);
+int64_t imps_layout_nelem(const imps_layout* L);
+int imps_layout_nblocks(const imps_layout* L);
+int imps_layout_nsym(const imps_layout* L);
+/* export the table (arrays sized nblocks*nsym for keys, nblocks otherwise; NULL skips) */
+int imps_layout_get(const imps_layout* L, int32_t* qin, int32_t* qout, int32_t* rows,
+                    int32_t* cols, int32_t* group, int64_t* off);
+/* GetMl (side 0) / GetMr (side 1) of an MPS tensor as a BlockDiagMat layout
+ * (MPSBlockMat.hpp:281-326) */
+int imps_layout_bond(const imps_layout* A, int side, imps_layout** out);
+
+/* ---- contraction plans: sector matching compiled once into grouped-GEMM tables ----------- */
+/* ApplyHA / ApplyHAvec (VUMPS_helpers.hpp:38-88).  Slots: 0 in, 1 out, 2 EHL, 3 EHR, 4 HL, 5 HR */
+int imps_plan_hac(imps_ctx* ctx, const imps_layout* AC, const imps_layout* EHL,
+                  const imps_layout* EHR, const imps_layout* HL, const imps_layout* HR, int d,
+                  imps_plan** out);
+/* ApplyHC / ApplyHCvec (VUMPS_helpers.hpp:91-133), h given as its nonzeros (row, col, value)
+ * in armadillo SpMat iteration order.  Slots: 0 in, 1 out, 2 EHL, 3 EHR, 4 AL, 5 AR; call
+ * imps_plan_prepare after binding/changing AL, AR. */
+int imps_plan_hc(imps_ctx* ctx, const imps_layout* C, const imps_layout* EHL,
+                 const imps_layout* EHR, const imps_layout* AL, const imps_layout* AR, int d,
+                 int nnz, const int32_t* hrow, const int32_t* hcol, const double* hval,
+                 imps_plan** out);
+/* ApplyTMLeft / ApplyTMRight on a unit cell (TMBlockFunctions.hpp:33-84, 155-205, 542-625).
+ * Slots: 0 in, 1 out, 2.. 2+nsites-1 A[k]. */
+int imps_plan_tm(imps_ctx* ctx, int nsites, const imps_layout* const* A, int dir,
+                 const imps_layout* in, const imps_layout* out, imps_plan** plan);
+/* ReducedOp (MPSBlockUtilities.hpp:37-74).  Slots: 0 A, 1 out (derived layout 0). */
+int imps_plan_redop(imps_ctx* ctx, const imps_layout* A, int d, int nnz, const int32_t* hrow,
+                    const int32_t* hcol, const double* hval, int dir, imps_plan** out);
+/* ApplyOpTMLeftDiag / ApplyOpTMRightDiag on the 2-site product A0*A1 (TMBlockFunctions.hpp:
+ * 797-836, MPSBlockMat.hpp:934-947).  Slots: 0 A0, 1 A1, 2 out. */
+int imps_plan_optm(imps_ctx* ctx, const imps_layout* A0, const imps_layout* A1, int d, int nnz,
+                   const int32_t* hrow, const int32_t* hcol, const double* hval, int dir,
+                   const imps_layout* out, imps_plan** plan);
+/* MPS x BlockDiagMat (side bit0 = 1: A*op(X); 0: op(X)*A; side bit1: op(X) = X^T), scaled by
+ * alpha (MPSBlockMat.hpp:1021-1043).  Slots: 0 A, 1 X, 2 out. */
+int imps_plan_mps_bd(imps_ctx* ctx, const imps_layout* A, const imps_layout* X, int side,
+                     double alpha, imps_plan** out);
+/* Tangent-space gradient of GradNormRight (VUMPS_helpers.hpp:145-153).
+ * Slots: 0 Y = H_AC(C*AR), 1 AR, 2 G (output, AR layout). */
+int imps_plan_grad_right(imps_ctx* ctx, const imps_layout* Y, const imps_layout* AR,
+                         imps_plan** out);
+int imps_plan_destroy(imps_plan* P);
+int imps_plan_derived_layout(const imps_plan* P, int which, imps_layout** out);
+int imps_plan_info(const imps_plan* P, int64_t* flops_apply, int64_t* flops_prep,
+                   int64_t* dropped, int* nslots, int* nstages);
+int imps_plan_slot_info(const imps_plan* P, int slot, int* kind, int64_t* nelem);
+/* bind a device pointer to an external slot (kept until rebound or the plan is destroyed) */
+int imps_plan_bind(imps_plan* P, int slot, double* device_ptr);
+int imps_plan_prepare(imps_plan* P);
+int imps_plan_run(imps_plan* P);
+/* export the sector-matching table of one stage: per output block its tag and term range;
+ * per term (a_slot, a_off, b_slot, b_off, k, alpha).  Pass NULL arrays to query sizes. */
+int imps_plan_table(const imps_plan* P, int prep, int stage, int64_t* n_outs, int64_t* n_terms,
+                    int32_t* out_tag, int32_t* out_t0, int32_t* out_t1, int32_t* term_aslot,
+                    int64_t* term_aoff, int32_t* term_bslot, int64_t* term_boff,
+                    int32_t* term_k, double* term_alpha);
+/* select the GEMM engine of a plan: IMPS_PREC_FP64 (DFMA) or IMPS_PREC_BF16X6 (tcgen05) */
+int imps_plan_set_precision(imps_plan* P, int prec);
+
+/* ---- reference-facing functors (the std::function<void(T*,T*)> handed to ARPACK) --------- */
+/* ApplyHAvec (VUMPS_helpers.hpp:55-88): operators bound to slots 2..5 beforehand */
+int imps_hac_apply(imps_plan* hac, const double* in, double* out, int mem);
+/* ApplyHCvec (VUMPS_helpers.hpp:114-133) */
+int imps_hc_apply(imps_plan* hc, const double* in, double* out, int mem);
+/* TMMultDiag with ApplyTMLeft/Right on the unit cell (EigsBlockFunctions.hpp:50-66) */
+int imps_tm_apply(imps_plan* tm, const double* in, double* out, int mem);
+/* InvEfun_proj (InvEBlockFunctions.hpp:12-47): out = in - T(in) + tr(in*rho_in)*rho_out */
+int imps_tm_proj_apply(imps_plan* tm, const double* in, const double* rho_in,
+                       const double* rho_out, double* out, int mem);
+
+/* ---- solvers ----------------------------------------------------------------------------- */
+/* eigs_rs(..., nev=1, "SA", tol, x0) (eigs.cpp:369-494) for a symmetric plan (H_AC or H_C):
+ * thick-restarted Lanczos with CGS2 re-orthogonalisation on the device.  x holds x0 on
+ * entry and the normalised eigenvector on exit.  ncv = 0 selects max(20, 2) capped at n. */
+int imps_eigs_rs(imps_plan* op, double* x, int mem, double tol, int ncv, int maxit,
+                 double* eval, int* n_applies);
+/* InvertE_proj (InvEBlockFunctions.hpp:201-266) on a TM plan: solves
+ *  dir l: y (1 - T + |R)(L|) = x (1 - |R)(L|),  dir r: (1 - T + |R)(L|) y = (1 - |R)(L|) x
+ * with restarted GMRES (Krylov size `krylov`, 0 = 40); y holds y0 on entry (NULL = zeros). */
+int imps_invert_e_proj(imps_plan* tm, const double* x, const double* L, const double* R,
+                       int dir, double* y, int mem, double tol, int maxit, int krylov,
+                       int* iters, double* relres);
+/* TMDominantEig (EigsBlockFunctions.hpp:91-172) for a left/right-isometric unit cell: the
+ * dominant eigenvalue is 1 and the fixed point solves (1 - T + |x0)(1|) v = x0; v is
+ * normalised to unit trace as in the reference.  x0 may be NULL (identity). */
+int imps_tm_dominant(imps_plan* tm, const double* x0, double* V, int mem, double tol,
+                     int maxit, double* eval, int* iters);
+/* GradNormRight (VUMPS_helpers.hpp:145-153): F = norm_scaled(Y N_R^T), from Y = H_AC(C*AR)
+ * already stored in the grad plan's slot 0 and AR in slot 1. */
+int imps_grad_norm_right(imps_plan* grad, double* F);
+
+/* ---- Krylov BLAS-1 (K5) on device vectors, for callers that drive their own solvers ---- */
+int imps_dot(imps_ctx* ctx, const double* x, const double* y, int64_t n, double* result);
+
+#ifdef __cplusplus
+}
+#endif
+#endif /* IMPS_GB300_H */

@@ -1,0 +1,977 @@
+"""CPU oracle (test infrastructure only): numpy restatement of IMPS_CPP_tools' hot path.
+
+Parity status: UNPINNED by the reference (no reference tests/golden vectors; the
+reference is not buildable here).  Pinned instead by dense re-evaluation, the
+reference's inline identities and the Heisenberg Bethe-ansatz energy (see tests).
+
+Data model, mirroring MPShelpers/include/Block/BlockObj.hpp and MPSBlockMat.hpp:
+  * charge keys are tuples of ints; ``sorted()`` on tuples is the lexicographic
+    ``std::vector<int>`` ``operator<`` that orders every ``std::map`` in the
+    reference (KeyTypes.hpp:19-59, ordering inherited from std::vector).
+  * BlockDiag  : dict  key -> 2-D ndarray            (BlockDiagMat, BlockObj.hpp:1360-1467)
+  * BlockMat   : dict  qin -> (qout, 2-D ndarray)    (BlockMat, BlockObj.hpp:506-600)
+  * MPS        : list over physical index s of BlockMat (MPSBlockMat.hpp:41-175)
+  * vectors    : concatenation of column-major blocks in key order, s-major for
+                 MPS (MPSBlockMat.hpp:448-465, BlockObj.hpp:767-780, 1712).
+Only U(1)^k charges are restated (all configurations use U(1) or U(1)xU(1)).
+"""
+from __future__ import annotations
+
+import math
+from functools import reduce
+
+import numpy as np
+
+# ----------------------------------------------------------------------------------------------
+# charges, I2K, dims  (KeyTypes.hpp:123-136, ItoKey.hpp:126-165, Models.cpp:13-32,216-295,642-733)
+# ----------------------------------------------------------------------------------------------
+
+
+def kadd(a, b):
+    return tuple(x + y for x, y in zip(a, b))
+
+
+def ksub(a, b):
+    return tuple(x - y for x, y in zip(a, b))
+
+
+def xxz_dQ(N, QN):
+    """XXZModel::GetdQ (Models.cpp:216-240), spin-1/2 case."""
+    m = QN[0]
+    if abs(m) >= N:
+        raise ValueError("|m| < N!")
+    div = math.gcd(N - m, N + m)
+    return [(2 * N // div, -((N + m) // div))]
+
+
+def xxz_i2k(N, QN, d=2):
+    """XXZModel::GetI2K (Models.cpp:262-295): I2K[k] = dQ.second + s*dQ.first, s = d-1 .. 0."""
+    dQ = xxz_dQ(N, QN)
+    return [(dQ[0][1] + s * dQ[0][0],) for s in range(d - 1, -1, -1)]
+
+
+def fhub_dQ(N, QN):
+    """FermiHubbardModel::GetdQ, (N,M) representation (Models.cpp:642-660)."""
+    n, m = QN
+    if n + m <= 0 or n + m >= 2 * N or n - m <= 0 or n - m >= 2 * N:
+        raise ValueError("QN out of range")
+    divn = math.gcd(math.gcd(N - n, 2 * N - n), n)
+    divm = math.gcd(math.gcd(N - m, N + m), m)
+    return [(N // divn, -(n // divn)), (N // divm, -((N + m) // divm))]
+
+
+def fhub_i2k(N, QN):
+    """FermiHubbardModel::GetI2K, (N,M) representation (Models.cpp:701-718)."""
+    (a1, a0), (b1, b0) = fhub_dQ(N, QN)
+    return [(a0, b0 + b1), (a0 + a1, b0), (a0 + a1, b0 + 2 * b1), (a0 + 2 * a1, b0 + b1)]
+
+
+def _path_iter(N, key, I2K, zero):
+    if N == 1:
+        for j, k in enumerate(I2K):
+            if kadd(key, k) == zero:
+                return True, [j]
+        return False, []
+    for j, k in enumerate(I2K):
+        ok, p = _path_iter(N - 1, kadd(key, k), I2K, zero)
+        if ok:
+            return True, p + [j]
+    return False, []
+
+
+def validpath(N, I2K):
+    """ItoKey.hpp:126-165 (starts at I2K.front(), zero key = I2K.front())."""
+    ok, p = _path_iter(N, I2K[0], I2K, I2K[0])
+    if not ok:
+        raise ValueError("validpath: no valid path found for current ItoKey")
+    return p
+
+
+def make_dims(dmap0, N, I2K):
+    """ModelBase::MakeDims (Models.cpp:13-32): dims of bond k, k=0..N-1."""
+    path = validpath(N, I2K)
+    out, cur = [], dict(dmap0)
+    for k in range(N):
+        out.append(dict(cur))
+        sh = I2K[path[N - k - 1]]
+        cur = {kadd(q, sh): m for q, m in cur.items()}
+    return out
+
+
+# ----------------------------------------------------------------------------------------------
+# two-site Hamiltonians (Models.cpp:57-93 XYZ/XXZ, :543-572 FHUB)
+# ----------------------------------------------------------------------------------------------
+
+
+def xxz_h(J=1.0, Delta=1.0, hz=0.0):
+    """ham = -Jx sx.sx + Jy syi.syi - Jz sz.sz - hz/2 (sz.1 + 1.sz), with Jx=Jy=J, Jz=Delta."""
+    sx = np.array([[0, 0.5], [0.5, 0]])
+    syi = np.array([[0, -0.5], [0.5, 0]])
+    sz = np.diag([0.5, -0.5])
+    I = np.eye(2)
+    return (-J * np.kron(sx, sx) + J * np.kron(syi, syi) - Delta * np.kron(sz, sz)
+            - 0.5 * hz * (np.kron(sz, I) + np.kron(I, sz)))
+
+
+def fhub_h(t=1.0, U=4.0, V=0.0, mu=0.0, hz=0.0):
+    cup = np.zeros((4, 4)); cup[0, 2] = 1; cup[1, 3] = 1
+    cdo = np.zeros((4, 4)); cdo[0, 1] = 1; cdo[2, 3] = -1
+    nup = np.diag([0, 0, 1.0, 1.0]); ndo = np.diag([0, 1.0, 0, 1.0])
+    I = np.eye(4); F = np.diag([1.0, -1, -1, 1])
+    nup2 = nup - 0.5 * I; ndo2 = ndo - 0.5 * I
+    nund = nup2 @ ndo2; nupnd = nup + ndo; nupnd2 = nup2 + ndo2; sz = 0.5 * (nup - ndo)
+    return (-t * (np.kron(cup.T @ F, cup) - np.kron(cup @ F, cup.T) + np.kron(cdo.T @ F, cdo)
+                  - np.kron(cdo @ F, cdo.T))
+            + 0.5 * U * (np.kron(nund, I) + np.kron(I, nund)) + V * np.kron(nupnd2, nupnd2)
+            - 0.5 * mu * (np.kron(nupnd, I) + np.kron(I, nupnd))
+            - 0.5 * hz * (np.kron(sz, I) + np.kron(I, sz)))
+
+
+def sparse_nnz(h):
+    """Nonzeros of an armadillo SpMat in its iteration order (column-major, rows ascending)."""
+    out = []
+    for c in range(h.shape[1]):
+        for r in range(h.shape[0]):
+            if h[r, c] != 0.0:
+                out.append((r, c, float(h[r, c])))
+    return out
+
+
+def num2ditvec(x, d):
+    """helpers.cpp:3-17 for N=2: (left site index, right site index)."""
+    return x // d, x % d
+
+
+# ----------------------------------------------------------------------------------------------
+# containers and layout (BlockObj.hpp, MPSBlockMat.hpp)
+# ----------------------------------------------------------------------------------------------
+
+
+def mps_rand(I2K, dl, dr, rng, dtype=np.float64):
+    """MPSBlockMat(I2K, ml, mr, fill::randn) (MPSBlockMat.hpp:221-236), blocks filled column-major."""
+    A = []
+    for sh in I2K:
+        bm = {}
+        for ql in sorted(dl):
+            qr = kadd(ql, sh)
+            if qr in dr:
+                ml, mr = dl[ql], dr[qr]
+                bm[ql] = (qr, rng.standard_normal(ml * mr).reshape(mr, ml).T.astype(dtype).copy())
+        A.append(bm)
+    return A
+
+
+def mps_sizes(A):
+    """MPSBlockMat::GetSizesVector (MPSBlockMat.hpp:336-347)."""
+    return [[(q, A[s][q][0], A[s][q][1].shape[0], A[s][q][1].shape[1]) for q in sorted(A[s])]
+            for s in range(len(A))]
+
+
+def mps_vec(A):
+    parts = [A[s][q][1].reshape(-1, order="F") for s in range(len(A)) for q in sorted(A[s])]
+    return np.concatenate(parts) if parts else np.zeros(0)
+
+
+def mps_from_vec(v, sizes):
+    A, pos = [], 0
+    for blocks in sizes:
+        bm = {}
+        for (qi, qo, ml, mr) in blocks:
+            bm[qi] = (qo, np.array(v[pos:pos + ml * mr]).reshape(mr, ml).T.copy())
+            pos += ml * mr
+        A.append(bm)
+    return A
+
+
+def mps_nelem(A):
+    return sum(b[1].size for bm in A for b in bm.values())
+
+
+def bd_sizes(X):
+    return [(q, X[q].shape[0]) for q in sorted(X)]
+
+
+def bd_vec(X):
+    parts = [X[q].reshape(-1, order="F") for q in sorted(X)]
+    return np.concatenate(parts) if parts else np.zeros(0)
+
+
+def bd_from_vec(v, sizes):
+    X, pos = {}, 0
+    for (q, m) in sizes:
+        X[q] = np.array(v[pos:pos + m * m]).reshape(m, m).T.copy()
+        pos += m * m
+    return X
+
+
+def bm_vec(X):
+    parts = [X[q][1].reshape(-1, order="F") for q in sorted(X)]
+    return np.concatenate(parts) if parts else np.zeros(0)
+
+
+def bm_from_vec(v, sizes):
+    X, pos = {}, 0
+    for (qi, qo, ml, mr) in sizes:
+        X[qi] = (qo, np.array(v[pos:pos + ml * mr]).reshape(mr, ml).T.copy())
+        pos += ml * mr
+    return X
+
+
+def bm_sizes(X):
+    return [(q, X[q][0], X[q][1].shape[0], X[q][1].shape[1]) for q in sorted(X)]
+
+
+def bd_eye(dims):
+    return {q: np.eye(m) for q, m in dims.items()}
+
+
+def bd_trace(X):
+    return sum(np.trace(X[q]) for q in sorted(X))
+
+
+def bm_t(X):
+    """BlockMat::t(): key Qout -> (Qin, M^T)."""
+    return {qo: (qi, M.T.copy()) for qi, (qo, M) in X.items()}
+
+
+def bm_mul(L, R):
+    """operator*(BlockMat, BlockMat) (BlockObj.hpp:2557-2568)."""
+    out = {}
+    for qi in sorted(L):
+        qo, M = L[qi]
+        if qo in R:
+            out[qi] = (R[qo][0], M @ R[qo][1])
+    return out
+
+
+def bm_mul_bd(L, D):
+    """operator*(BlockMat, BlockDiagMat) (BlockObj.hpp:2570-2589)."""
+    return {qi: (qo, M @ D[qo]) for qi, (qo, M) in L.items() if qo in D}
+
+
+def bd_mul_bm(D, R):
+    """operator*(BlockDiagMat, BlockMat) (BlockObj.hpp:2591-2610)."""
+    return {qi: (qo, D[qi] @ M) for qi, (qo, M) in R.items() if qi in D}
+
+
+def bd_mul(A, B):
+    return {q: A[q] @ B[q] for q in A if q in B}
+
+
+def bm_scale(X, a):
+    return {q: (qo, a * M) for q, (qo, M) in X.items()}
+
+
+def bm_iadd(X, Y):
+    """BlockMat::operator+= (BlockObj.hpp:1044-1063): adds, inserting missing sectors."""
+    for qi in sorted(Y):
+        qo, M = Y[qi]
+        if qi in X:
+            assert X[qi][0] == qo
+            X[qi] = (qo, X[qi][1] + M)
+        else:
+            X[qi] = (qo, M.copy())
+    return X
+
+
+def bd_iadd(X, Y):
+    for q, M in Y.items():
+        X[q] = X[q] + M if q in X else M.copy()
+    return X
+
+
+def bd_add(X, Y):
+    return bd_iadd({q: M.copy() for q, M in X.items()}, Y)
+
+
+def bd_t(X):
+    return {q: M.T.copy() for q, M in X.items()}
+
+
+def mps_mul_bd(A, D):
+    return [bm_mul_bd(a, D) for a in A]
+
+
+def bd_mul_mps(D, A):
+    return [bd_mul_bm(D, a) for a in A]
+
+
+def mps_mul_mps(A, B):
+    """2-site product (MPSBlockMat.hpp:934-947): out[i*d+j] = A[i]*B[j]."""
+    return [bm_mul(a, b) for a in A for b in B]
+
+
+def mps_sub(A, B):
+    out = []
+    for a, b in zip(A, B):
+        c = {q: (qo, M.copy()) for q, (qo, M) in a.items()}
+        bm_iadd(c, bm_scale(b, -1.0))
+        out.append(c)
+    return out
+
+
+def mps_norm_inf(A):
+    return max((np.abs(M).max() for bm in A for (_, M) in bm.values() if M.size), default=0.0)
+
+
+# ----------------------------------------------------------------------------------------------
+# H_AC / H_C (VUMPS/VUMPS_helpers.hpp:38-133)
+# ----------------------------------------------------------------------------------------------
+
+
+def _mps_add_into_existing(out, contrib):
+    """out[s] += contrib[s] where out is a view on a fixed buffer: sectors absent from out are
+    lost (the reference inserts them into the map of non-owning views, outside the buffer)."""
+    for s, bm in enumerate(contrib):
+        for qi, (qo, M) in bm.items():
+            if qi in out[s]:
+                assert out[s][qi][0] == qo
+                out[s][qi][1][...] += M
+
+
+def ApplyHA(inp, EHL, EHR, HL, HR):
+    """ApplyHA (VUMPS_helpers.hpp:38-53): out = EHL*in + in*EHR + sum_ij HL[i][j]*in[j] + in[j]*HR[i][j]."""
+    d = len(inp)
+    out = [{q: (qo, np.zeros_like(M)) for q, (qo, M) in bm.items()} for bm in inp]
+    t1 = bd_mul_mps(EHL, inp)
+    t2 = mps_mul_bd(inp, EHR)
+    _mps_add_into_existing(out, [bm_iadd(a, b) for a, b in zip(t1, t2)])
+    for i in range(d):
+        for j in range(d):
+            c = bm_iadd(bm_mul(HL[i][j], inp[j]), bm_mul(inp[j], HR[i][j]))
+            contrib = [dict() for _ in range(d)]
+            contrib[i] = c
+            _mps_add_into_existing(out, contrib)
+    return out
+
+
+def ApplyHAvec(vin, Adims, EHL, EHR, HL, HR):
+    """ApplyHAvec (VUMPS_helpers.hpp:55-88)."""
+    return mps_vec(ApplyHA(mps_from_vec(vin, Adims), EHL, EHR, HL, HR))
+
+
+def ApplyHC(inp, EHL, EHR, hnnz, d, AL, AR):
+    """ApplyHC (VUMPS_helpers.hpp:91-111), literal chained form per nonzero of h."""
+    out = {q: np.zeros_like(M) for q, M in inp.items()}
+    base = bd_add(bd_mul(EHL, inp), bd_mul(inp, EHR))
+    for q in out:
+        if q in base:
+            out[q] += base[q]
+    inp_bm = {q: (q, M) for q, M in inp.items()}
+    for (r, c, h) in hnnz:
+        i0, i1 = num2ditvec(r, d)
+        j0, j1 = num2ditvec(c, d)
+        X = bm_mul(bm_scale(bm_t(AL[i0]), h), AL[j0])
+        X = bm_mul(X, inp_bm)
+        X = bm_mul(X, AR[j1])
+        X = bm_mul(X, bm_t(AR[i1]))
+        for qi, (qo, M) in X.items():
+            assert qi == qo
+            if qi in out:
+                out[qi] += M
+    return out
+
+
+def ApplyHCvec(vin, Cdims, EHL, EHR, hnnz, d, AL, AR):
+    return bd_vec(ApplyHC(bd_from_vec(vin, Cdims), EHL, EHR, hnnz, d, AL, AR))
+
+
+# ----------------------------------------------------------------------------------------------
+# transfer matrices (MPShelpers/include/Block/TMBlockFunctions.hpp)
+# ----------------------------------------------------------------------------------------------
+
+
+def ApplyTMLeft(A, X):
+    """TMBlockFunctions.hpp:33-56: out(Qout) += A_s^T (X(Qin) A_s)."""
+    out = {}
+    for bm in A:
+        for qi in sorted(bm):
+            qo, M = bm[qi]
+            if qi in X:
+                c = M.T @ (X[qi] @ M)
+                out[qo] = out[qo] + c if qo in out else c
+    return out
+
+
+def ApplyTMRight(A, X):
+    """TMBlockFunctions.hpp:155-177: out(Qin) += (A_s X(Qout)) A_s^T."""
+    out = {}
+    for bm in A:
+        for qi in sorted(bm):
+            qo, M = bm[qi]
+            if qo in X:
+                c = (M @ X[qo]) @ M.T
+                out[qi] = out[qi] + c if qi in out else c
+    return out
+
+
+def ApplyTMLeftUC(Avec, X):
+    """TMBlockFunctions.hpp:557-563 (sites in order)."""
+    for A in Avec:
+        X = ApplyTMLeft(A, X)
+    return X
+
+
+def ApplyTMRightUC(Avec, X):
+    """TMBlockFunctions.hpp:600-606 (sites in reverse order)."""
+    for A in reversed(Avec):
+        X = ApplyTMRight(A, X)
+    return X
+
+
+def ApplyTMmixedLeftDiag(A, B):
+    """TMBlockFunctions.hpp:259-289: out(Qout(B_s)) += B_s^T A_s, B found by Qin(A)."""
+    out = {}
+    for s in range(len(A)):
+        if not A[s] or not B[s]:
+            continue
+        for qi in sorted(A[s]):
+            qa, MA = A[s][qi]
+            if qi in B[s]:
+                qb, MB = B[s][qi]
+                assert qb == qa
+                c = MB.T @ MA
+                out[qb] = out[qb] + c if qb in out else c
+    return out
+
+
+def ApplyTMmixedRightDiag(A, B):
+    """TMBlockFunctions.hpp:401-434: out(Qin(A_s)) += A_s B_s^T, B found by Qin(A)."""
+    out = {}
+    for s in range(len(A)):
+        if not A[s] or not B[s]:
+            continue
+        for qi in sorted(A[s]):
+            qa, MA = A[s][qi]
+            if qi in B[s]:
+                qb, MB = B[s][qi]
+                assert qb == qa
+                c = MA @ MB.T
+                out[qi] = out[qi] + c if qi in out else c
+    return out
+
+
+def bm_dK(X):
+    qi = next(iter(sorted(X)))
+    return ksub(X[qi][0], qi)
+
+
+def ApplyTMmixedRight(A, B):
+    """TMBlockFunctions.hpp:445-473 (general BlockMat result): out(Qin(A_s) -> Qin(B_s)) += A_s B_s^T,
+    B found by Qout(A_s) - dK(B_s)."""
+    out = {}
+    for s in range(len(A)):
+        if not A[s] or not B[s]:
+            continue
+        dKB = bm_dK(B[s])
+        for qi in sorted(A[s]):
+            qa, MA = A[s][qi]
+            qbi = ksub(qa, dKB)
+            if qbi in B[s]:
+                _, MB = B[s][qbi]
+                c = MA @ MB.T
+                if qi in out and out[qi][0] == qbi:
+                    out[qi] = (qbi, out[qi][1] + c)
+                else:
+                    out[qi] = (qbi, c)
+    return out
+
+
+def ApplyTMmixedLeft(A, B):
+    """TMBlockFunctions.hpp:306-330 (general BlockMat result): out(Qout(B_s) -> Qout(A_s)) += B_s^T A_s."""
+    out = {}
+    for s in range(len(A)):
+        if not A[s] or not B[s]:
+            continue
+        for qi in sorted(A[s]):
+            qa, MA = A[s][qi]
+            if qi in B[s]:
+                qb, MB = B[s][qi]
+                c = MB.T @ MA
+                if qb in out and out[qb][0] == qa:
+                    out[qb] = (qa, out[qb][1] + c)
+                else:
+                    out[qb] = (qa, c)
+    return out
+
+
+def ApplyOperator(A, hnnz):
+    """MPSBlockUtilities.hpp:17-34: out[ii] += h * in[jj]."""
+    out = [dict() for _ in A]
+    for (r, c, h) in hnnz:
+        bm_iadd(out[r], bm_scale(A[c], h))
+    return out
+
+
+def ApplyOpTMLeftDiag(hnnz, A):
+    """TMBlockFunctions.hpp:797-802."""
+    return ApplyTMmixedLeftDiag(ApplyOperator(A, hnnz), A)
+
+
+def ApplyOpTMRightDiag(hnnz, A):
+    """TMBlockFunctions.hpp:831-836."""
+    return ApplyTMmixedRightDiag(ApplyOperator(A, hnnz), A)
+
+
+def ReducedOp(hnnz, A, d, direction):
+    """MPSBlockUtilities.hpp:37-74."""
+    Ored = [[dict() for _ in range(d)] for _ in range(d)]
+    for (r, c, h) in hnnz:
+        i0, i1 = num2ditvec(r, d)
+        j0, j1 = num2ditvec(c, d)
+        if direction == "r":
+            term = bm_scale(bm_mul(A[j1], bm_t(A[i1])), h)
+            bm_iadd(Ored[i0][j0], term)
+        else:
+            term = bm_scale(bm_mul(bm_t(A[i0]), A[j0]), h)
+            bm_iadd(Ored[i1][j1], term)
+    return Ored
+
+
+def GetHL(ALvec, hnnz):
+    """VUMPS_helpers.hpp:3-18."""
+    HL = ApplyOpTMLeftDiag(hnnz, mps_mul_mps(ALvec[-1], ALvec[0]))
+    for k in range(1, len(ALvec)):
+        HL = bd_add(ApplyTMLeft(ALvec[k], HL), ApplyOpTMLeftDiag(hnnz, mps_mul_mps(ALvec[k - 1], ALvec[k])))
+    return HL
+
+
+def GetHR(ARvec, hnnz):
+    """VUMPS_helpers.hpp:20-36."""
+    N = len(ARvec)
+    HR = ApplyOpTMRightDiag(hnnz, mps_mul_mps(ARvec[-1], ARvec[0]))
+    for k in range(N - 2, -1, -1):
+        HR = bd_add(ApplyTMRight(ARvec[k], HR), ApplyOpTMRightDiag(hnnz, mps_mul_mps(ARvec[k], ARvec[k + 1])))
+    return HR
+
+
+# ----------------------------------------------------------------------------------------------
+# GMRES (IterativeSolvers.hpp:21-150) and environment solves (InvEBlockFunctions.hpp)
+# ----------------------------------------------------------------------------------------------
+
+
+def gmres(Afun, b, x0, tol, maxit, krylovdim=0):
+    """Unrestarted GMRES exactly as IterativeSolvers.hpp:21-150 (MGS, Givens, |r| < tol*|b|).
+    Returns (x, flag)."""
+    dim = b.size
+    cplx = np.iscomplexobj(b) or np.iscomplexobj(x0)
+    T = np.complex128 if cplx else np.float64
+    if maxit > dim:
+        maxit = dim
+    if krylovdim == 0:
+        krylovdim = min(dim, maxit)
+    krylovdim = min(krylovdim, dim)
+    flag = -1
+    r0 = b - Afun(x0)
+    x = x0.astype(T).copy()
+    bnorm = np.linalg.norm(b)
+    rnorm = np.linalg.norm(r0)
+    thresh = 2e-16
+    V = np.zeros((dim, krylovdim + 1), T)
+    H = np.zeros((krylovdim + 1, krylovdim + 1), T)
+    c = np.zeros(krylovdim + 1, T)
+    s = np.zeros(krylovdim + 1, T)
+    gamma = np.zeros(krylovdim + 1, T)
+    gamma[0] = rnorm
+    V[:, 0] = r0 / rnorm
+    kdim = 0
+    for j in range(krylovdim):
+        w = Afun(V[:, j]).astype(T)
+        for i in range(j + 1):
+            H[i, j] = np.vdot(V[:, i], w)
+            w = w - H[i, j] * V[:, i]
+        H[j + 1, j] = np.linalg.norm(w)
+        for i in range(j):
+            h1, h2 = H[i, j], H[i + 1, j]
+            H[i, j] = c[i] * h1 + s[i] * h2
+            H[i + 1, j] = -np.conj(s[i]) * h1 + c[i] * h2
+        beta = np.linalg.norm(H[j:j + 2, j])
+        if abs(beta) < thresh:
+            flag = -2
+            break
+        V[:, j + 1] = w / H[j + 1, j]
+        habs = abs(H[j, j])
+        phase = H[j, j] / habs
+        s[j] = phase * np.conj(H[j + 1, j]) / beta
+        c[j] = habs / beta
+        H[j, j] = phase * beta
+        H[j + 1, j] = 0
+        gamma[j + 1] = -np.conj(s[j]) * gamma[j]
+        gamma[j] *= c[j]
+        kdim += 1
+        rnorm = abs(gamma[j + 1])
+        if rnorm < tol * bnorm:
+            flag = kdim
+            break
+    Hk = H[:kdim, :kdim]
+    if kdim:
+        from scipy.linalg import solve_triangular
+        alpha = solve_triangular(Hk, gamma[:kdim], lower=False)
+        x = x + V[:, :kdim] @ alpha
+    return x, flag
+
+
+def InvEfun_proj(invec, TMfun, rho_inside, rho_outside, dims):
+    """InvEBlockFunctions.hpp:12-47: y = x - TM(x) + trace(x*rho_in) * rho_out."""
+    X = bd_from_vec(invec, dims)
+    tr = sum(np.trace(X[q] @ rho_inside[q]) for q, _ in dims)
+    Tx = TMfun(X)
+    Y = {q: X[q] + tr * rho_outside[q] - Tx[q] for q, _ in dims}
+    return bd_vec(Y)
+
+
+def InvertE_proj(MPSarr, x, L, R, direction, tol=1e-14, maxit=0, y0=None, rng=None):
+    """InvEBlockFunctions.hpp:201-266 for BlockDiagMat x on a unit cell."""
+    dims = bd_sizes(x)
+    m_tot = sum(m * m for _, m in dims)
+    if maxit == 0:
+        maxit = m_tot
+    if y0 is None or bd_sizes(y0) != dims:
+        rng = rng or np.random.default_rng(0)
+        y0 = {q: rng.standard_normal((m, m)) for q, m in dims}
+    xpv = bd_vec(x)
+    if direction == "l":
+        xpv = xpv - bd_trace(bd_mul(x, R)) * bd_vec(L)
+        Afun = lambda v: InvEfun_proj(v, lambda X: ApplyTMLeftUC(MPSarr, X), R, L, dims)
+    else:
+        xpv = xpv - bd_trace(bd_mul(L, x)) * bd_vec(R)
+        Afun = lambda v: InvEfun_proj(v, lambda X: ApplyTMRightUC(MPSarr, X), L, R, dims)
+    y, flag = gmres(Afun, xpv, bd_vec(y0), tol, maxit)
+    return bd_from_vec(y, dims), flag
+
+
+# ----------------------------------------------------------------------------------------------
+# eigensolvers: ARPACK as shipped in scipy stands in for eigs.cpp (eigs_rs / eigs_n)
+# ----------------------------------------------------------------------------------------------
+
+
+def eigs_rs(fun, N, tol, x0, nev=1, which="SA"):
+    """eigs.cpp:369-494: dsaupd/dseupd with ncv = min(max(20, 2 nev), N), maxit = N."""
+    from scipy.sparse.linalg import LinearOperator, eigsh
+    ncv = min(max(20, 2 * nev), N)
+    op = LinearOperator((N, N), matvec=lambda v: fun(np.asarray(v).ravel()), dtype=np.float64)
+    vals, vecs = eigsh(op, k=nev, which=which, tol=tol, v0=x0, ncv=ncv, maxiter=N)
+    order = np.argsort(vals)
+    return vals[order], vecs[:, order]
+
+
+def TMDominantEig(MPSarr, dims, direction, tol=1e-14, x0=None):
+    """EigsBlockFunctions.hpp:91-172 (eigs_n "LR", nev=1), normalised by its trace."""
+    from scipy.sparse.linalg import LinearOperator, eigs
+    sizes = sorted(dims.items())
+    D_tot = sum(m * m for _, m in sizes)
+    if direction == "l":
+        f = lambda v: bd_vec(ApplyTMLeftUC(MPSarr, bd_from_vec(v, sizes)))
+    else:
+        f = lambda v: bd_vec(ApplyTMRightUC(MPSarr, bd_from_vec(v, sizes)))
+    op = LinearOperator((D_tot, D_tot), matvec=lambda v: f(np.real(np.asarray(v).ravel())), dtype=np.float64)
+    v0 = bd_vec(x0) if x0 is not None else None
+    vals, vecs = eigs(op, k=1, which="LR", tol=tol, v0=v0, ncv=min(20, D_tot), maxiter=D_tot)
+    V = bd_from_vec(np.real(vecs[:, 0]), sizes)
+    tr = bd_trace(V)
+    V = {q: M / tr for q, M in V.items()}
+    return float(np.real(vals[0])), V
+
+
+# ----------------------------------------------------------------------------------------------
+# per-sector decompositions (helpers.hpp:181-195, MPSBlockUtilities.hpp:78-340, BlockObj.hpp:2422-2541)
+# ----------------------------------------------------------------------------------------------
+
+
+def qr_pos(X):
+    """qr_econ + sign fix so that diag(R) >= 0 (helpers.hpp:181-195)."""
+    Q, R = np.linalg.qr(X, mode="reduced")
+    sg = np.where(np.diag(R) < 0, -1.0, 1.0)
+    return Q * sg[None, :], R * sg[:, None]
+
+
+def GetDenseMat(A, direction):
+    """MPSBlockMat::GetDenseMat (MPSBlockMat.hpp:468-526) + GetSingleSecData (:636-719).
+    Returns {sector: (dense, [(s, other_key, start, size)], ml_tot, mr_tot)}."""
+    d = len(A)
+    secs = {}
+    if direction == "l":
+        for s in range(d):
+            for qi in sorted(A[s]):
+                qo, M = A[s][qi]
+                secs.setdefault(qo, {"mr": M.shape[1], "parts": {}})["parts"][s] = (qi, M)
+        out = {}
+        for qo in sorted(secs):
+            parts = secs[qo]["parts"]
+            rows, spans, pos = [], [], 0
+            for s in sorted(parts):
+                qi, M = parts[s]
+                rows.append(M)
+                spans.append((s, qi, pos, M.shape[0]))
+                pos += M.shape[0]
+            out[qo] = (np.vstack(rows), spans, pos, secs[qo]["mr"])
+        return out
+    for s in range(d):
+        for qi in sorted(A[s]):
+            qo, M = A[s][qi]
+            secs.setdefault(qi, {"ml": M.shape[0], "parts": {}})["parts"][s] = (qo, M)
+    out = {}
+    for qi in sorted(secs):
+        parts = secs[qi]["parts"]
+        cols, spans, pos = [], [], 0
+        for s in sorted(parts):
+            qo, M = parts[s]
+            cols.append(M)
+            spans.append((s, qo, pos, M.shape[1]))
+            pos += M.shape[1]
+        out[qi] = (np.hstack(cols), spans, secs[qi]["ml"], pos)
+    return out
+
+
+def qr_mps(A, direction):
+    """qr(R, MPS, dir) (MPSBlockUtilities.hpp:181-244): returns (Q MPS, R BlockDiag)."""
+    d = len(A)
+    Q = [dict() for _ in range(d)]
+    R = {}
+    for q, (M, spans, _, _) in GetDenseMat(A, direction).items():
+        if direction == "l":
+            Qm, Rm = qr_pos(M)
+            R[q] = Rm
+            for (s, qo, st, sz) in spans:
+                Q[s][qo] = (q, Qm[st:st + sz, :].copy())
+        else:
+            Qm, Rm = qr_pos(M.T)
+            R[q] = Rm.T.copy()
+            for (s, qo, st, sz) in spans:
+                Q[s][q] = (qo, Qm[st:st + sz, :].T.copy())
+    return Q, R
+
+
+def qr_bd(X, direction):
+    """qr(R, BlockDiagMat, dir) (BlockObj.hpp:2422-2459): returns (Q, R)."""
+    Q, R = {}, {}
+    for q in sorted(X):
+        if direction == "l":
+            Q[q], R[q] = qr_pos(X[q])
+        else:
+            Qt, Rt = qr_pos(X[q].T)
+            Q[q], R[q] = Qt.T.copy(), Rt.T.copy()
+    return Q, R
+
+
+def svd_mps(A, direction):
+    """svd(S, DiagIso, MPS, dir) (MPSBlockUtilities.hpp:78-153): returns (MPSIso, S, DiagIso)."""
+    d = len(A)
+    Iso = [dict() for _ in range(d)]
+    S, DI = {}, {}
+    for q, (M, spans, _, _) in GetDenseMat(A, direction).items():
+        U, sv, Vt = np.linalg.svd(M, full_matrices=False)
+        S[q] = sv
+        if direction == "l":
+            DI[q] = Vt.copy()
+            for (s, qo, st, sz) in spans:
+                Iso[s][qo] = (q, U[st:st + sz, :].copy())
+        else:
+            DI[q] = U.copy()
+            for (s, qo, st, sz) in spans:
+                Iso[s][q] = (qo, Vt[:, st:st + sz].copy())
+    return Iso, S, DI
+
+
+def svd_bd(X):
+    return {q: np.linalg.svd(X[q], compute_uv=False) for q in sorted(X)}
+
+
+def Nullspace(A, direction):
+    """MPSBlockUtilities.hpp:247-340 (sectors without a null space are omitted)."""
+    from scipy.linalg import null_space
+    d = len(A)
+    NS = [dict() for _ in range(d)]
+    for q, (M, spans, ml_tot, mr_tot) in GetDenseMat(A, direction).items():
+        if direction == "l":
+            if ml_tot > mr_tot:
+                B = null_space(M.T)
+                for (s, qo, st, sz) in spans:
+                    NS[s][qo] = (q, B[st:st + sz, :].copy())
+        else:
+            if mr_tot > ml_tot:
+                B = null_space(M)
+                for (s, qo, st, sz) in spans:
+                    NS[s][q] = (qo, B[st:st + sz, :].T.copy())
+    return NS
+
+
+def norm_scaled_bm(X):
+    """helpers.hpp:146 norm(x)/sqrt(x.size()) on a BlockMat (Frobenius over all blocks)."""
+    n = sum(M.size for (_, M) in X.values())
+    if n == 0:
+        return 0.0
+    return math.sqrt(sum(float(np.sum(np.abs(M) ** 2)) for (_, M) in X.values())) / math.sqrt(n)
+
+
+def GradNormRight(AR, C, HAfun):
+    """VUMPS_helpers.hpp:145-153."""
+    return norm_scaled_bm(ApplyTMmixedRight(HAfun(bd_mul_mps(C, AR)), Nullspace(AR, "r")))
+
+
+def GradNormLeft(AL, C, HAfun):
+    """VUMPS_helpers.hpp:135-143."""
+    return norm_scaled_bm(ApplyTMmixedLeft(HAfun(mps_mul_bd(AL, C)), Nullspace(AL, "l")))
+
+
+# ----------------------------------------------------------------------------------------------
+# state preparation and observables (MPSBlockUtilities.hpp:1017-1169)
+# ----------------------------------------------------------------------------------------------
+
+
+def randMPS_LR(N, I2K, dimvec, rng):
+    """MPSBlockUtilities.hpp:1093-1135: returns (ALvec, ARvec, Cvec)."""
+    ALvec = []
+    for n in range(1, N):
+        Q, _ = qr_mps(mps_rand(I2K, dimvec[n - 1], dimvec[n], rng), "l")
+        ALvec.append(Q)
+    Q, _ = qr_mps(mps_rand(I2K, dimvec[-1], dimvec[0], rng), "l")
+    ALvec.append(Q)
+    _, R = TMDominantEig(ALvec, dimvec[0], "r", tol=1e-14)
+    C = {}
+    for q in sorted(R):
+        U, sv, _ = np.linalg.svd(R[q])
+        X = U * np.sqrt(sv)[None, :]
+        Qt, Rt = qr_pos(X.T)
+        C[q] = Rt.T.copy()
+    Cvec, ARvec = [], []
+    Ctmp = C
+    for A in reversed(ALvec):
+        Cvec.insert(0, Ctmp)
+        Qr, Rr = qr_mps(mps_mul_bd(A, Ctmp), "r")
+        ARvec.insert(0, Qr)
+        Ctmp = Rr
+    return ALvec, ARvec, Cvec
+
+
+def shift(arr, k):
+    """MPSBlockUtilities.hpp:1154-1169 (shift(arr,-1) rotates left by one)."""
+    k %= len(arr)
+    return arr[-k:] + arr[:-k] if k else list(arr)
+
+
+def energy_right(hnnz, ARvec, Lvec):
+    """MeasureObservables(H, AR, L) (MPSBlockUtilities.hpp:1017-1073, dir = r):
+    E(n) = tr(L[n-1] * ApplyOpTMRight(H, AR[n] AR[n+1]))."""
+    N = len(ARvec)
+    E = []
+    for n in range(N):
+        AA = mps_mul_mps(ARvec[n], ARvec[(n + 1) % N])
+        X = ApplyOpTMRightDiag(hnnz, AA)
+        Lm = Lvec[(n - 1) % N]
+        E.append(sum(np.trace(Lm[q] @ X[q]) for q in X if q in Lm))
+    return np.array(E)
+
+
+# ----------------------------------------------------------------------------------------------
+# VUMPS driver (VUMPS/VUMPS_main.cpp:97-354), bond expansion disabled
+# ----------------------------------------------------------------------------------------------
+
+
+class VUMPS:
+    """Restatement of one VUMPS_main run with ExpandFromH disabled (mmax = D)."""
+
+    def __init__(self, h, d, I2K, dmap0, N=2, seed=1, InvETol=5e-15, InvEfac=2.0, fixed_tol=None,
+                 trueLR=True, svdthresh=5e-7):
+        self.hnnz = sparse_nnz(h)
+        self.d, self.N, self.I2K = d, N, I2K
+        self.InvETol, self.InvEfac, self.fixed_tol, self.trueLR = InvETol, InvEfac, fixed_tol, trueLR
+        self.svdthresh = svdthresh
+        self.rng = np.random.default_rng(seed)
+        dimvec = make_dims(dmap0, N, I2K)
+        AL, AR, C = randMPS_LR(N, I2K, dimvec, self.rng)
+        L = [bd_mul(bd_t(c), c) for c in C]
+        R = [bd_mul(c, bd_t(c)) for c in C]
+        AR = shift(AR, -1)
+        L = shift(L, -1)
+        self.AL, self.AR, self.C, self.L = AL, AR, C, L
+        hn = self.hnnz
+        self.HL = ReducedOp(hn, AL[-1], d, "l")
+        self.HR = ReducedOp(hn, AR[0], d, "r")
+        Rb = R[-1]
+        self.EHL, _ = InvertE_proj(AL, GetHL(AL, hn), bd_eye({q: m.shape[1] for q, m in C[-1].items()}), Rb, "l",
+                                   InvETol, rng=self.rng)
+        Lb = L[-1]
+        self.EHR, _ = InvertE_proj(AR, GetHR(AR, hn), Lb, bd_eye({q: m.shape[0] for q, m in C[0].items()}), "r",
+                                   InvETol, rng=self.rng)
+        self.EHL1 = bd_add(ApplyTMLeft(AL[0], self.EHL), ApplyOpTMLeftDiag(hn, mps_mul_mps(AL[-1], AL[0])))
+        self.EHR1 = bd_add(ApplyTMRight(AR[-1], self.EHR), ApplyOpTMRightDiag(hn, mps_mul_mps(AR[-1], AR[0])))
+        self.prec = np.ones(N)
+        self.F = np.ones(N)
+        self.dosvd = True
+        self.E = None
+        self.EHR0 = [None] * N   # persists across sweeps (VUMPS_main.cpp:119)
+
+    def site_update(self, nn):
+        d, N, hn = self.d, self.N, self.hnnz
+        self.EHR0[nn] = self.EHR
+        AL, AR, C = self.AL, self.AR, self.C
+        EHL, EHR, HL, HR = self.EHL, self.EHR, self.HL, self.HR
+        HA = lambda X: ApplyHA(X, EHL, EHR, HL, HR)
+        self.F[nn] = GradNormRight(AR[-1], C[-1], HA)
+        tol = self.fixed_tol if self.fixed_tol else min(max(self.prec[nn] / 100.0, 5e-16), 1e-6)
+        AC = bd_mul_mps(C[-1], AR[-1])
+        Adims = mps_sizes(AC)
+        Am = mps_nelem(AC)
+        _, v = eigs_rs(lambda x: ApplyHAvec(x, Adims, EHL, EHR, HL, HR), Am, tol, mps_vec(AC))
+        AC = mps_from_vec(v[:, 0], Adims)
+        CLd, CRd = bd_sizes(C[-1]), bd_sizes(C[0])
+        CLm, CRm = sum(m * m for _, m in CLd), sum(m * m for _, m in CRd)
+        _, cl = eigs_rs(lambda x: ApplyHCvec(x, CLd, EHL, self.EHR1, hn, d, AL[-1], AR[-1]), CLm, tol, bd_vec(C[-1]))
+        _, cr = eigs_rs(lambda x: ApplyHCvec(x, CRd, self.EHL1, EHR, hn, d, AL[0], AR[0]), CRm, tol, bd_vec(C[0]))
+        cl = cl[:, 0] / np.sign(cl[0, 0])
+        cr = cr[:, 0] / np.sign(cr[0, 0])
+        CL, CR = bd_from_vec(cl, CLd), bd_from_vec(cr, CRd)
+        if self.dosvd and self.prec[nn] < self.svdthresh:
+            self.dosvd = False
+        if self.dosvd:
+            QL, _, PL = svd_mps([bm_mul_bd(a, bd_t(CR)) for a in AC], "l")
+            ALnew = mps_mul_bd(QL, PL)
+            QR, _, PR = svd_mps(bd_mul_mps(bd_t(CL), AC), "r")
+            ARnew = bd_mul_mps(PR, QR)
+        else:
+            QL, _ = qr_mps(AC, "l")
+            PL, _ = qr_bd(CR, "l")
+            ALnew = mps_mul_bd(QL, bd_t(PL))
+            QR, _ = qr_mps(AC, "r")
+            PR, _ = qr_bd(CL, "r")
+            ARnew = bd_mul_mps(bd_t(PR), QR)
+        err_l = mps_norm_inf(mps_sub(AC, mps_mul_bd(ALnew, CR)))
+        err_r = mps_norm_inf(mps_sub(AC, bd_mul_mps(CL, ARnew)))
+        self.prec[nn] = max(err_l, err_r)
+        AL[0] = ALnew
+        AR[-1] = ARnew
+        C[0] = CR
+        C[-1] = CL
+        Rm = bd_mul(CL, bd_t(CL))
+        if self.trueLR:
+            _, Rm = TMDominantEig(AL, {q: m.shape[0] for q, m in Rm.items()}, "r", 1e-15, Rm)
+        HAL = GetHL(AL, hn)
+        AAL = mps_mul_mps(AL[-1], AL[0])
+        gtol = max(tol / self.InvEfac, self.InvETol)
+        EHL, _ = InvertE_proj(AL, HAL, bd_eye({q: m.shape[1] for q, m in C[-1].items()}), Rm, "l", gtol, 0, EHL)
+        AL[:] = shift(AL, -1)
+        AR[:] = shift(AR, -1)
+        C[:] = shift(C, -1)
+        EHLtmp = bd_add(ApplyOpTMLeftDiag(hn, AAL), ApplyTMLeft(AL[-1], EHL))
+        AAL = mps_mul_mps(AL[-1], AL[0])
+        self.EHL1 = bd_add(ApplyOpTMLeftDiag(hn, AAL), ApplyTMLeft(AL[0], EHLtmp))
+        Lm = bd_mul(bd_t(C[0]), C[0])
+        if self.trueLR:
+            _, Lm = TMDominantEig(AR, {q: m.shape[0] for q, m in Lm.items()}, "l", 1e-15, Lm)
+        HAR = GetHR(AR, hn)
+        EHR0_next = self.EHR0[(nn + 1) % N]
+        EHR, _ = InvertE_proj(AR, HAR, Lm, bd_eye({q: m.shape[0] for q, m in C[0].items()}), "r", gtol, 0, EHR0_next)
+        EHL = EHLtmp
+        self.EHR1 = bd_add(ApplyTMRight(AR[-1], EHR), ApplyOpTMRightDiag(hn, mps_mul_mps(AR[-1], AR[0])))
+        self.HL = ReducedOp(hn, AL[-1], d, "l")
+        self.HR = ReducedOp(hn, AR[0], d, "r")
+        self.EHL, self.EHR = EHL, EHR
+
+    def sweep(self):
+        for nn in range(self.N):
+            self.site_update(nn)
+        for n in range(self.N):
+            self.L[(n - 1) % self.N] = bd_mul(bd_t(self.C[n]), self.C[n])
+        self.E = energy_right(self.hnnz, self.AR, self.L)
+        return self.E, self.F.copy(), self.prec.copy()

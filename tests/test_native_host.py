@@ -1,0 +1,158 @@
+"""CPU tests of the native library: it loads, exports every declared symbol, and its sector
+planner (run in a host-only context, no GPU) produces exactly the block pairings the
+reference's std::map lookups produce."""
+import ctypes as C
+
+import numpy as np
+import pytest
+
+from imps_cpp_tools_gb300 import _native as N
+from imps_cpp_tools_gb300 import blocks as B
+from oracle import imps_oracle as O
+from tests import imps_testlib as T
+
+
+@pytest.fixture(scope="module")
+def host_ctx():
+    N.load()
+    return B.Context(-1)
+
+
+def test_exports_every_header_symbol():
+    lib = N.load()
+    syms = N.header_symbols()
+    assert len(syms) >= 30
+    missing = [s for s in syms if not hasattr(lib, s)]
+    assert not missing, missing
+    assert lib.imps_version() >= 100
+    assert N.load().imps_status_string(-2) == b"inconsistent sector table"
+
+
+def test_layout_rejects_unsorted_keys():
+    with pytest.raises(N.ImpsError) as e:
+        B.Layout([(0, (2,), (3,), 1, 1), (0, (0,), (1,), 1, 1)], 1)
+    assert e.value.status == -2
+    with pytest.raises(N.ImpsError):
+        B.Layout([(0, (0,), (1,), -1, 1)], 1)
+    L = B.Layout([(0, (0,), (1,), 2, 3), (0, (2,), (3,), 1, 4), (1, (0,), (-1,), 2, 2)], 1)
+    assert L.nelem == 6 + 4 + 4
+    bd = L.bond(0)
+    assert [b[1] for b in bd.blocks] == [(0,), (2,)] and [b[3] for b in bd.blocks] == [2, 1]
+
+
+def _offsets(blocks):
+    off, o = {}, 0
+    for (g, qi, qo, r, c) in blocks:
+        off[(g, qi)] = o
+        o += r * c
+    return off
+
+
+def _expected_hac(p):
+    """The products ApplyHA (VUMPS_helpers.hpp:48-52) forms, found with the reference's map
+    lookups on the oracle's dicts, as (slot, offset) pairs per output block."""
+    d, AC, EHL, EHR, HL, HR = p["d"], p["AC"], p["EHL"], p["EHR"], p["HL"], p["HR"]
+    oac = _offsets(T.mps_blocks(AC))
+    oel, oer = _offsets(T.bd_blocks(EHL)), _offsets(T.bd_blocks(EHR))
+    ohl, ohr = _offsets(T.redop_blocks(HL, d)), _offsets(T.redop_blocks(HR, d))
+    exp = []
+    for s in range(d):
+        for ql in sorted(AC[s]):
+            qr = AC[s][ql][0]
+            terms = []
+            if ql in EHL:
+                terms.append((2, oel[(0, ql)], 0, oac[(s, ql)]))
+            if qr in EHR:
+                terms.append((0, oac[(s, ql)], 3, oer[(0, qr)]))
+            for j in range(d):
+                if ql in HL[s][j]:
+                    ql2 = HL[s][j][ql][0]
+                    if ql2 in AC[j] and AC[j][ql2][0] == qr:
+                        terms.append((4, ohl[(s * d + j, ql)], 0, oac[(j, ql2)]))
+                if ql in AC[j]:
+                    qr2 = AC[j][ql][0]
+                    if qr2 in HR[s][j] and HR[s][j][qr2][0] == qr:
+                        terms.append((0, oac[(j, ql)], 5, ohr[(s * d + j, qr2)]))
+            exp.append(terms)
+    return exp
+
+
+@pytest.mark.parametrize("model,dims0", [
+    ("xxz", {(-4,): 1, (-2,): 3, (0,): 5, (2,): 3, (4,): 1}),
+    ("fhub", {(0, 0): 4, (1, 1): 2, (-1, -1): 2, (1, -1): 2, (-1, 1): 2, (2, 0): 1, (0, 2): 1}),
+])
+def test_hac_sector_matching_bit_exact(host_ctx, model, dims0):
+    p = T.hac_problem(model, dims0, seed=11)
+    d = p["d"]
+    lac = B.Layout(T.mps_blocks(p["AC"]), len(p["I2K"][0]))
+    lel, ler = B.Layout(T.bd_blocks(p["EHL"]), lac.nsym), B.Layout(T.bd_blocks(p["EHR"]), lac.nsym)
+    lhl, lhr = B.Layout(T.redop_blocks(p["HL"], d), lac.nsym), B.Layout(T.redop_blocks(p["HR"], d), lac.nsym)
+    plan = B.plan_hac(host_ctx, lac, lel, ler, lhl, lhr, d)
+    tab = plan.table(0)
+    got = [[(a, ao, b, bo) for (a, ao, b, bo, k, al) in terms] for (_, terms) in sorted(tab)]
+    assert got == _expected_hac(p)
+    assert plan.info()["dropped"] == 0
+    # useful flops of one apply = sum 2*M*N*K over the products
+    fl = sum(2 * r * c * k for (g, qi, qo, r, c), (_, terms) in zip(lac.blocks, sorted(tab))
+             for (_, _, _, _, k, _) in terms)
+    assert plan.info()["flops_apply"] == fl
+
+
+@pytest.mark.parametrize("direction", ["l", "r"])
+def test_redop_layout_matches_reference_structure(host_ctx, direction):
+    st = T.random_state("fhub", {(0, 0): 3, (1, 1): 2, (-1, -1): 2, (1, -1): 1, (-1, 1): 1}, seed=4)
+    d, A = st["d"], st["AL"][1] if direction == "l" else st["AR"][1]
+    R = O.ReducedOp(st["hnnz"], A, d, direction)
+    la = B.Layout(T.mps_blocks(A), 2)
+    plan = B.plan_redop(host_ctx, la, d, st["hnnz"], 0 if direction == "l" else 1)
+    got = plan.derived(0).blocks
+    assert got == [(g, qi, qo, r, c) for (g, qi, qo, r, c) in T.redop_blocks(R, d)]
+
+
+@pytest.mark.parametrize("direction", [0, 1])
+def test_tm_sector_matching(host_ctx, direction):
+    st = T.random_state("xxz", {(-2,): 2, (0,): 4, (2,): 2, (4,): 1}, seed=9)
+    AL, dv = st["AL"], st["dimvec"]
+    l0, l1 = B.Layout(T.mps_blocks(AL[0]), 1), B.Layout(T.mps_blocks(AL[1]), 1)
+    bond = B.Layout.blockdiag(dv[0])
+    plan = B.plan_tm(host_ctx, [l0, l1], direction, bond, bond)
+    info = plan.info()
+    assert info["nstages"] == 4
+    # stage 1 (first site reduction): every output sector gathers the A blocks whose
+    # Qout (left TM) / Qin (right TM) equals it, in physical-index order
+    A = AL[0] if direction == 0 else AL[1]
+    la = l0 if direction == 0 else l1
+    mid = la.bond(1 if direction == 0 else 0)
+    tab = plan.table(1)
+    oa = _offsets(la.blocks)
+    for (tag, terms), blk in zip(tab, mid.blocks):
+        q = blk[1]
+        exp = []
+        for s in range(len(A)):
+            for qi in sorted(A[s]):
+                qo = A[s][qi][0]
+                if (direction == 0 and qo == q) or (direction == 1 and qi == q):
+                    exp.append(oa[(s, qi)])
+        assert [t[1] for t in terms] == exp
+
+
+def test_dropped_sector_counted(host_ctx):
+    """A HL block pointing at an in[j] block whose Qout differs from the output block is not
+    added (the reference would insert it into a std::map of views outside the buffer)."""
+    ac = B.Layout([(0, (0,), (1,), 1, 1), (1, (0,), (-1,), 1, 1)], 1)
+    e = B.Layout([(0, (0,), (0,), 1, 1)], 1)
+    er = B.Layout([(0, (-1,), (-1,), 1, 1), (0, (1,), (1,), 1, 1)], 1)
+    hl = B.Layout([(1, (0,), (0,), 1, 1)], 1)  # HL[0][1]: maps 0 -> 0, but in[1](0) -> -1 != 1
+    hr = B.Layout([], 1)
+    plan = B.plan_hac(host_ctx, ac, e, er, hl, hr, 2)
+    assert plan.info()["dropped"] == 1
+
+
+def test_bad_dims_rejected(host_ctx):
+    ac = B.Layout([(0, (0,), (1,), 2, 1)], 1)
+    e = B.Layout([(0, (0,), (0,), 3, 3)], 1)  # EHL sector with wrong size
+    er = B.Layout([(0, (1,), (1,), 1, 1)], 1)
+    empty = B.Layout([], 1)
+    with pytest.raises(N.ImpsError) as ex:
+        B.plan_hac(host_ctx, ac, e, er, empty, empty, 1)
+    assert ex.value.status == -2
