@@ -39,6 +39,7 @@ _PROTOS = {
     "imps_ctx_destroy": (c_int, [c_vp]),
     "imps_ctx_set_stream": (c_int, [c_vp, c_vp]),
     "imps_ctx_synchronize": (c_int, [c_vp]),
+    "imps_ctx_use_own_stream": (c_int, [c_vp]),
     "imps_layout_create": (c_int, [c_int, c_int, P_i32, P_i32, P_i32, P_i32, P_i32, C.POINTER(c_vp)]),
     "imps_layout_destroy": (c_int, [c_vp]),
     "imps_layout_nelem": (c_i64, [c_vp]),
@@ -75,6 +76,14 @@ _PROTOS = {
     "imps_tm_dominant": (c_int, [c_vp, c_vp, c_vp, c_int, c_dbl, c_int, P_dbl, P_int]),
     "imps_grad_norm_right": (c_int, [c_vp, P_dbl]),
     "imps_dot": (c_int, [c_vp, c_vp, c_vp, c_i64, P_dbl]),
+    "imps_plan_decomp": (c_int, [c_vp, c_vp, c_int, C.POINTER(c_vp)]),
+    "imps_sector_qr": (c_int, [c_vp, c_vp, c_vp, c_vp, c_int]),
+    "imps_sector_svd": (c_int, [c_vp, c_vp, c_vp, c_vp, c_vp, c_int]),
+    "imps_sector_colscale": (c_int, [c_vp, c_vp, c_vp, c_dbl, c_int]),
+    "imps_bd_trace_prod": (c_int, [c_vp, c_vp, c_vp, c_vp, P_dbl]),
+    "imps_absmax": (c_int, [c_vp, c_vp, c_i64, P_dbl]),
+    "imps_axpby": (c_int, [c_vp, c_dbl, c_vp, c_dbl, c_vp, c_i64]),
+    "imps_sign_normalize": (c_int, [c_vp, c_vp, c_i64]),
 }
 
 _lib = None

@@ -291,3 +291,13 @@ def plan_grad_right(ctx, Y, AR):
     h = C.c_void_p()
     N.call("imps_plan_grad_right", ctx.handle, Y.handle, AR.handle, C.byref(h))
     return Plan(ctx, h, "grad")
+
+
+def plan_decomp(ctx, A, direction):
+    """Per-sector dense decomposition tables of A (GetDenseMat order); direction 'l'/'r'."""
+    h = C.c_void_p()
+    N.call("imps_plan_decomp", ctx.handle, A.handle, 0 if direction in ("l", 0) else 1, C.byref(h))
+    p = Plan(ctx, h, "decomp")
+    p.rlayout = p.derived(1)
+    p.nsv = sum(b[3] for b in p.rlayout.blocks)
+    return p

@@ -10,6 +10,7 @@
 #include <vector>
 
 #include "../../include/imps_gb300.h"
+#include "imps_decomp.h"
 #include "imps_internal.h"
 #include "imps_krylov.h"
 #include "imps_tc.h"
@@ -29,6 +30,13 @@ struct imps_ctx {
 
 struct imps_layout {
   Layout L;
+  // device copies of the block table (BlockDiagMat traces), uploaded on first use
+  int64_t* d_boff = nullptr;
+  int32_t* d_bdim = nullptr;
+  ~imps_layout() {
+    if (d_boff) cudaFree(d_boff);
+    if (d_bdim) cudaFree(d_bdim);
+  }
 };
 
 struct imps_plan {
@@ -49,7 +57,10 @@ struct imps_plan {
   int64_t count_elems = 0;
   int prec = IMPS_PREC_FP64;
   TcPlan* tc = nullptr;
+  DecompPlan* dc = nullptr;
 };
+
+constexpr int PLAN_DECOMP = 12;
 
 namespace {
 
@@ -272,7 +283,13 @@ int imps_ctx_destroy(imps_ctx* c) {
 
 int imps_ctx_set_stream(imps_ctx* c, void* s) {
   if (!c) return IMPS_ERR_BAD_ARG;
-  c->stream = s ? (cudaStream_t)s : c->own;
+  c->stream = (cudaStream_t)s;  // used as given: NULL is the CUDA legacy default stream
+  return IMPS_OK;
+}
+
+int imps_ctx_use_own_stream(imps_ctx* c) {
+  if (!c) return IMPS_ERR_BAD_ARG;
+  c->stream = c->own;
   return IMPS_OK;
 }
 
@@ -437,7 +454,7 @@ int imps_plan_grad_right(imps_ctx* ctx, const imps_layout* Y, const imps_layout*
 
 int imps_plan_destroy(imps_plan* p) {
   if (!p) return IMPS_OK;
-  if (p->ctx && p->ctx->device < 0) { delete p; return IMPS_OK; }
+  if (p->ctx && p->ctx->device < 0) { delete p->dc; delete p; return IMPS_OK; }
   if (p->ctx) cudaStreamSynchronize(p->ctx->stream);
   for (Slot& s : p->P.slots)
     if (s.kind == SLOT_INTERNAL && s.dptr) cudaFree(s.dptr);
@@ -455,6 +472,12 @@ int imps_plan_destroy(imps_plan* p) {
   cudaFree(p->d_soff);
   cudaFree(p->d_slen);
   if (p->tc) tc_destroy(p->tc);
+  if (p->dc) {
+    cudaFree(p->dc->d_ent); cudaFree(p->dc->d_mats); cudaFree(p->dc->dA); cudaFree(p->dc->dQ);
+    cudaFree(p->dc->dR); cudaFree(p->dc->dV2); cudaFree(p->dc->dS); cudaFree(p->dc->dW);
+    cudaFree(p->dc->dstatus);
+    delete p->dc;
+  }
   delete p;
   return IMPS_OK;
 }
@@ -936,6 +959,124 @@ int imps_grad_norm_right(imps_plan* p, double* F) {
   CK(cudaMemcpyAsync(&s, c->dscal + 7, 8, cudaMemcpyDeviceToHost, st));
   CK(cudaStreamSynchronize(st));
   *F = std::sqrt(s) / std::sqrt((double)p->count_elems);
+  return IMPS_OK;
+}
+
+// ---- per-sector decompositions ----
+int imps_plan_decomp(imps_ctx* ctx, const imps_layout* A, int dir, imps_plan** out) {
+  if (!ctx || !A || !out || (dir != 0 && dir != 1)) return IMPS_ERR_BAD_ARG;
+  DecompPlan* D = new (std::nothrow) DecompPlan();
+  if (!D) return IMPS_ERR_OOM;
+  int rc = build_decomp(*D, A->L, dir);
+  if (rc) { delete D; return rc; }
+  imps_plan* p = new (std::nothrow) imps_plan();
+  if (!p) { delete D; return IMPS_ERR_OOM; }
+  p->ctx = ctx;
+  p->P.kind = PLAN_DECOMP;
+  p->P.derived.push_back(A->L);
+  p->P.derived.push_back(D->rlayout);
+  p->dc = D;
+  *out = p;
+  if (ctx->device < 0) return IMPS_OK;
+  auto alloc = [&](double** ptr, int64_t n) -> int {
+    CK(cudaMalloc(ptr, std::max<int64_t>(n, 1) * sizeof(double)));
+    return IMPS_OK;
+  };
+  if (!D->ent.empty()) {
+    CK(cudaMalloc(&D->d_ent, D->ent.size() * sizeof(GatherEntry)));
+    CK(cudaMemcpy(D->d_ent, D->ent.data(), D->ent.size() * sizeof(GatherEntry), cudaMemcpyHostToDevice));
+  }
+  if (!D->mats.empty()) {
+    CK(cudaMalloc(&D->d_mats, D->mats.size() * sizeof(DenseMat)));
+    CK(cudaMemcpy(D->d_mats, D->mats.data(), D->mats.size() * sizeof(DenseMat), cudaMemcpyHostToDevice));
+  }
+  RC(alloc(&D->dA, D->dense_elems));
+  RC(alloc(&D->dQ, D->dense_elems));
+  RC(alloc(&D->dR, D->r_elems));
+  RC(alloc(&D->dV2, D->r_elems));
+  RC(alloc(&D->dS, D->s_elems));
+  RC(alloc(&D->dW, D->w_elems));
+  CK(cudaMalloc(&D->dstatus, sizeof(int)));
+  return IMPS_OK;
+}
+
+int imps_sector_qr(imps_plan* p, const double* A, double* Q, double* R, int mem) {
+  if (!p || p->P.kind != PLAN_DECOMP || !A || !Q || !R || mem != IMPS_MEM_DEVICE) return IMPS_ERR_BAD_ARG;
+  if (p->ctx->device < 0) return IMPS_ERR_NO_DEVICE;
+  DecompPlan* D = p->dc;
+  if (!D->tall) return IMPS_ERR_UNSUPPORTED;
+  cudaStream_t st = p->ctx->stream;
+  RC(dc_gather(D->d_ent, (int)D->ent.size(), A, D->dA, st));
+  RC(dc_qr(D->d_mats, (int)D->mats.size(), D->dA, D->dQ, R, D->dir == 1, st));
+  RC(dc_scatter(D->d_ent, (int)D->ent.size(), D->dQ, Q, st));
+  return IMPS_OK;
+}
+
+int imps_sector_svd(imps_plan* p, const double* A, double* U, double* S, double* Viso, int mem) {
+  if (!p || p->P.kind != PLAN_DECOMP || !A || mem != IMPS_MEM_DEVICE) return IMPS_ERR_BAD_ARG;
+  if (p->ctx->device < 0) return IMPS_ERR_NO_DEVICE;
+  DecompPlan* D = p->dc;
+  if (!D->tall) return IMPS_ERR_UNSUPPORTED;
+  cudaStream_t st = p->ctx->stream;
+  CK(cudaMemsetAsync(D->dstatus, 0, sizeof(int), st));
+  RC(dc_gather(D->d_ent, (int)D->ent.size(), A, D->dA, st));
+  RC(dc_svd(D->d_mats, (int)D->mats.size(), D->dA, S ? S : D->dS, D->dR, D->dW, D->dstatus, st));
+  if (U) RC(dc_scatter(D->d_ent, (int)D->ent.size(), D->dA, U, st));
+  if (Viso) {
+    if (D->dir == 0) RC(dc_transpose_sq(D->d_mats, (int)D->mats.size(), D->dR, Viso, st));  // V^T
+    else CK(cudaMemcpyAsync(Viso, D->dR, D->r_elems * 8, cudaMemcpyDeviceToDevice, st));   // V
+  }
+  int status = 0;
+  CK(cudaMemcpyAsync(&status, D->dstatus, sizeof(int), cudaMemcpyDeviceToHost, st));
+  CK(cudaStreamSynchronize(st));
+  return status ? IMPS_WARN_NOT_CONVERGED : IMPS_OK;
+}
+
+int imps_sector_colscale(imps_plan* p, double* X, const double* S, double power, int mem) {
+  if (!p || p->P.kind != PLAN_DECOMP || !X || !S || mem != IMPS_MEM_DEVICE) return IMPS_ERR_BAD_ARG;
+  if (p->ctx->device < 0) return IMPS_ERR_NO_DEVICE;
+  DecompPlan* D = p->dc;
+  for (const DenseMat& m : D->mats)
+    if (m.M != m.N) return IMPS_ERR_BAD_ARG;  // BlockDiagMat plans only
+  return dc_colscale(D->d_mats, (int)D->mats.size(), X, S, power, p->ctx->stream);
+}
+
+// ---- device-vector helpers for drivers ----
+int imps_bd_trace_prod(imps_ctx* c, imps_layout* L, const double* X, const double* Y, double* result) {
+  if (!c || !L || !X || !Y || !result) return IMPS_ERR_BAD_ARG;
+  if (!L->d_boff && !L->L.blocks.empty()) {
+    std::vector<int64_t> bo;
+    std::vector<int32_t> bd;
+    for (const Block& b : L->L.blocks) { bo.push_back(b.off); bd.push_back(b.rows); }
+    CK(cudaMalloc(&L->d_boff, bo.size() * 8));
+    CK(cudaMalloc(&L->d_bdim, bd.size() * 4));
+    CK(cudaMemcpy(L->d_boff, bo.data(), bo.size() * 8, cudaMemcpyHostToDevice));
+    CK(cudaMemcpy(L->d_bdim, bd.data(), bd.size() * 4, cudaMemcpyHostToDevice));
+  }
+  RC(kr_trace_prod(c->ws, X, Y, L->d_boff, L->d_bdim, (int)L->L.blocks.size(), c->dscal + 16, c->stream));
+  CK(cudaMemcpyAsync(result, c->dscal + 16, 8, cudaMemcpyDeviceToHost, c->stream));
+  CK(cudaStreamSynchronize(c->stream));
+  return IMPS_OK;
+}
+
+int imps_absmax(imps_ctx* c, const double* x, int64_t n, double* result) {
+  if (!c || !x || !result) return IMPS_ERR_BAD_ARG;
+  RC(kr_absmax(c->ws, x, n, c->dscal + 17, c->stream));
+  CK(cudaMemcpyAsync(result, c->dscal + 17, 8, cudaMemcpyDeviceToHost, c->stream));
+  CK(cudaStreamSynchronize(c->stream));
+  return IMPS_OK;
+}
+
+int imps_axpby(imps_ctx* c, double a, const double* x, double b, double* y, int64_t n) {
+  if (!c || !x || !y) return IMPS_ERR_BAD_ARG;
+  return kr_axpby(a, x, b, y, n, c->stream);
+}
+
+// x /= sign(x[0])  (VUMPS_main.cpp:201-202; sign(0) is taken as +1)
+int imps_sign_normalize(imps_ctx* c, double* x, int64_t n) {
+  if (!c || !x || n < 1) return IMPS_ERR_BAD_ARG;
+  RC(kr_sign_of_first(x, c->dscal + 18, c->stream));
+  RC(kr_scale_inv(x, c->dscal + 18, x, n, nullptr, c->stream));
   return IMPS_OK;
 }
 

@@ -1,0 +1,60 @@
+// Per-sector dense decomposition tables and kernels (decomp.cu).
+#pragma once
+#include <cuda_runtime.h>
+
+#include <cstdint>
+#include <vector>
+
+#include "imps_internal.h"
+
+namespace imps {
+
+// One block of a block-sparse object copied into (or out of) a packed dense sector matrix.
+struct GatherEntry {
+  int64_t src_off;  // block offset in the block-sparse vector
+  int64_t dst_off;  // offset of the dense matrix in the packed buffer
+  int32_t rows, cols;
+  int32_t r0, c0;   // position of the block inside the dense matrix
+  int32_t dst_ld;
+  int32_t transpose;  // 1: the dense matrix holds the transpose of the stacked blocks
+};
+
+// One dense sector matrix (M x N, "tall" orientation, M >= N expected).
+struct DenseMat {
+  int64_t a_off;  // packed M x N input / U output
+  int64_t q_off;  // Q (M x K) / U (M x N)
+  int64_t r_off;  // R (K x N) / V (N x N) / DiagIso
+  int64_t s_off;  // singular values (N)
+  int64_t w_off;  // scratch (N + M*N)
+  int32_t M, N;
+};
+
+struct DecompPlan {
+  int dir = 0;
+  std::vector<GatherEntry> ent;
+  std::vector<DenseMat> mats;
+  int64_t dense_elems = 0, r_elems = 0, s_elems = 0, w_elems = 0;
+  bool tall = true;  // every sector has M >= N
+  Layout rlayout;    // R / DiagIso BlockDiag layout over the sectors
+  GatherEntry* d_ent = nullptr;
+  DenseMat* d_mats = nullptr;
+  double* dA = nullptr;  // dense input (overwritten by QR / holds U for SVD)
+  double* dQ = nullptr;  // dense Q
+  double* dR = nullptr;  // R or V
+  double* dV2 = nullptr; // V^T (DiagIso for dir l)
+  double* dS = nullptr;
+  double* dW = nullptr;
+  int* dstatus = nullptr;
+};
+
+int build_decomp(DecompPlan& D, const Layout& A, int dir);
+
+int dc_gather(const GatherEntry* d_ent, int nent, const double* src, double* dense, cudaStream_t st);
+int dc_scatter(const GatherEntry* d_ent, int nent, const double* dense, double* dst, cudaStream_t st);
+int dc_qr(const DenseMat* d_mats, int nmat, double* A, double* Q, double* R, int transpose_r, cudaStream_t st);
+int dc_svd(const DenseMat* d_mats, int nmat, double* U, double* S, double* V, double* W, int* status,
+           cudaStream_t st);
+int dc_colscale(const DenseMat* d_mats, int nmat, double* X, const double* S, double power, cudaStream_t st);
+int dc_transpose_sq(const DenseMat* d_mats, int nmat, const double* X, double* Y, cudaStream_t st);
+
+}  // namespace imps

@@ -30,6 +30,7 @@ int kr_trace_prod(const KrylovWs& ws, const double* X, const double* R, const in
 int kr_segsq(const KrylovWs& ws, const double* X, const int64_t* soff, const int64_t* slen, int ns,
              double* out, cudaStream_t st);
 int kr_absmax(const KrylovWs& ws, const double* x, int64_t n, double* out, cudaStream_t st);
+int kr_sign_of_first(const double* x, double* s, cudaStream_t st);
 int kr_givens(double* Hcol, int j, double* cs, double* sn, double* gamma, double* R, int ldr,
               double* res, int* breakdown, cudaStream_t st);
 

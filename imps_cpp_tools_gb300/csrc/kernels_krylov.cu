@@ -258,6 +258,10 @@ __global__ void givens_kernel(double* __restrict__ Hcol, int j, double* __restri
   *res = fabs(gamma[j + 1]);
 }
 
+__global__ void sign_first_kernel(const double* __restrict__ x, double* __restrict__ s) {
+  if (threadIdx.x == 0 && blockIdx.x == 0) *s = x[0] < 0.0 ? -1.0 : 1.0;
+}
+
 int grid_for(int64_t n) {
   int64_t g = (n + 255) / 256;
   if (g > 152 * 8) g = 152 * 8;
@@ -330,6 +334,11 @@ int kr_absmax(const KrylovWs& ws, const double* x, int64_t n, double* out, cudaS
 int kr_givens(double* Hcol, int j, double* cs, double* sn, double* gamma, double* R, int ldr,
               double* res, int* breakdown, cudaStream_t st) {
   givens_kernel<<<1, 32, 0, st>>>(Hcol, j, cs, sn, gamma, R, ldr, res, breakdown);
+  return IMPS_OK;
+}
+
+int kr_sign_of_first(const double* x, double* s, cudaStream_t st) {
+  sign_first_kernel<<<1, 32, 0, st>>>(x, s);
   return IMPS_OK;
 }
 

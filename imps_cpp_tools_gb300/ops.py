@@ -69,6 +69,53 @@ def TMDominantEig(plan, V, x0=None, tol=1e-14, maxit=0):
     return ev.value, it.value, st == 0
 
 
+def qr(dec, A, Q, R):
+    """qr(R, MPS|BlockDiagMat, dir) with diag(R) >= 0 (MPSBlockUtilities.hpp:181-244,
+    BlockObj.hpp:2422-2459): Q in A's layout, R BlockDiagMat over the sectors."""
+    N.call("imps_sector_qr", dec.handle, _dptr(A), _dptr(Q), _dptr(R), N.MEM_DEVICE)
+    return Q, R
+
+
+def svd(dec, A, U=None, S=None, V=None):
+    """svd(S, DiagIso, MPS, dir) (MPSBlockUtilities.hpp:78-153): U = isometry in A's layout,
+    S = singular values (sector order, descending), V = DiagIso.  Returns True if converged."""
+    p = lambda t: None if t is None else _dptr(t)
+    st = N.call("imps_sector_svd", dec.handle, _dptr(A), p(U), p(S), p(V), N.MEM_DEVICE)
+    return st == 0
+
+
+def colscale(dec, X, S, power):
+    """X_q[:, j] *= S_q[j]**power on square sector blocks (BlockDiagMat << BlockLam)."""
+    N.call("imps_sector_colscale", dec.handle, _dptr(X), _dptr(S), float(power), N.MEM_DEVICE)
+    return X
+
+
+def bd_trace_prod(ctx, layout, X, Y):
+    """sum_q trace(X_q Y_q) over a BlockDiagMat layout."""
+    r = C.c_double()
+    N.call("imps_bd_trace_prod", ctx.handle, layout.handle, _dptr(X), _dptr(Y), C.byref(r))
+    return r.value
+
+
+def norm_inf(ctx, x):
+    """norm_inf (helpers.hpp:148-151) of a device vector."""
+    r = C.c_double()
+    N.call("imps_absmax", ctx.handle, _dptr(x), x.numel(), C.byref(r))
+    return r.value
+
+
+def axpby(ctx, a, x, b, y):
+    """y = a*x + b*y on the device."""
+    N.call("imps_axpby", ctx.handle, float(a), _dptr(x), float(b), _dptr(y), y.numel())
+    return y
+
+
+def sign_normalize(ctx, x):
+    """x /= sign(x[0]) (VUMPS_main.cpp:201-202)."""
+    N.call("imps_sign_normalize", ctx.handle, _dptr(x), x.numel())
+    return x
+
+
 def GradNormRight(plan):
     """GradNormRight (VUMPS_helpers.hpp:145-153) from Y = H_AC(C*AR) bound to slot 0 and AR to slot 1."""
     F = C.c_double()

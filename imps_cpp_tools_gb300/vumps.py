@@ -1,0 +1,333 @@
+"""VUMPS driver on the GPU: the loop of VUMPS/VUMPS_main.cpp:97-354 (two-site unit cell,
+bond expansion disabled) with every contraction, eigensolve, linear solve and decomposition
+on the device through the C ABI.
+
+Indices.  Site n (n = 0, 1) maps bond n -> bond n+1 (mod 2).  C[b] is the centre matrix on
+bond b (the reference's Cvec[n] is the C right of site n, i.e. C[n+1]).  The reference
+rotates its unit-cell arrays after every site update (shift(..,-1), VUMPS_main.cpp:256-259);
+here the rotation is replaced by explicit indices: updating site n uses
+  AC(n) = C[n] AR(n), HL from AL(n-1), HR from AR(n+1), CL = C[n], CR = C[n+1].
+"""
+from __future__ import annotations
+
+import numpy as np
+
+from . import _native as N
+from . import blocks as B
+from . import models, ops
+
+
+class VumpsGPU:
+    def __init__(self, ctx, model, dims0=None, dimvec=None, seed=1, InvETol=5e-15, InvEfac=2.0,
+                 fixed_tol=None, trueLR=True, svdthresh=5e-7, precision="fp64", init_state=None,
+                 lanczos_maxit=4000, gmres_maxit=20000, **params):
+        import torch
+        self.torch = torch
+        self.ctx = ctx
+        self.d, self.I2K, h = models.build_model(model, **params)
+        self.hnnz = models.h_nonzeros(h)
+        if dimvec is None:
+            dimvec = models.make_dims(dims0, 2, self.I2K)
+        self.dimvec = dimvec
+        self.InvETol, self.InvEfac, self.fixed_tol, self.trueLR = InvETol, InvEfac, fixed_tol, trueLR
+        self.svdthresh = svdthresh
+        self.lanczos_maxit, self.gmres_maxit = lanczos_maxit, gmres_maxit
+        self.precision = precision
+        self.rng = np.random.default_rng(seed)
+        self.stats = {"lanczos_applies": 0, "gmres_iters": 0, "hac_applies": 0}
+        d, hnnz = self.d, self.hnnz
+        self.LA = [B.Layout.mps(self.I2K, dimvec[n], dimvec[1 - n]) for n in range(2)]
+        self.LB = [B.Layout.blockdiag(dimvec[b]) for b in range(2)]
+        z = lambda lay: torch.zeros(lay.nelem, dtype=torch.float64, device="cuda")
+        self._z = z
+        self.AL = [z(self.LA[n]) for n in range(2)]
+        self.AR = [z(self.LA[n]) for n in range(2)]
+        self.C = [z(self.LB[b]) for b in range(2)]
+        self._build_plans()
+        if init_state is None:
+            self._rand_mps_lr()
+        else:
+            for n in range(2):
+                self.AL[n].copy_(init_state["AL"][n])
+                self.AR[n].copy_(init_state["AR"][n])
+                self.C[n].copy_(init_state["C"][n])
+        self._init_environments()
+
+    # ------------------------------------------------------------------ plans
+    def _build_plans(self):
+        ctx, d, hnnz, LA, LB = self.ctx, self.d, self.hnnz, self.LA, self.LB
+        self.redop_l = [B.plan_redop(ctx, LA[m], d, hnnz, 0) for m in range(2)]  # HL from AL(m): bond m+1
+        self.redop_r = [B.plan_redop(ctx, LA[m], d, hnnz, 1) for m in range(2)]  # HR from AR(m): bond m
+        self.lHL = [p.derived(0) for p in self.redop_l]
+        self.lHR = [p.derived(0) for p in self.redop_r]
+        self.HLbuf = [self._z(l) for l in self.lHL]  # HL built from AL(m) (lives on bond m+1)
+        self.HRbuf = [self._z(l) for l in self.lHR]  # HR built from AR(m) (lives on bond m)
+        self.p_ac, self.p_hac, self.p_grad, self.p_hcl, self.p_hcr = [], [], [], [], []
+        self.p_mul_r_t, self.p_mul_l_t, self.p_mul_r, self.p_mul_l = [], [], [], []
+        self.dec_ac_l, self.dec_ac_r = [], []
+        self.tm = {}
+        for n in range(2):
+            l, r, m = n, 1 - n, 1 - n
+            self.p_ac.append(B.plan_mps_bd(ctx, LA[n], LB[l], 0))                       # C[n] * AR(n)
+            self.p_hac.append(B.plan_hac(ctx, LA[n], LB[l], LB[r], self.lHL[m], self.lHR[m], d))
+            self.p_grad.append(B.plan_grad_right(ctx, LA[n], LA[n]))
+            self.p_hcl.append(B.plan_hc(ctx, LB[l], LB[l], LB[l], LA[m], LA[n], d, hnnz))  # CL = C[n]
+            self.p_hcr.append(B.plan_hc(ctx, LB[r], LB[r], LB[r], LA[n], LA[m], d, hnnz))  # CR = C[n+1]
+            self.p_mul_r_t.append(B.plan_mps_bd(ctx, LA[n], LB[r], 1, transpose_x=True))  # A * X^T
+            self.p_mul_l_t.append(B.plan_mps_bd(ctx, LA[n], LB[l], 0, transpose_x=True))  # X^T * A
+            self.p_mul_r.append(B.plan_mps_bd(ctx, LA[n], LB[r], 1))                      # A * X
+            self.p_mul_l.append(B.plan_mps_bd(ctx, LA[n], LB[l], 0))                      # X * A
+            self.dec_ac_l.append(B.plan_decomp(ctx, LA[n], "l"))
+            self.dec_ac_r.append(B.plan_decomp(ctx, LA[n], "r"))
+            # unit-cell transfer matrices starting at site n, on bond n
+            for kind, dirc in (("L", 0), ("R", 1)):
+                self.tm[(kind, n)] = B.plan_tm(ctx, [LA[n], LA[m]], dirc, LB[l], LB[l])
+            # single-site transfer matrices of site n: left bond n -> n+1, right bond n+1 -> n
+            self.tm[("L1", n)] = B.plan_tm(ctx, [LA[n]], 0, LB[l], LB[r])
+            self.tm[("R1", n)] = B.plan_tm(ctx, [LA[n]], 1, LB[r], LB[l])
+        self.dec_b_l = [B.plan_decomp(ctx, LB[b], "l") for b in range(2)]
+        self.dec_b_r = [B.plan_decomp(ctx, LB[b], "r") for b in range(2)]
+        # operator transfer matrices on 2-site products A(a) A(1-a): left -> right bond of A(1-a)
+        # (= bond a), right -> left bond of A(a) (= bond a)
+        self.optm_l = [B.plan_optm(ctx, LA[a], LA[1 - a], d, hnnz, 0, LB[a]) for a in range(2)]
+        self.optm_r = [B.plan_optm(ctx, LA[a], LA[1 - a], d, hnnz, 1, LB[a]) for a in range(2)]
+        for s in ("tm_l", "tm_r"):
+            pass
+        self.flops_hac = [p.info()["flops_apply"] for p in self.p_hac]
+        if self.precision == "bf16x6":
+            for p in self.p_hac + self.p_hcl + self.p_hcr:
+                p.set_precision(N.PREC_BF16X6)
+
+    # ------------------------------------------------------------------ small helpers
+    def _tm(self, key, A, vin, vout):
+        p = self.tm[key]
+        n = key[1]
+        if key[0] in ("L", "R"):
+            p.bind(2, A[n]); p.bind(3, A[1 - n])
+        else:
+            p.bind(2, A[n])
+        p.bind(0, vin); p.bind(1, vout)
+        p.run()
+        return vout
+
+    def _optm(self, left, a, A, out):
+        p = (self.optm_l if left else self.optm_r)[a]
+        p.bind(0, A[a]); p.bind(1, A[1 - a]); p.bind(2, out)
+        p.run()
+        return out
+
+    def _mul(self, plan, A, X, out):
+        plan.bind(0, A); plan.bind(1, X); plan.bind(2, out)
+        plan.run()
+        return out
+
+    def _eye(self, b):
+        v = np.zeros(self.LB[b].nelem)
+        for (g, qi, qo, r, c), o in zip(self.LB[b].blocks, self.LB[b].offsets):
+            v[o:o + r * c] = np.eye(r).reshape(-1)
+        return self.torch.tensor(v, dtype=self.torch.float64, device="cuda")
+
+    def _redops(self, sites=(0, 1)):
+        """ReducedOp (MPSBlockUtilities.hpp:37-74): HL from AL(m), HR from AR(m)."""
+        for m in sites:
+            p = self.redop_l[m]; p.bind(0, self.AL[m]); p.bind(1, self.HLbuf[m]); p.run()
+            p = self.redop_r[m]; p.bind(0, self.AR[m]); p.bind(1, self.HRbuf[m]); p.run()
+
+    def _get_hl(self, n):
+        """GetHL (VUMPS_helpers.hpp:3-18) of the unit cell [AL(n), AL(n+1)] -> bond n."""
+        m = 1 - n
+        t = self._optm(True, m, self.AL, self._z(self.LB[m]))       # OpTM(AL(n+1) AL(n)) on bond n+1
+        out = self._tm(("L1", m), self.AL, t, self._z(self.LB[n]))   # through AL(n+1) -> bond n
+        t2 = self._optm(True, n, self.AL, self._z(self.LB[n]))       # OpTM(AL(n) AL(n+1)) on bond n
+        return ops.axpby(self.ctx, 1.0, t2, 1.0, out)
+
+    def _get_hr(self, n):
+        """GetHR (VUMPS_helpers.hpp:20-36) of the unit cell [AR(n), AR(n+1)] -> bond n."""
+        m = 1 - n
+        t = self._optm(False, m, self.AR, self._z(self.LB[m]))      # OpTM(AR(n+1) AR(n)) on bond n+1
+        out = self._tm(("R1", n), self.AR, t, self._z(self.LB[n]))   # through AR(n) -> bond n
+        t2 = self._optm(False, n, self.AR, self._z(self.LB[n]))      # OpTM(AR(n) AR(n+1)) on bond n
+        return ops.axpby(self.ctx, 1.0, t2, 1.0, out)
+
+    def _invert_e(self, key, x, L, R, direction, y0, tol):
+        y = y0.clone() if y0 is not None else self._z_like(x)
+        it, rr, conv = ops.InvertE_proj(self.tm[key], x, L, R, direction, y, tol, maxit=self.gmres_maxit)
+        self.stats["gmres_iters"] += it
+        return y
+
+    def _z_like(self, x):
+        return self.torch.zeros_like(x)
+
+    def _tm_dominant(self, key, x0, tol):
+        V = self._z_like(x0)
+        _, it, _ = ops.TMDominantEig(self.tm[key], V, x0, tol, maxit=self.gmres_maxit)
+        self.stats["gmres_iters"] += it
+        return V
+
+    # ------------------------------------------------------------------ initial state
+    def _rand_mps_lr(self):
+        """randMPS_LR (MPSBlockUtilities.hpp:1093-1135) on the device."""
+        torch = self.torch
+        for n in range(2):
+            X = torch.tensor(self.rng.standard_normal(self.LA[n].nelem), dtype=torch.float64, device="cuda")
+            Rb = self._z(self.dec_ac_l[n].rlayout)
+            ops.qr(self.dec_ac_l[n], X, self.AL[n], Rb)
+        # right fixed point of [AL(0), AL(1)] on bond 0, C = qr(U sqrt(S), r).R
+        R = self._tm_dominant(("R", 0), None if False else self._eye(0), 1e-14)
+        U = self._z(self.LB[0])
+        S = torch.zeros(self.dec_b_l[0].nsv, dtype=torch.float64, device="cuda")
+        ops.svd(self.dec_b_l[0], R, U, S, None)
+        ops.colscale(self.dec_b_l[0], U, S, 0.5)
+        Qb = self._z(self.LB[0])
+        ops.qr(self.dec_b_r[0], U, Qb, self.C[0])
+        Ctmp = self.C[0]  # C on bond 0 (right of AL(1))
+        for n in (1, 0):
+            self.C[(n + 1) % 2].copy_(Ctmp)
+            X = self._mul(self.p_mul_r[n], self.AL[n], Ctmp, self._z(self.LA[n]))
+            Cn = self._z(self.LB[n])
+            ops.qr(self.dec_ac_r[n], X, self.AR[n], Cn)
+            Ctmp = Cn
+
+    def _init_environments(self):
+        """VUMPS_main.cpp:103-136: reduced operators, EHL/EHR, EHL1/EHR1."""
+        torch = self.torch
+        self._redops()
+        # R at bond 0 (right end of [AL(0), AL(1)]): C[0] C[0]^T ; L at bond 0 for [AR(0), AR(1)]:
+        # C[0]^T C[0] (the reference's initial shift puts these at the unit-cell boundary)
+        R = self._cct(0, right=True)
+        L = self._cct(0, right=False)
+        self.EHL = self._invert_e(("L", 0), self._get_hl(0), self._eye(0), R, "l", None, self.InvETol)
+        self.EHR = self._invert_e(("R", 1), self._get_hr(1), L if False else self._cct(1, right=False),
+                                  self._eye(1), "r", None, self.InvETol)
+        self.EHL1 = ops.axpby(self.ctx, 1.0, self._optm(True, 1, self.AL, self._z(self.LB[1])), 1.0,
+                              self._tm(("L1", 0), self.AL, self.EHL, self._z(self.LB[1])))
+        self.EHR1 = ops.axpby(self.ctx, 1.0, self._optm(False, 0, self.AR, self._z(self.LB[0])), 1.0,
+                              self._tm(("R1", 0), self.AR, self.EHR, self._z(self.LB[0])))
+        self.EHR0 = [None, None]
+        self.prec = np.ones(2)
+        self.F = np.ones(2)
+        self.dosvd = True
+        self.E = None
+        torch.cuda.synchronize()
+
+    def _cct(self, b, right=True):
+        """C C^T (right=True) or C^T C on bond b."""
+        out = self._z(self.LB[b])
+        ctx = self.ctx
+        # BlockDiag products through the MPS x BlockDiag plans with d = 1 (layout of a BD)
+        key = ("cct", b, right)
+        if key not in self.tm:
+            self.tm[key] = B.plan_mps_bd(ctx, self.LB[b], self.LB[b], 1 if right else 0, transpose_x=True)
+        p = self.tm[key]
+        # right: C * C^T ; left: C^T * C
+        return self._mul(p, self.C[b], self.C[b], out)
+
+    # ------------------------------------------------------------------ one site update
+    def site_update(self, n):
+        """One iteration of the site loop, VUMPS_main.cpp:171-313, for site n."""
+        torch, ctx = self.torch, self.ctx
+        l, r, m = n, 1 - n, 1 - n
+        self.EHR0[n] = self.EHR
+        hac = self.p_hac[n]
+        hac.bind(2, self.EHL); hac.bind(3, self.EHR)
+        hac.bind(4, self.HLbuf[m]); hac.bind(5, self.HRbuf[m])
+        # gradient norm (GradNormRight, VUMPS_helpers.hpp:145-153) at AC = C[n] AR(n)
+        AC = self._mul(self.p_ac[n], self.AR[n], self.C[l], self._z(self.LA[n]))
+        Y = self._z(self.LA[n])
+        ops.ApplyHAvec(hac, AC, Y)
+        g = self.p_grad[n]
+        g.bind(0, Y); g.bind(1, self.AR[n]); g.bind(2, self._z(self.LA[n]))
+        self.F[n] = ops.GradNormRight(g)
+        tol = self.fixed_tol if self.fixed_tol else min(max(self.prec[n] / 100.0, 5e-16), 1e-6)
+        # H_AC eigensolve (eigs_rs "SA", x0 = AC)
+        ev, na, _ = ops.eigs_rs(hac, AC, tol, maxit=self.lanczos_maxit)
+        self.stats["lanczos_applies"] += na
+        self.stats["hac_applies"] += na + 1
+        # H_C eigensolves for CL = C[n] (EHL, EHR1) and CR = C[n+1] (EHL1, EHR)
+        pl = self.p_hcl[n]
+        pl.bind(2, self.EHL); pl.bind(3, self.EHR1); pl.bind(4, self.AL[m]); pl.bind(5, self.AR[n]); pl.prepare()
+        pr = self.p_hcr[n]
+        pr.bind(2, self.EHL1); pr.bind(3, self.EHR); pr.bind(4, self.AL[n]); pr.bind(5, self.AR[m]); pr.prepare()
+        CL, CR = self.C[l].clone(), self.C[r].clone()
+        _, na1, _ = ops.eigs_rs(pl, CL, tol, maxit=self.lanczos_maxit)
+        _, na2, _ = ops.eigs_rs(pr, CR, tol, maxit=self.lanczos_maxit)
+        self.stats["lanczos_applies"] += na1 + na2
+        ops.sign_normalize(ctx, CL)
+        ops.sign_normalize(ctx, CR)
+        if self.dosvd and self.prec[n] < self.svdthresh:
+            self.dosvd = False
+        ALnew, ARnew = self._z(self.LA[n]), self._z(self.LA[n])
+        if self.dosvd:
+            # polar: AL = U V^T of AC CR^T ; AR = U V^T of CL^T AC  (VUMPS_main.cpp:213-220)
+            X = self._mul(self.p_mul_r_t[n], AC, CR, self._z(self.LA[n]))
+            U, V = self._z(self.LA[n]), self._z(self.dec_ac_l[n].rlayout)
+            ops.svd(self.dec_ac_l[n], X, U, None, V)
+            self._mul(self.p_mul_r[n], U, V, ALnew)
+            X = self._mul(self.p_mul_l_t[n], AC, CL, self._z(self.LA[n]))
+            U, V = self._z(self.LA[n]), self._z(self.dec_ac_r[n].rlayout)
+            ops.svd(self.dec_ac_r[n], X, U, None, V)
+            self._mul(self.p_mul_l[n], U, V, ARnew)
+        else:
+            # QR scheme (VUMPS_main.cpp:221-234)
+            QL, Rt = self._z(self.LA[n]), self._z(self.dec_ac_l[n].rlayout)
+            ops.qr(self.dec_ac_l[n], AC, QL, Rt)
+            PL = self._z(self.LB[r])
+            ops.qr(self.dec_b_l[r], CR, PL, self._z(self.LB[r]))
+            self._mul(self.p_mul_r_t[n], QL, PL, ALnew)
+            QR, Rt2 = self._z(self.LA[n]), self._z(self.dec_ac_r[n].rlayout)
+            ops.qr(self.dec_ac_r[n], AC, QR, Rt2)
+            PR = self._z(self.LB[l])
+            ops.qr(self.dec_b_r[l], CL, PR, self._z(self.LB[l]))
+            self._mul(self.p_mul_l_t[n], QR, PR, ARnew)
+        # errors err_l = |AC - AL CR|_inf, err_r = |AC - CL AR|_inf
+        t = self._mul(self.p_mul_r[n], ALnew, CR, self._z(self.LA[n]))
+        err_l = ops.norm_inf(ctx, ops.axpby(ctx, 1.0, AC, -1.0, t))
+        t = self._mul(self.p_mul_l[n], ARnew, CL, self._z(self.LA[n]))
+        err_r = ops.norm_inf(ctx, ops.axpby(ctx, 1.0, AC, -1.0, t))
+        self.prec[n] = max(err_l, err_r)
+        self.AL[n], self.AR[n], self.C[r], self.C[l] = ALnew, ARnew, CR, CL
+        # left environment: R = CL CL^T, fixed point of [AL(n), AL(n+1)], EHL on bond n
+        gtol = max(tol / self.InvEfac, self.InvETol)
+        R = self._cct(l, right=True)
+        if self.trueLR:
+            R = self._tm_dominant(("R", n), R, 1e-15)
+        HAL = self._get_hl(n)
+        self.EHL = self._invert_e(("L", n), HAL, self._eye(l), R, "l", self.EHL, gtol)
+        # shift to site n+1: EHLtmp = OpTM(AL(n-1) AL(n)) + T_L(AL(n), EHL) on bond n+1
+        EHLtmp = ops.axpby(ctx, 1.0, self._optm(True, m, self.AL, self._z(self.LB[r])), 1.0,
+                           self._tm(("L1", n), self.AL, self.EHL, self._z(self.LB[r])))
+        self.EHL1 = ops.axpby(ctx, 1.0, self._optm(True, n, self.AL, self._z(self.LB[l])), 1.0,
+                              self._tm(("L1", m), self.AL, EHLtmp, self._z(self.LB[l])))
+        # right environment for site n+1: L = C^T C on bond n (= bond n+2), [AR(n), AR(n+1)]
+        Lm = self._cct(l, right=False)
+        if self.trueLR:
+            Lm = self._tm_dominant(("L", n), Lm, 1e-15)
+        HAR = self._get_hr(n)
+        y0 = self.EHR0[m]
+        self.EHR = self._invert_e(("R", n), HAR, Lm, self._eye(l), "r", y0, gtol)
+        self.EHL = EHLtmp
+        self.EHR1 = ops.axpby(ctx, 1.0, self._tm(("R1", m), self.AR, self.EHR, self._z(self.LB[r])), 1.0,
+                              self._optm(False, m, self.AR, self._z(self.LB[r])))
+        # HL = ReducedOp(H, AL(n), l), HR = ReducedOp(H, AR(n), r) (VUMPS_main.cpp:311-312)
+        self._redops((n,))
+
+    def sweep(self):
+        """One iteration of the outer loop (VUMPS_main.cpp:165-354); returns (E, F, prec)."""
+        for n in range(2):
+            self.site_update(n)
+        self.E = self.energy()
+        return self.E, self.F.copy(), self.prec.copy()
+
+    def energy(self):
+        """MeasureObservables(H, AR, L) (MPSBlockUtilities.hpp:1017-1073): E(k) =
+        tr(L_k OpTM_R(AR(k) AR(k+1))) with L_k = C[k]^T C[k]."""
+        E = []
+        for k in range(2):
+            X = self._optm(False, k, self.AR, self._z(self.LB[k]))
+            Lk = self._cct(k, right=False)
+            E.append(ops.bd_trace_prod(self.ctx, self.LB[k], Lk, X))
+        return np.array(E)
+
+    def host_state(self):
+        t = lambda x: x.cpu().numpy()
+        return {"AL": [t(a) for a in self.AL], "AR": [t(a) for a in self.AR], "C": [t(c) for c in self.C]}

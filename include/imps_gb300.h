@@ -56,8 +56,11 @@ const char* imps_status_string(int status);
 int imps_version(void);
 int imps_ctx_create(int device, imps_ctx** out);
 int imps_ctx_destroy(imps_ctx* ctx);
-/* use an existing cudaStream_t (e.g. torch's current stream); NULL = the context's own stream */
+/* launch on an existing cudaStream_t (e.g. torch's current stream), used as given:
+ * NULL is the CUDA legacy default stream.  imps_ctx_use_own_stream restores the context's
+ * own non-blocking stream (the default after imps_ctx_create). */
 int imps_ctx_set_stream(imps_ctx* ctx, void* cuda_stream);
+int imps_ctx_use_own_stream(imps_ctx* ctx);
 int imps_ctx_synchronize(imps_ctx* ctx);
 
 /* ---- sector tables (replaces the std::map sector bookkeeping of BlockObj.hpp:506-600,
@@ -158,8 +161,35 @@ int imps_tm_dominant(imps_plan* tm, const double* x0, double* V, int mem, double
  * already stored in the grad plan's slot 0 and AR in slot 1. */
 int imps_grad_norm_right(imps_plan* grad, double* F);
 
-/* ---- Krylov BLAS-1 (K5) on device vectors, for callers that drive their own solvers ---- */
+/* ---- per-sector decompositions ------------------------------------------------------------ */
+/* Sector tables of GetDenseMat (MPSBlockMat.hpp:468-526): dir l groups blocks by outgoing
+ * charge (rows stacked over s), dir r by incoming charge (columns stacked over s).  A is an
+ * MPS layout or a BlockDiagMat layout.  Derived layout 0 = A's layout (Q / isometry),
+ * derived layout 1 = BlockDiagMat over the sectors (R / DiagIso). */
+int imps_plan_decomp(imps_ctx* ctx, const imps_layout* A, int dir, imps_plan** out);
+/* qr(R, MPS, dir) / qr(R, BlockDiagMat, dir) with qr_pos sign convention, diag(R) >= 0
+ * (MPSBlockUtilities.hpp:181-244, BlockObj.hpp:2422-2459, helpers.hpp:181-195).  Device
+ * pointers only; every sector needs stacked dimension >= sector dimension. */
+int imps_sector_qr(imps_plan* dec, const double* A, double* Q, double* R, int mem);
+/* svd(S, DiagIso, MPS, dir) (MPSBlockUtilities.hpp:78-153): U = MPSIso (A's layout), S =
+ * singular values per sector concatenated in sector order (descending), Viso = DiagIso
+ * (V^T for dir l, U for dir r).  Any output may be NULL.  One-sided Jacobi, FP64. */
+int imps_sector_svd(imps_plan* dec, const double* A, double* U, double* S, double* Viso, int mem);
+/* X_q[:, j] *= S_q[j]^power on a BlockDiagMat decomposition plan (BlockDiagMat << BlockLam,
+ * BlockObj.hpp:2316), e.g. U * sqrt(S) in randMPS_LR (MPSBlockUtilities.hpp:1116-1118) */
+int imps_sector_colscale(imps_plan* dec, double* X, const double* S, double power, int mem);
+
+/* ---- Krylov BLAS-1 (K5) and device-vector helpers for drivers ---------------------------- */
 int imps_dot(imps_ctx* ctx, const double* x, const double* y, int64_t n, double* result);
+/* sum over BlockDiagMat sectors of trace(X_q * Y_q) (InvEBlockFunctions.hpp:28-33) */
+int imps_bd_trace_prod(imps_ctx* ctx, imps_layout* L, const double* X, const double* Y,
+                       double* result);
+/* max_i |x_i| (norm_inf, helpers.hpp:148-151) */
+int imps_absmax(imps_ctx* ctx, const double* x, int64_t n, double* result);
+/* y = a*x + b*y */
+int imps_axpby(imps_ctx* ctx, double a, const double* x, double b, double* y, int64_t n);
+/* x /= sign(x[0]) (VUMPS_main.cpp:201-202) */
+int imps_sign_normalize(imps_ctx* ctx, double* x, int64_t n);
 
 #ifdef __cplusplus
 }

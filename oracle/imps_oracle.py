@@ -872,14 +872,18 @@ class VUMPS:
     """Restatement of one VUMPS_main run with ExpandFromH disabled (mmax = D)."""
 
     def __init__(self, h, d, I2K, dmap0, N=2, seed=1, InvETol=5e-15, InvEfac=2.0, fixed_tol=None,
-                 trueLR=True, svdthresh=5e-7):
+                 trueLR=True, svdthresh=5e-7, dimvec=None, init=None):
         self.hnnz = sparse_nnz(h)
         self.d, self.N, self.I2K = d, N, I2K
         self.InvETol, self.InvEfac, self.fixed_tol, self.trueLR = InvETol, InvEfac, fixed_tol, trueLR
         self.svdthresh = svdthresh
         self.rng = np.random.default_rng(seed)
-        dimvec = make_dims(dmap0, N, I2K)
-        AL, AR, C = randMPS_LR(N, I2K, dimvec, self.rng)
+        if dimvec is None:
+            dimvec = make_dims(dmap0, N, I2K)
+        if init is None:
+            AL, AR, C = randMPS_LR(N, I2K, dimvec, self.rng)
+        else:
+            AL, AR, C = [list(x) for x in init]
         L = [bd_mul(bd_t(c), c) for c in C]
         R = [bd_mul(c, bd_t(c)) for c in C]
         AR = shift(AR, -1)
