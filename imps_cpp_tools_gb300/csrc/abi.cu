@@ -61,6 +61,8 @@ struct imps_plan {
 };
 
 constexpr int PLAN_DECOMP = 12;
+constexpr double kMixedEigTol = 2e-7;    // Ritz-residual floor of split-BF16 applies
+constexpr double kMixedInnerTol = 1e-6;  // residual reduction per mixed GMRES cycle
 
 namespace {
 
@@ -129,10 +131,17 @@ int run_stages(imps_plan* p, std::vector<Stage>& stages) {
   if (p->ctx->device < 0) return IMPS_ERR_NO_DEVICE;
   imps_dslots sl{};
   for (size_t i = 0; i < p->P.slots.size() && i < (size_t)kMaxSlots; ++i) sl.p[i] = p->P.slots[i].dptr;
-  for (size_t i = 0; i < p->P.slots.size(); ++i)
-    if (!p->P.slots[i].dptr && p->P.slots[i].nelem > 0) return IMPS_ERR_BAD_ARG;  // unbound slot
+  // every slot the stages read or write must be bound
+  for (const Stage& S : stages) {
+    for (const Term& t : S.terms)
+      if (!sl.p[t.a_slot] || !sl.p[t.b_slot]) return IMPS_ERR_BAD_ARG;
+    for (const OutBlock& o : S.outs)
+      if (!sl.p[o.c_slot]) return IMPS_ERR_BAD_ARG;
+  }
+  // operator-dependent prepare stages always run in FP64; only apply stages use tensor cores
+  const bool tc = p->prec == IMPS_PREC_BF16X6 && p->tc && &stages == &p->P.stages;
   for (Stage& S : stages) {
-    if (p->prec == IMPS_PREC_BF16X6 && p->tc) {
+    if (tc) {
       RC(tc_run_stage(p->tc, S, sl, p->ctx->stream));
     } else {
       RC(imps_launch_grouped_f64(S.d_tiles, (int)S.tiles.size(), S.d_terms, sl, S.tile_m, p->ctx->stream));
@@ -511,6 +520,9 @@ int imps_plan_slot_info(const imps_plan* p, int slot, int* kind, int64_t* nelem)
 int imps_plan_bind(imps_plan* p, int slot, double* ptr) {
   if (!p || slot < 0 || slot >= (int)p->P.slots.size()) return IMPS_ERR_BAD_ARG;
   if (p->P.slots[slot].kind != SLOT_EXTERNAL) return IMPS_ERR_BAD_ARG;
+  // (re)binding an operator slot means its contents may have changed: the tensor-core
+  // operand packs are rebuilt on the next run
+  if (p->tc && slot != p->P.n_in && slot != p->P.n_out) tc_invalidate(p->tc);
   p->P.slots[slot].dptr = ptr;
   return IMPS_OK;
 }
@@ -647,7 +659,9 @@ int imps_eigs_rs(imps_plan* p, double* x, int mem, double tol, int ncv, int maxi
   if (m > n) m = (int)n;
   if (m > kMaxCols - 2) m = kMaxCols - 2;
   if (m < 2) m = 2;
+  // maxit counts restart cycles, as ARPACK's IPARAM(3) (eigs.cpp:384, 399)
   if (maxit <= 0) maxit = (int)std::min<int64_t>(n, 100000);
+  const int64_t max_applies = (int64_t)maxit * m;
   const int ld = m + 1;
   RC(arena_reserve(c, round256(n * 8) * (m + 4) + round256((size_t)ld * ld * 8) + 4096));
   Bump bp{c->arena};
@@ -686,7 +700,7 @@ int imps_eigs_rs(imps_plan* p, double* x, int mem, double tol, int ncv, int maxi
       RC(kr_multidot(c->ws, w, n, 1, w, n, tmp, 0, hc + j + 1, st));
       RC(kr_scale_inv(w, hc + j + 1, V + (size_t)(j + 1) * n, n, bflag, st));
       jlast = j;
-      const bool check = ((j + 1 - jstart) % chk == 0) || j == m - 1 || applies >= maxit;
+      const bool check = ((j + 1 - jstart) % chk == 0) || j == m - 1 || applies >= max_applies;
       if (!check) continue;
       // pull the new columns and solve the small projected problem
       CK(cudaMemcpyAsync(H.data() + (size_t)jstart * ld, Hd + (size_t)jstart * ld,
@@ -708,12 +722,14 @@ int imps_eigs_rs(imps_plan* p, double* x, int mem, double tol, int ncv, int maxi
       const double beta = H[(j + 1) + (size_t)j * ld];
       const double res = std::fabs(beta * y[k - 1]);
       if (!std::isfinite(theta)) return IMPS_ERR_NAN;
-      if (res <= tol * std::max(std::fabs(theta), 1e-300) || hbreak) {
+      // split-BF16 applies carry ~1e-7 relative error: their Ritz residual floors there
+      const double tol_eff = p->prec == IMPS_PREC_BF16X6 ? std::max(tol, kMixedEigTol) : tol;
+      if (res <= tol_eff * std::max(std::fabs(theta), 1e-300) || hbreak) {
         status = IMPS_OK;
         done = true;
         break;
       }
-      if (applies >= maxit) { done = true; break; }
+      if (applies >= max_applies) { done = true; break; }
     }
     // Ritz vector x = V[:, 0..k-1] y
     const int k = jlast + 1;
@@ -785,9 +801,17 @@ static int gmres_proj(imps_plan* p, const double* b, double* y, const double* rh
     return IMPS_OK;
   }
   std::vector<double> Rh((size_t)ld * ld), gh(ld), yh(ld);
+  // Mixed precision: every restart recomputes the true residual with the FP64 engine and the
+  // inner Krylov cycle (split-BF16 applies) only has to reduce it by kMixedInnerTol, i.e.
+  // restarted GMRES acts as iterative refinement with FP64 residuals.
+  const int prec_saved = p->prec;
+  const bool mixed = prec_saved == IMPS_PREC_BF16X6;
   for (int outer = 0; it < maxit; ++outer) {
     // r = b - A(y)  (FP64 residual)
-    RC(proj_apply_dev(p, y, rho_in, rho_out, w, t, dsc));
+    p->prec = IMPS_PREC_FP64;
+    int rc_res = proj_apply_dev(p, y, rho_in, rho_out, w, t, dsc);
+    p->prec = prec_saved;
+    RC(rc_res);
     RC(kr_axpby(1.0, b, -1.0, w, n, st));
     RC(kr_multidot(c->ws, w, n, 1, w, n, tmp, 0, dsc + 1, st));
     double rn = 0.0;
@@ -822,7 +846,7 @@ static int gmres_proj(imps_plan* p, const double* b, double* y, const double* rh
         CK(cudaStreamSynchronize(st));
         if (!std::isfinite(res)) return IMPS_ERR_NAN;
         if (brk) { kdim = j; break; }  // invariant subspace
-        if (res < tol * bnorm) break;
+        if (res < std::max(tol * bnorm, mixed ? kMixedInnerTol * rn : 0.0)) break;
       }
     }
     // y += V[:, :kdim] * R^{-1} gamma
@@ -841,8 +865,11 @@ static int gmres_proj(imps_plan* p, const double* b, double* y, const double* rh
     }
   }
   if (status != IMPS_OK) {
-    // final explicit residual
-    RC(proj_apply_dev(p, y, rho_in, rho_out, w, t, dsc));
+    // final explicit residual (FP64)
+    p->prec = IMPS_PREC_FP64;
+    int rc_res = proj_apply_dev(p, y, rho_in, rho_out, w, t, dsc);
+    p->prec = prec_saved;
+    RC(rc_res);
     RC(kr_axpby(1.0, b, -1.0, w, n, st));
     RC(kr_multidot(c->ws, w, n, 1, w, n, tmp, 0, dsc + 1, st));
     double rn = 0.0;

@@ -95,7 +95,10 @@ class VumpsGPU:
             pass
         self.flops_hac = [p.info()["flops_apply"] for p in self.p_hac]
         if self.precision == "bf16x6":
-            for p in self.p_hac + self.p_hcl + self.p_hcr:
+            # tensor-core applies inside the Krylov solvers; Krylov vectors, residuals,
+            # decompositions and the energy stay FP64
+            mixed = self.p_hac + self.p_hcl + self.p_hcr + [self.tm[(k, n)] for k in ("L", "R") for n in range(2)]
+            for p in mixed:
                 p.set_precision(N.PREC_BF16X6)
 
     # ------------------------------------------------------------------ small helpers
@@ -149,18 +152,26 @@ class VumpsGPU:
         t2 = self._optm(False, n, self.AR, self._z(self.LB[n]))      # OpTM(AR(n) AR(n+1)) on bond n
         return ops.axpby(self.ctx, 1.0, t2, 1.0, out)
 
-    def _invert_e(self, key, x, L, R, direction, y0, tol):
+    def _bind_uc(self, key, A):
+        p = self.tm[key]
+        n = key[1]
+        p.bind(2, A[n]); p.bind(3, A[1 - n])
+        return p
+
+    def _invert_e(self, key, A, x, L, R, direction, y0, tol):
+        """InvertE_proj on the unit cell [A(n), A(n+1)], n = key[1]."""
         y = y0.clone() if y0 is not None else self._z_like(x)
-        it, rr, conv = ops.InvertE_proj(self.tm[key], x, L, R, direction, y, tol, maxit=self.gmres_maxit)
+        it, rr, conv = ops.InvertE_proj(self._bind_uc(key, A), x, L, R, direction, y, tol, maxit=self.gmres_maxit)
         self.stats["gmres_iters"] += it
         return y
 
     def _z_like(self, x):
         return self.torch.zeros_like(x)
 
-    def _tm_dominant(self, key, x0, tol):
+    def _tm_dominant(self, key, A, x0, tol):
+        """TMDominantEig on the unit cell [A(n), A(n+1)], n = key[1]."""
         V = self._z_like(x0)
-        _, it, _ = ops.TMDominantEig(self.tm[key], V, x0, tol, maxit=self.gmres_maxit)
+        _, it, _ = ops.TMDominantEig(self._bind_uc(key, A), V, x0, tol, maxit=self.gmres_maxit)
         self.stats["gmres_iters"] += it
         return V
 
@@ -173,7 +184,7 @@ class VumpsGPU:
             Rb = self._z(self.dec_ac_l[n].rlayout)
             ops.qr(self.dec_ac_l[n], X, self.AL[n], Rb)
         # right fixed point of [AL(0), AL(1)] on bond 0, C = qr(U sqrt(S), r).R
-        R = self._tm_dominant(("R", 0), None if False else self._eye(0), 1e-14)
+        R = self._tm_dominant(("R", 0), self.AL, self._eye(0), 1e-14)
         U = self._z(self.LB[0])
         S = torch.zeros(self.dec_b_l[0].nsv, dtype=torch.float64, device="cuda")
         ops.svd(self.dec_b_l[0], R, U, S, None)
@@ -196,8 +207,8 @@ class VumpsGPU:
         # C[0]^T C[0] (the reference's initial shift puts these at the unit-cell boundary)
         R = self._cct(0, right=True)
         L = self._cct(0, right=False)
-        self.EHL = self._invert_e(("L", 0), self._get_hl(0), self._eye(0), R, "l", None, self.InvETol)
-        self.EHR = self._invert_e(("R", 1), self._get_hr(1), L if False else self._cct(1, right=False),
+        self.EHL = self._invert_e(("L", 0), self.AL, self._get_hl(0), self._eye(0), R, "l", None, self.InvETol)
+        self.EHR = self._invert_e(("R", 1), self.AR, self._get_hr(1), self._cct(1, right=False),
                                   self._eye(1), "r", None, self.InvETol)
         self.EHL1 = ops.axpby(self.ctx, 1.0, self._optm(True, 1, self.AL, self._z(self.LB[1])), 1.0,
                               self._tm(("L1", 0), self.AL, self.EHL, self._z(self.LB[1])))
@@ -231,6 +242,7 @@ class VumpsGPU:
         hac = self.p_hac[n]
         hac.bind(2, self.EHL); hac.bind(3, self.EHR)
         hac.bind(4, self.HLbuf[m]); hac.bind(5, self.HRbuf[m])
+        hac.prepare()  # operators changed (re-packs tensor-core operands in mixed mode)
         # gradient norm (GradNormRight, VUMPS_helpers.hpp:145-153) at AC = C[n] AR(n)
         AC = self._mul(self.p_ac[n], self.AR[n], self.C[l], self._z(self.LA[n]))
         Y = self._z(self.LA[n])
@@ -290,9 +302,9 @@ class VumpsGPU:
         gtol = max(tol / self.InvEfac, self.InvETol)
         R = self._cct(l, right=True)
         if self.trueLR:
-            R = self._tm_dominant(("R", n), R, 1e-15)
+            R = self._tm_dominant(("R", n), self.AL, R, 1e-15)
         HAL = self._get_hl(n)
-        self.EHL = self._invert_e(("L", n), HAL, self._eye(l), R, "l", self.EHL, gtol)
+        self.EHL = self._invert_e(("L", n), self.AL, HAL, self._eye(l), R, "l", self.EHL, gtol)
         # shift to site n+1: EHLtmp = OpTM(AL(n-1) AL(n)) + T_L(AL(n), EHL) on bond n+1
         EHLtmp = ops.axpby(ctx, 1.0, self._optm(True, m, self.AL, self._z(self.LB[r])), 1.0,
                            self._tm(("L1", n), self.AL, self.EHL, self._z(self.LB[r])))
@@ -301,10 +313,10 @@ class VumpsGPU:
         # right environment for site n+1: L = C^T C on bond n (= bond n+2), [AR(n), AR(n+1)]
         Lm = self._cct(l, right=False)
         if self.trueLR:
-            Lm = self._tm_dominant(("L", n), Lm, 1e-15)
+            Lm = self._tm_dominant(("L", n), self.AR, Lm, 1e-15)
         HAR = self._get_hr(n)
         y0 = self.EHR0[m]
-        self.EHR = self._invert_e(("R", n), HAR, Lm, self._eye(l), "r", y0, gtol)
+        self.EHR = self._invert_e(("R", n), self.AR, HAR, Lm, self._eye(l), "r", y0, gtol)
         self.EHL = EHLtmp
         self.EHR1 = ops.axpby(ctx, 1.0, self._tm(("R1", m), self.AR, self.EHR, self._z(self.LB[r])), 1.0,
                               self._optm(False, m, self.AR, self._z(self.LB[r])))
