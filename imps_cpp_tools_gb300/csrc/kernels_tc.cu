@@ -39,7 +39,10 @@ constexpr int TC_THREADS = 128;
 constexpr int A_STAGE_BYTES = TC_KSTAGE * 3 * TC_M * 32;     // 24 KB
 constexpr int B_STAGE_BYTES = TC_KSTAGE * 3 * TC_NMAX * 32;  // 24 KB
 constexpr int STAGE_BYTES = A_STAGE_BYTES + B_STAGE_BYTES;
-constexpr int SMEM_BYTES = TC_NSTAGE * STAGE_BYTES + 1024;   // + alignment slack
+// the whole opt-in shared memory of the SM: pipeline (4 x 48 KB) + alignment slack + headroom
+// so that every descriptor-addressed access stays inside this CTA's allocation
+constexpr int SMEM_BYTES = 232448;
+static_assert(TC_NSTAGE * STAGE_BYTES + 1024 <= SMEM_BYTES, "tcgen05 pipeline does not fit");
 constexpr uint32_t WAIT_LIMIT = 1u << 24;
 
 struct TcTerm {
