@@ -673,6 +673,8 @@ int imps_eigs_rs(imps_plan* p, double* x, int mem, double tol, int ncv, int maxi
   double* nrm = c->dscal + 8;
   int* bflag = c->dflag;
   CK(cudaMemsetAsync(bflag, 0, sizeof(int), st));
+  // projected matrix: rows below the subdiagonal are never written, they must read as zero
+  CK(cudaMemsetAsync(Hd, 0, (size_t)ld * ld * 8, st));
   if (mem == IMPS_MEM_HOST) CK(cudaMemcpyAsync(xr, x, n * 8, cudaMemcpyHostToDevice, st));
   else CK(cudaMemcpyAsync(xr, x, n * 8, cudaMemcpyDeviceToDevice, st));
   RC(kr_multidot(c->ws, xr, n, 1, xr, n, tmp, 0, nrm, st));

@@ -20,6 +20,7 @@
 
 #include <algorithm>
 #include <cstdint>
+#include <cstdio>
 #include <map>
 #include <tuple>
 #include <vector>
@@ -41,7 +42,7 @@ constexpr int B_STAGE_BYTES = TC_KSTAGE * 3 * TC_NMAX * 32;  // 24 KB
 constexpr int STAGE_BYTES = A_STAGE_BYTES + B_STAGE_BYTES;
 // the whole opt-in shared memory of the SM: pipeline (4 x 48 KB) + alignment slack + headroom
 // so that every descriptor-addressed access stays inside this CTA's allocation
-constexpr int SMEM_BYTES = 232448;
+constexpr int SMEM_BYTES = 230400;  // 225 KB (opt-in maximum 227 KB minus static shared memory)
 static_assert(TC_NSTAGE * STAGE_BYTES + 1024 <= SMEM_BYTES, "tcgen05 pipeline does not fit");
 constexpr uint32_t WAIT_LIMIT = 1u << 24;
 
@@ -421,9 +422,13 @@ int tc_create(TcPlan** out, const Plan& P, cudaStream_t st) {
     rc = IMPS_ERR_OOM;
   if (!rc && cudaMalloc(&T->d_err, sizeof(int)) != cudaSuccess) rc = IMPS_ERR_OOM;
   if (!rc) cudaMemsetAsync(T->d_err, 0, sizeof(int), st);
-  if (!rc && cudaFuncSetAttribute(tc_gemm_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, SMEM_BYTES) !=
-                 cudaSuccess)
-    rc = IMPS_ERR_CUDA;
+  if (!rc) {
+    cudaError_t e = cudaFuncSetAttribute(tc_gemm_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, SMEM_BYTES);
+    if (e != cudaSuccess) {
+      fprintf(stderr, "imps_gb300: tcgen05 kernel setup failed: %s\n", cudaGetErrorString(e));
+      rc = IMPS_ERR_CUDA;
+    }
+  }
   if (rc) { tc_destroy(T); return rc; }
   T->first_stage = P.stages.empty() ? nullptr : &P.stages[0];
   *out = T;

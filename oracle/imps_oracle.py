@@ -567,47 +567,50 @@ def gmres(Afun, b, x0, tol, maxit, krylovdim=0):
     bnorm = np.linalg.norm(b)
     rnorm = np.linalg.norm(r0)
     thresh = 2e-16
-    V = np.zeros((dim, krylovdim + 1), T)
-    H = np.zeros((krylovdim + 1, krylovdim + 1), T)
-    c = np.zeros(krylovdim + 1, T)
-    s = np.zeros(krylovdim + 1, T)
-    gamma = np.zeros(krylovdim + 1, T)
-    gamma[0] = rnorm
-    V[:, 0] = r0 / rnorm
+    # storage grows with the iteration count (the reference allocates dim x (krylovdim+1)
+    # uninitialised, which only touches the columns it uses)
+    V = [r0.astype(T) / rnorm]
+    Hcols = []
+    c, s = [], []
+    gamma = [T(rnorm)]
     kdim = 0
     for j in range(krylovdim):
-        w = Afun(V[:, j]).astype(T)
+        w = Afun(V[j]).astype(T)
+        h = np.zeros(j + 2, T)
         for i in range(j + 1):
-            H[i, j] = np.vdot(V[:, i], w)
-            w = w - H[i, j] * V[:, i]
-        H[j + 1, j] = np.linalg.norm(w)
+            h[i] = np.vdot(V[i], w)
+            w = w - h[i] * V[i]
+        h[j + 1] = np.linalg.norm(w)
         for i in range(j):
-            h1, h2 = H[i, j], H[i + 1, j]
-            H[i, j] = c[i] * h1 + s[i] * h2
-            H[i + 1, j] = -np.conj(s[i]) * h1 + c[i] * h2
-        beta = np.linalg.norm(H[j:j + 2, j])
+            h1, h2 = h[i], h[i + 1]
+            h[i] = c[i] * h1 + s[i] * h2
+            h[i + 1] = -np.conj(s[i]) * h1 + c[i] * h2
+        beta = np.linalg.norm(h[j:j + 2])
         if abs(beta) < thresh:
             flag = -2
             break
-        V[:, j + 1] = w / H[j + 1, j]
-        habs = abs(H[j, j])
-        phase = H[j, j] / habs
-        s[j] = phase * np.conj(H[j + 1, j]) / beta
-        c[j] = habs / beta
-        H[j, j] = phase * beta
-        H[j + 1, j] = 0
-        gamma[j + 1] = -np.conj(s[j]) * gamma[j]
+        V.append(w / h[j + 1])
+        habs = abs(h[j])
+        phase = h[j] / habs
+        s.append(phase * np.conj(h[j + 1]) / beta)
+        c.append(habs / beta)
+        h[j] = phase * beta
+        h[j + 1] = 0
+        gamma.append(-np.conj(s[j]) * gamma[j])
         gamma[j] *= c[j]
+        Hcols.append(h)
         kdim += 1
         rnorm = abs(gamma[j + 1])
         if rnorm < tol * bnorm:
             flag = kdim
             break
-    Hk = H[:kdim, :kdim]
     if kdim:
         from scipy.linalg import solve_triangular
-        alpha = solve_triangular(Hk, gamma[:kdim], lower=False)
-        x = x + V[:, :kdim] @ alpha
+        Hk = np.zeros((kdim, kdim), T)
+        for jj in range(kdim):
+            Hk[:jj + 1, jj] = Hcols[jj][:jj + 1]
+        alpha = solve_triangular(Hk, np.asarray(gamma[:kdim], T), lower=False)
+        x = x + np.stack(V[:kdim], axis=1) @ alpha
     return x, flag
 
 
