@@ -35,6 +35,7 @@ class ImpsError(RuntimeError):
 _PROTOS = {
     "imps_status_string": (C.c_char_p, [c_int]),
     "imps_version": (c_int, []),
+    "imps_launch_count": (c_i64, []),
     "imps_ctx_create": (c_int, [c_int, C.POINTER(c_vp)]),
     "imps_ctx_destroy": (c_int, [c_vp]),
     "imps_ctx_set_stream": (c_int, [c_vp, c_vp]),

@@ -60,6 +60,11 @@ struct imps_plan {
   DecompPlan* dc = nullptr;
 };
 
+std::atomic<long long>& imps::launch_counter() {
+  static std::atomic<long long> n{0};
+  return n;
+}
+
 constexpr int PLAN_DECOMP = 12;
 constexpr double kMixedEigTol = 2e-7;    // Ritz-residual floor of split-BF16 applies
 constexpr double kMixedInnerTol = 1e-6;  // residual reduction per mixed GMRES cycle
@@ -247,6 +252,8 @@ const char* imps_status_string(int s) {
 }
 
 int imps_version(void) { return 100; }
+
+int64_t imps_launch_count(void) { return (int64_t)imps::launch_counter().load(); }
 
 int imps_ctx_create(int device, imps_ctx** out) {
   if (!out) return IMPS_ERR_BAD_ARG;
@@ -945,6 +952,7 @@ int imps_tm_dominant(imps_plan* p, const double* x0, double* V, int mem, double 
   double* eye = bp.take(n);
   double* r0 = bp.take(n);
   double* v = bp.take(n);
+  imps::count_launch();
   imps_set_identity_kernel<<<std::max(p->nb_in, 1), 256, 0, st>>>(eye, p->d_boff, p->d_bdim, p->nb_in);
   if (x0) {
     CK(cudaMemcpyAsync(r0, x0, n * 8, mem == IMPS_MEM_HOST ? cudaMemcpyHostToDevice : cudaMemcpyDeviceToDevice, st));

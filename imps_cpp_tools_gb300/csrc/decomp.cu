@@ -294,32 +294,38 @@ __global__ void colscale_kernel(const imps::DenseMat* __restrict__ mats, double*
 namespace imps {
 
 int dc_colscale(const DenseMat* d_mats, int nmat, double* X, const double* S, double power, cudaStream_t st) {
+  if (nmat > 0) imps::count_launch();
   if (nmat > 0) colscale_kernel<<<nmat, 256, 0, st>>>(d_mats, X, S, power);
   return cudaGetLastError() == cudaSuccess ? IMPS_OK : IMPS_ERR_CUDA;
 }
 
 int dc_gather(const GatherEntry* d_ent, int nent, const double* src, double* dense, cudaStream_t st) {
+  if (nent > 0) imps::count_launch();
   if (nent > 0) gather_kernel<<<nent, 256, 0, st>>>(d_ent, nent, src, dense);
   return cudaGetLastError() == cudaSuccess ? IMPS_OK : IMPS_ERR_CUDA;
 }
 
 int dc_scatter(const GatherEntry* d_ent, int nent, const double* dense, double* dst, cudaStream_t st) {
+  if (nent > 0) imps::count_launch();
   if (nent > 0) scatter_kernel<<<nent, 256, 0, st>>>(d_ent, nent, dense, dst);
   return cudaGetLastError() == cudaSuccess ? IMPS_OK : IMPS_ERR_CUDA;
 }
 
 int dc_qr(const DenseMat* d_mats, int nmat, double* A, double* Q, double* R, int transpose_r, cudaStream_t st) {
+  if (nmat > 0) imps::count_launch();
   if (nmat > 0) qr_kernel<<<nmat, DT, 0, st>>>(d_mats, A, Q, R, transpose_r);
   return cudaGetLastError() == cudaSuccess ? IMPS_OK : IMPS_ERR_CUDA;
 }
 
 int dc_svd(const DenseMat* d_mats, int nmat, double* U, double* S, double* V, double* W, int* status,
            cudaStream_t st) {
+  if (nmat > 0) imps::count_launch();
   if (nmat > 0) svd_kernel<<<nmat, DT, 0, st>>>(d_mats, U, S, V, W, 40, status);
   return cudaGetLastError() == cudaSuccess ? IMPS_OK : IMPS_ERR_CUDA;
 }
 
 int dc_transpose_sq(const DenseMat* d_mats, int nmat, const double* X, double* Y, cudaStream_t st) {
+  if (nmat > 0) imps::count_launch();
   if (nmat > 0) transpose_kernel<<<nmat, 256, 0, st>>>(d_mats, X, Y, 1);
   return cudaGetLastError() == cudaSuccess ? IMPS_OK : IMPS_ERR_CUDA;
 }

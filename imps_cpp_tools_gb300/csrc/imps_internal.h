@@ -7,12 +7,17 @@
 // the reference performs in every apply) happens once, here, as integer tables; the GPU
 // only ever sees flat offsets into a few device buffers ("slots").
 #pragma once
+#include <atomic>
 #include <cstdint>
 #include <map>
 #include <string>
 #include <vector>
 
 namespace imps {
+
+// process-wide count of kernel launches issued by this library (imps_launch_count)
+std::atomic<long long>& launch_counter();
+inline void count_launch() { launch_counter().fetch_add(1, std::memory_order_relaxed); }
 
 using Key = std::vector<int32_t>;
 

@@ -5,6 +5,8 @@
 #include <cstddef>
 #include <cstdint>
 
+#include "imps_internal.h"
+
 namespace imps {
 
 constexpr int kMaxCols = 64;  // max Krylov basis size handled by one projection kernel

@@ -100,9 +100,11 @@ int imps_launch_grouped_f64(const void* d_tiles, int ntiles, const void* d_terms
   if (ntiles <= 0) return IMPS_OK;
   cudaStream_t st = (cudaStream_t)stream;
   if (tile_m == 16) {
+    imps::count_launch();
     grouped_gemm_f64_kernel<16, 16, 2, 2><<<ntiles, 64, 0, st>>>((const Tile*)d_tiles,
                                                                  (const Term*)d_terms, slots);
   } else {
+    imps::count_launch();
     grouped_gemm_f64_kernel<32, 32, 2, 4><<<ntiles, 128, 0, st>>>((const Tile*)d_tiles,
                                                                   (const Term*)d_terms, slots);
   }

@@ -279,46 +279,54 @@ int kr_multidot(const KrylovWs& ws, const double* V, int64_t ldv, int ncols, con
   int grid = (int)((n + RB - 1) / RB);
   if (grid > RGRID) grid = RGRID;
   if (grid < 1) grid = 1;
+  imps::count_launch();
   multidot_kernel<<<grid, RB, 0, st>>>(V, ldv, ncols, w, n, ws.partials, ws.counter, h, mode, out_sqrt);
   return IMPS_OK;
 }
 
 int kr_gemv_sub(const double* V, int64_t ldv, int ncols, const double* h, double* w, int64_t n,
                 cudaStream_t st) {
+  imps::count_launch();
   gemv_sub_kernel<<<grid_for(n), 256, 0, st>>>(V, ldv, ncols, h, w, n);
   return IMPS_OK;
 }
 
 int kr_gemv(const double* V, int64_t ldv, int ncols, const double* h, double* y, int64_t n,
             cudaStream_t st) {
+  imps::count_launch();
   gemv_kernel<<<grid_for(n), 256, 0, st>>>(V, ldv, ncols, h, y, n);
   return IMPS_OK;
 }
 
 int kr_scale_inv(const double* x, const double* nrm, double* y, int64_t n, int* flag, cudaStream_t st) {
+  imps::count_launch();
   scale_inv_kernel<<<grid_for(n), 256, 0, st>>>(x, nrm, y, n, flag);
   return IMPS_OK;
 }
 
 int kr_axpby(double a, const double* x, double b, double* y, int64_t n, cudaStream_t st) {
+  imps::count_launch();
   axpby_kernel<<<grid_for(n), 256, 0, st>>>(a, x, b, y, n);
   return IMPS_OK;
 }
 
 int kr_proj_epilogue(const double* x, const double* t, const double* s, const double* rho, double* y,
                      int64_t n, cudaStream_t st) {
+  imps::count_launch();
   proj_epilogue_kernel<<<grid_for(n), 256, 0, st>>>(x, t, s, rho, y, n);
   return IMPS_OK;
 }
 
 int kr_trace_prod(const KrylovWs& ws, const double* X, const double* R, const int64_t* boff,
                   const int32_t* bdim, int nb, double* out, cudaStream_t st) {
+  imps::count_launch();
   trace_prod_kernel<<<32, RB, 0, st>>>(X, R, boff, bdim, nb, ws.partials, ws.counter, out);
   return IMPS_OK;
 }
 
 int kr_segsq(const KrylovWs& ws, const double* X, const int64_t* soff, const int64_t* slen, int ns,
              double* out, cudaStream_t st) {
+  imps::count_launch();
   segsq_kernel<<<64, RB, 0, st>>>(X, soff, slen, ns, ws.partials, ws.counter, out);
   return IMPS_OK;
 }
@@ -327,17 +335,20 @@ int kr_absmax(const KrylovWs& ws, const double* x, int64_t n, double* out, cudaS
   int grid = (int)((n + RB - 1) / RB);
   if (grid > RGRID) grid = RGRID;
   if (grid < 1) grid = 1;
+  imps::count_launch();
   absmax_kernel<<<grid, RB, 0, st>>>(x, n, ws.partials, ws.counter, out);
   return IMPS_OK;
 }
 
 int kr_givens(double* Hcol, int j, double* cs, double* sn, double* gamma, double* R, int ldr,
               double* res, int* breakdown, cudaStream_t st) {
+  imps::count_launch();
   givens_kernel<<<1, 32, 0, st>>>(Hcol, j, cs, sn, gamma, R, ldr, res, breakdown);
   return IMPS_OK;
 }
 
 int kr_sign_of_first(const double* x, double* s, cudaStream_t st) {
+  imps::count_launch();
   sign_first_kernel<<<1, 32, 0, st>>>(x, s);
   return IMPS_OK;
 }

@@ -453,6 +453,7 @@ int tc_invalidate(TcPlan* T) {
 static int launch_pack(const PackJob* d_jobs, int n, const imps_dslots& slots, __nv_bfloat16* out, cudaStream_t st) {
   if (n <= 0) return IMPS_OK;
   dim3 grid(n, 4);
+  imps::count_launch();
   pack_kernel<<<grid, 256, 0, st>>>(d_jobs, slots, out);
   return cudaGetLastError() == cudaSuccess ? IMPS_OK : IMPS_ERR_CUDA;
 }
@@ -470,6 +471,7 @@ int tc_run_stage(TcPlan* T, const Stage& S, const imps_dslots& slots, cudaStream
   int rc = launch_pack(ts.d_dyn, (int)ts.dyn_jobs.size(), slots, T->packed, st);
   if (rc) return rc;
   if (!ts.tiles.empty()) {
+    imps::count_launch();
     tc_gemm_kernel<<<(int)ts.tiles.size(), TC_THREADS, SMEM_BYTES, st>>>(ts.d_tiles, ts.d_terms, T->packed, slots,
                                                                         T->d_err);
     if (cudaGetLastError() != cudaSuccess) return IMPS_ERR_CUDA;

@@ -331,10 +331,12 @@ class VumpsGPU:
         return self.E, self.F.copy(), self.prec.copy()
 
     def energy(self):
-        """MeasureObservables(H, AR, L) (MPSBlockUtilities.hpp:1017-1073): E(k) =
-        tr(L_k OpTM_R(AR(k) AR(k+1))) with L_k = C[k]^T C[k]."""
+        """MeasureObservables(H, AR, L) (MPSBlockUtilities.hpp:1017-1073): the bond energy
+        tr(L_k OpTM_R(AR(k) AR(k+1))) with L_k = C[k]^T C[k], listed in the reference's
+        output order (its AR array is rotated by one, VUMPS_main.cpp:112, so E(0) is the
+        bond that starts at site 1)."""
         E = []
-        for k in range(2):
+        for k in (1, 0):
             X = self._optm(False, k, self.AR, self._z(self.LB[k]))
             Lk = self._cct(k, right=False)
             E.append(ops.bd_trace_prod(self.ctx, self.LB[k], Lk, X))

@@ -54,6 +54,8 @@ typedef struct imps_plan imps_plan;
 /* ---- library / context ------------------------------------------------------------------ */
 const char* imps_status_string(int status);
 int imps_version(void);
+/* number of GPU kernels this library has launched in the process so far */
+int64_t imps_launch_count(void);
 int imps_ctx_create(int device, imps_ctx** out);
 int imps_ctx_destroy(imps_ctx* ctx);
 /* launch on an existing cudaStream_t (e.g. torch's current stream), used as given:

@@ -875,8 +875,9 @@ class VUMPS:
     """Restatement of one VUMPS_main run with ExpandFromH disabled (mmax = D)."""
 
     def __init__(self, h, d, I2K, dmap0, N=2, seed=1, InvETol=5e-15, InvEfac=2.0, fixed_tol=None,
-                 trueLR=True, svdthresh=5e-7, dimvec=None, init=None):
+                 trueLR=True, svdthresh=5e-7, dimvec=None, init=None, gmres_maxit=0):
         self.hnnz = sparse_nnz(h)
+        self.gmres_maxit = gmres_maxit  # 0: the reference's maxit = problem size
         self.d, self.N, self.I2K = d, N, I2K
         self.InvETol, self.InvEfac, self.fixed_tol, self.trueLR = InvETol, InvEfac, fixed_tol, trueLR
         self.svdthresh = svdthresh
@@ -897,10 +898,10 @@ class VUMPS:
         self.HR = ReducedOp(hn, AR[0], d, "r")
         Rb = R[-1]
         self.EHL, _ = InvertE_proj(AL, GetHL(AL, hn), bd_eye({q: m.shape[1] for q, m in C[-1].items()}), Rb, "l",
-                                   InvETol, rng=self.rng)
+                                   InvETol, gmres_maxit, rng=self.rng)
         Lb = L[-1]
         self.EHR, _ = InvertE_proj(AR, GetHR(AR, hn), Lb, bd_eye({q: m.shape[0] for q, m in C[0].items()}), "r",
-                                   InvETol, rng=self.rng)
+                                   InvETol, gmres_maxit, rng=self.rng)
         self.EHL1 = bd_add(ApplyTMLeft(AL[0], self.EHL), ApplyOpTMLeftDiag(hn, mps_mul_mps(AL[-1], AL[0])))
         self.EHR1 = bd_add(ApplyTMRight(AR[-1], self.EHR), ApplyOpTMRightDiag(hn, mps_mul_mps(AR[-1], AR[0])))
         self.prec = np.ones(N)
@@ -956,7 +957,7 @@ class VUMPS:
         HAL = GetHL(AL, hn)
         AAL = mps_mul_mps(AL[-1], AL[0])
         gtol = max(tol / self.InvEfac, self.InvETol)
-        EHL, _ = InvertE_proj(AL, HAL, bd_eye({q: m.shape[1] for q, m in C[-1].items()}), Rm, "l", gtol, 0, EHL)
+        EHL, _ = InvertE_proj(AL, HAL, bd_eye({q: m.shape[1] for q, m in C[-1].items()}), Rm, "l", gtol, self.gmres_maxit, EHL)
         AL[:] = shift(AL, -1)
         AR[:] = shift(AR, -1)
         C[:] = shift(C, -1)
@@ -968,7 +969,7 @@ class VUMPS:
             _, Lm = TMDominantEig(AR, {q: m.shape[0] for q, m in Lm.items()}, "l", 1e-15, Lm)
         HAR = GetHR(AR, hn)
         EHR0_next = self.EHR0[(nn + 1) % N]
-        EHR, _ = InvertE_proj(AR, HAR, Lm, bd_eye({q: m.shape[0] for q, m in C[0].items()}), "r", gtol, 0, EHR0_next)
+        EHR, _ = InvertE_proj(AR, HAR, Lm, bd_eye({q: m.shape[0] for q, m in C[0].items()}), "r", gtol, self.gmres_maxit, EHR0_next)
         EHL = EHLtmp
         self.EHR1 = bd_add(ApplyTMRight(AR[-1], EHR), ApplyOpTMRightDiag(hn, mps_mul_mps(AR[-1], AR[0])))
         self.HL = ReducedOp(hn, AL[-1], d, "l")
