@@ -208,7 +208,8 @@ def _run_vumps(torch, ctx, precision, steps, warmup, stream, clocks=None):
     from imps_cpp_tools_gb300 import _native as N
     from imps_cpp_tools_gb300.vumps import VumpsGPU
     model, dims0, params = _xxz_params()
-    v = VumpsGPU(ctx, model, dims0=dims0, seed=1, fixed_tol=1e-12, InvETol=1e-12, precision=precision, **params)
+    v = VumpsGPU(ctx, model, dims0=dims0, seed=1, fixed_tol=1e-12, InvETol=1e-12, precision=precision,
+                 verbose=True, **params)
     for _ in range(warmup):
         v.sweep()
     torch.cuda.synchronize()

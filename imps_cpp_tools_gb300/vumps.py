@@ -20,9 +20,10 @@ from . import models, ops
 class VumpsGPU:
     def __init__(self, ctx, model, dims0=None, dimvec=None, seed=1, InvETol=5e-15, InvEfac=2.0,
                  fixed_tol=None, trueLR=True, svdthresh=5e-7, precision="fp64", init_state=None,
-                 lanczos_maxit=4000, gmres_maxit=20000, **params):
+                 lanczos_maxit=300, gmres_maxit=4000, verbose=False, **params):
         import torch
         self.torch = torch
+        self.verbose = verbose
         self.ctx = ctx
         self.d, self.I2K, h = models.build_model(model, **params)
         self.hnnz = models.h_nonzeros(h)
@@ -325,9 +326,17 @@ class VumpsGPU:
 
     def sweep(self):
         """One iteration of the outer loop (VUMPS_main.cpp:165-354); returns (E, F, prec)."""
+        import sys
+        import time
+        t0 = time.perf_counter()
+        s0 = dict(self.stats)
         for n in range(2):
             self.site_update(n)
         self.E = self.energy()
+        if self.verbose:
+            d = {k: self.stats[k] - s0.get(k, 0) for k in self.stats}
+            print(f"[vumps {self.precision}] sweep {time.perf_counter() - t0:.3f}s E={self.E.mean():.12f} "
+                  f"F={self.F.max():.3e} prec={self.prec.max():.3e} {d}", file=sys.stderr, flush=True)
         return self.E, self.F.copy(), self.prec.copy()
 
     def energy(self):
