@@ -1,0 +1,112 @@
+"""Checks against the committed golden fixtures (tests/golden/, made by make_golden.py with the
+oracle).  CPU: the planner reproduces the full-size sector-matching tables bit-exactly and the
+oracle reproduces its own stored outputs.  GPU: the kernels and the VUMPS driver reproduce the
+stored outputs (FP64 1e-12 relative; sweep energies 1e-9)."""
+import os
+
+import numpy as np
+import pytest
+
+from imps_cpp_tools_gb300 import blocks as B
+from oracle import imps_oracle as O
+
+HERE = os.path.join(os.path.dirname(os.path.abspath(__file__)), "golden")
+
+
+def load(name):
+    return dict(np.load(os.path.join(HERE, name)))
+
+
+def blocks_of(f, prefix):
+    g, qi, qo, r, c = (f[prefix + k] for k in ("_g", "_qin", "_qout", "_r", "_c"))
+    return [(int(g[i]), tuple(int(x) for x in qi[i]), tuple(int(x) for x in qo[i]), int(r[i]), int(c[i]))
+            for i in range(len(r))]
+
+
+def layout_of(f, prefix):
+    return B.Layout(blocks_of(f, prefix), int(f["nsym"]))
+
+
+@pytest.mark.parametrize("cfg", ["xxz_d512", "hubbard_d1024"])
+def test_full_size_sector_tables_bit_exact(cfg):
+    f = load(f"tables_{cfg}.npz")
+    ctx = B.Context(-1)
+    plan = B.plan_hac(ctx, layout_of(f, "ac"), layout_of(f, "ehl"), layout_of(f, "ehr"), layout_of(f, "hl"),
+                      layout_of(f, "hr"), int(f["d"]))
+    rows = []
+    for blk, (tag, terms) in enumerate(sorted(plan.table(0))):
+        for (a, ao, b, bo, k, al) in terms:
+            rows.append((tag, a, ao, b, bo))
+    got = np.array(rows, np.int64)
+    assert got.shape == f["pairs"].shape
+    assert np.array_equal(got, f["pairs"])
+
+
+def _sizes(blocks, d):
+    return [[(qi, qo, r, c) for (g, qi, qo, r, c) in blocks if g == s] for s in range(d)]
+
+
+def _redop(vec, blocks, d):
+    R = [[dict() for _ in range(d)] for _ in range(d)]
+    o = 0
+    for (g, qi, qo, r, c) in blocks:
+        R[g // d][g % d][qi] = (qo, vec[o:o + r * c].reshape(c, r).T.copy())
+        o += r * c
+    return R
+
+
+@pytest.mark.parametrize("model", ["xxz", "fhub"])
+def test_oracle_reproduces_hac_fixture(model):
+    f = load(f"hac_{model}.npz")
+    d = int(f["d"])
+    EHL = O.bd_from_vec(f["EHL"], [(b[1], b[3]) for b in blocks_of(f, "ehl")])
+    EHR = O.bd_from_vec(f["EHR"], [(b[1], b[3]) for b in blocks_of(f, "ehr")])
+    HL, HR = _redop(f["HL"], blocks_of(f, "hl"), d), _redop(f["HR"], blocks_of(f, "hr"), d)
+    y = O.ApplyHAvec(f["x"], _sizes(blocks_of(f, "ac"), d), EHL, EHR, HL, HR)
+    assert np.abs(y - f["y"]).max() <= 1e-13 * np.abs(f["y"]).max()
+
+
+@pytest.mark.gpu
+@pytest.mark.parametrize("model", ["xxz", "fhub"])
+def test_gpu_hac_matches_fixture(cuda_ctx, model):
+    from imps_cpp_tools_gb300 import ops
+    from tests.test_gpu_parity import dev, host, relerr
+    f = load(f"hac_{model}.npz")
+    plan = B.plan_hac(cuda_ctx, layout_of(f, "ac"), layout_of(f, "ehl"), layout_of(f, "ehr"), layout_of(f, "hl"),
+                      layout_of(f, "hr"), int(f["d"]))
+    for s, k in ((2, "EHL"), (3, "EHR"), (4, "HL"), (5, "HR")):
+        plan.bind(s, dev(f[k]))
+    out = dev(np.zeros_like(f["y"]))
+    ops.ApplyHAvec(plan, dev(f["x"]), out)
+    assert relerr(host(out), f["y"]) < 1e-12
+
+
+@pytest.mark.gpu
+@pytest.mark.parametrize("direction,key", [(0, "YL"), (1, "YR")])
+def test_gpu_tm_matches_fixture(cuda_ctx, direction, key):
+    from imps_cpp_tools_gb300 import ops
+    from tests.test_gpu_parity import dev, host, relerr
+    f = load("tm_xxz.npz")
+    bond = layout_of(f, "bond")
+    plan = B.plan_tm(cuda_ctx, [layout_of(f, "a0"), layout_of(f, "a1")], direction, bond, bond)
+    plan.bind(2, dev(f["A0"]))
+    plan.bind(3, dev(f["A1"]))
+    out = dev(np.zeros_like(f[key]))
+    ops.ApplyTM(plan, dev(f["X"]), out)
+    assert relerr(host(out), f[key]) < 1e-12
+
+
+@pytest.mark.gpu
+def test_gpu_vumps_matches_fixture(cuda_ctx):
+    from imps_cpp_tools_gb300.vumps import VumpsGPU
+    from tests.test_gpu_parity import dev
+    f = load("vumps_xxz.npz")
+    b0 = {(-4,): 3, (-2,): 8, (0,): 10, (2,): 8, (4,): 3}
+    b1 = {(-5,): 1, (-3,): 5, (-1,): 10, (1,): 10, (3,): 5, (5,): 1}
+    init = {"AL": [dev(f["AL0"]), dev(f["AL1"])], "AR": [dev(f["AR0"]), dev(f["AR1"])],
+            "C": [dev(f["C_bond0"]), dev(f["C_bond1"])]}
+    v = VumpsGPU(cuda_ctx, "xxz", dimvec=[b0, b1], init_state=init, fixed_tol=1e-12, J=1.0, Delta=-1.0)
+    for i in range(3):
+        E, F, prec = v.sweep()
+        assert np.abs(E - f["E"][i]).max() < 1e-9, (i, E, f["E"][i])
+        assert np.allclose(F, f["F"][i], rtol=1e-5, atol=1e-12)
