@@ -9,7 +9,8 @@
 
 namespace imps {
 
-constexpr int kMaxCols = 64;  // max Krylov basis size handled by one projection kernel
+constexpr int kMaxCols = 128;  // max Krylov basis size handled by one projection kernel
+constexpr int kGmresKrylov = 80;  // default restart length of the device GMRES
 
 struct KrylovWs {
   double* partials = nullptr;     // kr_partials_elems() doubles
