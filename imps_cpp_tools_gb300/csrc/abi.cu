@@ -781,7 +781,7 @@ static int gmres_proj(imps_plan* p, const double* b, double* y, const double* rh
   imps_ctx* c = p->ctx;
   cudaStream_t st = c->stream;
   const int64_t n = p->P.slots[0].nelem;
-  int m = krylov > 0 ? krylov : 40;
+  int m = krylov > 0 ? krylov : kGmresKrylov;
   if (m > kMaxCols - 2) m = kMaxCols - 2;
   if (m > n) m = (int)n;
   const int ld = m + 1;
@@ -902,7 +902,7 @@ int imps_invert_e_proj(imps_plan* p, const double* x, const double* L, const dou
   cudaStream_t st = c->stream;
   const int64_t n = p->P.slots[0].nelem;
   if (p->P.slots[1].nelem != n) return IMPS_ERR_BAD_ARG;
-  int m = krylov > 0 ? std::min(krylov, kMaxCols - 2) : 40;
+  int m = krylov > 0 ? std::min(krylov, kMaxCols - 2) : kGmresKrylov;
   if (maxit <= 0) maxit = (int)std::min<int64_t>(n, 100000);
   RC(arena_reserve(c, round256(n * 8) * (m + 12) + round256((size_t)(m + 1) * (m + 1) * 8) + 16 * 4096));
   Bump bp{c->arena};
@@ -948,7 +948,7 @@ int imps_tm_dominant(imps_plan* p, const double* x0, double* V, int mem, double 
   cudaStream_t st = c->stream;
   const int64_t n = p->P.slots[0].nelem;
   if (p->P.slots[1].nelem != n) return IMPS_ERR_BAD_ARG;
-  const int m = 40;
+  const int m = kGmresKrylov;
   if (maxit <= 0) maxit = (int)std::min<int64_t>(n, 100000);
   RC(arena_reserve(c, round256(n * 8) * (m + 14) + round256((size_t)(m + 1) * (m + 1) * 8) + 16 * 4096));
   Bump bp{c->arena};
