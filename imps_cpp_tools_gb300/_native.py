@@ -19,7 +19,8 @@ P_int = C.POINTER(C.c_int)
 
 STATUS = {0: "ok", 1: "not converged", -1: "bad argument", -2: "inconsistent sector table",
           -3: "CUDA error", -4: "NaN/Inf detected", -5: "timeout", -6: "no CUDA device",
-          -7: "out of device memory", -8: "unsupported"}
+          -7: "out of device memory", -8: "unsupported",
+          -9: "problem exceeds the fixed scratch of the no-allocation entry point"}
 
 MEM_HOST, MEM_DEVICE = 0, 1
 DIR_LEFT, DIR_RIGHT = 0, 1
@@ -71,6 +72,7 @@ _PROTOS = {
     "imps_hc_apply": (c_int, [c_vp, c_vp, c_vp, c_int]),
     "imps_tm_apply": (c_int, [c_vp, c_vp, c_vp, c_int]),
     "imps_tm_proj_apply": (c_int, [c_vp, c_vp, c_vp, c_vp, c_vp, c_int]),
+    "imps_tm_apply_noalloc": (c_int, [c_vp, c_vp, c_vp, c_int, c_vp, c_vp, c_vp, c_vp]),
     "imps_eigs_rs": (c_int, [c_vp, c_vp, c_int, c_dbl, c_int, c_int, P_dbl, P_int]),
     "imps_invert_e_proj": (c_int, [c_vp, c_vp, c_vp, c_vp, c_int, c_vp, c_int, c_dbl, c_int, c_int,
                                    P_int, P_dbl]),

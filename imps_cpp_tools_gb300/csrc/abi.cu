@@ -250,6 +250,7 @@ const char* imps_status_string(int s) {
     case IMPS_ERR_NO_DEVICE: return "no CUDA device";
     case IMPS_ERR_OOM: return "out of device memory";
     case IMPS_ERR_UNSUPPORTED: return "unsupported";
+    case IMPS_ERR_TOO_LARGE: return "problem exceeds the fixed scratch of the no-allocation entry point";
     default: return "unknown status";
   }
 }

@@ -11,3 +11,4 @@
 #define IMPS_ERR_NO_DEVICE -6
 #define IMPS_ERR_OOM -7
 #define IMPS_ERR_UNSUPPORTED -8
+#define IMPS_ERR_TOO_LARGE -9

@@ -37,6 +37,7 @@ extern "C" {
 #define IMPS_ERR_NO_DEVICE -6
 #define IMPS_ERR_OOM -7
 #define IMPS_ERR_UNSUPPORTED -8
+#define IMPS_ERR_TOO_LARGE -9 /* problem exceeds the fixed scratch of imps_tm_apply_noalloc */
 
 #define IMPS_MEM_HOST 0
 #define IMPS_MEM_DEVICE 1
@@ -162,6 +163,21 @@ int imps_tm_dominant(imps_plan* tm, const double* x0, double* V, int mem, double
 /* GradNormRight (VUMPS_helpers.hpp:145-153): F = norm_scaled(Y N_R^T), from Y = H_AC(C*AR)
  * already stored in the grad plan's slot 0 and AR in slot 1. */
 int imps_grad_norm_right(imps_plan* grad, double* F);
+
+/* ---- transfer-matrix apply without device allocation ------------------------------------
+ * No counterpart in the reference.  For callers that cannot call cudaMalloc when they apply
+ * the transfer matrix (device memory fully reserved up front by another allocator, or a
+ * latency-critical loop that must not pay cudaMalloc's implicit device synchronisation):
+ * Y = sum_s A_s^T X A_s (dir 0, as ApplyTMLeft) or sum_s A_s X A_s^T (dir 1, as
+ * ApplyTMRight) for one MPS tensor A (layout A, device data A_data) and BlockDiagMat X, Y
+ * (layouts in / out, device pointers), launched on cuda_stream.  Scratch and task tables live
+ * in fixed file-scope device arrays: A may hold at most 1,048,576 elements (8 MiB of
+ * scratch) and each of the two stages at most 8192 output tiles / 8192 GEMM terms; larger
+ * problems return IMPS_ERR_TOO_LARGE.  The first call on a device looks up the arrays'
+ * device address (do it before any stream capture).  All calls share the arrays: calls that
+ * overlap on the GPU race, and calls from several host threads must be serialised. */
+int imps_tm_apply_noalloc(const imps_layout* A, const imps_layout* in, const imps_layout* out, int dir,
+                          const double* A_data, const double* X, double* Y, void* cuda_stream);
 
 /* ---- per-sector decompositions ------------------------------------------------------------ */
 /* Sector tables of GetDenseMat (MPSBlockMat.hpp:468-526): dir l groups blocks by outgoing
