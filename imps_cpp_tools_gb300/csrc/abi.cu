@@ -674,9 +674,11 @@ int imps_eigs_rs(imps_plan* p, double* x, int mem, double tol, int ncv, int maxi
   if (maxit <= 0) maxit = (int)std::min<int64_t>(n, 100000);
   const int64_t max_applies = (int64_t)maxit * m;
   const int ld = m + 1;
-  RC(arena_reserve(c, round256(n * 8) * (m + 4) + round256((size_t)ld * ld * 8) + 4096));
+  const int kk = std::max(1, std::min(m / 2, m - 3));  // Ritz vectors kept at a thick restart
+  RC(arena_reserve(c, round256(n * 8) * (m + 4 + kk) + round256((size_t)ld * ld * 8) + 4096));
   Bump bp{c->arena};
   double* V = bp.take((size_t)n * (m + 1));
+  double* Wk = bp.take((size_t)n * kk);
   double* w = bp.take(n);
   double* xr = bp.take(n);
   double* Hd = bp.take((size_t)ld * ld);
@@ -749,17 +751,32 @@ int imps_eigs_rs(imps_plan* p, double* x, int mem, double tol, int ncv, int maxi
     CK(cudaMemcpyAsync(tmp, y.data(), k * 8, cudaMemcpyHostToDevice, st));
     RC(kr_gemv(V, n, k, tmp, xr, n, st));
     if (done) break;
-    // thick restart with (Ritz vector, residual direction)
+    // Thick restart (Wu & Simon): keep the kk lowest Ritz pairs of the m-step projection and
+    // the residual direction v_m; the projected matrix restarts as diag(theta_i) bordered by
+    // the couplings beta_m * y_i[m-1] (an arrowhead), and Lanczos continues from v_m with
+    // full CGS2 re-orthogonalisation against the kept vectors.
+    std::vector<int> idx(m);
+    for (int i = 0; i < m; ++i) idx[i] = i;
+    std::sort(idx.begin(), idx.end(), [&](int a, int b) { return evals[a] < evals[b]; });
     const double beta = H[(size_t)m + (size_t)(m - 1) * ld];
-    const double coup = beta * y[m - 1];
-    CK(cudaMemcpyAsync(V, xr, n * 8, cudaMemcpyDeviceToDevice, st));
-    CK(cudaMemcpyAsync(V + n, V + (size_t)m * n, n * 8, cudaMemcpyDeviceToDevice, st));
+    for (int i = 0; i < kk; ++i) {
+      std::vector<double> yi(m);
+      for (int r = 0; r < m; ++r) yi[r] = evecs[(size_t)r * m + idx[i]];
+      CK(cudaMemcpyAsync(tmp, yi.data(), m * 8, cudaMemcpyHostToDevice, st));
+      RC(kr_gemv(V, n, m, tmp, Wk + (size_t)i * n, n, st));
+      CK(cudaStreamSynchronize(st));  // tmp is reused by the next Ritz vector
+    }
+    CK(cudaMemcpyAsync(V, Wk, (size_t)kk * n * 8, cudaMemcpyDeviceToDevice, st));
+    CK(cudaMemcpyAsync(V + (size_t)kk * n, V + (size_t)m * n, n * 8, cudaMemcpyDeviceToDevice, st));
     std::fill(H.begin(), H.end(), 0.0);
-    H[0] = theta;
-    H[1] = coup;            // H(1,0)
-    H[(size_t)ld] = coup;   // H(0,1) (filled again by the device for column 1)
+    for (int i = 0; i < kk; ++i) {
+      const double coup = beta * evecs[(size_t)(m - 1) * m + idx[i]];
+      H[(size_t)i + (size_t)i * ld] = evals[idx[i]];
+      H[(size_t)kk + (size_t)i * ld] = coup;  // H(kk, i)
+      H[(size_t)i + (size_t)kk * ld] = coup;  // H(i, kk) (recomputed by the device for column kk)
+    }
     CK(cudaStreamSynchronize(st));
-    jstart = 1;
+    jstart = kk;
   }
   // normalise
   RC(kr_multidot(c->ws, xr, n, 1, xr, n, tmp, 0, nrm, st));
