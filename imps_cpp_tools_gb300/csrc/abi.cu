@@ -180,6 +180,15 @@ struct Bump {
 
 size_t round256(size_t b) { return ((b + 255) / 256) * 256; }
 
+// IMPS_DEBUG=1 in the environment prints one line per solver call to stderr
+bool debug_on() {
+  static const bool on = [] {
+    const char* e = getenv("IMPS_DEBUG");
+    return e && e[0] && e[0] != '0';
+  }();
+  return on;
+}
+
 int stage_host(imps_plan* p, double** buf, int64_t n) {
   if (!*buf) CK(cudaMalloc(buf, std::max<int64_t>(n, 1) * sizeof(double)));
   return IMPS_OK;
@@ -697,7 +706,7 @@ int imps_eigs_rs(imps_plan* p, double* x, int mem, double tol, int ncv, int maxi
   std::vector<double> col(ld);
   std::vector<double> evals, evecs, y;
   int jstart = 0, applies = 0, status = IMPS_WARN_NOT_CONVERGED;
-  double theta = 0.0;
+  double theta = 0.0, last_res = 0.0;
   const int chk = 4;
   bool done = false;
   while (!done) {
@@ -736,6 +745,7 @@ int imps_eigs_rs(imps_plan* p, double* x, int mem, double tol, int ncv, int maxi
       for (int r = 0; r < k; ++r) y[r] = evecs[r * k + imin];
       const double beta = H[(j + 1) + (size_t)j * ld];
       const double res = std::fabs(beta * y[k - 1]);
+      last_res = res;
       if (!std::isfinite(theta)) return IMPS_ERR_NAN;
       // split-BF16 applies carry ~1e-7 relative error: their Ritz residual floors there
       const double tol_eff = p->prec == IMPS_PREC_BF16X6 ? std::max(tol, kMixedEigTol) : tol;
@@ -789,6 +799,9 @@ int imps_eigs_rs(imps_plan* p, double* x, int mem, double tol, int ncv, int maxi
   CK(cudaStreamSynchronize(st));
   if (eval) *eval = theta;
   if (n_applies) *n_applies = applies;
+  if (debug_on())
+    fprintf(stderr, "[imps eigs_rs] n=%lld prec=%d applies=%d theta=%.15g res=%.3e tol=%.1e status=%d\n",
+            (long long)n, p->prec, applies, theta, last_res, tol, status);
   return status;
 }
 
@@ -909,6 +922,9 @@ static int gmres_proj(imps_plan* p, const double* b, double* y, const double* rh
     if (rn < tol * bnorm) status = IMPS_OK;
   }
   if (iters) *iters = it;
+  if (debug_on())
+    fprintf(stderr, "[imps gmres] n=%lld prec=%d iters=%d relres=%.3e tol=%.1e status=%d\n", (long long)n,
+            p->prec, it, rel, tol, status);
   if (relres) *relres = rel;
   return status;
 }

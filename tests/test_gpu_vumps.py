@@ -45,7 +45,7 @@ def test_vumps_sweeps_match_oracle(cuda_ctx, model, dimvec, params):
     for sweep in range(3):
         Eo, Fo, po = ora.sweep()
         Eg, Fg, pg = gpu.sweep()
-        tol = 1e-9 if sweep == 0 else 1e-6
+        tol = 1e-9 if sweep == 0 else 1e-5
         assert np.abs(Eg - Eo).max() < tol, (sweep, Eg, Eo)
         assert np.allclose(Fg, Fo, rtol=1e-3 if sweep else 1e-5, atol=1e-12), (sweep, Fg, Fo)
         assert np.allclose(pg, po, rtol=1e-3 if sweep else 1e-4, atol=1e-12), (sweep, pg, po)
