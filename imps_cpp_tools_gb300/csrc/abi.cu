@@ -5,7 +5,9 @@
 #include <algorithm>
 #include <cmath>
 #include <cstdio>
+#include <cstdlib>
 #include <cstring>
+#include <limits>
 #include <new>
 #include <vector>
 
@@ -15,6 +17,7 @@
 #include "imps_internal.h"
 #include "imps_krylov.h"
 #include "imps_tc.h"
+#include "imps_tridiag.h"
 
 using namespace imps;
 
@@ -181,13 +184,14 @@ struct Bump {
 size_t round256(size_t b) { return ((b + 255) / 256) * 256; }
 
 // IMPS_DEBUG=1 in the environment prints one line per solver call to stderr
-bool debug_on() {
-  static const bool on = [] {
+int debug_level() {
+  static const int lvl = [] {
     const char* e = getenv("IMPS_DEBUG");
-    return e && e[0] && e[0] != '0';
+    return e && e[0] ? atoi(e) : 0;
   }();
-  return on;
+  return lvl;
 }
+bool debug_on() { return debug_level() > 0; }
 
 int stage_host(imps_plan* p, double** buf, int64_t n) {
   if (!*buf) CK(cudaMalloc(buf, std::max<int64_t>(n, 1) * sizeof(double)));
@@ -199,47 +203,6 @@ int apply_dev(imps_plan* p, const double* in, double* out) {
   p->P.slots[p->P.n_in].dptr = const_cast<double*>(in);
   p->P.slots[p->P.n_out].dptr = out;
   return run_stages(p, p->P.stages);
-}
-
-// ---- small dense symmetric eigensolver on the host (cyclic Jacobi), n <= kMaxCols ----
-void jacobi_eig(int n, std::vector<double> A, std::vector<double>& w, std::vector<double>& V) {
-  V.assign(n * n, 0.0);
-  for (int i = 0; i < n; ++i) V[i * n + i] = 1.0;
-  for (int sweep = 0; sweep < 100; ++sweep) {
-    double off = 0.0, tot = 0.0;
-    for (int i = 0; i < n; ++i)
-      for (int j = 0; j < n; ++j) {
-        tot += A[i * n + j] * A[i * n + j];
-        if (i != j) off += A[i * n + j] * A[i * n + j];
-      }
-    if (off <= 1e-34 * tot || off == 0.0) break;
-    for (int p = 0; p < n - 1; ++p)
-      for (int q = p + 1; q < n; ++q) {
-        const double apq = A[p * n + q];
-        if (apq == 0.0) continue;
-        const double app = A[p * n + p], aqq = A[q * n + q];
-        const double theta = (aqq - app) / (2.0 * apq);
-        const double t = (theta >= 0 ? 1.0 : -1.0) / (std::fabs(theta) + std::sqrt(theta * theta + 1.0));
-        const double c = 1.0 / std::sqrt(t * t + 1.0), s = t * c;
-        for (int k = 0; k < n; ++k) {  // rows p,q
-          const double akp = A[k * n + p], akq = A[k * n + q];
-          A[k * n + p] = c * akp - s * akq;
-          A[k * n + q] = s * akp + c * akq;
-        }
-        for (int k = 0; k < n; ++k) {  // cols p,q
-          const double apk = A[p * n + k], aqk = A[q * n + k];
-          A[p * n + k] = c * apk - s * aqk;
-          A[q * n + k] = s * apk + c * aqk;
-        }
-        for (int k = 0; k < n; ++k) {
-          const double vkp = V[k * n + p], vkq = V[k * n + q];
-          V[k * n + p] = c * vkp - s * vkq;
-          V[k * n + q] = s * vkp + c * vkq;
-        }
-      }
-  }
-  w.resize(n);
-  for (int i = 0; i < n; ++i) w[i] = A[i * n + i];
 }
 
 }  // namespace
@@ -684,110 +647,108 @@ int imps_eigs_rs(imps_plan* p, double* x, int mem, double tol, int ncv, int maxi
   const int64_t max_applies = (int64_t)maxit * m;
   const int ld = m + 1;
   const int kk = std::max(1, std::min(m / 2, m - 3));  // Ritz vectors kept at a thick restart
-  RC(arena_reserve(c, round256(n * 8) * (m + 4 + kk) + round256((size_t)ld * ld * 8) + 4096));
+  RC(arena_reserve(c, round256(n * 8) * (m + 4 + kk) + round256((size_t)ld * ld * 8) +
+                          round256((size_t)m * kk * 8) + 4096));
   Bump bp{c->arena};
   double* V = bp.take((size_t)n * (m + 1));
   double* Wk = bp.take((size_t)n * kk);
   double* w = bp.take(n);
   double* xr = bp.take(n);
   double* Hd = bp.take((size_t)ld * ld);
+  double* Wrot = bp.take((size_t)m * kk);
   double* tmp = bp.take(ld);
   double* nrm = c->dscal + 8;
   int* bflag = c->dflag;
   CK(cudaMemsetAsync(bflag, 0, sizeof(int), st));
-  // projected matrix: rows below the subdiagonal are never written, they must read as zero
   CK(cudaMemsetAsync(Hd, 0, (size_t)ld * ld * 8, st));
   if (mem == IMPS_MEM_HOST) CK(cudaMemcpyAsync(xr, x, n * 8, cudaMemcpyHostToDevice, st));
   else CK(cudaMemcpyAsync(xr, x, n * 8, cudaMemcpyDeviceToDevice, st));
   RC(kr_multidot(c->ws, xr, n, 1, xr, n, tmp, 0, nrm, st));
   RC(kr_scale_inv(xr, nrm, V, n, bflag, st));
 
-  std::vector<double> H((size_t)ld * ld, 0.0);  // host projected matrix, column-major
-  std::vector<double> col(ld);
-  std::vector<double> evals, evecs, y;
-  int jstart = 0, applies = 0, status = IMPS_WARN_NOT_CONVERGED;
+  // The device keeps full CGS2 columns h = V^T A v_j; the host keeps the tridiagonal part
+  // (alpha_j = h_j, beta_j = |w_j|), exact up to rounding because the basis is kept
+  // orthonormal and a thick restart re-tridiagonalises the kept block (arrow_tridiag).
+  std::vector<double> H((size_t)ld * ld, 0.0);
+  std::vector<double> ta(m + 1, 0.0), tb(m + 1, 0.0), z(m, 0.0);
+  std::vector<double> th(kk), Z((size_t)m * kk), sv(kk), Q((size_t)kk * kk), qa(kk), qb(kk),
+      Wr((size_t)m * kk);
+  int jstart = 0, jpulled = 0, applies = 0, status = IMPS_WARN_NOT_CONVERGED, kfinal = 0;
   double theta = 0.0, last_res = 0.0;
   const int chk = 4;
+  // ARPACK's Ritz test (dsconv): |beta * y_k| <= tol * max(eps^(2/3), |theta|)
+  const double eps23 = std::cbrt(kEps * kEps);
+  const double tol_eff = p->prec == IMPS_PREC_BF16X6 ? std::max(tol, kMixedEigTol) : tol;
   bool done = false;
   while (!done) {
-    int jlast = -1;
     for (int j = jstart; j < m; ++j) {
       double* vj = V + (size_t)j * n;
       double* hc = Hd + (size_t)j * ld;
       RC(apply_dev(p, vj, w));
       ++applies;
-      RC(kr_multidot(c->ws, V, n, j + 1, w, n, hc, 0, nullptr, st));
-      RC(kr_gemv_sub(V, n, j + 1, hc, w, n, st));
-      RC(kr_multidot(c->ws, V, n, j + 1, w, n, tmp, 0, nullptr, st));
-      RC(kr_gemv_sub(V, n, j + 1, tmp, w, n, st));
-      RC(kr_axpby(1.0, tmp, 1.0, hc, j + 1, st));
-      RC(kr_multidot(c->ws, w, n, 1, w, n, tmp, 0, hc + j + 1, st));
-      RC(kr_scale_inv(w, hc + j + 1, V + (size_t)(j + 1) * n, n, bflag, st));
-      jlast = j;
+      RC(kr_cgs2_step(c->ws, V, n, j + 1, w, n, hc, tmp, V + (size_t)(j + 1) * n, bflag, st));
       const bool check = ((j + 1 - jstart) % chk == 0) || j == m - 1 || applies >= max_applies;
       if (!check) continue;
-      // pull the new columns and solve the small projected problem
-      CK(cudaMemcpyAsync(H.data() + (size_t)jstart * ld, Hd + (size_t)jstart * ld,
-                         (size_t)(j + 1 - jstart) * ld * 8, cudaMemcpyDeviceToHost, st));
+      CK(cudaMemcpyAsync(H.data() + (size_t)jpulled * ld, Hd + (size_t)jpulled * ld,
+                         (size_t)(j + 1 - jpulled) * ld * 8, cudaMemcpyDeviceToHost, st));
       int hbreak = 0;
       CK(cudaMemcpyAsync(&hbreak, bflag, sizeof(int), cudaMemcpyDeviceToHost, st));
       CK(cudaStreamSynchronize(st));
+      for (int q = jpulled; q <= j; ++q) {
+        ta[q] = H[(size_t)q + (size_t)q * ld];
+        tb[q] = H[(size_t)q + 1 + (size_t)q * ld];
+      }
+      jpulled = j + 1;
       const int k = j + 1;
-      std::vector<double> A((size_t)k * k);
-      for (int r = 0; r < k; ++r)
-        for (int q = 0; q < k; ++q)
-          A[r * k + q] = 0.5 * (H[r + (size_t)q * ld] + H[q + (size_t)r * ld]);
-      jacobi_eig(k, A, evals, evecs);
-      int imin = 0;
-      for (int i = 1; i < k; ++i) if (evals[i] < evals[imin]) imin = i;
-      theta = evals[imin];
-      y.assign(k, 0.0);
-      for (int r = 0; r < k; ++r) y[r] = evecs[r * k + imin];
-      const double beta = H[(j + 1) + (size_t)j * ld];
-      const double res = std::fabs(beta * y[k - 1]);
-      last_res = res;
+      const double tn = tri_norm(k, ta.data(), tb.data());
+      theta = tri_eigval(k, ta.data(), tb.data(), 0);
       if (!std::isfinite(theta)) return IMPS_ERR_NAN;
-      // split-BF16 applies carry ~1e-7 relative error: their Ritz residual floors there
-      const double tol_eff = p->prec == IMPS_PREC_BF16X6 ? std::max(tol, kMixedEigTol) : tol;
-      if (res <= tol_eff * std::max(std::fabs(theta), 1e-300) || hbreak) {
+      tri_eigvec(k, ta.data(), tb.data(), theta, tn, z.data(), nullptr, nullptr, 0);
+      const double res = std::fabs(tb[k - 1] * z[k - 1]);
+      last_res = res;
+      kfinal = k;
+      if (res <= tol_eff * std::max(std::fabs(theta), eps23) || hbreak) {
         status = IMPS_OK;
         done = true;
         break;
       }
       if (applies >= max_applies) { done = true; break; }
     }
-    // Ritz vector x = V[:, 0..k-1] y
-    const int k = jlast + 1;
-    CK(cudaMemcpyAsync(tmp, y.data(), k * 8, cudaMemcpyHostToDevice, st));
-    RC(kr_gemv(V, n, k, tmp, xr, n, st));
     if (done) break;
-    // Thick restart (Wu & Simon): keep the kk lowest Ritz pairs of the m-step projection and
-    // the residual direction v_m; the projected matrix restarts as diag(theta_i) bordered by
-    // the couplings beta_m * y_i[m-1] (an arrowhead), and Lanczos continues from v_m with
-    // full CGS2 re-orthogonalisation against the kept vectors.
-    std::vector<int> idx(m);
-    for (int i = 0; i < m; ++i) idx[i] = i;
-    std::sort(idx.begin(), idx.end(), [&](int a, int b) { return evals[a] < evals[b]; });
-    const double beta = H[(size_t)m + (size_t)(m - 1) * ld];
-    for (int i = 0; i < kk; ++i) {
-      std::vector<double> yi(m);
-      for (int r = 0; r < m; ++r) yi[r] = evecs[(size_t)r * m + idx[i]];
-      CK(cudaMemcpyAsync(tmp, yi.data(), m * 8, cudaMemcpyHostToDevice, st));
-      RC(kr_gemv(V, n, m, tmp, Wk + (size_t)i * n, n, st));
-      CK(cudaStreamSynchronize(st));  // tmp is reused by the next Ritz vector
+    // Thick restart (Wu & Simon): keep the kk lowest Ritz pairs of T_m and the residual
+    // direction v_m.  The kept block is rotated so that T stays tridiagonal, with only its
+    // last vector coupled to v_m (coupling |s|, s_i = beta_{m-1} * y_i[m-1]).
+    const double tn = tri_norm(m, ta.data(), tb.data());
+    for (int i = 0; i < kk; ++i) th[i] = tri_eigval(m, ta.data(), tb.data(), i);
+    for (int i = 0; i < kk; ++i)
+      tri_eigvec(m, ta.data(), tb.data(), th[i], tn, Z.data() + (size_t)i * m, Z.data(), th.data(), i);
+    for (int i = 0; i < kk; ++i) sv[i] = tb[m - 1] * Z[(size_t)(m - 1) + (size_t)i * m];
+    arrow_tridiag(kk, th.data(), sv.data(), Q.data(), qa.data(), qb.data());
+    double sn = 0.0;
+    for (int i = 0; i < kk; ++i) sn += sv[i] * sv[i];
+    sn = std::sqrt(sn);
+    // new kept column p = Z * Q[:, kk-1-p], so that column kk-1 is the one coupled to v_m
+    for (int pc = 0; pc < kk; ++pc) {
+      const double* q = Q.data() + (size_t)(kk - 1 - pc) * kk;
+      for (int r = 0; r < m; ++r) {
+        double acc = 0.0;
+        for (int i = 0; i < kk; ++i) acc += Z[(size_t)r + (size_t)i * m] * q[i];
+        Wr[(size_t)r + (size_t)pc * m] = acc;
+      }
     }
+    CK(cudaMemcpyAsync(Wrot, Wr.data(), (size_t)m * kk * 8, cudaMemcpyHostToDevice, st));
+    RC(kr_basis_rotate(V, n, m, Wrot, kk, Wk, n, n, st));
     CK(cudaMemcpyAsync(V, Wk, (size_t)kk * n * 8, cudaMemcpyDeviceToDevice, st));
     CK(cudaMemcpyAsync(V + (size_t)kk * n, V + (size_t)m * n, n * 8, cudaMemcpyDeviceToDevice, st));
-    std::fill(H.begin(), H.end(), 0.0);
-    for (int i = 0; i < kk; ++i) {
-      const double coup = beta * evecs[(size_t)(m - 1) * m + idx[i]];
-      H[(size_t)i + (size_t)i * ld] = evals[idx[i]];
-      H[(size_t)kk + (size_t)i * ld] = coup;  // H(kk, i)
-      H[(size_t)i + (size_t)kk * ld] = coup;  // H(i, kk) (recomputed by the device for column kk)
-    }
+    for (int pc = 0; pc < kk; ++pc) ta[pc] = qa[kk - 1 - pc];
+    for (int pc = 0; pc + 1 < kk; ++pc) tb[pc] = qb[kk - 2 - pc];
+    tb[kk - 1] = sn;
     CK(cudaStreamSynchronize(st));
-    jstart = kk;
+    jstart = jpulled = kk;
   }
+  // Ritz vector x = V[:, 0..k-1] z
+  CK(cudaMemcpyAsync(tmp, z.data(), kfinal * 8, cudaMemcpyHostToDevice, st));
+  RC(kr_gemv(V, n, kfinal, tmp, xr, n, st));
   // normalise
   RC(kr_multidot(c->ws, xr, n, 1, xr, n, tmp, 0, nrm, st));
   if (mem == IMPS_MEM_HOST) {
@@ -862,6 +823,8 @@ static int gmres_proj(imps_plan* p, const double* b, double* y, const double* rh
     CK(cudaStreamSynchronize(st));
     if (!std::isfinite(rn)) return IMPS_ERR_NAN;
     rel = rn / bnorm;
+    if (debug_level() > 1)
+      fprintf(stderr, "[imps gmres]   outer=%d it=%d relres=%.3e\n", outer, it, rel);
     if (rn < tol * bnorm) { status = IMPS_OK; break; }
     CK(cudaMemsetAsync(bflag, 0, sizeof(int), st));
     RC(kr_scale_inv(w, dsc + 1, V, n, bflag, st));
@@ -872,13 +835,7 @@ static int gmres_proj(imps_plan* p, const double* b, double* y, const double* rh
       double* vj = V + (size_t)j * n;
       RC(proj_apply_dev(p, vj, rho_in, rho_out, w, t, dsc));
       ++it;
-      RC(kr_multidot(c->ws, V, n, j + 1, w, n, Hc, 0, nullptr, st));
-      RC(kr_gemv_sub(V, n, j + 1, Hc, w, n, st));
-      RC(kr_multidot(c->ws, V, n, j + 1, w, n, tmp, 0, nullptr, st));
-      RC(kr_gemv_sub(V, n, j + 1, tmp, w, n, st));
-      RC(kr_axpby(1.0, tmp, 1.0, Hc, j + 1, st));
-      RC(kr_multidot(c->ws, w, n, 1, w, n, tmp, 0, Hc + j + 1, st));
-      RC(kr_scale_inv(w, Hc + j + 1, V + (size_t)(j + 1) * n, n, nullptr, st));
+      RC(kr_cgs2_step(c->ws, V, n, j + 1, w, n, Hc, tmp, V + (size_t)(j + 1) * n, nullptr, st));
       RC(kr_givens(Hc, j, cs, sn, gam, R, ld, dsc + 3, bflag, st));
       kdim = j + 1;
       if ((j + 1) % 4 == 0 || j == m - 1 || it >= maxit) {

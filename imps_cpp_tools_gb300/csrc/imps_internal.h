@@ -17,7 +17,7 @@ namespace imps {
 
 // process-wide count of kernel launches issued by this library (imps_launch_count)
 std::atomic<long long>& launch_counter();
-inline void count_launch() { launch_counter().fetch_add(1, std::memory_order_relaxed); }
+inline void count_launch(int k = 1) { launch_counter().fetch_add(k, std::memory_order_relaxed); }
 
 using Key = std::vector<int32_t>;
 

@@ -24,6 +24,13 @@ int kr_gemv_sub(const double* V, int64_t ldv, int ncols, const double* h, double
                 cudaStream_t st);
 int kr_gemv(const double* V, int64_t ldv, int ncols, const double* h, double* y, int64_t n,
             cudaStream_t st);
+// One CGS2 Lanczos/Arnoldi step on w = A v_{nc-1} against V[:, 0..nc-1]: h[0..nc-1] = total
+// projection coefficients, h[nc] = |w| after projection, vnext = w / h[nc] (flag set when
+// |w| underflows); h2 (nc doubles) is scratch.  Four launches.
+int kr_cgs2_step(const KrylovWs& ws, const double* V, int64_t ldv, int nc, double* w, int64_t n,
+                 double* h, double* h2, double* vnext, int* flag, cudaStream_t st);
+int kr_basis_rotate(const double* V, int64_t ldv, int m, const double* W, int kk, double* out,
+                    int64_t ldo, int64_t n, cudaStream_t st);
 int kr_scale_inv(const double* x, const double* nrm, double* y, int64_t n, int* flag, cudaStream_t st);
 int kr_axpby(double a, const double* x, double b, double* y, int64_t n, cudaStream_t st);
 int kr_proj_epilogue(const double* x, const double* t, const double* s, const double* rho, double* y,

@@ -4,6 +4,7 @@
 // result is bitwise reproducible run to run (no floating-point atomics).
 #include <cuda_runtime.h>
 
+#include <algorithm>
 #include <cmath>
 #include <cstdint>
 
@@ -13,7 +14,9 @@
 namespace {
 
 constexpr int RB = 256;      // threads per reduction block
-constexpr int RGRID = 128;   // fixed reduction grid (partials buffer is RGRID * kMaxCols)
+constexpr int RGRID = 128;   // fixed reduction grid of multidot (RGRID * kMaxCols partials)
+constexpr int CGRID = 608;   // max grid of the fused CGS2 kernels (4 blocks per SM)
+constexpr int CSUB = 1024;   // rows of w staged in shared memory per CGS2 sub-chunk
 
 __device__ __forceinline__ double warp_sum(double v) {
 #pragma unroll
@@ -72,6 +75,117 @@ __global__ void __launch_bounds__(RB) multidot_kernel(const double* __restrict__
   if (threadIdx.x == 0) *counter = 0u;
 }
 
+// One fused pass of classical Gram-Schmidt over the basis V[:, 0..nc-1] (nc <= kMaxCols):
+//   MODE 0:  h = V^T w
+//   MODE 1:  w -= V hin;  h = V^T w;  hacc += h      (second CGS pass)
+//   MODE 2:  w -= V hin;  *hout = |w|
+// Each block walks sub-chunks of <= CSUB rows (grid-stride): the (updated) rows of w are
+// staged in shared memory, then warps take groups of 4 columns and lanes stride the rows, so
+// V is read coalesced and the chunk just read for the update is re-read from L2.  Per-block
+// column sums go to partials[c * gridDim.x + block]; the last block to finish reduces them in
+// a fixed order (bitwise reproducible) and resets the counter.
+template <int MODE>
+__global__ void __launch_bounds__(256) cgs_pass_kernel(const double* __restrict__ V, int64_t ldv, int nc,
+                                                      double* __restrict__ w, int64_t n, int sub,
+                                                      const double* hin, double* hout, double* hacc,
+                                                      double* __restrict__ partials,
+                                                      unsigned int* __restrict__ counter) {
+  __shared__ double wsm[CSUB];
+  __shared__ double hs[imps::kMaxCols];
+  __shared__ double sacc[imps::kMaxCols];
+  __shared__ double sh[32];
+  __shared__ bool last;
+  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  if (MODE != 0)
+    for (int c = threadIdx.x; c < nc; c += blockDim.x) hs[c] = hin[c];
+  for (int c = threadIdx.x; c < imps::kMaxCols; c += blockDim.x) sacc[c] = 0.0;
+  double nacc = 0.0;
+  __syncthreads();
+  for (int64_t base = (int64_t)blockIdx.x * sub; base < n; base += (int64_t)gridDim.x * sub) {
+    const int len = (int)min((int64_t)sub, n - base);
+    for (int t = threadIdx.x; t < len; t += blockDim.x) {
+      const int64_t r = base + t;
+      double x = w[r];
+      if (MODE != 0) {
+        const double* vr = V + r;
+        double x1 = 0.0, x2 = 0.0, x3 = 0.0;
+        int c = 0;
+        for (; c + 4 <= nc; c += 4) {
+          x = fma(-vr[(int64_t)c * ldv], hs[c], x);
+          x1 = fma(-vr[(int64_t)(c + 1) * ldv], hs[c + 1], x1);
+          x2 = fma(-vr[(int64_t)(c + 2) * ldv], hs[c + 2], x2);
+          x3 = fma(-vr[(int64_t)(c + 3) * ldv], hs[c + 3], x3);
+        }
+        for (; c < nc; ++c) x = fma(-vr[(int64_t)c * ldv], hs[c], x);
+        x = (x + x1) + (x2 + x3);
+        w[r] = x;
+      }
+      if (MODE == 2) nacc = fma(x, x, nacc);
+      else wsm[t] = x;
+    }
+    if (MODE == 2) continue;
+    __syncthreads();
+    for (int c0 = warp * 4; c0 < nc; c0 += 32) {
+      // columns past nc read column nc-1 (valid memory) and are discarded
+      const double* v0 = V + base + (int64_t)min(c0, nc - 1) * ldv;
+      const double* v1 = V + base + (int64_t)min(c0 + 1, nc - 1) * ldv;
+      const double* v2 = V + base + (int64_t)min(c0 + 2, nc - 1) * ldv;
+      const double* v3 = V + base + (int64_t)min(c0 + 3, nc - 1) * ldv;
+      double a0 = 0.0, a1 = 0.0, a2 = 0.0, a3 = 0.0;
+      for (int t = lane; t < len; t += 32) {
+        const double x = wsm[t];
+        a0 = fma(v0[t], x, a0);
+        a1 = fma(v1[t], x, a1);
+        a2 = fma(v2[t], x, a2);
+        a3 = fma(v3[t], x, a3);
+      }
+      a0 = warp_sum(a0);
+      a1 = warp_sum(a1);
+      a2 = warp_sum(a2);
+      a3 = warp_sum(a3);
+      if (lane == 0) {
+        sacc[c0] += a0;
+        if (c0 + 1 < nc) sacc[c0 + 1] += a1;
+        if (c0 + 2 < nc) sacc[c0 + 2] += a2;
+        if (c0 + 3 < nc) sacc[c0 + 3] += a3;
+      }
+    }
+    __syncthreads();
+  }
+  const int G = gridDim.x;
+  if (MODE == 2) {
+    nacc = block_sum(nacc, sh);
+    if (threadIdx.x == 0) partials[blockIdx.x] = nacc;
+  } else {
+    __syncthreads();
+    for (int c = threadIdx.x; c < nc; c += blockDim.x) partials[(int64_t)c * G + blockIdx.x] = sacc[c];
+  }
+  __threadfence();
+  __syncthreads();
+  if (threadIdx.x == 0) last = (atomicAdd(counter, 1u) == (unsigned)G - 1);
+  __syncthreads();
+  if (!last) return;
+  __threadfence();
+  const volatile double* pv = partials;
+  if (MODE == 2) {
+    double v = 0.0;
+    for (int b = threadIdx.x; b < G; b += blockDim.x) v += pv[b];
+    v = block_sum(v, sh);
+    if (threadIdx.x == 0) *hout = sqrt(v);
+  } else {
+    for (int c = warp; c < nc; c += 8) {
+      double v = 0.0;
+      for (int b = lane; b < G; b += 32) v += pv[(int64_t)c * G + b];
+      v = warp_sum(v);
+      if (lane == 0) {
+        hout[c] = v;
+        if (MODE == 1) hacc[c] += v;
+      }
+    }
+  }
+  if (threadIdx.x == 0) *counter = 0u;
+}
+
 // w[r] -= sum_c V[r + c*ldv] * h[c]
 __global__ void gemv_sub_kernel(const double* __restrict__ V, int64_t ldv, int ncols,
                                 const double* __restrict__ h, double* __restrict__ w, int64_t n) {
@@ -101,6 +215,39 @@ __global__ void gemv_kernel(const double* __restrict__ V, int64_t ldv, int ncols
 }
 
 // y = x / *nrm  (guarded: a zero norm writes zeros and raises the breakdown flag)
+// out[:, t] = sum_i V[:, i] * W[i + t*m] for t < kk (column-major W, m <= kMaxCols): the
+// basis rotation of a thick restart, one pass over V per 16 output columns (V stays in L2).
+__global__ void __launch_bounds__(256) basis_rotate_kernel(const double* __restrict__ V, int64_t ldv,
+                                                           int m, const double* __restrict__ W, int kk,
+                                                           double* __restrict__ out, int64_t ldo,
+                                                           int64_t n) {
+  constexpr int CT = 16;
+  __shared__ double ws[imps::kMaxCols * CT];
+  for (int t0 = 0; t0 < kk; t0 += CT) {
+    const int nt = min(CT, kk - t0);
+    __syncthreads();
+    for (int e = threadIdx.x; e < m * CT; e += blockDim.x) {
+      const int i = e / CT, t = e % CT;
+      ws[e] = t < nt ? W[i + (int64_t)(t0 + t) * m] : 0.0;
+    }
+    __syncthreads();
+    for (int64_t r = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; r < n;
+         r += (int64_t)gridDim.x * blockDim.x) {
+      double acc[CT];
+#pragma unroll
+      for (int t = 0; t < CT; ++t) acc[t] = 0.0;
+      for (int i = 0; i < m; ++i) {
+        const double v = V[r + i * ldv];
+#pragma unroll
+        for (int t = 0; t < CT; ++t) acc[t] = fma(v, ws[i * CT + t], acc[t]);
+      }
+#pragma unroll
+      for (int t = 0; t < CT; ++t)
+        if (t < nt) out[r + (int64_t)(t0 + t) * ldo] = acc[t];
+    }
+  }
+}
+
 __global__ void scale_inv_kernel(const double* __restrict__ x, const double* __restrict__ nrm,
                                  double* __restrict__ y, int64_t n, int* __restrict__ flag) {
   const double s = *nrm;
@@ -298,6 +445,34 @@ int kr_gemv(const double* V, int64_t ldv, int ncols, const double* h, double* y,
   return IMPS_OK;
 }
 
+int kr_basis_rotate(const double* V, int64_t ldv, int m, const double* W, int kk, double* out,
+                    int64_t ldo, int64_t n, cudaStream_t st) {
+  if (m < 1 || m > kMaxCols || kk < 1 || n < 1) return IMPS_ERR_BAD_ARG;
+  imps::count_launch();
+  basis_rotate_kernel<<<grid_for(n), 256, 0, st>>>(V, ldv, m, W, kk, out, ldo, n);
+  return IMPS_OK;
+}
+
+int kr_cgs2_step(const KrylovWs& ws, const double* V, int64_t ldv, int nc, double* w, int64_t n,
+                 double* h, double* h2, double* vnext, int* flag, cudaStream_t st) {
+  if (nc < 1 || nc > kMaxCols) return IMPS_ERR_BAD_ARG;
+  int64_t g = (n + 127) / 128;
+  if (g > CGRID) g = CGRID;
+  if (g < 1) g = 1;
+  const int grid = (int)g;
+  int64_t sub = (n + grid - 1) / grid;
+  sub = ((sub + 31) / 32) * 32;
+  if (sub > CSUB) sub = CSUB;
+  imps::count_launch(4);
+  cgs_pass_kernel<0><<<grid, 256, 0, st>>>(V, ldv, nc, w, n, (int)sub, nullptr, h, nullptr, ws.partials,
+                                           ws.counter);
+  cgs_pass_kernel<1><<<grid, 256, 0, st>>>(V, ldv, nc, w, n, (int)sub, h, h2, h, ws.partials, ws.counter);
+  cgs_pass_kernel<2><<<grid, 256, 0, st>>>(V, ldv, nc, w, n, (int)sub, h2, h + nc, nullptr, ws.partials,
+                                           ws.counter);
+  scale_inv_kernel<<<grid_for(n), 256, 0, st>>>(w, h + nc, vnext, n, flag);
+  return IMPS_OK;
+}
+
 int kr_scale_inv(const double* x, const double* nrm, double* y, int64_t n, int* flag, cudaStream_t st) {
   imps::count_launch();
   scale_inv_kernel<<<grid_for(n), 256, 0, st>>>(x, nrm, y, n, flag);
@@ -353,6 +528,8 @@ int kr_sign_of_first(const double* x, double* s, cudaStream_t st) {
   return IMPS_OK;
 }
 
-size_t kr_partials_elems() { return (size_t)RGRID * kMaxCols; }
+size_t kr_partials_elems() {
+  return std::max((size_t)RGRID * kMaxCols, (size_t)CGRID * kMaxCols);
+}
 
 }  // namespace imps

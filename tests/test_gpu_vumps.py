@@ -58,3 +58,41 @@ def test_vumps_gpu_bethe_ansatz(cuda_ctx):
     assert abs(E.mean() - (0.25 - math.log(2))) < 2e-4
     assert F.max() < 1e-3
     assert np.isfinite(E).all()
+
+
+@pytest.fixture(scope="module")
+def oracle_ground_state():
+    """The oracle's VUMPS (VUMPS_main.cpp restated) run to |grad| < 1e-11 from a seeded state,
+    reference tolerance schedule (tol = min(max(prec/100, 5e-16), 1e-6))."""
+    d, I2K, h = models.build_model("xxz", J=1.0, Delta=-1.0)
+    rng = np.random.default_rng(11)
+    AL, AR, C = O.randMPS_LR(2, I2K, [B0, B1], rng)
+    ora = O.VUMPS(h, d, I2K, B0, dimvec=[B0, B1], init=(AL, AR, C), InvETol=1e-13, seed=11)
+    for _ in range(250):
+        E, F, _ = ora.sweep()
+        if F.max() < 1e-11:
+            break
+    assert F.max() < 1e-11
+    return (AL, AR, C), E
+
+
+@pytest.mark.parametrize("precision,tol_abs", [("fp64", None), ("bf16x6", 1e-9)])
+def test_vumps_ground_state_energy_matches_oracle(cuda_ctx, oracle_ground_state, precision, tol_abs):
+    """Independent runs to convergence from the same state: the FP64 ground-state energy density
+    agrees with the oracle's to 1e-10 relative, the mixed (split-BF16) one to 1e-9."""
+    (AL, AR, C), Eo = oracle_ground_state
+    init = {"AL": [dev(O.mps_vec(a)) for a in AL], "AR": [dev(O.mps_vec(a)) for a in AR],
+            "C": [dev(O.bd_vec(C[1])), dev(O.bd_vec(C[0]))]}
+    gpu = VumpsGPU(cuda_ctx, "xxz", dimvec=[B0, B1], init_state=init, InvETol=1e-13, precision=precision,
+                   J=1.0, Delta=-1.0)
+    fmin, Eg = np.inf, None
+    for _ in range(250):
+        E, F, _ = gpu.sweep()
+        if F.max() < fmin:
+            fmin, Eg = F.max(), E
+        if F.max() < 1e-11:
+            break
+    bound = 1e-10 * abs(Eo.mean()) if tol_abs is None else tol_abs
+    assert abs(Eg.mean() - Eo.mean()) <= bound, (precision, Eg, Eo, fmin)
+    if precision == "fp64":
+        assert fmin < 1e-11
