@@ -2,12 +2,18 @@
 
 Workload (default): XXZ spin-1/2 chain, J=1, Delta=1 (antiferromagnet; --Delta=-1 in the
 reference's sign convention), two-site unit cell, U(1) Sz sectors q=-10..10 with dims
-~exp(-q^2/18) summing to D=512, seeded random initial state, fixed eigensolver / GMRES
-tolerance 1e-12, bond expansion off.  A step is one VUMPS sweep (both site updates of
-VUMPS_main.cpp:165-354).  The headline value is the split-BF16 (tcgen05) path; the FP64 path
-runs the same sweeps from the same initial state and is reported beside it.
+~exp(-q^2/18) summing to D=512, seeded random initial state, the reference's eigensolver
+tolerance schedule tol = min(max(prec/100, tolmin), tolmax) (VUMPS_main.cpp:37-38, 177) with
+tolmin = GMRES tolerance = 1e-12, bond expansion off.  A step is one VUMPS sweep (both site
+updates of VUMPS_main.cpp:165-354); the default 3 warm-up + 47 timed steps are the 50 sweeps
+of the workload.  The headline value is the split-BF16 (tcgen05) path; the FP64 path runs the
+same sweeps from the same initial state and is reported beside it, with the energy difference
+of the two after the last sweep.
 
 --mode hac times H_AC applies only (ApplyHAvec; a step = 20 applies).
+--mode krylov times one bounded thick-restart Lanczos solve (eigs_rs, ncv 64, 8 restart
+cycles = 288 applies, unreachable tolerance) on the synthetic H_AC, next to the same number of
+bare applies: the difference is the per-iteration orthogonalisation and launch cost.
 The reference arm (--impl reference) times the CPU restatement of the same sweeps (the
 reference itself cannot be built: armadillo/ARPACK are not available).
 """
@@ -29,8 +35,9 @@ sys.path.insert(0, ROOT)
 METRIC = "VUMPS sweeps/s + H_AC TFLOP/s, mixed vs FP64 on one GB300 at |dE|<=1e-9"
 APPLIES_PER_STEP = 20
 L2_FLUSH_BYTES = 512 << 20
-WORKLOAD_DESC = ("XXZ D=512 (21 U(1) sectors, dims ~exp(-q^2/18)), 2-site VUMPS sweep, "
-                 "Lanczos/GMRES tol 1e-12, expansion off")
+TOLMIN = 1e-12  # floor of the eigensolver tolerance schedule and the GMRES tolerance
+WORKLOAD_DESC = ("XXZ D=512 (21 U(1) sectors, dims ~exp(-q^2/18)), 2-site VUMPS sweep, tolerance schedule "
+                 "min(max(prec/100, 1e-12), 1e-6) (VUMPS_main.cpp:177), GMRES tol 1e-12, expansion off")
 
 
 def _peaks():
@@ -133,7 +140,7 @@ def cpu_sweeps(n_sweeps, seed=1, warm=0):
     from oracle import imps_oracle as O
     model, dims0, params = _xxz_params()
     d, I2K, h = models.build_model(model, **params)
-    v = O.VUMPS(h, d, I2K, dims0, seed=seed, fixed_tol=1e-12, InvETol=1e-12, gmres_maxit=300)
+    v = O.VUMPS(h, d, I2K, dims0, seed=seed, tolmin=TOLMIN, InvETol=TOLMIN, gmres_maxit=300)
     for _ in range(warm):
         v.sweep()
     times = []
@@ -153,7 +160,7 @@ def run_reference(args):
     from oracle import imps_oracle as O
     model, dims0, params = _xxz_params()
     d, I2K, h = models.build_model(model, **params)
-    v = O.VUMPS(h, d, I2K, dims0, seed=1, fixed_tol=1e-12, InvETol=1e-12, gmres_maxit=300)
+    v = O.VUMPS(h, d, I2K, dims0, seed=1, tolmin=TOLMIN, InvETol=TOLMIN, gmres_maxit=300)
     budget, per, n = 120.0, [], 0
     t_start = time.perf_counter()
     while n < 1 + args.steps and (n < 2 or time.perf_counter() - t_start < budget):
@@ -204,33 +211,58 @@ def _time_hac_applies(torch, plan, n, stream, reps=APPLIES_PER_STEP):
     return float(np.median(times))
 
 
-def _run_vumps(torch, ctx, precision, steps, warmup, stream, clocks=None):
-    from imps_cpp_tools_gb300 import _native as N
+def _new_vumps(precision):
     from imps_cpp_tools_gb300.vumps import VumpsGPU
     model, dims0, params = _xxz_params()
-    v = VumpsGPU(ctx, model, dims0=dims0, seed=1, fixed_tol=1e-12, InvETol=1e-12, precision=precision,
-                 verbose=True, **params)
+    return VumpsGPU(_CTX[0], model, dims0=dims0, seed=1, tolmin=TOLMIN, InvETol=TOLMIN, precision=precision,
+                    verbose=True, **params)
+
+
+_CTX = [None]
+
+
+def _run_vumps(torch, precision, steps, warmup, stream, clocks=None, e2e=False):
+    """W warm-up sweeps, then K device-timed sweeps (CUDA events on the launching stream).
+    With e2e, every timed step also uploads the MPS state from pinned host memory before the
+    sweep and reads the state and the energies back after it (wall clock around all three)."""
+    from imps_cpp_tools_gb300 import _native as N
+    v = _new_vumps(precision)
     for _ in range(warmup):
         v.sweep()
     torch.cuda.synchronize()
     lib = N.load()
+    host = {k: [t.detach().cpu().pin_memory() for t in getattr(v, k)] for k in ("AL", "AR", "C")} if e2e else None
+    h2d = sum(t.numel() * 8 for k in host for t in host[k]) if e2e else 0
     l0 = lib.imps_launch_count()
     s0 = dict(v.stats)
     if clocks:
         clocks.start()
-    times = []
+    times, walls = [], []
+    torch.cuda.nvtx.range_push(f"timed_sweeps_{precision}")  # ncu --nvtx-include selects these
     for _ in range(steps):
         torch.cuda.synchronize()
+        w0 = time.perf_counter()
+        if e2e:
+            for k in ("AL", "AR", "C"):
+                for j, t in enumerate(host[k]):
+                    getattr(v, k)[j].copy_(t, non_blocking=True)
         e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
         e0.record(stream)
         E, F, prec = v.sweep()
         e1.record(stream)
+        if e2e:
+            for k in ("AL", "AR", "C"):
+                for j, t in enumerate(getattr(v, k)):
+                    host[k][j].copy_(t, non_blocking=True)
         torch.cuda.synchronize()
+        walls.append(time.perf_counter() - w0)
         times.append(e0.elapsed_time(e1) * 1e-3)
+    torch.cuda.nvtx.range_pop()
     clk = clocks.stop() if clocks else None
     launches = lib.imps_launch_count() - l0
     counts = {k: v.stats[k] - s0.get(k, 0) for k in v.stats}
-    return v, times, E, F, prec, launches, counts, clk
+    return {"v": v, "times": times, "walls": walls, "E": E, "F": F, "prec": prec, "launches": launches,
+            "counts": counts, "clocks": clk, "h2d": h2d}
 
 
 def run_vumps(args):
@@ -243,25 +275,27 @@ def run_vumps(args):
     if ws > 1:
         dist.init_process_group("nccl")
     ctx = B.Context(local)
+    _CTX[0] = ctx
     stream = torch.cuda.current_stream()
     ctx.set_stream(stream)
 
-    # FP64 path (plain form) and split-BF16 path from the same seeded initial state
-    v64, t64, E64, F64, p64, _, c64, _ = _run_vumps(torch, ctx, "fp64", args.steps, args.warmup, stream)
+    # plain FP64 path and the chosen split-BF16 path, from the same seeded initial state
+    r64 = _run_vumps(torch, "fp64", args.steps, args.warmup, stream)
     if ws > 1:
         dist.barrier()
-    clocks = ClockSampler(local)
-    vmx, tmx, Emx, Fmx, pmx, launches, cmx, clk = _run_vumps(torch, ctx, args.precision, args.steps, args.warmup,
-                                                               stream, clocks)
-    t_step = float(np.mean(tmx))
+    rmx = _run_vumps(torch, args.precision, args.steps, args.warmup, stream, ClockSampler(local), e2e=True)
+    t_step = float(np.mean(rmx["times"]))
+    t_wall = float(np.mean(rmx["walls"]))
     if ws > 1:
-        tt = torch.tensor([t_step], device="cuda", dtype=torch.float64)
+        tt = torch.tensor([t_step, t_wall], device="cuda", dtype=torch.float64)
         dist.all_reduce(tt, op=dist.ReduceOp.MAX)
-        t_step = float(tt.item())
+        t_step, t_wall = (float(x) for x in tt.tolist())
     value = ws / t_step  # replicas: every rank runs its own sweeps
+    E64, Emx = r64["E"], rmx["E"]
     dE = float(abs(Emx.mean() - E64.mean()))
 
-    # H_AC TFLOP/s on the converged-state plans (site 0)
+    # H_AC TFLOP/s on the final-state plans (site 0)
+    v64, vmx = r64["v"], rmx["v"]
     n = v64.LA[0].nelem
     flops = v64.flops_hac[0]
     t_hac64 = _time_hac_applies(torch, v64.p_hac[0], n, stream)
@@ -287,47 +321,31 @@ def run_vumps(args):
                 "frac": achieved / fp64_peak, "traffic": None,
                 "peak_source": "dense FP64 matmul measured in this run", "kernel": "grouped_gemm_f64 (H_AC apply)"}
 
-    # e2e: the public driver with the MPS state in pinned HOST memory; every step uploads the
-    # state, runs one sweep and reads back the state and the energies
-    state_h = {k: [t.detach().cpu().pin_memory() for t in getattr(vmx, k)] for k in ("AL", "AR", "C")}
-    h2d = sum(t.numel() * 8 for k in state_h for t in state_h[k])
-    et = []
-    for i in range(args.steps + 1):
-        t0 = time.perf_counter()
-        for k in ("AL", "AR", "C"):
-            for j, t in enumerate(state_h[k]):
-                getattr(vmx, k)[j].copy_(t, non_blocking=True)
-        E, F, prec = vmx.sweep()
-        for k in ("AL", "AR", "C"):
-            for j, t in enumerate(getattr(vmx, k)):
-                state_h[k][j].copy_(t, non_blocking=True)
-        torch.cuda.synchronize()
-        if i > 0:
-            et.append(time.perf_counter() - t0)
-    e2e = {"value": ws / float(np.mean(et)), "unit": "sweeps/s", "h2d_bytes_per_step": h2d,
-           "d2h_bytes_per_step": h2d + 16, "ms_per_step": 1e3 * float(np.mean(et)),
-           "path": "VumpsGPU.sweep with the MPS state copied host->device and back every sweep"}
+    e2e = {"value": ws / t_wall, "unit": "sweeps/s", "h2d_bytes_per_step": rmx["h2d"],
+           "d2h_bytes_per_step": rmx["h2d"] + 16, "ms_per_step": 1e3 * t_wall,
+           "path": "VumpsGPU.sweep (public driver) with the MPS state uploaded from pinned host memory before "
+                   "and read back after every timed sweep"}
 
     cpu = None
     if rank == 0 and not args.no_cpu:
         times, _ = cpu_sweeps(1, warm=1)
         cpu = {"value": 1.0 / float(np.mean(times)), "unit": "sweeps/s", "cores": os.cpu_count(), "kind": "port",
-               "sample": "1 VUMPS sweep (after 1 warm-up sweep) of the numpy restatement on XXZ D=512, all host "
-                         "threads, GMRES capped at 300 iterations/solve"}
+               "sample": "sweep 2 (after 1 warm-up sweep) of the numpy restatement of VUMPS_main on XXZ D=512, "
+                         "same tolerance schedule, all host threads, GMRES capped at 300 iterations/solve"}
     line = {"metric": METRIC, "value": value, "unit": "sweeps/s", "n_gpus": ws, "steps": args.steps,
             "warmup": args.warmup, "ms_per_step": t_step * 1e3, "higher_is_better": True, "scaling": "weak",
             "vs_baseline": None, "dtype": "bf16x6->f32 applies, f64 Krylov/decompositions" if args.precision == "bf16x6"
             else "f64", "data": "synthetic",
             "config": {"workload": WORKLOAD_DESC, "precision": args.precision, "seed": 1,
-                       "l2": "working set (~5 MB) is L2-resident by design; H_AC timing flushes L2 (512 MB write)",
+                       "l2": "working set (~40 MB) is L2-resident by design; H_AC timing flushes L2 (512 MB write)",
                        "parallelism": f"replicas x{ws}"},
-            "fp64": {"sweeps_per_s": 1.0 / float(np.mean(t64)), "ms_per_step": 1e3 * float(np.mean(t64)),
-                     "energy": float(E64.mean()), "grad_norm": float(F64.max()), "counts": c64},
-            "mixed": {"sweeps_per_s": 1.0 / float(np.mean(tmx)), "energy": float(Emx.mean()),
-                      "grad_norm": float(Fmx.max()), "counts": cmx},
-            "dE_mixed_vs_fp64": dE, "speedup_mixed_vs_fp64": float(np.mean(t64)) / float(np.mean(tmx)),
-            "h_ac": h_ac, "roofline": roof, "cpu_baseline": cpu, "e2e": e2e, "gpu_launches": launches,
-            "clocks": clk}
+            "fp64": {"sweeps_per_s": 1.0 / float(np.mean(r64["times"])), "ms_per_step": 1e3 * float(np.mean(r64["times"])),
+                     "energy": float(E64.mean()), "grad_norm": float(r64["F"].max()), "counts": r64["counts"]},
+            "mixed": {"sweeps_per_s": 1.0 / t_step, "energy": float(Emx.mean()),
+                      "grad_norm": float(rmx["F"].max()), "counts": rmx["counts"]},
+            "dE_mixed_vs_fp64": dE, "speedup_mixed_vs_fp64": float(np.mean(r64["times"])) / t_step,
+            "h_ac": h_ac, "roofline": roof, "cpu_baseline": cpu, "e2e": e2e, "gpu_launches": rmx["launches"],
+            "clocks": rmx["clocks"]}
     if rank == 0:
         print(json.dumps(line), flush=True)
     if ws > 1:
@@ -352,13 +370,55 @@ def run_hac(args):
                       "bytes_per_apply": w.bytes_per_apply()}), flush=True)
 
 
+def run_krylov(args):
+    import torch
+    from imps_cpp_tools_gb300 import _native as N
+    from imps_cpp_tools_gb300 import blocks as B
+    from imps_cpp_tools_gb300 import ops
+    from imps_cpp_tools_gb300.workload import HacWorkload
+    ctx = B.Context(0)
+    stream = torch.cuda.current_stream()
+    ctx.set_stream(stream)
+    w = HacWorkload(ctx, args.workload)
+    if args.precision == "bf16x6":
+        w.plan.set_precision(N.PREC_BF16X6)
+    lib = N.load()
+    x0 = torch.randn(w.n, dtype=torch.float64, device="cuda")
+    y = torch.empty_like(x0)
+    res = []
+    for rep in range(4):
+        x = x0.clone()
+        torch.cuda.synchronize()
+        l0 = lib.imps_launch_count()
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        e0.record(stream)
+        ev, na, conv = ops.eigs_rs(w.plan, x, 1e-30, ncv=64, maxit=8)
+        e1.record(stream)
+        torch.cuda.synchronize()
+        t_solve = e0.elapsed_time(e1) * 1e-3
+        launches = lib.imps_launch_count() - l0
+        e0.record(stream)
+        for _ in range(na):
+            lib.imps_hac_apply(w.plan.handle, x0.data_ptr(), y.data_ptr(), N.MEM_DEVICE)
+        e1.record(stream)
+        torch.cuda.synchronize()
+        t_apply = e0.elapsed_time(e1) * 1e-3
+        if rep:
+            res.append((t_solve, t_apply, na, launches))
+    t_solve, t_apply, na, launches = (float(np.median([r[i] for r in res])) for i in range(4))
+    print(json.dumps({"mode": "krylov", "workload": args.workload, "precision": args.precision, "applies": na,
+                      "us_per_iteration": 1e6 * t_solve / na, "us_per_apply": 1e6 * t_apply / na,
+                      "us_overhead_per_iteration": 1e6 * (t_solve - t_apply) / na,
+                      "launches_per_iteration": launches / na}), flush=True)
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
-    ap.add_argument("--steps", type=int, default=8)
-    ap.add_argument("--warmup", type=int, default=4)
+    ap.add_argument("--steps", type=int, default=47)
+    ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
-    ap.add_argument("--mode", default="vumps", choices=["vumps", "hac"])
+    ap.add_argument("--mode", default="vumps", choices=["vumps", "hac", "krylov"])
     ap.add_argument("--workload", default="xxz_d512")
     ap.add_argument("--precision", default="bf16x6", choices=["fp64", "bf16x6"])
     ap.add_argument("--no-cpu", action="store_true")
@@ -368,6 +428,8 @@ def main():
         run_reference(args)
     elif args.mode == "hac":
         run_hac(args)
+    elif args.mode == "krylov":
+        run_krylov(args)
     else:
         run_vumps(args)
 

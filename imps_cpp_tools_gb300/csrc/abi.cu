@@ -659,12 +659,8 @@ int imps_eigs_rs(imps_plan* p, double* x, int mem, double tol, int ncv, int maxi
   double* tmp = bp.take(ld);
   double* nrm = c->dscal + 8;
   int* bflag = c->dflag;
-  CK(cudaMemsetAsync(bflag, 0, sizeof(int), st));
-  CK(cudaMemsetAsync(Hd, 0, (size_t)ld * ld * 8, st));
   if (mem == IMPS_MEM_HOST) CK(cudaMemcpyAsync(xr, x, n * 8, cudaMemcpyHostToDevice, st));
   else CK(cudaMemcpyAsync(xr, x, n * 8, cudaMemcpyDeviceToDevice, st));
-  RC(kr_multidot(c->ws, xr, n, 1, xr, n, tmp, 0, nrm, st));
-  RC(kr_scale_inv(xr, nrm, V, n, bflag, st));
 
   // The device keeps full CGS2 columns h = V^T A v_j; the host keeps the tridiagonal part
   // (alpha_j = h_j, beta_j = |w_j|), exact up to rounding because the basis is kept
@@ -673,82 +669,119 @@ int imps_eigs_rs(imps_plan* p, double* x, int mem, double tol, int ncv, int maxi
   std::vector<double> ta(m + 1, 0.0), tb(m + 1, 0.0), z(m, 0.0);
   std::vector<double> th(kk), Z((size_t)m * kk), sv(kk), Q((size_t)kk * kk), qa(kk), qb(kk),
       Wr((size_t)m * kk);
-  int jstart = 0, jpulled = 0, applies = 0, status = IMPS_WARN_NOT_CONVERGED, kfinal = 0;
+  int applies = 0;
   double theta = 0.0, last_res = 0.0;
   const int chk = 4;
   // ARPACK's Ritz test (dsconv): |beta * y_k| <= tol * max(eps^(2/3), |theta|)
   const double eps23 = std::cbrt(kEps * kEps);
-  const double tol_eff = p->prec == IMPS_PREC_BF16X6 ? std::max(tol, kMixedEigTol) : tol;
-  bool done = false;
-  while (!done) {
-    for (int j = jstart; j < m; ++j) {
-      double* vj = V + (size_t)j * n;
-      double* hc = Hd + (size_t)j * ld;
-      RC(apply_dev(p, vj, w));
-      ++applies;
-      RC(kr_cgs2_step(c->ws, V, n, j + 1, w, n, hc, tmp, V + (size_t)(j + 1) * n, bflag, st));
-      const bool check = ((j + 1 - jstart) % chk == 0) || j == m - 1 || applies >= max_applies;
-      if (!check) continue;
-      CK(cudaMemcpyAsync(H.data() + (size_t)jpulled * ld, Hd + (size_t)jpulled * ld,
-                         (size_t)(j + 1 - jpulled) * ld * 8, cudaMemcpyDeviceToHost, st));
-      int hbreak = 0;
-      CK(cudaMemcpyAsync(&hbreak, bflag, sizeof(int), cudaMemcpyDeviceToHost, st));
+
+  // One thick-restart Lanczos run started from xr, at most `budget` applies; leaves the
+  // (unnormalised) lowest Ritz vector in xr.  With stall_exit the run also ends (not
+  // converged) once the Ritz residual has not halved over ~3 restart cycles: the floor of an
+  // inexact operator.
+  auto lanczos = [&](double tol_eff, int64_t budget, bool stall_exit) -> int {
+    CK(cudaMemsetAsync(bflag, 0, sizeof(int), st));
+    CK(cudaMemsetAsync(Hd, 0, (size_t)ld * ld * 8, st));
+    RC(kr_multidot(c->ws, xr, n, 1, xr, n, tmp, 0, nrm, st));
+    RC(kr_scale_inv(xr, nrm, V, n, bflag, st));
+    int jstart = 0, jpulled = 0, status = IMPS_WARN_NOT_CONVERGED, kfinal = 0;
+    int64_t used = 0, best_at = 0;
+    double best = std::numeric_limits<double>::infinity();
+    const int64_t stall_window = 3 * (int64_t)(m - kk) + m;
+    bool done = false;
+    while (!done) {
+      for (int j = jstart; j < m; ++j) {
+        double* vj = V + (size_t)j * n;
+        double* hc = Hd + (size_t)j * ld;
+        RC(apply_dev(p, vj, w));
+        ++applies;
+        ++used;
+        RC(kr_cgs2_step(c->ws, V, n, j + 1, w, n, hc, tmp, V + (size_t)(j + 1) * n, bflag, st));
+        const bool check = ((j + 1 - jstart) % chk == 0) || j == m - 1 || used >= budget;
+        if (!check) continue;
+        CK(cudaMemcpyAsync(H.data() + (size_t)jpulled * ld, Hd + (size_t)jpulled * ld,
+                           (size_t)(j + 1 - jpulled) * ld * 8, cudaMemcpyDeviceToHost, st));
+        int hbreak = 0;
+        CK(cudaMemcpyAsync(&hbreak, bflag, sizeof(int), cudaMemcpyDeviceToHost, st));
+        CK(cudaStreamSynchronize(st));
+        for (int q = jpulled; q <= j; ++q) {
+          ta[q] = H[(size_t)q + (size_t)q * ld];
+          tb[q] = H[(size_t)q + 1 + (size_t)q * ld];
+        }
+        jpulled = j + 1;
+        const int k = j + 1;
+        const double tn = tri_norm(k, ta.data(), tb.data());
+        theta = tri_eigval(k, ta.data(), tb.data(), 0);
+        if (!std::isfinite(theta)) return IMPS_ERR_NAN;
+        tri_eigvec(k, ta.data(), tb.data(), theta, tn, z.data(), nullptr, nullptr, 0);
+        const double res = std::fabs(tb[k - 1] * z[k - 1]);
+        last_res = res;
+        kfinal = k;
+        if (res <= tol_eff * std::max(std::fabs(theta), eps23) || hbreak) {
+          status = IMPS_OK;
+          done = true;
+          break;
+        }
+        if (used >= budget) { done = true; break; }
+        if (res < 0.5 * best) {
+          best = res;
+          best_at = used;
+        } else if (stall_exit && used - best_at > stall_window) {
+          done = true;
+          break;
+        }
+      }
+      if (done) break;
+      // Thick restart (Wu & Simon): keep the kk lowest Ritz pairs of T_m and the residual
+      // direction v_m.  The kept block is rotated so that T stays tridiagonal, with only its
+      // last vector coupled to v_m (coupling |s|, s_i = beta_{m-1} * y_i[m-1]).
+      const double tn = tri_norm(m, ta.data(), tb.data());
+      for (int i = 0; i < kk; ++i) th[i] = tri_eigval(m, ta.data(), tb.data(), i);
+      for (int i = 0; i < kk; ++i)
+        tri_eigvec(m, ta.data(), tb.data(), th[i], tn, Z.data() + (size_t)i * m, Z.data(), th.data(), i);
+      for (int i = 0; i < kk; ++i) sv[i] = tb[m - 1] * Z[(size_t)(m - 1) + (size_t)i * m];
+      arrow_tridiag(kk, th.data(), sv.data(), Q.data(), qa.data(), qb.data());
+      double sn = 0.0;
+      for (int i = 0; i < kk; ++i) sn += sv[i] * sv[i];
+      sn = std::sqrt(sn);
+      // new kept column p = Z * Q[:, kk-1-p], so that column kk-1 is the one coupled to v_m
+      for (int pc = 0; pc < kk; ++pc) {
+        const double* q = Q.data() + (size_t)(kk - 1 - pc) * kk;
+        for (int r = 0; r < m; ++r) {
+          double acc = 0.0;
+          for (int i = 0; i < kk; ++i) acc += Z[(size_t)r + (size_t)i * m] * q[i];
+          Wr[(size_t)r + (size_t)pc * m] = acc;
+        }
+      }
+      CK(cudaMemcpyAsync(Wrot, Wr.data(), (size_t)m * kk * 8, cudaMemcpyHostToDevice, st));
+      RC(kr_basis_rotate(V, n, m, Wrot, kk, Wk, n, n, st));
+      CK(cudaMemcpyAsync(V, Wk, (size_t)kk * n * 8, cudaMemcpyDeviceToDevice, st));
+      CK(cudaMemcpyAsync(V + (size_t)kk * n, V + (size_t)m * n, n * 8, cudaMemcpyDeviceToDevice, st));
+      for (int pc = 0; pc < kk; ++pc) ta[pc] = qa[kk - 1 - pc];
+      for (int pc = 0; pc + 1 < kk; ++pc) tb[pc] = qb[kk - 2 - pc];
+      tb[kk - 1] = sn;
       CK(cudaStreamSynchronize(st));
-      for (int q = jpulled; q <= j; ++q) {
-        ta[q] = H[(size_t)q + (size_t)q * ld];
-        tb[q] = H[(size_t)q + 1 + (size_t)q * ld];
-      }
-      jpulled = j + 1;
-      const int k = j + 1;
-      const double tn = tri_norm(k, ta.data(), tb.data());
-      theta = tri_eigval(k, ta.data(), tb.data(), 0);
-      if (!std::isfinite(theta)) return IMPS_ERR_NAN;
-      tri_eigvec(k, ta.data(), tb.data(), theta, tn, z.data(), nullptr, nullptr, 0);
-      const double res = std::fabs(tb[k - 1] * z[k - 1]);
-      last_res = res;
-      kfinal = k;
-      if (res <= tol_eff * std::max(std::fabs(theta), eps23) || hbreak) {
-        status = IMPS_OK;
-        done = true;
-        break;
-      }
-      if (applies >= max_applies) { done = true; break; }
+      jstart = jpulled = kk;
     }
-    if (done) break;
-    // Thick restart (Wu & Simon): keep the kk lowest Ritz pairs of T_m and the residual
-    // direction v_m.  The kept block is rotated so that T stays tridiagonal, with only its
-    // last vector coupled to v_m (coupling |s|, s_i = beta_{m-1} * y_i[m-1]).
-    const double tn = tri_norm(m, ta.data(), tb.data());
-    for (int i = 0; i < kk; ++i) th[i] = tri_eigval(m, ta.data(), tb.data(), i);
-    for (int i = 0; i < kk; ++i)
-      tri_eigvec(m, ta.data(), tb.data(), th[i], tn, Z.data() + (size_t)i * m, Z.data(), th.data(), i);
-    for (int i = 0; i < kk; ++i) sv[i] = tb[m - 1] * Z[(size_t)(m - 1) + (size_t)i * m];
-    arrow_tridiag(kk, th.data(), sv.data(), Q.data(), qa.data(), qb.data());
-    double sn = 0.0;
-    for (int i = 0; i < kk; ++i) sn += sv[i] * sv[i];
-    sn = std::sqrt(sn);
-    // new kept column p = Z * Q[:, kk-1-p], so that column kk-1 is the one coupled to v_m
-    for (int pc = 0; pc < kk; ++pc) {
-      const double* q = Q.data() + (size_t)(kk - 1 - pc) * kk;
-      for (int r = 0; r < m; ++r) {
-        double acc = 0.0;
-        for (int i = 0; i < kk; ++i) acc += Z[(size_t)r + (size_t)i * m] * q[i];
-        Wr[(size_t)r + (size_t)pc * m] = acc;
-      }
-    }
-    CK(cudaMemcpyAsync(Wrot, Wr.data(), (size_t)m * kk * 8, cudaMemcpyHostToDevice, st));
-    RC(kr_basis_rotate(V, n, m, Wrot, kk, Wk, n, n, st));
-    CK(cudaMemcpyAsync(V, Wk, (size_t)kk * n * 8, cudaMemcpyDeviceToDevice, st));
-    CK(cudaMemcpyAsync(V + (size_t)kk * n, V + (size_t)m * n, n * 8, cudaMemcpyDeviceToDevice, st));
-    for (int pc = 0; pc < kk; ++pc) ta[pc] = qa[kk - 1 - pc];
-    for (int pc = 0; pc + 1 < kk; ++pc) tb[pc] = qb[kk - 2 - pc];
-    tb[kk - 1] = sn;
+    // Ritz vector x = V[:, 0..k-1] z
+    CK(cudaMemcpyAsync(tmp, z.data(), kfinal * 8, cudaMemcpyHostToDevice, st));
+    RC(kr_gemv(V, n, kfinal, tmp, xr, n, st));
     CK(cudaStreamSynchronize(st));
-    jstart = jpulled = kk;
+    return status;
+  };
+
+  const bool mixed = p->prec == IMPS_PREC_BF16X6;
+  int status = lanczos(mixed ? std::max(tol, kMixedEigTol) : tol, max_applies, mixed);
+  const int applies_mixed = mixed ? applies : 0;
+  if (status >= 0 && mixed && (status != IMPS_OK || tol < kMixedEigTol) && applies < max_applies) {
+    // Splitting operands into BF16 terms rounds, so the split-BF16 operator is linear only to
+    // ~1e-7 |H| and its Lanczos residual floors there; FP64 applies finish the solve from
+    // the mixed Ritz vector.
+    p->prec = IMPS_PREC_FP64;
+    status = lanczos(tol, std::max<int64_t>(max_applies - applies, m), false);
+    p->prec = IMPS_PREC_BF16X6;
   }
-  // Ritz vector x = V[:, 0..k-1] z
-  CK(cudaMemcpyAsync(tmp, z.data(), kfinal * 8, cudaMemcpyHostToDevice, st));
-  RC(kr_gemv(V, n, kfinal, tmp, xr, n, st));
+  if (status < 0) return status;
   // normalise
   RC(kr_multidot(c->ws, xr, n, 1, xr, n, tmp, 0, nrm, st));
   if (mem == IMPS_MEM_HOST) {
@@ -761,8 +794,9 @@ int imps_eigs_rs(imps_plan* p, double* x, int mem, double tol, int ncv, int maxi
   if (eval) *eval = theta;
   if (n_applies) *n_applies = applies;
   if (debug_on())
-    fprintf(stderr, "[imps eigs_rs] n=%lld prec=%d applies=%d theta=%.15g res=%.3e tol=%.1e status=%d\n",
-            (long long)n, p->prec, applies, theta, last_res, tol, status);
+    fprintf(stderr,
+            "[imps eigs_rs] n=%lld prec=%d applies=%d (split-bf16 %d) theta=%.15g res=%.3e tol=%.1e status=%d\n",
+            (long long)n, p->prec, applies, applies_mixed, theta, last_res, tol, status);
   return status;
 }
 
@@ -810,6 +844,8 @@ static int gmres_proj(imps_plan* p, const double* b, double* y, const double* rh
   // restarted GMRES acts as iterative refinement with FP64 residuals.
   const int prec_saved = p->prec;
   const bool mixed = prec_saved == IMPS_PREC_BF16X6;
+  int stall = 0;
+  double rn_prev = 0.0;
   for (int outer = 0; it < maxit; ++outer) {
     // r = b - A(y)  (FP64 residual)
     p->prec = IMPS_PREC_FP64;
@@ -826,6 +862,12 @@ static int gmres_proj(imps_plan* p, const double* b, double* y, const double* rh
     if (debug_level() > 1)
       fprintf(stderr, "[imps gmres]   outer=%d it=%d relres=%.3e\n", outer, it, rel);
     if (rn < tol * bnorm) { status = IMPS_OK; break; }
+    // At the attainable accuracy (~eps * |A| |y| / |b|) the recomputed residual stops falling
+    // while the Krylov estimate keeps "converging": three restarts that gain < 10% each end
+    // the solve (not converged, result returned) instead of running into maxit.
+    stall = outer > 0 && rn > 0.9 * rn_prev ? stall + 1 : 0;
+    rn_prev = rn;
+    if (stall >= 3) break;
     CK(cudaMemsetAsync(bflag, 0, sizeof(int), st));
     RC(kr_scale_inv(w, dsc + 1, V, n, bflag, st));
     CK(cudaMemsetAsync(gam, 0, ld * 8, st));

@@ -19,8 +19,8 @@ from . import models, ops
 
 class VumpsGPU:
     def __init__(self, ctx, model, dims0=None, dimvec=None, seed=1, InvETol=5e-15, InvEfac=2.0,
-                 fixed_tol=None, trueLR=True, svdthresh=5e-7, precision="fp64", init_state=None,
-                 lanczos_maxit=300, gmres_maxit=4000, lanczos_ncv=64, verbose=False, **params):
+                 fixed_tol=None, tolmin=5e-16, tolmax=1e-6, trueLR=True, svdthresh=5e-7, precision="fp64",
+                 init_state=None, lanczos_maxit=300, gmres_maxit=4000, lanczos_ncv=64, verbose=False, **params):
         import torch
         self.torch = torch
         self.verbose = verbose
@@ -31,6 +31,7 @@ class VumpsGPU:
             dimvec = models.make_dims(dims0, 2, self.I2K)
         self.dimvec = dimvec
         self.InvETol, self.InvEfac, self.fixed_tol, self.trueLR = InvETol, InvEfac, fixed_tol, trueLR
+        self.tolmin, self.tolmax = tolmin, tolmax  # VUMPS_main.cpp:37-38
         self.svdthresh = svdthresh
         self.lanczos_maxit, self.gmres_maxit = lanczos_maxit, gmres_maxit
         # Krylov dimension of the H_AC / H_C eigensolves.  eigs.cpp:4 uses 20; the effective
@@ -97,8 +98,6 @@ class VumpsGPU:
         # (= bond a), right -> left bond of A(a) (= bond a)
         self.optm_l = [B.plan_optm(ctx, LA[a], LA[1 - a], d, hnnz, 0, LB[a]) for a in range(2)]
         self.optm_r = [B.plan_optm(ctx, LA[a], LA[1 - a], d, hnnz, 1, LB[a]) for a in range(2)]
-        for s in ("tm_l", "tm_r"):
-            pass
         self.flops_hac = [p.info()["flops_apply"] for p in self.p_hac]
         if self.precision == "bf16x6":
             # tensor-core applies inside the Krylov solvers; Krylov vectors, residuals,
@@ -252,11 +251,16 @@ class VumpsGPU:
         # gradient norm (GradNormRight, VUMPS_helpers.hpp:145-153) at AC = C[n] AR(n)
         AC = self._mul(self.p_ac[n], self.AR[n], self.C[l], self._z(self.LA[n]))
         Y = self._z(self.LA[n])
+        # the gradient H_AC.AC - AL.H_C.C is a convergence measure: always FP64
+        if self.precision == "bf16x6":
+            hac.set_precision(N.PREC_FP64)
         ops.ApplyHAvec(hac, AC, Y)
+        if self.precision == "bf16x6":
+            hac.set_precision(N.PREC_BF16X6)
         g = self.p_grad[n]
         g.bind(0, Y); g.bind(1, self.AR[n]); g.bind(2, self._z(self.LA[n]))
         self.F[n] = ops.GradNormRight(g)
-        tol = self.fixed_tol if self.fixed_tol else min(max(self.prec[n] / 100.0, 5e-16), 1e-6)
+        tol = self.fixed_tol if self.fixed_tol else min(max(self.prec[n] / 100.0, self.tolmin), self.tolmax)
         # H_AC eigensolve (eigs_rs "SA", x0 = AC)
         ev, na, _ = ops.eigs_rs(hac, AC, tol, ncv=self.lanczos_ncv, maxit=self.lanczos_maxit)
         self.stats["lanczos_applies"] += na

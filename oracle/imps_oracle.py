@@ -875,11 +875,12 @@ class VUMPS:
     """Restatement of one VUMPS_main run with ExpandFromH disabled (mmax = D)."""
 
     def __init__(self, h, d, I2K, dmap0, N=2, seed=1, InvETol=5e-15, InvEfac=2.0, fixed_tol=None,
-                 trueLR=True, svdthresh=5e-7, dimvec=None, init=None, gmres_maxit=0):
+                 tolmin=5e-16, tolmax=1e-6, trueLR=True, svdthresh=5e-7, dimvec=None, init=None, gmres_maxit=0):
         self.hnnz = sparse_nnz(h)
         self.gmres_maxit = gmres_maxit  # 0: the reference's maxit = problem size
         self.d, self.N, self.I2K = d, N, I2K
         self.InvETol, self.InvEfac, self.fixed_tol, self.trueLR = InvETol, InvEfac, fixed_tol, trueLR
+        self.tolmin, self.tolmax = tolmin, tolmax  # VUMPS_main.cpp:37-38
         self.svdthresh = svdthresh
         self.rng = np.random.default_rng(seed)
         if dimvec is None:
@@ -917,7 +918,7 @@ class VUMPS:
         EHL, EHR, HL, HR = self.EHL, self.EHR, self.HL, self.HR
         HA = lambda X: ApplyHA(X, EHL, EHR, HL, HR)
         self.F[nn] = GradNormRight(AR[-1], C[-1], HA)
-        tol = self.fixed_tol if self.fixed_tol else min(max(self.prec[nn] / 100.0, 5e-16), 1e-6)
+        tol = self.fixed_tol if self.fixed_tol else min(max(self.prec[nn] / 100.0, self.tolmin), self.tolmax)
         AC = bd_mul_mps(C[-1], AR[-1])
         Adims = mps_sizes(AC)
         Am = mps_nelem(AC)
