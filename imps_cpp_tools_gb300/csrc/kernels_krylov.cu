@@ -15,7 +15,7 @@ namespace {
 
 constexpr int RB = 256;      // threads per reduction block
 constexpr int RGRID = 128;   // fixed reduction grid of multidot (RGRID * kMaxCols partials)
-constexpr int CGRID = 608;   // max grid of the fused CGS2 kernels (4 blocks per SM)
+constexpr int CGRID = 152;   // max grid of the fused CGS2 kernels (one block per SM)
 constexpr int CSUB = 1024;   // rows of w staged in shared memory per CGS2 sub-chunk
 
 __device__ __forceinline__ double warp_sum(double v) {
@@ -79,22 +79,25 @@ __global__ void __launch_bounds__(RB) multidot_kernel(const double* __restrict__
 //   MODE 0:  h = V^T w
 //   MODE 1:  w -= V hin;  h = V^T w;  hacc += h      (second CGS pass)
 //   MODE 2:  w -= V hin;  *hout = |w|
-// Each block walks sub-chunks of <= CSUB rows (grid-stride): the (updated) rows of w are
-// staged in shared memory, then warps take groups of 4 columns and lanes stride the rows, so
-// V is read coalesced and the chunk just read for the update is re-read from L2.  Per-block
-// column sums go to partials[c * gridDim.x + block]; the last block to finish reduces them in
-// a fixed order (bitwise reproducible) and resets the counter.
+// At most one block per SM (CT threads); each walks sub-chunks of <= CSUB rows (grid-stride).
+// The (updated) rows of w are staged in shared memory, then warps take groups of 4 columns and
+// lanes stride the rows, so V is read coalesced and the chunk just read for the update is
+// re-read from L2.  Per-block column sums go to partials[c * gridDim.x + block]; the last
+// block to finish reduces them in a fixed order (bitwise reproducible), with L2 loads unrolled
+// four deep so that the tail is one round of latency per column group, and resets the counter.
+constexpr int CT = 512;
 template <int MODE>
-__global__ void __launch_bounds__(256) cgs_pass_kernel(const double* __restrict__ V, int64_t ldv, int nc,
-                                                      double* __restrict__ w, int64_t n, int sub,
-                                                      const double* hin, double* hout, double* hacc,
-                                                      double* __restrict__ partials,
-                                                      unsigned int* __restrict__ counter) {
+__global__ void __launch_bounds__(CT) cgs_pass_kernel(const double* __restrict__ V, int64_t ldv, int nc,
+                                                     double* __restrict__ w, int64_t n, int sub,
+                                                     const double* hin, double* hout, double* hacc,
+                                                     double* __restrict__ partials,
+                                                     unsigned int* __restrict__ counter) {
   __shared__ double wsm[CSUB];
   __shared__ double hs[imps::kMaxCols];
   __shared__ double sacc[imps::kMaxCols];
   __shared__ double sh[32];
   __shared__ bool last;
+  constexpr int NW = CT / 32;
   const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
   if (MODE != 0)
     for (int c = threadIdx.x; c < nc; c += blockDim.x) hs[c] = hin[c];
@@ -108,16 +111,14 @@ __global__ void __launch_bounds__(256) cgs_pass_kernel(const double* __restrict_
       double x = w[r];
       if (MODE != 0) {
         const double* vr = V + r;
-        double x1 = 0.0, x2 = 0.0, x3 = 0.0;
+        double a[8] = {0.0, 0.0, 0.0, 0.0, 0.0, 0.0, 0.0, 0.0};
         int c = 0;
-        for (; c + 4 <= nc; c += 4) {
-          x = fma(-vr[(int64_t)c * ldv], hs[c], x);
-          x1 = fma(-vr[(int64_t)(c + 1) * ldv], hs[c + 1], x1);
-          x2 = fma(-vr[(int64_t)(c + 2) * ldv], hs[c + 2], x2);
-          x3 = fma(-vr[(int64_t)(c + 3) * ldv], hs[c + 3], x3);
+        for (; c + 8 <= nc; c += 8) {
+#pragma unroll
+          for (int q = 0; q < 8; ++q) a[q] = fma(-vr[(int64_t)(c + q) * ldv], hs[c + q], a[q]);
         }
-        for (; c < nc; ++c) x = fma(-vr[(int64_t)c * ldv], hs[c], x);
-        x = (x + x1) + (x2 + x3);
+        for (; c < nc; ++c) a[0] = fma(-vr[(int64_t)c * ldv], hs[c], a[0]);
+        x += ((a[0] + a[1]) + (a[2] + a[3])) + ((a[4] + a[5]) + (a[6] + a[7]));
         w[r] = x;
       }
       if (MODE == 2) nacc = fma(x, x, nacc);
@@ -125,7 +126,7 @@ __global__ void __launch_bounds__(256) cgs_pass_kernel(const double* __restrict_
     }
     if (MODE == 2) continue;
     __syncthreads();
-    for (int c0 = warp * 4; c0 < nc; c0 += 32) {
+    for (int c0 = warp * 4; c0 < nc; c0 += 4 * NW) {
       // columns past nc read column nc-1 (valid memory) and are discarded
       const double* v0 = V + base + (int64_t)min(c0, nc - 1) * ldv;
       const double* v1 = V + base + (int64_t)min(c0 + 1, nc - 1) * ldv;
@@ -166,17 +167,25 @@ __global__ void __launch_bounds__(256) cgs_pass_kernel(const double* __restrict_
   __syncthreads();
   if (!last) return;
   __threadfence();
-  const volatile double* pv = partials;
+  // partials written by other blocks: read through L2 (__ldcg), never a stale L1 line
   if (MODE == 2) {
     double v = 0.0;
-    for (int b = threadIdx.x; b < G; b += blockDim.x) v += pv[b];
+    for (int b = threadIdx.x; b < G; b += blockDim.x) v += __ldcg(partials + b);
     v = block_sum(v, sh);
     if (threadIdx.x == 0) *hout = sqrt(v);
   } else {
-    for (int c = warp; c < nc; c += 8) {
-      double v = 0.0;
-      for (int b = lane; b < G; b += 32) v += pv[(int64_t)c * G + b];
-      v = warp_sum(v);
+    for (int c = warp; c < nc; c += NW) {
+      const double* pc = partials + (int64_t)c * G;
+      double s0 = 0.0, s1 = 0.0, s2 = 0.0, s3 = 0.0;
+      int b = lane;
+      for (; b + 96 < G; b += 128) {
+        s0 += __ldcg(pc + b);
+        s1 += __ldcg(pc + b + 32);
+        s2 += __ldcg(pc + b + 64);
+        s3 += __ldcg(pc + b + 96);
+      }
+      for (; b < G; b += 32) s0 += __ldcg(pc + b);
+      double v = warp_sum((s0 + s1) + (s2 + s3));
       if (lane == 0) {
         hout[c] = v;
         if (MODE == 1) hacc[c] += v;
@@ -456,7 +465,7 @@ int kr_basis_rotate(const double* V, int64_t ldv, int m, const double* W, int kk
 int kr_cgs2_step(const KrylovWs& ws, const double* V, int64_t ldv, int nc, double* w, int64_t n,
                  double* h, double* h2, double* vnext, int* flag, cudaStream_t st) {
   if (nc < 1 || nc > kMaxCols) return IMPS_ERR_BAD_ARG;
-  int64_t g = (n + 127) / 128;
+  int64_t g = (n + 255) / 256;  // >= 256 rows per block, at most one block per SM
   if (g > CGRID) g = CGRID;
   if (g < 1) g = 1;
   const int grid = (int)g;
@@ -464,11 +473,11 @@ int kr_cgs2_step(const KrylovWs& ws, const double* V, int64_t ldv, int nc, doubl
   sub = ((sub + 31) / 32) * 32;
   if (sub > CSUB) sub = CSUB;
   imps::count_launch(4);
-  cgs_pass_kernel<0><<<grid, 256, 0, st>>>(V, ldv, nc, w, n, (int)sub, nullptr, h, nullptr, ws.partials,
-                                           ws.counter);
-  cgs_pass_kernel<1><<<grid, 256, 0, st>>>(V, ldv, nc, w, n, (int)sub, h, h2, h, ws.partials, ws.counter);
-  cgs_pass_kernel<2><<<grid, 256, 0, st>>>(V, ldv, nc, w, n, (int)sub, h2, h + nc, nullptr, ws.partials,
-                                           ws.counter);
+  cgs_pass_kernel<0><<<grid, CT, 0, st>>>(V, ldv, nc, w, n, (int)sub, nullptr, h, nullptr, ws.partials,
+                                          ws.counter);
+  cgs_pass_kernel<1><<<grid, CT, 0, st>>>(V, ldv, nc, w, n, (int)sub, h, h2, h, ws.partials, ws.counter);
+  cgs_pass_kernel<2><<<grid, CT, 0, st>>>(V, ldv, nc, w, n, (int)sub, h2, h + nc, nullptr, ws.partials,
+                                          ws.counter);
   scale_inv_kernel<<<grid_for(n), 256, 0, st>>>(w, h + nc, vnext, n, flag);
   return IMPS_OK;
 }

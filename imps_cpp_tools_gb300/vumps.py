@@ -41,7 +41,7 @@ class VumpsGPU:
         self.lanczos_ncv = lanczos_ncv
         self.precision = precision
         self.rng = np.random.default_rng(seed)
-        self.stats = {"lanczos_applies": 0, "gmres_iters": 0, "hac_applies": 0}
+        self.stats = {"lanczos_applies": 0, "gmres_iters": 0, "hac_applies": 0, "hc_applies": 0}
         d, hnnz = self.d, self.hnnz
         self.LA = [B.Layout.mps(self.I2K, dimvec[n], dimvec[1 - n]) for n in range(2)]
         self.LB = [B.Layout.blockdiag(dimvec[b]) for b in range(2)]
@@ -274,6 +274,7 @@ class VumpsGPU:
         _, na1, _ = ops.eigs_rs(pl, CL, tol, ncv=self.lanczos_ncv, maxit=self.lanczos_maxit)
         _, na2, _ = ops.eigs_rs(pr, CR, tol, ncv=self.lanczos_ncv, maxit=self.lanczos_maxit)
         self.stats["lanczos_applies"] += na1 + na2
+        self.stats["hc_applies"] += na1 + na2
         ops.sign_normalize(ctx, CL)
         ops.sign_normalize(ctx, CR)
         if self.dosvd and self.prec[n] < self.svdthresh:
