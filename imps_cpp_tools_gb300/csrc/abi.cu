@@ -255,6 +255,8 @@ int imps_ctx_create(int device, imps_ctx** out) {
   CK(cudaMemset(c->dscal, 0, 64 * sizeof(double)));
   CK(cudaMalloc(&c->dflag, 16 * sizeof(int)));
   CK(cudaMemset(c->dflag, 0, 16 * sizeof(int)));
+  c->ws.sync = c->ws.counter + 1;  // counter[0]: last-block reductions; [1], [2]: grid barrier
+  c->ws.err = c->dflag + 4;
   *out = c;
   return IMPS_OK;
 }
@@ -701,9 +703,14 @@ int imps_eigs_rs(imps_plan* p, double* x, int mem, double tol, int ncv, int maxi
         if (!check) continue;
         CK(cudaMemcpyAsync(H.data() + (size_t)jpulled * ld, Hd + (size_t)jpulled * ld,
                            (size_t)(j + 1 - jpulled) * ld * 8, cudaMemcpyDeviceToHost, st));
-        int hbreak = 0;
+        int hbreak = 0, terr = 0;
         CK(cudaMemcpyAsync(&hbreak, bflag, sizeof(int), cudaMemcpyDeviceToHost, st));
+        CK(cudaMemcpyAsync(&terr, c->ws.err, sizeof(int), cudaMemcpyDeviceToHost, st));
         CK(cudaStreamSynchronize(st));
+        if (terr) {  // a grid-barrier wait of the CGS2 step ran out: report, re-arm the flag
+          CK(cudaMemsetAsync(c->ws.err, 0, sizeof(int), st));
+          return IMPS_ERR_TIMEOUT;
+        }
         for (int q = jpulled; q <= j; ++q) {
           ta[q] = H[(size_t)q + (size_t)q * ld];
           tb[q] = H[(size_t)q + 1 + (size_t)q * ld];
@@ -882,10 +889,15 @@ static int gmres_proj(imps_plan* p, const double* b, double* y, const double* rh
       kdim = j + 1;
       if ((j + 1) % 4 == 0 || j == m - 1 || it >= maxit) {
         double res = 0.0;
-        int brk = 0;
+        int brk = 0, terr = 0;
         CK(cudaMemcpyAsync(&res, dsc + 3, 8, cudaMemcpyDeviceToHost, st));
         CK(cudaMemcpyAsync(&brk, bflag, sizeof(int), cudaMemcpyDeviceToHost, st));
+        CK(cudaMemcpyAsync(&terr, c->ws.err, sizeof(int), cudaMemcpyDeviceToHost, st));
         CK(cudaStreamSynchronize(st));
+        if (terr) {
+          CK(cudaMemsetAsync(c->ws.err, 0, sizeof(int), st));
+          return IMPS_ERR_TIMEOUT;
+        }
         if (!std::isfinite(res)) return IMPS_ERR_NAN;
         if (brk) { kdim = j; break; }  // invariant subspace
         if (res < std::max(tol * bnorm, mixed ? kMixedInnerTol * rn : 0.0)) break;

@@ -15,6 +15,8 @@ constexpr int kGmresKrylov = 80;  // default restart length of the device GMRES
 struct KrylovWs {
   double* partials = nullptr;     // kr_partials_elems() doubles
   unsigned int* counter = nullptr;
+  unsigned int* sync = nullptr;   // 2 zeroed counters of the cooperative CGS2 step (grid barrier)
+  int* err = nullptr;             // set when a grid-barrier wait times out
 };
 
 size_t kr_partials_elems();
@@ -26,7 +28,8 @@ int kr_gemv(const double* V, int64_t ldv, int ncols, const double* h, double* y,
             cudaStream_t st);
 // One CGS2 Lanczos/Arnoldi step on w = A v_{nc-1} against V[:, 0..nc-1]: h[0..nc-1] = total
 // projection coefficients, h[nc] = |w| after projection, vnext = w / h[nc] (flag set when
-// |w| underflows); h2 (nc doubles) is scratch.  Four launches.
+// |w| underflows); h2 (nc doubles) is scratch.  One cooperative launch when n <= 152 * 2048
+// (else, or when the cooperative launch is refused, four launches).
 int kr_cgs2_step(const KrylovWs& ws, const double* V, int64_t ldv, int nc, double* w, int64_t n,
                  double* h, double* h2, double* vnext, int* flag, cudaStream_t st);
 int kr_basis_rotate(const double* V, int64_t ldv, int m, const double* W, int kk, double* out,

@@ -195,6 +195,185 @@ __global__ void __launch_bounds__(CT) cgs_pass_kernel(const double* __restrict__
   if (threadIdx.x == 0) *counter = 0u;
 }
 
+// ---- single-launch CGS2 step (cooperative grid, all blocks co-resident) ----------------------
+// Block b owns rows [b*sub, (b+1)*sub) of w (sub <= COOP_SUB), kept in shared memory through the
+// three passes.  Each reduction is one grid barrier: every block writes its per-column partial
+// sums, then every block sums all partials itself in the same fixed order (identical,
+// reproducible results in every block).  Barrier waits are bounded: on timeout *err is set, the
+// remaining work is skipped, and the exit protocol still resets the counters.
+constexpr int COOP_SUB = 2048;
+
+__device__ __forceinline__ unsigned ld_acquire_u32(const unsigned int* p) {
+  unsigned v;
+  asm volatile("ld.acquire.gpu.global.u32 %0, [%1];" : "=r"(v) : "l"(p) : "memory");
+  return v;
+}
+
+// arrival counter sync[0] grows by gridDim.x per barrier; target = k * gridDim.x at barrier k
+__device__ bool grid_barrier(unsigned int* sync, unsigned target, int* err, bool ok) {
+  __shared__ int good;
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    int g = ok ? 1 : 0;
+    __threadfence();
+    atomicAdd(sync, 1u);
+    if (g) {
+      for (long long it = 0; ld_acquire_u32(sync) < target; ++it) {
+        if (it > (1ll << 22) || *(volatile int*)err) {
+          atomicExch(err, 1);
+          g = 0;
+          break;
+        }
+        __nanosleep(32);
+      }
+    }
+    good = g;
+  }
+  __syncthreads();
+  return good != 0;
+}
+
+// dst[c] = sum_b P[c*G + b] for c < nc (warps over columns, lanes over blocks, L2 loads)
+__device__ void reduce_partials(const double* P, int G, int nc, double* dst) {
+  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31, nw = blockDim.x >> 5;
+  for (int c = warp; c < nc; c += nw) {
+    const double* pc = P + (int64_t)c * G;
+    double s0 = 0.0, s1 = 0.0, s2 = 0.0, s3 = 0.0;
+    int b = lane;
+    for (; b + 96 < G; b += 128) {
+      s0 += __ldcg(pc + b);
+      s1 += __ldcg(pc + b + 32);
+      s2 += __ldcg(pc + b + 64);
+      s3 += __ldcg(pc + b + 96);
+    }
+    for (; b < G; b += 32) s0 += __ldcg(pc + b);
+    const double v = warp_sum((s0 + s1) + (s2 + s3));
+    if (lane == 0) dst[c] = v;
+  }
+}
+
+// P[c*G + block] = sum_{t < len} Vb[t + c*ldv] * x[t]  (x in shared memory)
+__device__ void block_dots(const double* __restrict__ Vb, int64_t ldv, int nc, const double* x, int len,
+                           double* P, int G) {
+  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31, nw = blockDim.x >> 5;
+  for (int c0 = warp * 4; c0 < nc; c0 += 4 * nw) {
+    const double* v0 = Vb + (int64_t)min(c0, nc - 1) * ldv;
+    const double* v1 = Vb + (int64_t)min(c0 + 1, nc - 1) * ldv;
+    const double* v2 = Vb + (int64_t)min(c0 + 2, nc - 1) * ldv;
+    const double* v3 = Vb + (int64_t)min(c0 + 3, nc - 1) * ldv;
+    double a0 = 0.0, a1 = 0.0, a2 = 0.0, a3 = 0.0;
+    for (int t = lane; t < len; t += 32) {
+      const double xt = x[t];
+      a0 = fma(v0[t], xt, a0);
+      a1 = fma(v1[t], xt, a1);
+      a2 = fma(v2[t], xt, a2);
+      a3 = fma(v3[t], xt, a3);
+    }
+    a0 = warp_sum(a0);
+    a1 = warp_sum(a1);
+    a2 = warp_sum(a2);
+    a3 = warp_sum(a3);
+    if (lane == 0) {
+      P[(int64_t)c0 * G + blockIdx.x] = a0;
+      if (c0 + 1 < nc) P[(int64_t)(c0 + 1) * G + blockIdx.x] = a1;
+      if (c0 + 2 < nc) P[(int64_t)(c0 + 2) * G + blockIdx.x] = a2;
+      if (c0 + 3 < nc) P[(int64_t)(c0 + 3) * G + blockIdx.x] = a3;
+    }
+  }
+}
+
+// x[t] -= sum_c Vb[t + c*ldv] * hs[c]
+__device__ void update_rows(const double* __restrict__ Vb, int64_t ldv, int nc, const double* hs, double* x,
+                            int len) {
+  for (int t = threadIdx.x; t < len; t += blockDim.x) {
+    const double* vr = Vb + t;
+    double a[8] = {0.0, 0.0, 0.0, 0.0, 0.0, 0.0, 0.0, 0.0};
+    int c = 0;
+    for (; c + 8 <= nc; c += 8) {
+#pragma unroll
+      for (int q = 0; q < 8; ++q) a[q] = fma(-vr[(int64_t)(c + q) * ldv], hs[c + q], a[q]);
+    }
+    for (; c < nc; ++c) a[0] = fma(-vr[(int64_t)c * ldv], hs[c], a[0]);
+    x[t] += ((a[0] + a[1]) + (a[2] + a[3])) + ((a[4] + a[5]) + (a[6] + a[7]));
+  }
+}
+
+__global__ void __launch_bounds__(CT) cgs2_coop_kernel(const double* __restrict__ V, int64_t ldv, int nc,
+                                                      double* __restrict__ w, int64_t n, int sub, double* h,
+                                                      double* __restrict__ vnext, int* flag,
+                                                      double* __restrict__ partials, unsigned int* sync,
+                                                      int* err) {
+  __shared__ double wsm[COOP_SUB];
+  __shared__ double h1[imps::kMaxCols];
+  __shared__ double h2[imps::kMaxCols];
+  __shared__ double sh[32];
+  __shared__ double beta;
+  const int G = gridDim.x;
+  const int64_t base = (int64_t)blockIdx.x * sub;
+  const int len = (int)max((int64_t)0, min((int64_t)sub, n - base));
+  const double* Vb = V + base;
+  double* P0 = partials;
+  double* P1 = partials + (int64_t)G * imps::kMaxCols;
+  double* P2 = P1 + (int64_t)G * imps::kMaxCols;
+  bool ok = true;
+  for (int t = threadIdx.x; t < len; t += blockDim.x) wsm[t] = w[base + t];
+  __syncthreads();
+  // pass 1: h1 = V^T w
+  block_dots(Vb, ldv, nc, wsm, len, P0, G);
+  ok = grid_barrier(sync, (unsigned)G, err, ok);
+  if (ok) reduce_partials(P0, G, nc, h1);
+  __syncthreads();
+  // pass 2: w -= V h1; h2 = V^T w
+  if (ok) {
+    update_rows(Vb, ldv, nc, h1, wsm, len);
+    __syncthreads();
+    block_dots(Vb, ldv, nc, wsm, len, P1, G);
+  }
+  ok = grid_barrier(sync, 2u * G, err, ok);
+  if (ok) reduce_partials(P1, G, nc, h2);
+  __syncthreads();
+  // pass 3: w -= V h2; beta = |w|
+  double nacc = 0.0;
+  if (ok) {
+    update_rows(Vb, ldv, nc, h2, wsm, len);
+    __syncthreads();
+    for (int t = threadIdx.x; t < len; t += blockDim.x) nacc = fma(wsm[t], wsm[t], nacc);
+  }
+  nacc = block_sum(nacc, sh);
+  if (threadIdx.x == 0) P2[blockIdx.x] = nacc;
+  ok = grid_barrier(sync, 3u * G, err, ok);
+  if (ok) {
+    reduce_partials(P2, G, 1, sh);  // warp 0 writes sh[0]
+    __syncthreads();
+    if (threadIdx.x == 0) beta = sqrt(sh[0]);
+    __syncthreads();
+    const double bt = beta;
+    const bool bad = !(fabs(bt) > 1e-300) || !isfinite(bt);
+    const double inv = bad ? 0.0 : 1.0 / bt;
+    for (int t = threadIdx.x; t < len; t += blockDim.x) {
+      w[base + t] = wsm[t];
+      vnext[base + t] = wsm[t] * inv;
+    }
+    if (blockIdx.x == 0) {
+      for (int c = threadIdx.x; c < nc; c += blockDim.x) h[c] = h1[c] + h2[c];
+      if (threadIdx.x == 0) {
+        h[nc] = bt;
+        if (bad && flag) *flag = 1;
+      }
+    }
+  }
+  // exit: the last block out resets both counters (every block has passed every barrier)
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    __threadfence();
+    if (atomicAdd(sync + 1, 1u) == (unsigned)G - 1) {
+      sync[0] = 0u;
+      sync[1] = 0u;
+      __threadfence();
+    }
+  }
+}
+
 // w[r] -= sum_c V[r + c*ldv] * h[c]
 __global__ void gemv_sub_kernel(const double* __restrict__ V, int64_t ldv, int ncols,
                                 const double* __restrict__ h, double* __restrict__ w, int64_t n) {
@@ -465,6 +644,26 @@ int kr_basis_rotate(const double* V, int64_t ldv, int m, const double* W, int kk
 int kr_cgs2_step(const KrylovWs& ws, const double* V, int64_t ldv, int nc, double* w, int64_t n,
                  double* h, double* h2, double* vnext, int* flag, cudaStream_t st) {
   if (nc < 1 || nc > kMaxCols) return IMPS_ERR_BAD_ARG;
+  if (ws.sync && ws.err && n <= (int64_t)CGRID * COOP_SUB) {
+    // one cooperative launch: w stays in shared memory, one grid barrier per reduction
+    int64_t gc = (n + 255) / 256;
+    if (gc > CGRID) gc = CGRID;
+    int64_t subc = (n + gc - 1) / gc;
+    subc = ((subc + 31) / 32) * 32;
+    const int gridc = (int)((n + subc - 1) / subc);
+    int subi = (int)subc;
+    double* partials = ws.partials;
+    unsigned int* sync = ws.sync;
+    int* err = ws.err;
+    void* args[] = {(void*)&V, (void*)&ldv, (void*)&nc, (void*)&w, (void*)&n, (void*)&subi, (void*)&h,
+                    (void*)&vnext, (void*)&flag, (void*)&partials, (void*)&sync, (void*)&err};
+    if (cudaLaunchCooperativeKernel((const void*)cgs2_coop_kernel, dim3(gridc), dim3(CT), args, 0, st) ==
+        cudaSuccess) {
+      imps::count_launch();
+      return IMPS_OK;
+    }
+    (void)cudaGetLastError();  // not co-resident here: fall back to four launches
+  }
   int64_t g = (n + 255) / 256;  // >= 256 rows per block, at most one block per SM
   if (g > CGRID) g = CGRID;
   if (g < 1) g = 1;
@@ -538,7 +737,7 @@ int kr_sign_of_first(const double* x, double* s, cudaStream_t st) {
 }
 
 size_t kr_partials_elems() {
-  return std::max((size_t)RGRID * kMaxCols, (size_t)CGRID * kMaxCols);
+  return std::max((size_t)RGRID * kMaxCols, (size_t)3 * CGRID * kMaxCols);
 }
 
 }  // namespace imps
