@@ -30,7 +30,13 @@ struct imps_ctx {
   int* dflag = nullptr;     // 16 device flags
   char* arena = nullptr;
   size_t arena_bytes = 0;
+  // pinned staging of solver convergence data (projected-matrix columns + flags), so that the
+  // device-to-host copies are asynchronous and a check can be evaluated while the next
+  // Krylov step runs
+  double* hpin = nullptr;   // kPinDoubles doubles, then 16 ints
+  cudaEvent_t ev_check = nullptr;
 };
+constexpr size_t kPinDoubles = (size_t)(imps::kMaxCols + 1) * (imps::kMaxCols + 1);
 
 
 struct imps_plan {
@@ -257,6 +263,8 @@ int imps_ctx_create(int device, imps_ctx** out) {
   CK(cudaMemset(c->dflag, 0, 16 * sizeof(int)));
   c->ws.sync = c->ws.counter + 1;  // counter[0]: last-block reductions; [1], [2]: grid barrier
   c->ws.err = c->dflag + 4;
+  CK(cudaMallocHost(&c->hpin, kPinDoubles * sizeof(double) + 16 * sizeof(int)));
+  CK(cudaEventCreateWithFlags(&c->ev_check, cudaEventDisableTiming));
   *out = c;
   return IMPS_OK;
 }
@@ -269,6 +277,8 @@ int imps_ctx_destroy(imps_ctx* c) {
   cudaFree(c->ws.counter);
   cudaFree(c->dscal);
   cudaFree(c->dflag);
+  if (c->hpin) cudaFreeHost(c->hpin);
+  if (c->ev_check) cudaEventDestroy(c->ev_check);
   if (c->arena) cudaFree(c->arena);
   if (c->own) cudaStreamDestroy(c->own);
   delete c;
@@ -686,66 +696,84 @@ int imps_eigs_rs(imps_plan* p, double* x, int mem, double tol, int ncv, int maxi
     CK(cudaMemsetAsync(Hd, 0, (size_t)ld * ld * 8, st));
     RC(kr_multidot(c->ws, xr, n, 1, xr, n, tmp, 0, nrm, st));
     RC(kr_scale_inv(xr, nrm, V, n, bflag, st));
-    int jstart = 0, jpulled = 0, status = IMPS_WARN_NOT_CONVERGED, kfinal = 0;
+    int jstart = 0, jpulled = 0, status = IMPS_WARN_NOT_CONVERGED, kfinal = 0, pending = -1;
     int64_t used = 0, best_at = 0;
     double best = std::numeric_limits<double>::infinity();
     const int64_t stall_window = 3 * (int64_t)(m - kk) + m;
-    bool done = false;
+    bool done = false, pre_applied = false;
+    int* pin_flags = (int*)(c->hpin + kPinDoubles);
+    // queue the copies of columns jpulled..j and the flags into pinned memory, then an event
+    auto stage = [&](int j) -> int {
+      CK(cudaMemcpyAsync(c->hpin, Hd + (size_t)jpulled * ld, (size_t)(j + 1 - jpulled) * ld * 8,
+                         cudaMemcpyDeviceToHost, st));
+      CK(cudaMemcpyAsync(pin_flags, bflag, sizeof(int), cudaMemcpyDeviceToHost, st));
+      CK(cudaMemcpyAsync(pin_flags + 1, c->ws.err, sizeof(int), cudaMemcpyDeviceToHost, st));
+      CK(cudaEventRecord(c->ev_check, st));
+      return IMPS_OK;
+    };
+    // convergence test of step j from the staged data: 1 = finished, 0 = go on, < 0 error
+    auto evaluate = [&](int j) -> int {
+      CK(cudaEventSynchronize(c->ev_check));
+      if (pin_flags[1]) {  // a grid-barrier wait of the CGS2 step ran out: report, re-arm
+        CK(cudaMemsetAsync(c->ws.err, 0, sizeof(int), st));
+        return IMPS_ERR_TIMEOUT;
+      }
+      for (int q = jpulled; q <= j; ++q) {
+        ta[q] = c->hpin[(size_t)(q - jpulled) * ld + q];
+        tb[q] = c->hpin[(size_t)(q - jpulled) * ld + q + 1];
+      }
+      jpulled = j + 1;
+      const int k = j + 1;
+      tri_lowest_pairs(k, ta.data(), tb.data(), 1, &theta, z.data());
+      if (!std::isfinite(theta)) return IMPS_ERR_NAN;
+      const double res = std::fabs(tb[k - 1] * z[k - 1]);
+      last_res = res;
+      kfinal = k;
+      if (res <= tol_eff * std::max(std::fabs(theta), eps23) || pin_flags[0]) {
+        status = IMPS_OK;
+        return 1;
+      }
+      if (used >= budget) return 1;
+      if (res < 0.5 * best) {
+        best = res;
+        best_at = used;
+      } else if (stall_exit && used - best_at > stall_window) {
+        return 1;
+      }
+      return 0;
+    };
     while (!done) {
       for (int j = jstart; j < m; ++j) {
-        double* vj = V + (size_t)j * n;
-        double* hc = Hd + (size_t)j * ld;
-        RC(apply_dev(p, vj, w));
+        if (!(pre_applied && j == jstart)) RC(apply_dev(p, V + (size_t)j * n, w));
+        pre_applied = false;
         ++applies;
         ++used;
-        RC(kr_cgs2_step(c->ws, V, n, j + 1, w, n, hc, tmp, V + (size_t)(j + 1) * n, bflag, st));
-        const bool check = ((j + 1 - jstart) % chk == 0) || j == m - 1 || used >= budget;
-        if (!check) continue;
-        CK(cudaMemcpyAsync(H.data() + (size_t)jpulled * ld, Hd + (size_t)jpulled * ld,
-                           (size_t)(j + 1 - jpulled) * ld * 8, cudaMemcpyDeviceToHost, st));
-        int hbreak = 0, terr = 0;
-        CK(cudaMemcpyAsync(&hbreak, bflag, sizeof(int), cudaMemcpyDeviceToHost, st));
-        CK(cudaMemcpyAsync(&terr, c->ws.err, sizeof(int), cudaMemcpyDeviceToHost, st));
-        CK(cudaStreamSynchronize(st));
-        if (terr) {  // a grid-barrier wait of the CGS2 step ran out: report, re-arm the flag
-          CK(cudaMemsetAsync(c->ws.err, 0, sizeof(int), st));
-          return IMPS_ERR_TIMEOUT;
+        RC(kr_cgs2_step(c->ws, V, n, j + 1, w, n, Hd + (size_t)j * ld, tmp, V + (size_t)(j + 1) * n, bflag, st));
+        if (pending >= 0) {  // the check of an earlier step, evaluated while step j runs
+          const int r = evaluate(pending);
+          pending = -1;
+          if (r < 0) return r;
+          if (r) { done = true; break; }
         }
-        for (int q = jpulled; q <= j; ++q) {
-          ta[q] = H[(size_t)q + (size_t)q * ld];
-          tb[q] = H[(size_t)q + 1 + (size_t)q * ld];
+        const bool last_step = j == m - 1 || used >= budget;
+        if (!(((j + 1 - jstart) % chk == 0) || last_step)) continue;
+        RC(stage(j));
+        if (!last_step) { pending = j; continue; }
+        // restart point: the first apply of the next cycle (on the residual direction v_m)
+        // runs on the device while the host evaluates the check and computes the restart
+        if (j == m - 1) {
+          RC(apply_dev(p, V + (size_t)m * n, w));
+          pre_applied = true;
         }
-        jpulled = j + 1;
-        const int k = j + 1;
-        const double tn = tri_norm(k, ta.data(), tb.data());
-        theta = tri_eigval(k, ta.data(), tb.data(), 0);
-        if (!std::isfinite(theta)) return IMPS_ERR_NAN;
-        tri_eigvec(k, ta.data(), tb.data(), theta, tn, z.data(), nullptr, nullptr, 0);
-        const double res = std::fabs(tb[k - 1] * z[k - 1]);
-        last_res = res;
-        kfinal = k;
-        if (res <= tol_eff * std::max(std::fabs(theta), eps23) || hbreak) {
-          status = IMPS_OK;
-          done = true;
-          break;
-        }
-        if (used >= budget) { done = true; break; }
-        if (res < 0.5 * best) {
-          best = res;
-          best_at = used;
-        } else if (stall_exit && used - best_at > stall_window) {
-          done = true;
-          break;
-        }
+        const int r = evaluate(j);
+        if (r < 0) return r;
+        if (r) { done = true; break; }
       }
       if (done) break;
       // Thick restart (Wu & Simon): keep the kk lowest Ritz pairs of T_m and the residual
       // direction v_m.  The kept block is rotated so that T stays tridiagonal, with only its
       // last vector coupled to v_m (coupling |s|, s_i = beta_{m-1} * y_i[m-1]).
-      const double tn = tri_norm(m, ta.data(), tb.data());
-      for (int i = 0; i < kk; ++i) th[i] = tri_eigval(m, ta.data(), tb.data(), i);
-      for (int i = 0; i < kk; ++i)
-        tri_eigvec(m, ta.data(), tb.data(), th[i], tn, Z.data() + (size_t)i * m, Z.data(), th.data(), i);
+      tri_lowest_pairs(m, ta.data(), tb.data(), kk, th.data(), Z.data());
       for (int i = 0; i < kk; ++i) sv[i] = tb[m - 1] * Z[(size_t)(m - 1) + (size_t)i * m];
       arrow_tridiag(kk, th.data(), sv.data(), Q.data(), qa.data(), qb.data());
       double sn = 0.0;
@@ -760,18 +788,21 @@ int imps_eigs_rs(imps_plan* p, double* x, int mem, double tol, int ncv, int maxi
           Wr[(size_t)r + (size_t)pc * m] = acc;
         }
       }
-      CK(cudaMemcpyAsync(Wrot, Wr.data(), (size_t)m * kk * 8, cudaMemcpyHostToDevice, st));
+      std::copy(Wr.begin(), Wr.end(), c->hpin);  // pinned: the upload is asynchronous
+      CK(cudaMemcpyAsync(Wrot, c->hpin, (size_t)m * kk * 8, cudaMemcpyHostToDevice, st));
       RC(kr_basis_rotate(V, n, m, Wrot, kk, Wk, n, n, st));
       CK(cudaMemcpyAsync(V, Wk, (size_t)kk * n * 8, cudaMemcpyDeviceToDevice, st));
       CK(cudaMemcpyAsync(V + (size_t)kk * n, V + (size_t)m * n, n * 8, cudaMemcpyDeviceToDevice, st));
       for (int pc = 0; pc < kk; ++pc) ta[pc] = qa[kk - 1 - pc];
       for (int pc = 0; pc + 1 < kk; ++pc) tb[pc] = qb[kk - 2 - pc];
       tb[kk - 1] = sn;
-      CK(cudaStreamSynchronize(st));
       jstart = jpulled = kk;
     }
+    // the staging buffer is reused below: wait for the rotation upload to be consumed
+    CK(cudaStreamSynchronize(st));
     // Ritz vector x = V[:, 0..k-1] z
-    CK(cudaMemcpyAsync(tmp, z.data(), kfinal * 8, cudaMemcpyHostToDevice, st));
+    std::copy(z.begin(), z.begin() + kfinal, c->hpin);
+    CK(cudaMemcpyAsync(tmp, c->hpin, kfinal * 8, cudaMemcpyHostToDevice, st));
     RC(kr_gemv(V, n, kfinal, tmp, xr, n, st));
     CK(cudaStreamSynchronize(st));
     return status;

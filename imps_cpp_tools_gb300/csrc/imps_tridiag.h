@@ -35,27 +35,86 @@ inline int sturm_below(int k, const double* a, const double* b, double x, double
   return cnt;
 }
 
-// i-th smallest eigenvalue (0-based), bisection on the Gershgorin interval
-inline double tri_eigval(int k, const double* a, const double* b, int i) {
-  double lo = a[0], hi = a[0], bmax2 = 0.0;
+// Gershgorin interval of T (widened by rounding) and the pivot floor of its Sturm sequences
+inline void tri_bounds(int k, const double* a, const double* b, double* lo, double* hi, double* pivmin) {
+  double l = a[0], h = a[0], bmax2 = 0.0;
   for (int r = 0; r < k; ++r) {
     const double rad = (r ? std::fabs(b[r - 1]) : 0.0) + (r < k - 1 ? std::fabs(b[r]) : 0.0);
-    lo = std::min(lo, a[r] - rad);
-    hi = std::max(hi, a[r] + rad);
+    l = std::min(l, a[r] - rad);
+    h = std::max(h, a[r] + rad);
     if (r < k - 1) bmax2 = std::max(bmax2, b[r] * b[r]);
   }
-  const double pivmin = std::numeric_limits<double>::min() * std::max(1.0, bmax2);
-  const double widen = 2.0 * kEps * std::max(std::fabs(lo), std::fabs(hi)) + pivmin;
-  lo -= widen;
-  hi += widen;
-  for (int it = 0; it < 256; ++it) {
-    const double mid = 0.5 * (lo + hi);
-    if (hi - lo <= 2.0 * kEps * std::max(std::fabs(lo), std::fabs(hi)) + pivmin || mid <= lo || mid >= hi)
-      break;
-    if (sturm_below(k, a, b, mid, pivmin) > i) hi = mid;
-    else lo = mid;
+  *pivmin = std::numeric_limits<double>::min() * std::max(1.0, bmax2);
+  const double widen = 2.0 * kEps * std::max(std::fabs(l), std::fabs(h)) + *pivmin;
+  *lo = l - widen;
+  *hi = h + widen;
+}
+
+// Sturm counts at kMulti shifts in lockstep: the kMulti division chains are independent, so
+// their latencies overlap (one pass over T costs about one chain).
+constexpr int kMulti = 8;
+inline void sturm_multi(int k, const double* a, const double* b, const double* x, double pivmin, int* cnt) {
+  double d[kMulti];
+  int c[kMulti];
+  for (int s = 0; s < kMulti; ++s) { d[s] = 1.0; c[s] = 0; }
+  for (int i = 0; i < k; ++i) {
+    const double bb = i ? b[i - 1] * b[i - 1] : 0.0;
+    for (int s = 0; s < kMulti; ++s) {
+      double di = (a[i] - x[s]) - (i ? bb / d[s] : 0.0);
+      if (std::fabs(di) < pivmin) di = -pivmin;
+      d[s] = di;
+      c[s] += di < 0.0;
+    }
   }
-  return 0.5 * (lo + hi);
+  for (int s = 0; s < kMulti; ++s) cnt[s] = c[s];
+}
+
+// The nlow smallest eigenvalues (ascending) by multisection: each round probes kMulti points
+// (midpoints of the unconverged brackets, or an even split of the few that remain) and every
+// Sturm count tightens the brackets of all wanted eigenvalues at once.
+inline void tri_eigvals_lowest(int k, const double* a, const double* b, int nlow, double* w,
+                               double xtol = 0.0) {
+  double glo, ghi, pivmin;
+  tri_bounds(k, a, b, &glo, &ghi, &pivmin);
+  std::vector<double> lo(nlow, glo), hi(nlow, ghi);
+  double x[kMulti];
+  int cnt[kMulti];
+  std::vector<int> open;
+  open.reserve(nlow);
+  for (int round = 0; round < 8192; ++round) {
+    open.clear();
+    for (int j = 0; j < nlow; ++j) {
+      const bool same = !open.empty() && lo[open.back()] == lo[j] && hi[open.back()] == hi[j];
+      const double tolx = std::max(2.0 * kEps * std::max(std::fabs(lo[j]), std::fabs(hi[j])) + pivmin, xtol);
+      if (hi[j] - lo[j] > tolx && !same) open.push_back(j);
+    }
+    if (open.empty()) break;
+    const int no = (int)open.size();
+    if (no >= kMulti) {
+      for (int s = 0; s < kMulti; ++s) x[s] = 0.5 * (lo[open[s]] + hi[open[s]]);
+    } else {
+      int s = 0;
+      for (int q = 0; q < no; ++q) {
+        const int np = kMulti / no + (q < kMulti % no ? 1 : 0);
+        const double l = lo[open[q]], h = hi[open[q]];
+        for (int p = 1; p <= np; ++p) x[s++] = l + (h - l) * p / (np + 1);
+      }
+    }
+    sturm_multi(k, a, b, x, pivmin, cnt);
+    for (int s = 0; s < kMulti; ++s)
+      for (int j = 0; j < nlow; ++j) {
+        if (cnt[s] > j) hi[j] = std::min(hi[j], x[s]);
+        else lo[j] = std::max(lo[j], x[s]);
+      }
+  }
+  for (int j = 0; j < nlow; ++j) w[j] = 0.5 * (lo[j] + hi[j]);
+}
+
+// i-th smallest eigenvalue (0-based)
+inline double tri_eigval(int k, const double* a, const double* b, int i) {
+  std::vector<double> w(i + 1);
+  tri_eigvals_lowest(k, a, b, i + 1, w.data());
+  return w[i];
 }
 
 // Unit eigenvector z of T for the eigenvalue lam: inverse iteration with a tridiagonal LU
@@ -90,7 +149,7 @@ inline void tri_eigvec(int k, const double* a, const double* b, double lam, doub
     }
   }
   if (std::fabs(d[k - 1]) < tiny) d[k - 1] = tiny;
-  for (int i = 0; i < k; ++i) z[i] = 1.0 + 0.25 * std::sin(1.7 * i + 0.3 * nprev);
+  for (int i = 0; i < k; ++i) z[i] = 1.0 + 0.125 * (double)((i * 7 + nprev * 3) % 11);
   std::vector<int> cl;
   for (int c = 0; c < nprev; ++c)
     if (std::fabs(prev_lam[c] - lam) <= 1e-3 * tnorm) cl.push_back(c);
@@ -189,6 +248,26 @@ inline void arrow_tridiag(int kk, const double* th, const double* s, double* Q, 
       at += th[i] * r[i] * r[i];
     }
     qa[t] = at;
+  }
+}
+
+// The nlow lowest eigenpairs (w ascending, Z column-major k x nlow): multisection brackets to
+// 1e-9 |T|, inverse iteration from those shifts (clusters orthogonalised), then each
+// eigenvalue as the Rayleigh quotient of its vector (error ~ |T| * (vector error)^2).
+inline void tri_lowest_pairs(int k, const double* a, const double* b, int nlow, double* w, double* Z) {
+  const double tn = std::max(tri_norm(k, a, b), 1e-300);
+  tri_eigvals_lowest(k, a, b, nlow, w, 1e-9 * tn);
+  for (int i = 0; i < nlow; ++i) tri_eigvec(k, a, b, w[i], tn, Z + (size_t)i * k, Z, w, i);
+  for (int i = 0; i < nlow; ++i) {
+    const double* z = Z + (size_t)i * k;
+    double rq = 0.0;
+    for (int r = 0; r < k; ++r) {
+      double tz = a[r] * z[r];
+      if (r) tz += b[r - 1] * z[r - 1];
+      if (r < k - 1) tz += b[r] * z[r + 1];
+      rq += z[r] * tz;
+    }
+    w[i] = rq;
   }
 }
 

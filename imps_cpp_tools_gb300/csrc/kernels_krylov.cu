@@ -262,6 +262,7 @@ __device__ void block_dots(const double* __restrict__ Vb, int64_t ldv, int nc, c
     const double* v2 = Vb + (int64_t)min(c0 + 2, nc - 1) * ldv;
     const double* v3 = Vb + (int64_t)min(c0 + 3, nc - 1) * ldv;
     double a0 = 0.0, a1 = 0.0, a2 = 0.0, a3 = 0.0;
+#pragma unroll 2
     for (int t = lane; t < len; t += 32) {
       const double xt = x[t];
       a0 = fma(v0[t], xt, a0);
@@ -424,8 +425,18 @@ __global__ void __launch_bounds__(256) basis_rotate_kernel(const double* __restr
       double acc[CT];
 #pragma unroll
       for (int t = 0; t < CT; ++t) acc[t] = 0.0;
-      for (int i = 0; i < m; ++i) {
-        const double v = V[r + i * ldv];
+      int i = 0;
+      for (; i + 8 <= m; i += 8) {  // eight loads in flight per thread
+        double v[8];
+#pragma unroll
+        for (int q = 0; q < 8; ++q) v[q] = V[r + (int64_t)(i + q) * ldv];
+#pragma unroll
+        for (int q = 0; q < 8; ++q)
+#pragma unroll
+          for (int t = 0; t < CT; ++t) acc[t] = fma(v[q], ws[(i + q) * CT + t], acc[t]);
+      }
+      for (; i < m; ++i) {
+        const double v = V[r + (int64_t)i * ldv];
 #pragma unroll
         for (int t = 0; t < CT; ++t) acc[t] = fma(v, ws[i * CT + t], acc[t]);
       }

@@ -8,9 +8,7 @@ double shim_tri_eigval(int k, const double* a, const double* b, int i) {
 }
 // the nlow lowest eigenpairs, vectors column-major k x nlow
 void shim_tri_lowest(int k, const double* a, const double* b, int nlow, double* w, double* Z) {
-  const double tn = imps::tri_norm(k, a, b);
-  for (int i = 0; i < nlow; ++i) w[i] = imps::tri_eigval(k, a, b, i);
-  for (int i = 0; i < nlow; ++i) imps::tri_eigvec(k, a, b, w[i], tn, Z + (size_t)i * k, Z, w, i);
+  imps::tri_lowest_pairs(k, a, b, nlow, w, Z);
 }
 void shim_arrow_tridiag(int kk, const double* th, const double* s, double* Q, double* qa, double* qb) {
   imps::arrow_tridiag(kk, th, s, Q, qa, qb);
