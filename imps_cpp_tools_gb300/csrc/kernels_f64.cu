@@ -1,9 +1,10 @@
 // FP64 kernels for the block-sparse hot path on sm_103a.
 //
 //  * grouped_gemm_f64: output-stationary grouped GEMM over the planner's tile/term tables.
-//    One CTA per output tile; every term of the tile is accumulated in registers and the
-//    tile is written once (deterministic, no atomics, no separate zero-fill: the first
-//    write also performs the reference's memset of `out`, VUMPS_helpers.hpp:69).
+//    One CTA per output tile; every term of the tile is accumulated in registers (split over
+//    K groups inside the CTA, summed in a fixed order) and the tile is written once
+//    (deterministic, no atomics, no separate zero-fill: the first write also performs the
+//    reference's memset of `out`, VUMPS_helpers.hpp:69).
 //  * Krylov BLAS-1 (reductions without atomics: fixed-grid partials + one finishing block).
 #include <cuda_runtime.h>
 
@@ -19,30 +20,45 @@ namespace {
 
 constexpr int TK = 16;
 
-// TMxTN tile computed by (TM/RM)*(TN/RN) threads, each holding RM x RN accumulators.
-template <int TM, int TN, int RM, int RN>
-__global__ void __launch_bounds__((TM / RM) * (TN / RN))
+// Named barrier over the NT threads of one K group (ids 1..KS; 0 is __syncthreads).
+__device__ __forceinline__ void group_sync(int id, int nthreads) {
+  asm volatile("bar.sync %0, %1;" ::"r"(id), "r"(nthreads) : "memory");
+}
+
+// TMxTN tile computed by KS groups of (TM/RM)*(TN/RN) threads, each thread holding RM x RN
+// accumulators.  The tile's K chunks (TK wide, over all of its terms in order) are dealt
+// round-robin to the KS groups, so a tile with few rows still keeps KS times more warps busy;
+// the groups' partial tiles are summed in a fixed order through shared memory (deterministic).
+template <int TM, int TN, int RM, int RN, int KS>
+__global__ void __launch_bounds__((TM / RM) * (TN / RN) * KS)
 grouped_gemm_f64_kernel(const Tile* __restrict__ tiles, const Term* __restrict__ terms,
                         imps_dslots slots) {
   constexpr int NT = (TM / RM) * (TN / RN);
   constexpr int TX = TN / RN;  // threads along n
-  __shared__ double As[TK][TM + 1];
-  __shared__ double Bs[TK][TN + 1];
+  constexpr int AS = TK * (TM + 1), BS = TK * (TN + 1);
+  constexpr int STAGE = KS * (AS + BS);
+  constexpr int RED = (KS - 1) * NT * RM * RN;
+  __shared__ double smem[STAGE > RED ? STAGE : RED];
   const Tile tl = tiles[blockIdx.x];
-  const int tid = threadIdx.x;
+  const int g = threadIdx.x / NT;
+  const int tid = threadIdx.x - g * NT;
   const int tx = tid % TX, ty = tid / TX;
+  double* As = smem + g * (AS + BS);  // [TK][TM + 1]
+  double* Bs = As + AS;               // [TK][TN + 1]
   double acc[RM][RN];
 #pragma unroll
   for (int i = 0; i < RM; ++i)
 #pragma unroll
     for (int j = 0; j < RN; ++j) acc[i][j] = 0.0;
 
+  int chunk = 0;
   for (int t = tl.t0; t < tl.t1; ++t) {
     const Term tm = terms[t];
     const double* __restrict__ A = slots.p[tm.a_slot] + tm.a_off;
     const double* __restrict__ B = slots.p[tm.b_slot] + tm.b_off;
     const double alpha = tm.alpha;
-    for (int k0 = 0; k0 < tm.k; k0 += TK) {
+    for (int k0 = 0; k0 < tm.k; k0 += TK, ++chunk) {
+      if (chunk % KS != g) continue;
       // A tile: rows m0..m0+TM, cols k0..k0+TK of op(A)
       for (int e = tid; e < TM * TK; e += NT) {
         int m, k;
@@ -51,7 +67,7 @@ grouped_gemm_f64_kernel(const Tile* __restrict__ tiles, const Term* __restrict__
         double v = 0.0;
         if (m < tl.mt && gk < tm.k)
           v = tm.a_t ? A[(int64_t)gm * tm.a_ld + gk] : A[gm + (int64_t)gk * tm.a_ld];
-        As[k][m] = alpha * v;
+        As[k * (TM + 1) + m] = alpha * v;
       }
       for (int e = tid; e < TN * TK; e += NT) {
         int n, k;
@@ -60,23 +76,40 @@ grouped_gemm_f64_kernel(const Tile* __restrict__ tiles, const Term* __restrict__
         double v = 0.0;
         if (n < tl.nt && gk < tm.k)
           v = tm.b_t ? B[gn + (int64_t)gk * tm.b_ld] : B[gk + (int64_t)gn * tm.b_ld];
-        Bs[k][n] = v;
+        Bs[k * (TN + 1) + n] = v;
       }
-      __syncthreads();
+      group_sync(g + 1, NT);
       const int kmax = min(TK, tm.k - k0);
       for (int k = 0; k < kmax; ++k) {
         double a[RM], b[RN];
 #pragma unroll
-        for (int i = 0; i < RM; ++i) a[i] = As[k][ty + i * (TM / RM)];
+        for (int i = 0; i < RM; ++i) a[i] = As[k * (TM + 1) + ty + i * (TM / RM)];
 #pragma unroll
-        for (int j = 0; j < RN; ++j) b[j] = Bs[k][tx + j * TX];
+        for (int j = 0; j < RN; ++j) b[j] = Bs[k * (TN + 1) + tx + j * TX];
 #pragma unroll
         for (int i = 0; i < RM; ++i)
 #pragma unroll
           for (int j = 0; j < RN; ++j) acc[i][j] = fma(a[i], b[j], acc[i][j]);
       }
-      __syncthreads();
+      group_sync(g + 1, NT);
     }
+  }
+  if (KS > 1) {
+    __syncthreads();  // every group is done with its staging buffers: reuse them for the sums
+    double* red = smem;
+    if (g > 0) {
+#pragma unroll
+      for (int i = 0; i < RM; ++i)
+#pragma unroll
+        for (int j = 0; j < RN; ++j) red[(((g - 1) * NT + tid) * RM + i) * RN + j] = acc[i][j];
+    }
+    __syncthreads();
+    if (g > 0) return;
+    for (int q = 1; q < KS; ++q)
+#pragma unroll
+      for (int i = 0; i < RM; ++i)
+#pragma unroll
+        for (int j = 0; j < RN; ++j) acc[i][j] += red[(((q - 1) * NT + tid) * RM + i) * RN + j];
   }
   double* __restrict__ C = slots.p[tl.c_slot] + tl.c_off;
 #pragma unroll
@@ -101,12 +134,12 @@ int imps_launch_grouped_f64(const void* d_tiles, int ntiles, const void* d_terms
   cudaStream_t st = (cudaStream_t)stream;
   if (tile_m == 16) {
     imps::count_launch();
-    grouped_gemm_f64_kernel<16, 16, 2, 2><<<ntiles, 64, 0, st>>>((const Tile*)d_tiles,
-                                                                 (const Term*)d_terms, slots);
+    grouped_gemm_f64_kernel<16, 16, 2, 2, 4><<<ntiles, 256, 0, st>>>((const Tile*)d_tiles,
+                                                                    (const Term*)d_terms, slots);
   } else {
     imps::count_launch();
-    grouped_gemm_f64_kernel<32, 32, 2, 4><<<ntiles, 128, 0, st>>>((const Tile*)d_tiles,
-                                                                  (const Term*)d_terms, slots);
+    grouped_gemm_f64_kernel<32, 32, 2, 4, 2><<<ntiles, 256, 0, st>>>((const Tile*)d_tiles,
+                                                                     (const Term*)d_terms, slots);
   }
   return cudaGetLastError() == cudaSuccess ? IMPS_OK : IMPS_ERR_CUDA;
 }

@@ -161,37 +161,43 @@ __device__ __forceinline__ void tmem_ld16(uint32_t taddr, float* v) {
 }
 
 // ------------------------------------------------------------------ kernels
+// One block row per job (blockIdx.x), grid-stride over the padded rpad x kpad operand.  The
+// FP64 value is rounded once to FP32 and split there into hi + mid + lo BF16 terms: each
+// difference xf - bf16(xf) is exact in FP32, so the three terms carry all 24 significand bits
+// of xf (relative error 2^-24, the order of the dropped lo*lo-type products) while the FP64
+// pipe, slow on this GPU, sees one conversion per element.  32-bit index arithmetic.
 __global__ void pack_kernel(const PackJob* __restrict__ jobs, imps_dslots slots, __nv_bfloat16* __restrict__ out) {
   const PackJob jb = jobs[blockIdx.x];
   const double* S = slots.p[jb.slot] + jb.src_off;
-  const int64_t total = (int64_t)jb.rpad * jb.kpad;
-  const int rg_count = jb.rpad / 8;
-  for (int64_t t = threadIdx.x + (int64_t)blockIdx.y * blockDim.x; t < total; t += (int64_t)gridDim.y * blockDim.x) {
-    const int r = (int)(t % jb.rpad), k = (int)(t / jb.rpad);
-    double x = 0.0;
+  const int rpad = jb.rpad;
+  const int total = rpad * jb.kpad;
+  const float alpha = (float)jb.alpha;
+  const int split_elems = rpad * 16;
+  for (int t = threadIdx.x + blockIdx.y * blockDim.x; t < total; t += gridDim.y * blockDim.x) {
+    const int k = t / rpad, r = t - k * rpad;
+    float xf = 0.0f;
     const int gr = jb.r0 + r;
     if (r < jb.rows && k < jb.k) {
+      double x;
       if (jb.role == 0)  // op(A)(gr, k)
         x = jb.trans ? S[k + (int64_t)gr * jb.src_ld] : S[gr + (int64_t)k * jb.src_ld];
       else  // op(B)(k, gr)
         x = jb.trans ? S[gr + (int64_t)k * jb.src_ld] : S[k + (int64_t)gr * jb.src_ld];
-      x *= jb.alpha;
+      xf = __double2float_rn(x) * alpha;
     }
-    const __nv_bfloat16 hi = __double2bfloat16(x);
-    const double x1 = x - (double)__bfloat162float(hi);
-    const __nv_bfloat16 mid = __double2bfloat16(x1);
-    const double x2 = x1 - (double)__bfloat162float(mid);
-    const __nv_bfloat16 lo = __double2bfloat16(x2);
+    const __nv_bfloat16 hi = __float2bfloat16_rn(xf);
+    const float x1 = xf - __bfloat162float(hi);
+    const __nv_bfloat16 mid = __float2bfloat16_rn(x1);
+    const float x2 = x1 - __bfloat162float(mid);
+    const __nv_bfloat16 lo = __float2bfloat16_rn(x2);
     const int kstep = k >> 4, kk = k & 15, chunk = kk >> 3, e = kk & 7;
     const int rgi = r >> 3, rr = r & 7;
-    const int64_t split_elems = (int64_t)jb.rpad * 16;
-    const int64_t base = jb.dst_off + (int64_t)kstep * 3 * split_elems + (int64_t)chunk * jb.rpad * 8 +
+    const int64_t base = jb.dst_off + (int64_t)kstep * 3 * split_elems + (int64_t)chunk * rpad * 8 +
                          (int64_t)rgi * 64 + rr * 8 + e;
     out[base] = hi;
     out[base + split_elems] = mid;
     out[base + 2 * split_elems] = lo;
   }
-  (void)rg_count;
 }
 
 __global__ void __launch_bounds__(TC_THREADS, 1)
@@ -357,9 +363,11 @@ int tc_create(TcPlan** out, const Plan& P, cudaStream_t st) {
     for (const OutBlock& o : S.outs) T->dynamic_slot[o.c_slot] = 1;
   std::map<std::tuple<int, int64_t, int, int, int, int, int, int, double>, int64_t> seen;
   int64_t off = 0;
+  bool too_large = false;  // the pack kernel indexes one operand slice with 32-bit integers
   auto pack_for = [&](int slot, int64_t src, int ld, int trans, int role, int r0, int rows, int k, int rpad,
                       double alpha, std::vector<PackJob>& jobs) -> int64_t {
     const int kpad = round_up(std::max(k, 1), 16);
+    if ((int64_t)rpad * kpad * 3 >= ((int64_t)1 << 31)) too_large = true;
     auto key = std::make_tuple(slot, src, ld, trans, role, r0, rows, k, alpha);
     auto it = seen.find(key);
     if (it != seen.end()) return it->second;
@@ -411,8 +419,9 @@ int tc_create(TcPlan** out, const Plan& P, cudaStream_t st) {
     if (cudaMemcpy(*d, h, bytes, cudaMemcpyHostToDevice) != cudaSuccess) return IMPS_ERR_CUDA;
     return IMPS_OK;
   };
-  int rc = IMPS_OK;
+  int rc = too_large ? IMPS_ERR_TOO_LARGE : IMPS_OK;
   for (TcStage& ts : T->stages) {
+    if (rc) break;
     if ((rc = up((void**)&ts.d_tiles, ts.tiles.data(), ts.tiles.size() * sizeof(TcTile)))) break;
     if ((rc = up((void**)&ts.d_terms, ts.terms.data(), ts.terms.size() * sizeof(TcTerm)))) break;
     if ((rc = up((void**)&ts.d_dyn, ts.dyn_jobs.data(), ts.dyn_jobs.size() * sizeof(PackJob)))) break;
