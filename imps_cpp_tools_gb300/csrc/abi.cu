@@ -884,6 +884,7 @@ static int gmres_proj(imps_plan* p, const double* b, double* y, const double* rh
   const bool mixed = prec_saved == IMPS_PREC_BF16X6;
   int stall = 0;
   double rn_prev = 0.0;
+  bool inner_hit = false;  // the last cycle ended on its Krylov residual estimate
   for (int outer = 0; it < maxit; ++outer) {
     // r = b - A(y)  (FP64 residual)
     p->prec = IMPS_PREC_FP64;
@@ -900,12 +901,14 @@ static int gmres_proj(imps_plan* p, const double* b, double* y, const double* rh
     if (debug_level() > 1)
       fprintf(stderr, "[imps gmres]   outer=%d it=%d relres=%.3e\n", outer, it, rel);
     if (rn < tol * bnorm) { status = IMPS_OK; break; }
-    // At the attainable accuracy (~eps * |A| |y| / |b|) the recomputed residual stops falling
-    // while the Krylov estimate keeps "converging": three restarts that gain < 10% each end
-    // the solve (not converged, result returned) instead of running into maxit.
-    stall = outer > 0 && rn > 0.9 * rn_prev ? stall + 1 : 0;
+    // At the attainable accuracy (~eps * |A| |y| / |b|) the Krylov estimate of a cycle reaches
+    // its target while the recomputed residual stops falling.  Three such cycles in a row that
+    // gain < 10% each end the solve (not converged, result returned) instead of running into
+    // maxit; cycles that used their whole Krylov space (slow but steady) never count.
+    stall = outer > 0 && inner_hit && rn > 0.9 * rn_prev ? stall + 1 : 0;
     rn_prev = rn;
     if (stall >= 3) break;
+    inner_hit = false;
     CK(cudaMemsetAsync(bflag, 0, sizeof(int), st));
     RC(kr_scale_inv(w, dsc + 1, V, n, bflag, st));
     CK(cudaMemsetAsync(gam, 0, ld * 8, st));
@@ -931,7 +934,10 @@ static int gmres_proj(imps_plan* p, const double* b, double* y, const double* rh
         }
         if (!std::isfinite(res)) return IMPS_ERR_NAN;
         if (brk) { kdim = j; break; }  // invariant subspace
-        if (res < std::max(tol * bnorm, mixed ? kMixedInnerTol * rn : 0.0)) break;
+        if (res < std::max(tol * bnorm, mixed ? kMixedInnerTol * rn : 0.0)) {
+          inner_hit = true;
+          break;
+        }
       }
     }
     // y += V[:, :kdim] * R^{-1} gamma
