@@ -251,24 +251,14 @@ inline void arrow_tridiag(int kk, const double* th, const double* s, double* Q, 
   }
 }
 
-// The nlow lowest eigenpairs (w ascending, Z column-major k x nlow): multisection brackets to
-// 1e-9 |T|, inverse iteration from those shifts (clusters orthogonalised), then each
-// eigenvalue as the Rayleigh quotient of its vector (error ~ |T| * (vector error)^2).
+// The nlow lowest eigenpairs (w ascending, Z column-major k x nlow): eigenvalues bracketed to
+// full precision by multisection (a bracket merely as wide as 1e-9 |T| cannot separate a
+// nearly degenerate lowest pair, and inverse iteration from it returns a mixture of the two),
+// then inverse iteration from those shifts with the members of each cluster orthogonalised.
 inline void tri_lowest_pairs(int k, const double* a, const double* b, int nlow, double* w, double* Z) {
   const double tn = std::max(tri_norm(k, a, b), 1e-300);
-  tri_eigvals_lowest(k, a, b, nlow, w, 1e-9 * tn);
+  tri_eigvals_lowest(k, a, b, nlow, w);
   for (int i = 0; i < nlow; ++i) tri_eigvec(k, a, b, w[i], tn, Z + (size_t)i * k, Z, w, i);
-  for (int i = 0; i < nlow; ++i) {
-    const double* z = Z + (size_t)i * k;
-    double rq = 0.0;
-    for (int r = 0; r < k; ++r) {
-      double tz = a[r] * z[r];
-      if (r) tz += b[r - 1] * z[r - 1];
-      if (r < k - 1) tz += b[r] * z[r + 1];
-      rq += z[r] * tz;
-    }
-    w[i] = rq;
-  }
 }
 
 }  // namespace imps

@@ -121,3 +121,30 @@ def test_arrow_tridiagonalisation(shim, case):
     Tq[kk - 1, kk] = Tq[kk, kk - 1] = np.linalg.norm(s)
     Tq[kk, kk] = alpha
     assert np.allclose(np.linalg.eigvalsh(A), np.linalg.eigvalsh(Tq), atol=1e-12)
+
+
+def test_nearly_degenerate_lowest_pair_large_norm(shim):
+    """A lowest pair split by 6e-10 under |T| ~ 1e3 (the H_C spectra of a converged VUMPS
+    state): eigenvalues in order and eigenvectors separated, not mixed."""
+    rng = np.random.default_rng(9)
+    k = 64
+    Q, _ = np.linalg.qr(rng.standard_normal((k, k)))
+    lam = np.concatenate([[-1.2980078565, -1.2980078559], np.sort(rng.uniform(-1.0, 1e3, k - 2))])
+    A = (Q * lam) @ Q.T
+    # Householder tridiagonalisation of A (numpy only): T = P^T A P
+    T = A.copy()
+    for j in range(k - 2):
+        x = T[j + 1:, j].copy()
+        v = x.copy()
+        v[0] += np.copysign(np.linalg.norm(x), x[0])
+        v /= np.linalg.norm(v)
+        H = np.eye(k - j - 1) - 2.0 * np.outer(v, v)
+        T[j + 1:, :] = H @ T[j + 1:, :]
+        T[:, j + 1:] = T[:, j + 1:] @ H
+    a, b = np.diag(T).copy(), np.diag(T, 1).copy()
+    w, Z = _lowest(shim, a, b, 2)
+    Td = _dense(a, b)
+    wr = np.linalg.eigvalsh(Td)[:2]
+    assert np.abs(w - wr).max() < 1e-12 * 1e3
+    assert w[0] < w[1]
+    assert np.linalg.norm(Td @ Z - Z * w, axis=0).max() < 1e-9
