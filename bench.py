@@ -37,6 +37,10 @@ METRIC = "VUMPS sweeps/s + H_AC TFLOP/s, mixed vs FP64 on one GB300 at |dE|<=1e-
 APPLIES_PER_STEP = 20
 L2_FLUSH_BYTES = 512 << 20
 TOLMIN = 1e-12  # floor of the eigensolver tolerance schedule and the GMRES tolerance
+# DRAM bytes (read + write) of one H_AC apply from one ncu capture of `bench.py --mode hac`
+# (profiles/tc_gemm_hac_xxz_d512.md: tc_gemm 5.26 MB + pack 0.40 MB;
+# profiles/grouped_gemm_f64_hac_xxz_d512.md: 2.36 MB), cold caches
+NCU_TRAFFIC_BYTES = {"bf16x6": 5.66e6, "fp64": 2.36e6}
 WORKLOAD_DESC = ("XXZ D=512 (21 U(1) sectors, dims ~exp(-q^2/18)), 2-site VUMPS sweep, tolerance schedule "
                  "min(max(prec/100, 1e-12), 1e-6) (VUMPS_main.cpp:177), GMRES tol 1e-12, expansion off")
 
@@ -346,7 +350,7 @@ def run_vumps(args):
     if args.precision == "bf16x6":
         achieved = 6 * flops / t_hacmx / 1e12
         roof = {"bound": "tensor", "achieved": achieved, "peak": bf16_peak, "unit": "TFLOP/s",
-                "frac": achieved / bf16_peak, "traffic": None,
+                "frac": achieved / bf16_peak, "traffic": NCU_TRAFFIC_BYTES["bf16x6"],
                 "peak_source": "MEASURED_PEAKS.json bf16_tflops (burst), of measured",
                 "kernel": "tc_gemm_kernel + pack_kernel (H_AC apply, 6 split-BF16 products per FP64 flop)",
                 "achieved_fp64_equivalent_tflops": flops / t_hacmx / 1e12,
@@ -356,7 +360,7 @@ def run_vumps(args):
     else:
         achieved = flops / t_hac64 / 1e12
         roof = {"bound": "tensor", "achieved": achieved, "peak": fp64_peak, "unit": "TFLOP/s",
-                "frac": achieved / fp64_peak, "traffic": None,
+                "frac": achieved / fp64_peak, "traffic": NCU_TRAFFIC_BYTES["fp64"],
                 "peak_source": "dense FP64 matmul measured in this run", "kernel": "grouped_gemm_f64 (H_AC apply)"}
 
     e2e = {"value": ws / t_wall, "unit": "sweeps/s", "h2d_bytes_per_step": rmx["h2d"],
