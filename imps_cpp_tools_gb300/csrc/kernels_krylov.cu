@@ -306,7 +306,7 @@ __global__ void __launch_bounds__(CT) cgs2_coop_kernel(const double* __restrict_
                                                       int* err) {
   __shared__ double wsm[COOP_SUB];
   __shared__ double h1[imps::kMaxCols];
-  __shared__ double h2[imps::kMaxCols];
+  __shared__ double h2[imps::kMaxCols + 1];
   __shared__ double sh[32];
   __shared__ double beta;
   const int G = gridDim.x;
@@ -330,23 +330,42 @@ __global__ void __launch_bounds__(CT) cgs2_coop_kernel(const double* __restrict_
     __syncthreads();
     block_dots(Vb, ldv, nc, wsm, len, P1, G);
   }
-  ok = grid_barrier(sync, 2u * G, err, ok);
-  if (ok) reduce_partials(P1, G, nc, h2);
-  __syncthreads();
-  // pass 3: w -= V h2; beta = |w|
-  double nacc = 0.0;
-  if (ok) {
-    update_rows(Vb, ldv, nc, h2, wsm, len);
-    __syncthreads();
-    for (int t = threadIdx.x; t < len; t += blockDim.x) nacc = fma(wsm[t], wsm[t], nacc);
+  // |w|^2 before the second update rides along as column nc of the same partials
+  {
+    double n1 = 0.0;
+    if (ok)
+      for (int t = threadIdx.x; t < len; t += blockDim.x) n1 = fma(wsm[t], wsm[t], n1);
+    n1 = block_sum(n1, sh);
+    if (threadIdx.x == 0) P1[(int64_t)nc * G + blockIdx.x] = n1;
   }
-  nacc = block_sum(nacc, sh);
-  if (threadIdx.x == 0) P2[blockIdx.x] = nacc;
-  ok = grid_barrier(sync, 3u * G, err, ok);
-  if (ok) {
-    reduce_partials(P2, G, 1, sh);  // warp 0 writes sh[0]
+  ok = grid_barrier(sync, 2u * G, err, ok);
+  if (ok) reduce_partials(P1, G, nc + 1, h2);  // h2[nc] = |w1|^2
+  __syncthreads();
+  // pass 3: w -= V h2; beta = |w|.  V orthonormal: |w2|^2 = |w1|^2 - |h2|^2 exactly, and the
+  // second-pass coefficients are tiny unless w1 nearly lies in span(V); then (identically in
+  // every block, which all hold the same reduced values) the norm is reduced explicitly.
+  __shared__ bool pyth;
+  if (threadIdx.x == 0) {
+    double s2 = 0.0;
+    for (int c = 0; c < nc; ++c) s2 = fma(h2[c], h2[c], s2);
+    pyth = s2 <= 0.1 * h2[nc];
+    if (pyth) beta = sqrt(h2[nc] - s2);
+  }
+  __syncthreads();
+  if (ok) update_rows(Vb, ldv, nc, h2, wsm, len);
+  __syncthreads();
+  if (!pyth) {
+    double nacc = 0.0;
+    if (ok)
+      for (int t = threadIdx.x; t < len; t += blockDim.x) nacc = fma(wsm[t], wsm[t], nacc);
+    nacc = block_sum(nacc, sh);
+    if (threadIdx.x == 0) P2[blockIdx.x] = nacc;
+    ok = grid_barrier(sync, 3u * G, err, ok);
+    if (ok) reduce_partials(P2, G, 1, sh);  // warp 0 writes sh[0]
     __syncthreads();
-    if (threadIdx.x == 0) beta = sqrt(sh[0]);
+    if (threadIdx.x == 0 && ok) beta = sqrt(sh[0]);
+  }
+  if (ok) {
     __syncthreads();
     const double bt = beta;
     const bool bad = !(fabs(bt) > 1e-300) || !isfinite(bt);
@@ -655,7 +674,8 @@ int kr_basis_rotate(const double* V, int64_t ldv, int m, const double* W, int kk
 int kr_cgs2_step(const KrylovWs& ws, const double* V, int64_t ldv, int nc, double* w, int64_t n,
                  double* h, double* h2, double* vnext, int* flag, cudaStream_t st) {
   if (nc < 1 || nc > kMaxCols) return IMPS_ERR_BAD_ARG;
-  if (ws.sync && ws.err && n <= (int64_t)CGRID * COOP_SUB) {
+  // (column nc of the second partials region carries |w|^2, hence nc < kMaxCols)
+  if (ws.sync && ws.err && n <= (int64_t)CGRID * COOP_SUB && nc < kMaxCols) {
     // one cooperative launch: w stays in shared memory, one grid barrier per reduction
     int64_t gc = (n + 255) / 256;
     if (gc > CGRID) gc = CGRID;
