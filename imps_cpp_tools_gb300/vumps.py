@@ -41,6 +41,7 @@ class VumpsGPU:
         # orthogonalisation cost per apply.
         self.lanczos_ncv = lanczos_ncv
         self.eig_margin = eig_margin
+        self.mixed_tm = mixed_tm
         self.precision = precision
         self.rng = np.random.default_rng(seed)
         self.stats = {"lanczos_applies": 0, "gmres_iters": 0, "hac_applies": 0, "hc_applies": 0}
@@ -105,7 +106,7 @@ class VumpsGPU:
             # tensor-core applies inside the Krylov solvers; Krylov vectors, residuals,
             # decompositions and the energy stay FP64
             mixed = self.p_hac + self.p_hcl + self.p_hcr
-            if mixed_tm:  # transfer matrices of the GMRES environment / fixed-point solves
+            if self.mixed_tm:  # transfer matrices of the GMRES environment / fixed-point solves
                 mixed += [self.tm[(k, n)] for k in ("L", "R") for n in range(2)]
             for p in mixed:
                 p.set_precision(N.PREC_BF16X6)
