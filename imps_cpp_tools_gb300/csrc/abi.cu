@@ -808,17 +808,21 @@ int imps_eigs_rs(imps_plan* p, double* x, int mem, double tol, int ncv, int maxi
     return status;
   };
 
-  const bool mixed = p->prec == IMPS_PREC_BF16X6;
-  int status = lanczos(mixed ? std::max(tol, kMixedEigTol) : tol, max_applies, mixed);
+  // Precision ladder.  Splitting operands into BF16 terms rounds, so the split-BF16 operator is
+  // linear only to ~1e-7 |H| and its Lanczos residual floors there.  A tolerance at or above
+  // that floor runs on the tensor cores (FP64 applies finish only if the mixed run stalls); a
+  // tolerance below it runs in FP64 from the start — a mixed run followed by an FP64 run that
+  // restarts from its Ritz vector costs more than the FP64 run alone.
+  const int prec_saved = p->prec;
+  const bool mixed = p->prec == IMPS_PREC_BF16X6 && tol >= kMixedEigTol;
+  p->prec = mixed ? IMPS_PREC_BF16X6 : IMPS_PREC_FP64;
+  int status = lanczos(tol, max_applies, mixed);
   const int applies_mixed = mixed ? applies : 0;
-  if (status >= 0 && mixed && (status != IMPS_OK || tol < kMixedEigTol) && applies < max_applies) {
-    // Splitting operands into BF16 terms rounds, so the split-BF16 operator is linear only to
-    // ~1e-7 |H| and its Lanczos residual floors there; FP64 applies finish the solve from
-    // the mixed Ritz vector.
+  if (status >= 0 && mixed && status != IMPS_OK && applies < max_applies) {
     p->prec = IMPS_PREC_FP64;
     status = lanczos(tol, std::max<int64_t>(max_applies - applies, m), false);
-    p->prec = IMPS_PREC_BF16X6;
   }
+  p->prec = prec_saved;
   if (status < 0) return status;
   // normalise
   RC(kr_multidot(c->ws, xr, n, 1, xr, n, tmp, 0, nrm, st));

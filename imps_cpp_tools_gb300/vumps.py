@@ -21,7 +21,7 @@ class VumpsGPU:
     def __init__(self, ctx, model, dims0=None, dimvec=None, seed=1, InvETol=5e-15, InvEfac=2.0,
                  fixed_tol=None, tolmin=5e-16, tolmax=1e-6, trueLR=True, svdthresh=5e-7, precision="fp64",
                  init_state=None, lanczos_maxit=300, gmres_maxit=4000, lanczos_ncv=64, eig_margin=0.1,
-                 mixed_tm=True, verbose=False, **params):
+                 mixed_tm=False, verbose=False, **params):
         import torch
         self.torch = torch
         self.verbose = verbose
@@ -106,7 +106,10 @@ class VumpsGPU:
             # tensor-core applies inside the Krylov solvers; Krylov vectors, residuals,
             # decompositions and the energy stay FP64
             mixed = self.p_hac + self.p_hcl + self.p_hcr
-            if self.mixed_tm:  # transfer matrices of the GMRES environment / fixed-point solves
+            # transfer matrices of the GMRES environment / fixed-point solves: FP64 by default —
+            # split-BF16 TM applies are cheaper, but the iterative refinement that brings their
+            # GMRES back to FP64 accuracy restarts the Krylov space and doubles the iterations
+            if self.mixed_tm:
                 mixed += [self.tm[(k, n)] for k in ("L", "R") for n in range(2)]
             for p in mixed:
                 p.set_precision(N.PREC_BF16X6)
