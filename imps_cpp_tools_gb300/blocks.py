@@ -264,6 +264,16 @@ def plan_tm(ctx, A_layouts, direction, lin, lout):
     return Plan(ctx, h, "tm")
 
 
+def plan_tm_mixed(ctx, A_layouts, B_layouts, direction, lin, lout):
+    """ApplyTMmixedLeft/Right(A, B, X) on a unit cell (A lower, B upper layer)."""
+    arr_a = (C.c_void_p * len(A_layouts))(*[a.handle.value for a in A_layouts])
+    arr_b = (C.c_void_p * len(B_layouts))(*[b.handle.value for b in B_layouts])
+    h = C.c_void_p()
+    N.call("imps_plan_tm_mixed", ctx.handle, len(A_layouts), arr_a, arr_b, int(direction), lin.handle,
+           lout.handle, C.byref(h))
+    return Plan(ctx, h, "tmx")
+
+
 def plan_redop(ctx, A, d, hnnz, direction):
     r, c, v = _hnnz_arrays(hnnz)
     h = C.c_void_p()

@@ -7,6 +7,7 @@
 #include <cstdio>
 #include <cstdlib>
 #include <cstring>
+#include <functional>
 #include <limits>
 #include <new>
 #include <vector>
@@ -47,7 +48,8 @@ struct imps_plan {
   double* stage_aux[2] = {nullptr, nullptr};
   // in-layout tables (TM plans): block offsets / dims for traces
   int64_t* d_boff = nullptr;
-  int32_t* d_bdim = nullptr;
+  int32_t* d_bdim = nullptr;   // rows
+  int32_t* d_bcols = nullptr;  // cols (mixed TM plans: general BlockMat input)
   int nb_in = 0;
   Layout in_layout;
   // gradient plan segments
@@ -398,6 +400,35 @@ int imps_plan_tm(imps_ctx* ctx, int nsites, const imps_layout* const* A, int dir
   return IMPS_OK;
 }
 
+int imps_plan_tm_mixed(imps_ctx* ctx, int nsites, const imps_layout* const* A, const imps_layout* const* B,
+                       int dir, const imps_layout* in, const imps_layout* outl, imps_plan** out) {
+  if (!ctx || !A || !B || !in || !outl || !out || nsites < 1 || (dir != 0 && dir != 1)) return IMPS_ERR_BAD_ARG;
+  std::vector<const Layout*> As, Bs;
+  for (int k = 0; k < nsites; ++k) {
+    if (!A[k] || !B[k]) return IMPS_ERR_BAD_ARG;
+    As.push_back(&A[k]->L);
+    Bs.push_back(&B[k]->L);
+  }
+  Plan P;
+  RC(build_tm_mixed(P, As, Bs, dir, in->L, outl->L));
+  RC(finish_plan(ctx, P, out));
+  imps_plan* p = *out;
+  p->in_layout = in->L;
+  std::vector<int64_t> bo;
+  std::vector<int32_t> br, bc;
+  for (const Block& b : in->L.blocks) { bo.push_back(b.off); br.push_back(b.rows); bc.push_back(b.cols); }
+  p->nb_in = (int)bo.size();
+  if (p->nb_in && ctx->device >= 0) {
+    CK(cudaMalloc(&p->d_boff, bo.size() * sizeof(int64_t)));
+    CK(cudaMalloc(&p->d_bdim, br.size() * sizeof(int32_t)));
+    CK(cudaMalloc(&p->d_bcols, bc.size() * sizeof(int32_t)));
+    CK(cudaMemcpy(p->d_boff, bo.data(), bo.size() * sizeof(int64_t), cudaMemcpyHostToDevice));
+    CK(cudaMemcpy(p->d_bdim, br.data(), br.size() * sizeof(int32_t), cudaMemcpyHostToDevice));
+    CK(cudaMemcpy(p->d_bcols, bc.data(), bc.size() * sizeof(int32_t), cudaMemcpyHostToDevice));
+  }
+  return IMPS_OK;
+}
+
 int imps_plan_redop(imps_ctx* ctx, const imps_layout* A, int d, int nnz, const int32_t* hrow,
                     const int32_t* hcol, const double* hval, int dir, imps_plan** out) {
   if (!ctx || !A || !out || d <= 0 || nnz < 0) return IMPS_ERR_BAD_ARG;
@@ -473,6 +504,7 @@ int imps_plan_destroy(imps_plan* p) {
   cudaFree(p->stage_aux[1]);
   cudaFree(p->d_boff);
   cudaFree(p->d_bdim);
+  cudaFree(p->d_bcols);
   cudaFree(p->d_soff);
   cudaFree(p->d_slen);
   if (p->tc) tc_destroy(p->tc);
@@ -595,8 +627,12 @@ int imps_hc_apply(imps_plan* p, const double* in, double* out, int mem) {
   return apply_mem(p, in, out, mem);
 }
 
+static bool is_mixed_tm(const imps_plan* p) {
+  return p && (p->P.kind == PLAN_TMMIXED_L || p->P.kind == PLAN_TMMIXED_R);
+}
+
 int imps_tm_apply(imps_plan* p, const double* in, double* out, int mem) {
-  if (!p || p->P.kind != PLAN_TM) return IMPS_ERR_BAD_ARG;
+  if (!p || (p->P.kind != PLAN_TM && !is_mixed_tm(p))) return IMPS_ERR_BAD_ARG;
   return apply_mem(p, in, out, mem);
 }
 
@@ -842,13 +878,16 @@ int imps_eigs_rs(imps_plan* p, double* x, int mem, double tol, int ncv, int maxi
   return status;
 }
 
-// ---- GMRES core on the projected operator A(v) = v - T(v) + tr(v*rho_in)*rho_out ----
-static int gmres_proj(imps_plan* p, const double* b, double* y, const double* rho_in,
-                      const double* rho_out, double tol, int maxit, int krylov, int* iters,
-                      double* relres, Bump& bp) {
-  imps_ctx* c = p->ctx;
+// ---- device GMRES (generic operator) ----
+// Operator of a device GMRES: out = A(in) on device vectors; `fp64` asks for the FP64 engine
+// (the residual of a mixed-precision solve), otherwise the operator's own precision.
+using DevOp = std::function<int(const double* in, double* out, bool fp64)>;
+
+// Restarted GMRES(krylov) on the device for A y = b (y holds y0 on entry): CGS2 Arnoldi,
+// Givens rotations on the device, the residual recomputed (in FP64) at every restart.
+static int gmres_dev(imps_ctx* c, int64_t n, const DevOp& A, bool mixed, const double* b, double* y,
+                     double tol, int maxit, int krylov, int* iters, double* relres, Bump& bp) {
   cudaStream_t st = c->stream;
-  const int64_t n = p->P.slots[0].nelem;
   int m = krylov > 0 ? krylov : kGmresKrylov;
   if (m > kMaxCols - 2) m = kMaxCols - 2;
   if (m > n) m = (int)n;
@@ -884,17 +923,12 @@ static int gmres_proj(imps_plan* p, const double* b, double* y, const double* rh
   // Mixed precision: every restart recomputes the true residual with the FP64 engine and the
   // inner Krylov cycle (split-BF16 applies) only has to reduce it by kMixedInnerTol, i.e.
   // restarted GMRES acts as iterative refinement with FP64 residuals.
-  const int prec_saved = p->prec;
-  const bool mixed = prec_saved == IMPS_PREC_BF16X6;
   int stall = 0;
   double rn_prev = 0.0;
   bool inner_hit = false;  // the last cycle ended on its Krylov residual estimate
   for (int outer = 0; it < maxit; ++outer) {
     // r = b - A(y)  (FP64 residual)
-    p->prec = IMPS_PREC_FP64;
-    int rc_res = proj_apply_dev(p, y, rho_in, rho_out, w, t, dsc);
-    p->prec = prec_saved;
-    RC(rc_res);
+    RC(A(y, w, true));
     RC(kr_axpby(1.0, b, -1.0, w, n, st));
     RC(kr_multidot(c->ws, w, n, 1, w, n, tmp, 0, dsc + 1, st));
     double rn = 0.0;
@@ -920,7 +954,7 @@ static int gmres_proj(imps_plan* p, const double* b, double* y, const double* rh
     int kdim = 0;
     for (int j = 0; j < m && it < maxit; ++j) {
       double* vj = V + (size_t)j * n;
-      RC(proj_apply_dev(p, vj, rho_in, rho_out, w, t, dsc));
+      RC(A(vj, w, false));
       ++it;
       RC(kr_cgs2_step(c->ws, V, n, j + 1, w, n, Hc, tmp, V + (size_t)(j + 1) * n, nullptr, st));
       RC(kr_givens(Hc, j, cs, sn, gam, R, ld, dsc + 3, bflag, st));
@@ -961,10 +995,7 @@ static int gmres_proj(imps_plan* p, const double* b, double* y, const double* rh
   }
   if (status != IMPS_OK) {
     // final explicit residual (FP64)
-    p->prec = IMPS_PREC_FP64;
-    int rc_res = proj_apply_dev(p, y, rho_in, rho_out, w, t, dsc);
-    p->prec = prec_saved;
-    RC(rc_res);
+    RC(A(y, w, true));
     RC(kr_axpby(1.0, b, -1.0, w, n, st));
     RC(kr_multidot(c->ws, w, n, 1, w, n, tmp, 0, dsc + 1, st));
     double rn = 0.0;
@@ -975,10 +1006,27 @@ static int gmres_proj(imps_plan* p, const double* b, double* y, const double* rh
   }
   if (iters) *iters = it;
   if (debug_on())
-    fprintf(stderr, "[imps gmres] n=%lld prec=%d iters=%d relres=%.3e tol=%.1e status=%d\n", (long long)n,
-            p->prec, it, rel, tol, status);
+    fprintf(stderr, "[imps gmres] n=%lld mixed=%d iters=%d relres=%.3e tol=%.1e status=%d\n", (long long)n,
+            (int)mixed, it, rel, tol, status);
   if (relres) *relres = rel;
   return status;
+}
+
+// GMRES on the projected operator A(v) = v - T(v) + tr(v*rho_in)*rho_out of a TM plan
+static int gmres_proj(imps_plan* p, const double* b, double* y, const double* rho_in,
+                      const double* rho_out, double tol, int maxit, int krylov, int* iters,
+                      double* relres, Bump& bp) {
+  imps_ctx* c = p->ctx;
+  const int64_t n = p->P.slots[0].nelem;
+  double* t = bp.take(n);
+  const int prec_saved = p->prec;
+  DevOp A = [&](const double* in, double* out, bool fp64) -> int {
+    if (fp64) p->prec = IMPS_PREC_FP64;
+    const int rc = proj_apply_dev(p, in, rho_in, rho_out, out, t, c->dscal);
+    p->prec = prec_saved;
+    return rc;
+  };
+  return gmres_dev(c, n, A, prec_saved == IMPS_PREC_BF16X6, b, y, tol, maxit, krylov, iters, relres, bp);
 }
 
 int imps_invert_e_proj(imps_plan* p, const double* x, const double* L, const double* R, int dir,
@@ -1025,6 +1073,94 @@ __global__ void imps_set_identity_kernel(double* X, const int64_t* boff, const i
   const int m = bdim[b];
   double* x = X + boff[b];
   for (int64_t e = threadIdx.x; e < (int64_t)m * m; e += blockDim.x) x[e] = (e % (m + 1) == 0) ? 1.0 : 0.0;
+}
+
+// ---- InvertE_fac / InvertE_proj_fac on split complex planes ----
+// Solves (1 - fac T) y = x (InvEBlockFunctions.hpp:413-451 with InvEfun_fac :166-197) or,
+// with rho, the projected (1 - fac T + |rho_out)(rho_in|) y = x - tr(x rho_in) rho_out
+// (:277-330 with InvEfun_proj_fac :90-125).  x, y complex as separate real and imaginary
+// planes; T is the real mixed transfer matrix of the plan, so the complex system is the real
+// system on the stacked vector [re; im] and the device GMRES solves it in FP64.
+static int invert_fac_impl(imps_plan* p, const double* xre, const double* xim, const double* L,
+                           const double* R, int dir, bool proj, double fre, double fim, double* yre,
+                           double* yim, int mem, double tol, int maxit, int krylov, int* iters, double* relres) {
+  if (!is_mixed_tm(p) || !xre || !xim || !yre || !yim || (proj && (!L || !R))) return IMPS_ERR_BAD_ARG;
+  imps_ctx* c = p->ctx;
+  if (c->device < 0) return IMPS_ERR_NO_DEVICE;
+  cudaStream_t st = c->stream;
+  const int64_t n = p->P.slots[p->P.n_in].nelem;
+  if (p->P.slots[p->P.n_out].nelem != n) return IMPS_ERR_BAD_ARG;
+  int m = krylov > 0 ? std::min(krylov, kMaxCols - 2) : kGmresKrylov;
+  if (maxit <= 0) maxit = (int)std::min<int64_t>(2 * n, 100000);
+  RC(arena_reserve(c, round256(2 * n * 8) * (m + 12) + round256((size_t)(m + 1) * (m + 1) * 8) + 16 * 4096));
+  Bump bp{c->arena};
+  double* x = bp.take(2 * n);
+  double* y = bp.take(2 * n);
+  double* t = bp.take(2 * n);
+  double* b = bp.take(2 * n);
+  double *dL = nullptr, *dR = nullptr;
+  const cudaMemcpyKind k_in = mem == IMPS_MEM_HOST ? cudaMemcpyHostToDevice : cudaMemcpyDeviceToDevice;
+  CK(cudaMemcpyAsync(x, xre, n * 8, k_in, st));
+  CK(cudaMemcpyAsync(x + n, xim, n * 8, k_in, st));
+  CK(cudaMemcpyAsync(y, yre, n * 8, k_in, st));
+  CK(cudaMemcpyAsync(y + n, yim, n * 8, k_in, st));
+  if (proj) {
+    dL = bp.take(n);
+    dR = bp.take(n);
+    CK(cudaMemcpyAsync(dL, L, n * 8, k_in, st));
+    CK(cudaMemcpyAsync(dR, R, n * 8, k_in, st));
+  }
+  // rho_in / rho_out: dir l -> (R, L), dir r -> (L, R) (InvEBlockFunctions.hpp:313-328)
+  const double* rin = proj ? (dir == 0 ? dR : dL) : nullptr;
+  const double* rout = proj ? (dir == 0 ? dL : dR) : nullptr;
+  double* tau = c->dscal + 16;  // (re, im) of tr(v rho_in)
+  auto traces = [&](const double* v) -> int {
+    RC(kr_trace_prod(c->ws, v, rin, p->d_boff, p->d_bdim, p->nb_in, tau, st, p->d_bcols));
+    RC(kr_trace_prod(c->ws, v + n, rin, p->d_boff, p->d_bdim, p->nb_in, tau + 1, st, p->d_bcols));
+    return IMPS_OK;
+  };
+  // b = x - tr(x rho_in) rho_out  (x unchanged without projection)
+  if (proj) {
+    RC(traces(x));
+    CK(cudaMemsetAsync(t, 0, 2 * n * 8, st));
+    // b = x - 0 + tau rho_out, then flip the projector's sign: b = 2x - b
+    RC(kr_fac_epilogue(x, x + n, t, t + n, 0.0, 0.0, tau, rout, b, b + n, n, st));
+    RC(kr_axpby(2.0, x, -1.0, b, 2 * n, st));
+  } else {
+    CK(cudaMemcpyAsync(b, x, 2 * n * 8, cudaMemcpyDeviceToDevice, st));
+  }
+  DevOp A = [&](const double* u, double* out, bool) -> int {
+    RC(apply_dev(p, u, t));
+    RC(apply_dev(p, u + n, t + n));
+    if (proj) RC(traces(u));
+    return kr_fac_epilogue(u, u + n, t, t + n, fre, fim, proj ? tau : nullptr, rout, out, out + n, n, st);
+  };
+  const int prec_saved = p->prec;
+  p->prec = IMPS_PREC_FP64;
+  int rc = gmres_dev(c, 2 * n, A, false, b, y, tol, maxit, m, iters, relres, bp);
+  p->prec = prec_saved;
+  if (rc < 0) return rc;
+  const cudaMemcpyKind k_out = mem == IMPS_MEM_HOST ? cudaMemcpyDeviceToHost : cudaMemcpyDeviceToDevice;
+  CK(cudaMemcpyAsync(yre, y, n * 8, k_out, st));
+  CK(cudaMemcpyAsync(yim, y + n, n * 8, k_out, st));
+  CK(cudaStreamSynchronize(st));
+  return rc;
+}
+
+int imps_invert_e_fac(imps_plan* p, const double* x_re, const double* x_im, double fac_re, double fac_im,
+                      double* y_re, double* y_im, int mem, double tol, int maxit, int krylov, int* iters,
+                      double* relres) {
+  return invert_fac_impl(p, x_re, x_im, nullptr, nullptr, 0, false, fac_re, fac_im, y_re, y_im, mem, tol,
+                         maxit, krylov, iters, relres);
+}
+
+int imps_invert_e_proj_fac(imps_plan* p, const double* x_re, const double* x_im, const double* L,
+                           const double* R, int dir, double fac_re, double fac_im, double* y_re, double* y_im,
+                           int mem, double tol, int maxit, int krylov, int* iters, double* relres) {
+  if ((dir != 0 && dir != 1) || !is_mixed_tm(p) || dir != (p->P.kind == PLAN_TMMIXED_L ? 0 : 1))
+    return IMPS_ERR_BAD_ARG;  // the plan's direction and the projector's roles must agree
+  return invert_fac_impl(p, x_re, x_im, L, R, dir, true, fac_re, fac_im, y_re, y_im, mem, tol, maxit, krylov,
+                         iters, relres);
 }
 
 int imps_tm_dominant(imps_plan* p, const double* x0, double* V, int mem, double tol, int maxit,

@@ -133,6 +133,8 @@ int build_hc(Plan& P, const Layout& C, const Layout& EHL, const Layout& EHR,
              const Layout& AL, const Layout& AR, int d, const std::vector<HNnz>& h);
 int build_tm(Plan& P, const std::vector<const Layout*>& A, int dir, const Layout& in,
              const Layout& out);
+int build_tm_mixed(Plan& P, const std::vector<const Layout*>& A, const std::vector<const Layout*>& B,
+                   int dir, const Layout& in, const Layout& out);
 int build_redop(Plan& P, const Layout& A, int d, const std::vector<HNnz>& h, int dir);
 int build_optm(Plan& P, const Layout& A0, const Layout& A1, int d, const std::vector<HNnz>& h,
                int dir, const Layout& out);

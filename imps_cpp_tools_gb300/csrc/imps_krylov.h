@@ -39,7 +39,10 @@ int kr_axpby(double a, const double* x, double b, double* y, int64_t n, cudaStre
 int kr_proj_epilogue(const double* x, const double* t, const double* s, const double* rho, double* y,
                      int64_t n, cudaStream_t st);
 int kr_trace_prod(const KrylovWs& ws, const double* X, const double* R, const int64_t* boff,
-                  const int32_t* bdim, int nb, double* out, cudaStream_t st);
+                  const int32_t* bdim, int nb, double* out, cudaStream_t st, const int32_t* bcols = nullptr);
+int kr_fac_epilogue(const double* ure, const double* uim, const double* tre, const double* tim, double c,
+                    double s, const double* tau, const double* rho, double* ore, double* oim, int64_t n,
+                    cudaStream_t st);
 int kr_segsq(const KrylovWs& ws, const double* X, const int64_t* soff, const int64_t* slen, int ns,
              double* out, cudaStream_t st);
 int kr_absmax(const KrylovWs& ws, const double* x, int64_t n, double* out, cudaStream_t st);

@@ -496,10 +496,13 @@ __global__ void proj_epilogue_kernel(const double* __restrict__ x, const double*
 }
 
 // sum over blocks q of trace(X_q * R_q) = sum_{i,j} X_q[i + j m] * R_q[j + i m]
+// sum_b tr(X_b R_b): X_b is rows x cols at boff[b], R_b the cols x rows block at the same
+// offset (blocks paired in order; bcols == nullptr: square blocks)
 __global__ void __launch_bounds__(RB) trace_prod_kernel(const double* __restrict__ X,
                                                         const double* __restrict__ R,
                                                         const int64_t* __restrict__ boff,
-                                                        const int32_t* __restrict__ bdim, int nb,
+                                                        const int32_t* __restrict__ bdim,
+                                                        const int32_t* __restrict__ bcols, int nb,
                                                         double* __restrict__ partials,
                                                         unsigned int* __restrict__ counter,
                                                         double* __restrict__ out) {
@@ -509,11 +512,12 @@ __global__ void __launch_bounds__(RB) trace_prod_kernel(const double* __restrict
   // flatten (block, element) pairs with a grid-stride loop over blocks x elements
   for (int b = 0; b < nb; ++b) {
     const int m = bdim[b];
+    const int nc = bcols ? bcols[b] : m;
     const int64_t o = boff[b];
-    const int64_t mm = (int64_t)m * m;
+    const int64_t mm = (int64_t)m * nc;
     for (int64_t e = (int64_t)blockIdx.x * RB + threadIdx.x; e < mm; e += (int64_t)gridDim.x * RB) {
       const int64_t i = e % m, j = e / m;
-      acc = fma(X[o + e], R[o + j + i * m], acc);
+      acc = fma(X[o + e], R[o + j + i * nc], acc);
     }
   }
   acc = block_sum(acc, sh);
@@ -732,9 +736,32 @@ int kr_proj_epilogue(const double* x, const double* t, const double* s, const do
 }
 
 int kr_trace_prod(const KrylovWs& ws, const double* X, const double* R, const int64_t* boff,
-                  const int32_t* bdim, int nb, double* out, cudaStream_t st) {
+                  const int32_t* bdim, int nb, double* out, cudaStream_t st, const int32_t* bcols) {
   imps::count_launch();
-  trace_prod_kernel<<<32, RB, 0, st>>>(X, R, boff, bdim, nb, ws.partials, ws.counter, out);
+  trace_prod_kernel<<<32, RB, 0, st>>>(X, R, boff, bdim, bcols, nb, ws.partials, ws.counter, out);
+  return IMPS_OK;
+}
+
+// out = u - fac * t + tau * rho on split complex planes (fac = c + i s; tau, rho optional):
+//   out_re = u_re - (c t_re - s t_im) + tau_re rho,  out_im = u_im - (s t_re + c t_im) + tau_im rho
+__global__ void fac_epilogue_kernel(const double* __restrict__ ure, const double* __restrict__ uim,
+                                    const double* __restrict__ tre, const double* __restrict__ tim, double c,
+                                    double sn, const double* __restrict__ tau, const double* __restrict__ rho,
+                                    double* __restrict__ ore, double* __restrict__ oim, int64_t n) {
+  const double tr = tau ? tau[0] : 0.0, ti = tau ? tau[1] : 0.0;
+  for (int64_t r = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; r < n; r += (int64_t)gridDim.x * blockDim.x) {
+    const double a = tre[r], b = tim[r];
+    const double p = rho ? rho[r] : 0.0;
+    ore[r] = ure[r] - (c * a - sn * b) + tr * p;
+    oim[r] = uim[r] - (sn * a + c * b) + ti * p;
+  }
+}
+
+int kr_fac_epilogue(const double* ure, const double* uim, const double* tre, const double* tim, double c,
+                    double s, const double* tau, const double* rho, double* ore, double* oim, int64_t n,
+                    cudaStream_t st) {
+  imps::count_launch();
+  fac_epilogue_kernel<<<grid_for(n), 256, 0, st>>>(ure, uim, tre, tim, c, s, tau, rho, ore, oim, n);
   return IMPS_OK;
 }
 

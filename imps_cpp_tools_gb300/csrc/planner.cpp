@@ -318,6 +318,143 @@ int build_tm(Plan& P, const std::vector<const Layout*>& A, int dir, const Layout
   return IMPS_OK;
 }
 
+// Mixed transfer matrix of two unit cells on a general BlockMat X (one block per Qin, a
+// fixed charge offset):
+//   dir 0 (left, sites in order):   out(Qout(B_s) -> Qout(A_s)) += B_s^T X(Qin(B_s) -> Qin(A_s)) A_s
+//   dir 1 (right, sites reversed):  out(Qin(A_s) -> Qin(B_s))   += A_s X(Qout(A_s) -> Qout(B_s)) B_s^T
+// (TMBlockFunctions.hpp:336-344 / 474-482 as in*A resp. A*in followed by the mixed product
+// with B, chained over the unit cell at :669-676 / :737-744).  A is the lower layer, B the
+// upper one.  Two stages per site: W = X_x A_a (left) or A_a X_x (right) for every matched
+// (block of X, physical index) pair, then the output blocks sum B^T W (left) or W B^T
+// (right) over their pairs.  Products whose output sector is absent from `out` are counted
+// in `dropped` (the reference prints "not present" and skips them, :380-384, 521-525).
+// Slots: 0 in, 1 out, 2..n+1 A_k, n+2..2n+1 B_k, then internal scratch.
+int build_tm_mixed(Plan& P, const std::vector<const Layout*>& A, const std::vector<const Layout*>& B,
+                   int dir, const Layout& in, const Layout& out) {
+  P = Plan();
+  P.kind = dir == 0 ? PLAN_TMMIXED_L : PLAN_TMMIXED_R;
+  const int n = (int)A.size();
+  if (n < 1 || (int)B.size() != n) return IMPS_ERR_BAD_ARG;
+  const int IN = add_slot(P, SLOT_EXTERNAL, in.nelem, "in");
+  const int OUT = add_slot(P, SLOT_EXTERNAL, out.nelem, "out");
+  std::vector<int> SA(n), SB(n);
+  for (int k = 0; k < n; ++k) SA[k] = add_slot(P, SLOT_EXTERNAL, A[k]->nelem, "A");
+  for (int k = 0; k < n; ++k) SB[k] = add_slot(P, SLOT_EXTERNAL, B[k]->nelem, "B");
+  P.n_in = IN;
+  P.n_out = OUT;
+  struct Pair { int x, a, b; int64_t woff; Key oin, oout; int orows, ocols; };
+  std::vector<Layout> mids;
+  const Layout* cur = &in;
+  int cur_slot = IN;
+  for (int step = 0; step < n; ++step) {
+    const int k = dir == 0 ? step : n - 1 - step;
+    const Layout& LA = *A[k];
+    const Layout& LB = *B[k];
+    if (LA.ngroups != LB.ngroups) return IMPS_ERR_BAD_TABLE;
+    // matched pairs and their scratch
+    std::vector<Pair> pairs;
+    int64_t woff = 0;
+    for (int xi = 0; xi < (int)cur->blocks.size(); ++xi) {
+      const Block& x = cur->blocks[xi];
+      for (int g = 0; g < LA.ngroups; ++g) {
+        const int a = dir == 0 ? LA.find_in(g, x.qout) : LA.find_out(g, x.qin);
+        const int b = dir == 0 ? LB.find_in(g, x.qin) : LB.find_out(g, x.qout);
+        if (a < 0 || b < 0) continue;
+        const Block& ba = LA.blocks[a];
+        const Block& bb = LB.blocks[b];
+        Pair pr{xi, a, b, woff, {}, {}, 0, 0};
+        if (dir == 0) {
+          if (x.cols != ba.rows || x.rows != bb.rows) return IMPS_ERR_BAD_TABLE;
+          pr.oin = bb.qout; pr.oout = ba.qout; pr.orows = bb.cols; pr.ocols = ba.cols;
+          woff += (int64_t)x.rows * ba.cols;
+        } else {
+          if (ba.cols != x.rows || x.cols != bb.cols) return IMPS_ERR_BAD_TABLE;
+          pr.oin = ba.qin; pr.oout = bb.qin; pr.orows = ba.rows; pr.ocols = bb.rows;
+          woff += (int64_t)ba.rows * x.cols;
+        }
+        pairs.push_back(pr);
+      }
+    }
+    const int SW = add_slot(P, SLOT_INTERNAL, std::max<int64_t>(woff, 1), "W");
+    // output layout of this step: the given one, or derived from the pairs (std::map order)
+    const bool last = step == n - 1;
+    if (!last) {
+      std::map<Key, std::pair<Key, std::pair<int, int>>> keys;
+      for (const Pair& pr : pairs) {
+        auto it = keys.find(pr.oin);
+        if (it == keys.end()) keys.emplace(pr.oin, std::make_pair(pr.oout, std::make_pair(pr.orows, pr.ocols)));
+        else if (it->second.first != pr.oout || it->second.second != std::make_pair(pr.orows, pr.ocols))
+          return IMPS_ERR_BAD_TABLE;  // not a BlockMat: two outgoing charges for one incoming
+      }
+      Layout M;
+      M.nsym = in.nsym;
+      int64_t off = 0;
+      for (auto& kv : keys) {
+        Block bl;
+        bl.qin = kv.first;
+        bl.qout = kv.second.first;
+        bl.rows = kv.second.second.first;
+        bl.cols = kv.second.second.second;
+        bl.off = off;
+        off += (int64_t)bl.rows * bl.cols;
+        M.blocks.push_back(bl);
+      }
+      M.nelem = off;
+      layout_index(M);
+      mids.push_back(M);
+    }
+    const Layout* O = last ? &out : &mids.back();
+    const int o_slot = last ? OUT : add_slot(P, SLOT_INTERNAL, std::max<int64_t>(O->nelem, 1), "Y");
+    // stage 1: W
+    P.stages.emplace_back();
+    {
+      StageBuilder sb(P.stages.back());
+      for (int pi = 0; pi < (int)pairs.size(); ++pi) {
+        const Pair& pr = pairs[pi];
+        const Block& x = cur->blocks[pr.x];
+        const Block& ba = LA.blocks[pr.a];
+        if (dir == 0) {
+          sb.begin(SW, pr.woff, x.rows, x.rows, ba.cols, 0, pi);
+          sb.term(cur_slot, x.off, x.rows, 0, SA[k], ba.off, ba.rows, 0, x.cols, 1.0);
+        } else {
+          sb.begin(SW, pr.woff, ba.rows, ba.rows, x.cols, 0, pi);
+          sb.term(SA[k], ba.off, ba.rows, 0, cur_slot, x.off, x.rows, 0, x.rows, 1.0);
+        }
+        sb.end();
+      }
+    }
+    // stage 2: output blocks
+    P.stages.emplace_back();
+    {
+      StageBuilder sb(P.stages.back());
+      std::vector<int> used(pairs.size(), 0);
+      for (int oi = 0; oi < (int)O->blocks.size(); ++oi) {
+        const Block& o = O->blocks[oi];
+        sb.begin(o_slot, o.off, o.rows, o.rows, o.cols, 0, oi);
+        for (int pi = 0; pi < (int)pairs.size(); ++pi) {
+          const Pair& pr = pairs[pi];
+          if (pr.oin != o.qin) continue;
+          if (pr.oout != o.qout || pr.orows != o.rows || pr.ocols != o.cols) return IMPS_ERR_BAD_TABLE;
+          used[pi] = 1;
+          const Block& x = cur->blocks[pr.x];
+          const Block& bb = LB.blocks[pr.b];
+          if (dir == 0)  // out += B_b^T W
+            sb.term(SB[k], bb.off, bb.rows, 1, SW, pr.woff, x.rows, 0, x.rows, 1.0);
+          else  // out += W B_b^T
+            sb.term(SW, pr.woff, o.rows, 0, SB[k], bb.off, bb.rows, 1, x.cols, 1.0);
+        }
+        sb.end();
+      }
+      for (int u : used) P.dropped += u ? 0 : 1;
+    }
+    cur = O;
+    cur_slot = o_slot;
+  }
+  P.derived = mids;
+  for (auto& st : P.stages) P.flops_apply += st.flops;
+  return IMPS_OK;
+}
+
 // ReducedOp (MPSBlockUtilities.hpp:37-74).  dir 0 (l): HL[i1][j1] += h * A[i0]^T * A[j0];
 // dir 1 (r): HR[i0][j0] += h * A[j1] * A[i1]^T.  The output RedOp layout (group i*d+j,
 // BlockMat key order) is derived here.  Slots: 0 A, 1 out.

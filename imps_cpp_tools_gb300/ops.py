@@ -48,6 +48,29 @@ def eigs_rs(plan, x, tol, ncv=0, maxit=0):
     return ev.value, na.value, st == 0
 
 
+def InvertE_fac(plan, x_re, x_im, fac, y_re, y_im, tol, maxit=0, krylov=0):
+    """InvertE_fac(A, B, x, dir, fac) (InvEBlockFunctions.hpp:413-451) for the mixed TM ``plan``:
+    (1 - fac T) y = x with complex x, y as real / imaginary device planes (y holds y0 on entry).
+    Returns (iterations, relative residual, converged)."""
+    it, rr = C.c_int(), C.c_double()
+    fac = complex(fac)
+    st = N.call("imps_invert_e_fac", plan.handle, _dptr(x_re), _dptr(x_im), fac.real, fac.imag, _dptr(y_re),
+                _dptr(y_im), N.MEM_DEVICE, float(tol), int(maxit), int(krylov), C.byref(it), C.byref(rr))
+    return it.value, rr.value, st == 0
+
+
+def InvertE_proj_fac(plan, x_re, x_im, L, R, direction, fac, y_re, y_im, tol, maxit=0, krylov=0):
+    """InvertE_proj_fac(A, B, x, L, R, dir, fac) (InvEBlockFunctions.hpp:277-330) for the mixed TM
+    ``plan``; L, R real BlockMats paired block by block with x."""
+    it, rr = C.c_int(), C.c_double()
+    fac = complex(fac)
+    d = N.DIR_LEFT if direction in ("l", 0) else N.DIR_RIGHT
+    st = N.call("imps_invert_e_proj_fac", plan.handle, _dptr(x_re), _dptr(x_im), _dptr(L), _dptr(R), d,
+                fac.real, fac.imag, _dptr(y_re), _dptr(y_im), N.MEM_DEVICE, float(tol), int(maxit), int(krylov),
+                C.byref(it), C.byref(rr))
+    return it.value, rr.value, st == 0
+
+
 def InvertE_proj(plan, x, L, R, direction, y, tol, maxit=0, krylov=0):
     """InvertE_proj (InvEBlockFunctions.hpp:201-266) for BlockDiagMat x on the unit cell of ``plan``.
 

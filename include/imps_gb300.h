@@ -98,6 +98,15 @@ int imps_plan_hc(imps_ctx* ctx, const imps_layout* C, const imps_layout* EHL,
  * Slots: 0 in, 1 out, 2.. 2+nsites-1 A[k]. */
 int imps_plan_tm(imps_ctx* ctx, int nsites, const imps_layout* const* A, int dir,
                  const imps_layout* in, const imps_layout* out, imps_plan** plan);
+/* Mixed transfer matrix of two unit cells on a general BlockMat (one block per incoming
+ * charge, a fixed charge offset): ApplyTMmixedLeft(A, B, X) / ApplyTMmixedRight(A, B, X)
+ * (TMBlockFunctions.hpp:336-344, 474-482; unit-cell chains :669-676 in site order, :737-744
+ * in reverse).  dir 0: out(Qout(B_s) -> Qout(A_s)) += B_s^T X A_s; dir 1:
+ * out(Qin(A_s) -> Qin(B_s)) += A_s X B_s^T.  A is the lower, B the upper layer.  Apply with
+ * imps_tm_apply (real vectors; a complex vector is applied plane by plane).
+ * Slots: 0 in, 1 out, 2.. A[k], 2+nsites.. B[k]. */
+int imps_plan_tm_mixed(imps_ctx* ctx, int nsites, const imps_layout* const* A, const imps_layout* const* B,
+                       int dir, const imps_layout* in, const imps_layout* out, imps_plan** plan);
 /* ReducedOp (MPSBlockUtilities.hpp:37-74).  Slots: 0 A, 1 out (derived layout 0). */
 int imps_plan_redop(imps_ctx* ctx, const imps_layout* A, int d, int nnz, const int32_t* hrow,
                     const int32_t* hcol, const double* hval, int dir, imps_plan** out);
@@ -155,6 +164,21 @@ int imps_eigs_rs(imps_plan* op, double* x, int mem, double tol, int ncv, int max
 int imps_invert_e_proj(imps_plan* tm, const double* x, const double* L, const double* R,
                        int dir, double* y, int mem, double tol, int maxit, int krylov,
                        int* iters, double* relres);
+/* InvertE_fac(A, B, x, dir, fac) (InvEBlockFunctions.hpp:413-451, operator InvEfun_fac
+ * :166-197): solves (1 - fac T) y = x for the mixed TM plan `tmx` (direction fixed by the
+ * plan), complex x and y given as separate real / imaginary planes in the plan's in-layout
+ * order; y holds y0 on entry.  Restarted GMRES(krylov) on the device (0: 80), stop
+ * |r| < tol |b|.  Status 1 = not converged (y returned). */
+int imps_invert_e_fac(imps_plan* tmx, const double* x_re, const double* x_im, double fac_re, double fac_im,
+                      double* y_re, double* y_im, int mem, double tol, int maxit, int krylov, int* iters,
+                      double* relres);
+/* InvertE_proj_fac(A, B, x, L, R, dir, fac) (InvEBlockFunctions.hpp:277-330, operator
+ * InvEfun_proj_fac :90-125): (1 - fac T + |rho_out)(rho_in|) y = x - tr(x rho_in) rho_out with
+ * (rho_in, rho_out) = (R, L) for dir 0, (L, R) for dir 1 (dir must match the plan); L, R are
+ * real BlockMats whose blocks pair with x's in order (tr(x rho) = sum_b tr(x_b rho_b)). */
+int imps_invert_e_proj_fac(imps_plan* tmx, const double* x_re, const double* x_im, const double* L,
+                           const double* R, int dir, double fac_re, double fac_im, double* y_re, double* y_im,
+                           int mem, double tol, int maxit, int krylov, int* iters, double* relres);
 /* TMDominantEig (EigsBlockFunctions.hpp:91-172) for a left/right-isometric unit cell: the
  * dominant eigenvalue is 1 and the fixed point solves (1 - T + |x0)(1|) v = x0; v is
  * normalised to unit trace as in the reference.  x0 may be NULL (identity). */

@@ -495,6 +495,102 @@ def ApplyTMmixedLeft(A, B):
     return out
 
 
+def ApplyTMmixedLeftX(A, B, X):
+    """ApplyTMmixedLeft(A, B, in) on a general BlockMat (TMBlockFunctions.hpp:336-344):
+    ApplyTMmixedLeft(in*A, B), i.e. out(Qout(B_s) -> Qout(A_s)) += B_s^T X A_s."""
+    return ApplyTMmixedLeft([bm_mul(X, a) for a in A], B)
+
+
+def ApplyTMmixedRightX(A, B, X):
+    """ApplyTMmixedRight(A, B, in) on a general BlockMat (TMBlockFunctions.hpp:474-482):
+    ApplyTMmixedRight(A*in, B), i.e. out(Qin(A_s) -> Qin(B_s)) += A_s X B_s^T."""
+    return ApplyTMmixedRight([bm_mul(a, X) for a in A], B)
+
+
+def ApplyTMmixedLeftUC(Avec, Bvec, X):
+    """Unit-cell chain in site order (TMBlockFunctions.hpp:669-676)."""
+    for A, B in zip(Avec, Bvec):
+        X = ApplyTMmixedLeftX(A, B, X)
+    return X
+
+
+def ApplyTMmixedRightUC(Avec, Bvec, X):
+    """Unit-cell chain in reverse site order (TMBlockFunctions.hpp:737-744)."""
+    for A, B in zip(reversed(Avec), reversed(Bvec)):
+        X = ApplyTMmixedRightX(A, B, X)
+    return X
+
+
+def bm_trace_pairs(X, Rho):
+    """sum_b tr(X_b Rho_b) with the blocks paired in iteration order, as
+    InvEfun_proj_fac does (InvEBlockFunctions.hpp:104-108)."""
+    return sum(np.trace(X[qx][1] @ Rho[qr][1]) for qx, qr in zip(sorted(X), sorted(Rho)))
+
+
+def InvEfun_fac(invec, TMfun, sizes, fac):
+    """InvEfun_fac for BlockMat (InvEBlockFunctions.hpp:166-197): y = x - fac * TM(x)."""
+    x = bm_from_vec(invec, sizes)
+    Tx = TMfun(x)
+    y = np.array(invec, dtype=np.result_type(invec, fac)).copy()
+    pos = 0
+    for (qi, qo, ml, mr) in sizes:
+        y[pos:pos + ml * mr] -= fac * Tx[qi][1].reshape(-1, order="F")
+        pos += ml * mr
+    return y
+
+
+def InvEfun_proj_fac(invec, TMfun, rho_inside, rho_outside, sizes, fac):
+    """InvEfun_proj_fac for BlockMat (InvEBlockFunctions.hpp:90-125):
+    y = x - fac * TM(x) + tr(x * rho_in) * rho_out."""
+    x = bm_from_vec(invec, sizes)
+    tr = bm_trace_pairs(x, rho_inside)
+    return InvEfun_fac(invec, TMfun, sizes, fac) + tr * bm_vec(rho_outside)
+
+
+def InvertE_fac(Avec, Bvec, x, direction, fac, tol=1e-14, maxit=0, y0=None, rng=None):
+    """InvertE_fac(A, B, x, dir, fac) (InvEBlockFunctions.hpp:413-451) with the reference's GMRES.
+    Returns (y as BlockMat, flag)."""
+    sizes = bm_sizes(x)
+    mtot = sum(ml * mr for (_, _, ml, mr) in sizes)
+    if maxit == 0:
+        maxit = mtot
+    if y0 is None:
+        rng = rng if rng is not None else np.random.default_rng(0)
+        y0v = rng.standard_normal(mtot) + 0j
+    else:
+        y0v = bm_vec(y0) + 0j
+    TMfun = (lambda X: ApplyTMmixedLeftUC(Avec, Bvec, X)) if direction == "l" else \
+        (lambda X: ApplyTMmixedRightUC(Avec, Bvec, X))
+    y, flag = gmres(lambda v: InvEfun_fac(v, TMfun, sizes, fac), bm_vec(x) + 0j, y0v, tol, maxit)
+    return bm_from_vec(y, sizes), flag
+
+
+def InvertE_proj_fac(Avec, Bvec, x, L, R, direction, fac, tol=1e-14, maxit=0, y0=None, rng=None):
+    """InvertE_proj_fac(A, B, x, L, R, dir, fac) (InvEBlockFunctions.hpp:277-330):
+    dir l: b = x - tr(x R) L, operator with (rho_in, rho_out) = (R, L); dir r: b = x - tr(L x) R,
+    (rho_in, rho_out) = (L, R)."""
+    sizes = bm_sizes(x)
+    mtot = sum(ml * mr for (_, _, ml, mr) in sizes)
+    if maxit == 0:
+        maxit = mtot
+    if y0 is None:
+        rng = rng if rng is not None else np.random.default_rng(0)
+        y0v = rng.standard_normal(mtot) + 0j
+    else:
+        y0v = bm_vec(y0) + 0j
+    xv = bm_vec(x) + 0j
+    if direction == "l":
+        xv = xv - bm_trace_pairs(x, R) * bm_vec(L)
+        TMfun = lambda X: ApplyTMmixedLeftUC(Avec, Bvec, X)
+        Afun = lambda v: InvEfun_proj_fac(v, TMfun, R, L, sizes, fac)
+    else:
+        xv = xv - bm_trace_pairs(x, L) * bm_vec(R)
+        TMfun = lambda X: ApplyTMmixedRightUC(Avec, Bvec, X)
+        Afun = lambda v: InvEfun_proj_fac(v, TMfun, L, R, sizes, fac)
+    y, flag = gmres(Afun, xv, y0v, tol, maxit)
+    return bm_from_vec(y, sizes), flag
+
+
 def ApplyOperator(A, hnnz):
     """MPSBlockUtilities.hpp:17-34: out[ii] += h * in[jj]."""
     out = [dict() for _ in A]

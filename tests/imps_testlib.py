@@ -17,6 +17,11 @@ def bd_blocks(X):
     return [(0, q, q, X[q].shape[0], X[q].shape[1]) for q in sorted(X)]
 
 
+def bm_blocks(X):
+    """General BlockMat (one block per incoming charge)."""
+    return [(0, q, X[q][0], X[q][1].shape[0], X[q][1].shape[1]) for q in sorted(X)]
+
+
 def redop_blocks(R, d):
     return [(i * d + j, qi, R[i][j][qi][0], R[i][j][qi][1].shape[0], R[i][j][qi][1].shape[1])
             for i in range(d) for j in range(d) for qi in sorted(R[i][j])]

@@ -1,0 +1,96 @@
+"""Mixed transfer matrices on general BlockMats and the factored environment solves of the
+excitation ansatz (TMBlockFunctions.hpp:336-344, 474-482, 669-744; InvEBlockFunctions.hpp:
+90-197, 277-451): device plans and solvers against the oracle."""
+import numpy as np
+import pytest
+
+from imps_cpp_tools_gb300 import blocks as B
+from imps_cpp_tools_gb300 import ops
+from oracle import imps_oracle as O
+from tests import imps_testlib as T
+from tests.test_gpu_parity import dev, host, relerr
+from tests.test_oracle_excitations import B0, offset_bm
+
+pytestmark = pytest.mark.gpu
+
+
+@pytest.fixture(scope="module")
+def state():
+    return T.random_state("xxz", B0, seed=3, J=1.0, Delta=-1.0)
+
+
+def _layouts(st):
+    ns = len(st["I2K"][0])
+    lay = lambda A: [B.Layout(T.mps_blocks(a), ns) for a in A]
+    return ns, lay(st["AL"]), lay(st["AR"])
+
+
+@pytest.mark.parametrize("direction", ["l", "r"])
+@pytest.mark.parametrize("K", [(2,), (0,), (-2,)])
+def test_mixed_tm_apply_matches_oracle(cuda_ctx, state, direction, K):
+    ns, LAL, LAR = _layouts(state)
+    AL, AR = state["AL"], state["AR"]
+    rng = np.random.default_rng(5)
+    X = offset_bm(state["dimvec"][0], K, rng)
+    lx = B.Layout(T.bm_blocks(X), ns)
+    if direction == "l":  # lower AR, upper AL: out = sum_s AL_s^T X AR_s (the EHBL chain)
+        plan = B.plan_tm_mixed(cuda_ctx, LAR, LAL, 0, lx, lx)
+        A, Bm, ref = AR, AL, O.ApplyTMmixedLeftUC(AR, AL, X)
+    else:  # lower AL, upper AR: out = sum_s AL_s X AR_s^T (the EBR chain)
+        plan = B.plan_tm_mixed(cuda_ctx, LAL, LAR, 1, lx, lx)
+        A, Bm, ref = AL, AR, O.ApplyTMmixedRightUC(AL, AR, X)
+    for k in range(2):
+        plan.bind(2 + k, dev(O.mps_vec(A[k])))
+        plan.bind(4 + k, dev(O.mps_vec(Bm[k])))
+    out = dev(np.zeros(lx.nelem))
+    ops.ApplyTM(plan, dev(O.bm_vec(X)), out)
+    refv = np.concatenate([ref[q][1].reshape(-1, order="F") for q in sorted(X)])
+    assert relerr(host(out), refv) < 1e-12
+
+
+def _solve_pair(cuda_ctx, state, direction, K, fac, proj):
+    ns, LAL, LAR = _layouts(state)
+    AL, AR = state["AL"], state["AR"]
+    rng = np.random.default_rng(6)
+    x = offset_bm(state["dimvec"][0], K, rng, cplx=True)
+    lx = B.Layout(T.bm_blocks(x), ns)
+    if direction == "r":
+        Avec, Bvec, code = AL, AR, 1
+    else:
+        Avec, Bvec, code = AR, AL, 0
+    plan = B.plan_tm_mixed(cuda_ctx, [B.Layout(T.mps_blocks(a), ns) for a in Avec],
+                           [B.Layout(T.mps_blocks(b), ns) for b in Bvec], code, lx, lx)
+    for k in range(2):
+        plan.bind(2 + k, dev(O.mps_vec(Avec[k])))
+        plan.bind(4 + k, dev(O.mps_vec(Bvec[k])))
+    xv = O.bm_vec(x)
+    y0 = np.random.default_rng(7).standard_normal(xv.size) + 0j
+    yre, yim = dev(y0.real.copy()), dev(y0.imag.copy())
+    if proj:
+        # any L, R of the transposed structure define a regular projected system for |fac| < 1
+        L = {qo: (qi, 0.1 * rng.standard_normal(M.shape[::-1])) for qi, (qo, M) in x.items()}
+        R = {qo: (qi, 0.1 * rng.standard_normal(M.shape[::-1])) for qi, (qo, M) in x.items()}
+        it, rr, conv = ops.InvertE_proj_fac(plan, dev(xv.real.copy()), dev(xv.imag.copy()), dev(O.bm_vec(L)),
+                                            dev(O.bm_vec(R)), direction, fac, yre, yim, 1e-12)
+        yo, flag = O.InvertE_proj_fac(Avec, Bvec, x, L, R, direction, fac, tol=1e-12,
+                                      y0=O.bm_from_vec(y0, O.bm_sizes(x)))
+    else:
+        it, rr, conv = ops.InvertE_fac(plan, dev(xv.real.copy()), dev(xv.imag.copy()), fac, yre, yim, 1e-12)
+        yo, flag = O.InvertE_fac(Avec, Bvec, x, direction, fac, tol=1e-12, y0=O.bm_from_vec(y0, O.bm_sizes(x)))
+    assert conv and flag >= 0
+    yg = host(yre) + 1j * host(yim)
+    return yg, O.bm_vec(yo)
+
+
+@pytest.mark.parametrize("direction", ["l", "r"])
+@pytest.mark.parametrize("K,p", [((2,), 0.7), ((-2,), 2.1), ((0,), 1.3)])
+def test_invert_e_fac_matches_oracle(cuda_ctx, state, direction, K, p):
+    """Charge offset K != 0, or momentum p != 0: (1 - e^{ip} T) is regular, no projection."""
+    yg, yo = _solve_pair(cuda_ctx, state, direction, K, np.exp(1j * p), proj=False)
+    assert np.linalg.norm(yg - yo) / np.linalg.norm(yo) < 1e-9
+
+
+@pytest.mark.parametrize("direction", ["l", "r"])
+def test_invert_e_proj_fac_matches_oracle(cuda_ctx, state, direction):
+    yg, yo = _solve_pair(cuda_ctx, state, direction, (0,), 0.9 * np.exp(0.4j), proj=True)
+    assert np.linalg.norm(yg - yo) / np.linalg.norm(yo) < 1e-9
