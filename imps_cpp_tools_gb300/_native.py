@@ -77,6 +77,7 @@ _PROTOS = {
     "imps_invert_e_proj": (c_int, [c_vp, c_vp, c_vp, c_vp, c_int, c_vp, c_int, c_dbl, c_int, c_int,
                                    P_int, P_dbl]),
     "imps_tm_dominant": (c_int, [c_vp, c_vp, c_vp, c_int, c_dbl, c_int, P_dbl, P_int]),
+    "imps_plan_program": (c_int, [c_vp, c_int, P_i64, c_int, P_i32, P_i64, P_i64, P_dbl, C.POINTER(c_vp)]),
     "imps_plan_tm_mixed": (c_int, [c_vp, c_int, C.POINTER(c_vp), C.POINTER(c_vp), c_int, c_vp, c_vp,
                                    C.POINTER(c_vp)]),
     "imps_invert_e_fac": (c_int, [c_vp, c_vp, c_vp, c_dbl, c_dbl, c_vp, c_vp, c_int, c_dbl, c_int, c_int,

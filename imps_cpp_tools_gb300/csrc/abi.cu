@@ -429,6 +429,80 @@ int imps_plan_tm_mixed(imps_ctx* ctx, int nsites, const imps_layout* const* A, c
   return IMPS_OK;
 }
 
+// A grouped-GEMM program given as explicit tables (every slot external): used for
+// contractions whose sector matching is compiled by a caller (the excitation effective
+// Hamiltonian).  Every term's operands and every output region are bounds-checked against
+// the slot sizes here, so a table can never make a kernel access memory outside its slots.
+int imps_plan_program(imps_ctx* ctx, int nslots, const int64_t* slot_nelem, int nstages,
+                      const int32_t* stage_nouts, const int64_t* outs, const int64_t* terms,
+                      const double* alphas, imps_plan** out) {
+  if (!ctx || !slot_nelem || nslots < 1 || nslots > kMaxSlots || nstages < 0 || (nstages && !stage_nouts) || !out)
+    return IMPS_ERR_BAD_ARG;
+  Plan P;
+  P.kind = PLAN_PROGRAM;
+  for (int i = 0; i < nslots; ++i) {
+    if (slot_nelem[i] < 0) return IMPS_ERR_BAD_ARG;
+    Slot sl;
+    sl.kind = SLOT_EXTERNAL;
+    sl.nelem = slot_nelem[i];
+    sl.name = "p";
+    P.slots.push_back(sl);
+  }
+  P.n_in = 0;
+  P.n_out = nslots > 1 ? 1 : 0;
+  auto within = [&](int64_t slot, int64_t off, int64_t ld, int64_t r, int64_t c) {
+    if (slot < 0 || slot >= nslots || off < 0 || r < 0 || c < 0) return false;
+    if (r == 0 || c == 0) return true;
+    if (ld < r) return false;
+    return off + (r - 1) + (c - 1) * ld < slot_nelem[slot];
+  };
+  int64_t o = 0, t = 0;
+  for (int sidx = 0; sidx < nstages; ++sidx) {
+    P.stages.emplace_back();
+    Stage& S = P.stages.back();
+    for (int q = 0; q < stage_nouts[sidx]; ++q, ++o) {
+      const int64_t* od = outs + 7 * o;
+      const int64_t cs = od[0], coff = od[1], cld = od[2], M = od[3], N = od[4], acc = od[5], nt = od[6];
+      if (!within(cs, coff, cld, M, N) || nt < 0 || M > INT32_MAX || N > INT32_MAX) return IMPS_ERR_BAD_TABLE;
+      OutBlock ob{};
+      ob.c_slot = (int16_t)cs;
+      ob.c_off = coff;
+      ob.c_ld = (int32_t)std::max<int64_t>(cld, 1);
+      ob.M = (int32_t)M;
+      ob.N = (int32_t)N;
+      ob.accumulate = (int16_t)(acc ? 1 : 0);
+      ob.tag = q;
+      ob.t0 = (int32_t)S.terms.size();
+      for (int64_t e = 0; e < nt; ++e, ++t) {
+        const int64_t* td = terms + 9 * t;
+        const int64_t as = td[0], aoff = td[1], ald = td[2], at = td[3], bs = td[4], boff = td[5], bld = td[6],
+                      bt = td[7], k = td[8];
+        // op(A) is M x k (stored k x M when transposed), op(B) is k x N (stored N x k)
+        const bool okA = at ? within(as, aoff, ald, k, M) : within(as, aoff, ald, M, k);
+        const bool okB = bt ? within(bs, boff, bld, N, k) : within(bs, boff, bld, k, N);
+        if (!okA || !okB || k < 0 || k > INT32_MAX || ald > INT32_MAX || bld > INT32_MAX) return IMPS_ERR_BAD_TABLE;
+        Term tm{};
+        tm.a_slot = (int16_t)as;
+        tm.a_off = aoff;
+        tm.a_ld = (int32_t)std::max<int64_t>(ald, 1);
+        tm.a_t = (int8_t)(at ? 1 : 0);
+        tm.b_slot = (int16_t)bs;
+        tm.b_off = boff;
+        tm.b_ld = (int32_t)std::max<int64_t>(bld, 1);
+        tm.b_t = (int8_t)(bt ? 1 : 0);
+        tm.k = (int32_t)k;
+        tm.alpha = alphas[t];
+        S.terms.push_back(tm);
+        S.flops += 2LL * M * N * k;
+      }
+      ob.t1 = (int32_t)S.terms.size();
+      S.outs.push_back(ob);
+    }
+  }
+  for (auto& st : P.stages) P.flops_apply += st.flops;
+  return finish_plan(ctx, P, out);
+}
+
 int imps_plan_redop(imps_ctx* ctx, const imps_layout* A, int d, int nnz, const int32_t* hrow,
                     const int32_t* hcol, const double* hval, int dir, imps_plan** out) {
   if (!ctx || !A || !out || d <= 0 || nnz < 0) return IMPS_ERR_BAD_ARG;

@@ -103,7 +103,8 @@ constexpr int kMaxSlots = 16;
 
 enum PlanKind {
   PLAN_HAC = 1, PLAN_HC = 2, PLAN_TM = 3, PLAN_REDOP = 4, PLAN_OPTM = 5, PLAN_MPS_BD = 6,
-  PLAN_GRAD = 7, PLAN_AA = 8, PLAN_BD_MPS = 9, PLAN_TMMIXED_R = 10, PLAN_TMMIXED_L = 11
+  PLAN_GRAD = 7, PLAN_AA = 8, PLAN_BD_MPS = 9, PLAN_TMMIXED_R = 10, PLAN_TMMIXED_L = 11,
+  PLAN_PROGRAM = 12
 };
 
 // A compiled contraction: slots + prepare stages (operator-dependent precomputation,

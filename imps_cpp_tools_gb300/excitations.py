@@ -1,0 +1,471 @@
+"""Effective Hamiltonian of the excitation ansatz on the GPU (Excitations_helpers.hpp:20-228).
+
+ApplyHeff is compiled once per structure into two grouped-GEMM programs (imps_plan_program)
+around the two factored environment solves (imps_invert_e_fac):
+
+* the sector matching of every block product is done here, on the host, exactly once;
+* complex tensors (X, B = N_L X, the environments of B) are pairs of real planes; every
+  product has one real operand (AL, AR, N_L, the environments of the ground state), so
+  a complex scalar (e^{ip}) or a sum of tensors becomes several GEMM terms with real alphas
+  accumulated into the same output block, and ApplyOperator becomes terms weighted by the
+  nonzeros of h;
+* a product whose operand is itself a product is materialised first (one stage per
+  materialisation, in order).
+
+Block structures are passed as the reference's map-of-blocks: an MPS tensor is a list over the
+physical index s of {qin: (qout, matrix)}, a BlockMat is {qin: (qout, matrix)}, a BlockDiagMat
+is {q: matrix}.  Vectors use the reference's Vectorize order (s-major, std::map key order,
+blocks column-major).
+"""
+from __future__ import annotations
+
+import ctypes as C
+
+import numpy as np
+
+from . import _native as N
+from . import blocks as B
+from . import ops
+
+OPS, XS, OUT, SCR, ES, RHS = range(6)
+
+
+def _kadd(a, b):
+    return tuple(x + y for x, y in zip(a, b))
+
+
+class Tensor:
+    """A materialised real block tensor in one slot: blocks[(g, qin)] = (qout, rows, cols, off)."""
+
+    def __init__(self, slot, blocks, ngroups):
+        self.slot, self.blocks, self.ngroups = slot, blocks, ngroups
+
+    def nelem(self):
+        return sum(r * c for (_, r, c, _) in self.blocks.values())
+
+    def view(self, group=None, t=False):
+        return View(self, group, t)
+
+
+class View:
+    """Blocks of a tensor, optionally one physical group only (relabelled to group 0) and/or
+    transposed: items (g, key_in, key_out, rows, cols, slot, off, ld, trans)."""
+
+    def __init__(self, tensor, group=None, t=False):
+        self.tensor, self.group, self.t = tensor, group, t
+
+    def items(self):
+        for (g, qi), (qo, r, c, off) in self.tensor.blocks.items():
+            if self.group is not None and g != self.group:
+                continue
+            gg = 0 if self.group is not None else g
+            if self.t:
+                yield gg, qo, qi, c, r, self.tensor.slot, off, r, 1
+            else:
+                yield gg, qi, qo, r, c, self.tensor.slot, off, r, 0
+
+
+def expr(ct, coef=1.0, group=None, t=False):
+    """Linear expression of a complex (re, im) or real (re, None) tensor pair."""
+    re, im = ct
+    out = [(complex(coef), re.view(group, t))]
+    if im is not None:
+        out.append((complex(coef) * 1j, im.view(group, t)))
+    return out
+
+
+def scale(e, c):
+    return [(coef * c, v) for coef, v in e]
+
+
+class Program:
+    """Stages of a grouped-GEMM program being compiled."""
+
+    def __init__(self, sizes):
+        self.sizes = dict(sizes)  # slot -> elements used
+        self.stages = []
+        self.closed = False  # set once a later program depends on this one's results
+
+    def alloc(self, slot, n):
+        off = self.sizes.get(slot, 0)
+        self.sizes[slot] = off + n
+        return off
+
+    def materialize(self, products, ngroups, slot=SCR, target=None, force_complex=False):
+        """Sum of products sum_p c_p op(A_p) op(B_p) into a new tensor pair (re, im).  products:
+        list of (exprA, exprB, rule) with rule(gA, gB) -> output group or None.  target: a
+        (re, im) pair of tensors with a fixed structure (sectors outside it are dropped)."""
+        if self.closed:
+            raise RuntimeError("materialisation into a closed program")
+        terms = {}  # (plane, gkey) -> list of term tuples
+        shape = {}  # gkey -> (qout, rows, cols)
+        dropped = 0
+        for ea, eb, rule in products:
+            for ca, va in ea:
+                for ca2, vb in eb:
+                    idx = {}
+                    for bi in vb.items():
+                        idx.setdefault(bi[1], []).append(bi)
+                    c = ca * ca2
+                    for (ga, ki, ko, ra, kk, sa, oa, la, ta) in va.items():
+                        for (gb, kbi, kbo, rb, cb, sb, ob, lb, tb) in idx.get(ko, ()):
+                            g = rule(ga, gb)
+                            if g is None:
+                                continue
+                            if kk != rb:
+                                raise ValueError("inner dimensions do not match")
+                            key = (g, ki)
+                            if target is not None and key not in target[0].blocks:
+                                dropped += 1
+                                continue
+                            sh = (kbo, ra, cb)
+                            if shape.setdefault(key, sh) != sh:
+                                raise ValueError("inconsistent output sector")
+                            term = (sa, oa, la, ta, sb, ob, lb, tb, kk)
+                            if c.real != 0.0:
+                                terms.setdefault((0, key), []).append(term + (c.real,))
+                            if c.imag != 0.0:
+                                terms.setdefault((1, key), []).append(term + (c.imag,))
+        cplx = force_complex or any(p == 1 for (p, _) in terms) or target is not None
+        if target is None:
+            blocks = {}
+            off = 0
+            keys = sorted(shape)
+            nel = sum(shape[k][1] * shape[k][2] for k in keys)
+            base_re = self.alloc(slot, nel)
+            base_im = self.alloc(slot, nel) if cplx else None
+            re_blocks, im_blocks = {}, {}
+            for k in keys:
+                qo, r, c = shape[k]
+                re_blocks[k] = (qo, r, c, base_re + off)
+                if cplx:
+                    im_blocks[k] = (qo, r, c, base_im + off)
+                off += r * c
+            re = Tensor(slot, re_blocks, ngroups)
+            im = Tensor(slot, im_blocks, ngroups) if cplx else None
+        else:
+            re, im = target
+        outs = []
+        for plane, t in ((0, re), (1, im)):
+            if t is None:
+                continue
+            for key, (qo, r, c, off) in sorted(t.blocks.items()):
+                outs.append((t.slot, off, r, r, c, 0, terms.get((plane, key), [])))
+        self.stages.append(outs)
+        return (re, im), dropped
+
+    def tables(self):
+        nouts = np.array([len(st) for st in self.stages], np.int32)
+        outs, terms, alphas = [], [], []
+        for st in self.stages:
+            for (cs, coff, cld, M, Nn, acc, tl) in st:
+                outs.append((cs, coff, max(cld, 1), M, Nn, acc, len(tl)))
+                for tm in tl:
+                    terms.append(tm[:9])
+                    alphas.append(tm[9])
+        return (nouts, np.array(outs, np.int64).reshape(-1, 7), np.array(terms, np.int64).reshape(-1, 9),
+                np.array(alphas, np.float64))
+
+
+def _same_group(ga, gb):
+    return 0 if ga == gb else None
+
+
+def _left_group(ga, gb):
+    return ga
+
+
+def _right_group(ga, gb):
+    return gb
+
+
+def _bm(ga, gb):
+    return 0
+
+
+class HeffProgram:
+    """Host compilation of ApplyHeff for a unit cell of N sites at momentum factor kfac and a
+    charge offset of X (unprojected solves: K != 0 or p != 0).  AL, AR, NL: lists (sites) of
+    MPS tensors; HLtot, HRtot: lists of BlockDiagMats; hnnz: (row, col, value) nonzeros of the
+    two-site h with E0 subtracted; xdims: per site [(qin, qout, rows, cols)] of X (XDims order).
+    Produces program A (up to the right-hand sides of the two solves), the solves' structures,
+    and program B (from their solutions to X_out), over six slots: operands, X, X_out, scratch,
+    solutions, right-hand sides."""
+
+    def __init__(self, AL, AR, NL, HLtot, HRtot, hnnz, d, xdims, kfac):
+        self.d = d
+        self.kfac = complex(kfac)
+        self.NS = len(AL)
+        ns = len(next(iter(xdims[0]))[0]) if xdims[0] else len(next(iter(AL[0][0])))
+        self.nsym = ns
+        Ns = self.NS
+        P = lambda x: (x + Ns) % Ns
+        prog_a = Program({})
+        # ---- operands in the OPS slot (real) ----
+        vals = []
+
+        def add_mps(A):
+            blocks = {}
+            for s, bm in enumerate(A):
+                for qi in sorted(bm):
+                    qo, M = bm[qi]
+                    off = prog_a.alloc(OPS, M.size)
+                    blocks[(s, tuple(qi))] = (tuple(qo), M.shape[0], M.shape[1], off)
+                    vals.append(np.asarray(M, np.float64).reshape(-1, order="F"))
+            return (Tensor(OPS, blocks, len(A)), None)
+
+        def add_bd(X):
+            blocks = {}
+            for q in sorted(X):
+                M = X[q]
+                off = prog_a.alloc(OPS, M.size)
+                blocks[(0, tuple(q))] = (tuple(q), M.shape[0], M.shape[1], off)
+                vals.append(np.asarray(M, np.float64).reshape(-1, order="F"))
+            return (Tensor(OPS, blocks, 1), None)
+
+        self.AL = [add_mps(a) for a in AL]
+        self.AR = [add_mps(a) for a in AR]
+        self.NL = [add_mps(a) for a in NL]
+        self.HL = [add_bd(x) for x in HLtot]
+        self.HR = [add_bd(x) for x in HRtot]
+        self.ops_vec = np.concatenate(vals) if vals else np.zeros(1)
+        # ---- X and the output (XS, OUT slots): per site [re | im] ----
+        self.xdims = xdims
+        self.X, self.Y, self.xoff = [], [], []
+        xo = 0
+        for dims in xdims:
+            n = sum(r * c for (_, _, r, c) in dims)
+            re, im, off = {}, {}, 0
+            for (qi, qo, r, c) in dims:
+                re[(0, tuple(qi))] = (tuple(qo), r, c, xo + off)
+                im[(0, tuple(qi))] = (tuple(qo), r, c, xo + n + off)
+                off += r * c
+            self.X.append((Tensor(XS, re, 1), Tensor(XS, im, 1)))
+            self.Y.append((Tensor(OUT, dict(re), 1), Tensor(OUT, dict(im), 1)))
+            self.xoff.append((xo, n))
+            xo += 2 * n
+        self.mtot = sum(n for (_, n) in self.xoff)
+        prog_a.sizes[XS] = prog_a.sizes[OUT] = xo
+        kf, ck = self.kfac, self.kfac.conjugate()
+        mat = prog_a.materialize
+        ALe = lambda n, **kw: expr(self.AL[n], **kw)
+        ARe = lambda n, **kw: expr(self.AR[n], **kw)
+        # ---- program A: B = NL X, ABR chain, HBL chain ----
+        Bin = [mat([(expr(self.NL[n]), expr(self.X[n]), _left_group)], d)[0] for n in range(Ns)]
+        ABR = [None] * Ns
+
+        def mixed_right(e_a, n):  # sum_s A_s AR[n]_s^T  (unity right, A an expression)
+            return [(e_a, ARe(n, t=True), _same_group)]
+
+        ABR[Ns - 1] = mat(mixed_right(expr(Bin[Ns - 1]), Ns - 1), 1, force_complex=True,
+                          slot=RHS if Ns == 1 else SCR)[0]
+        for n in range(Ns - 1, 0, -1):
+            alabr = mat([(ALe(n - 1), expr(ABR[n]), _left_group)], d)[0]
+            ABR[n - 1] = mat(mixed_right(expr(Bin[n - 1]) + expr(alabr), n - 1), 1, force_complex=True,
+                             slot=RHS if n - 1 == 0 else SCR)[0]
+        self.ABR = ABR
+
+        def op_group(t2, ii):  # ApplyOperator(t2, h)[ii] as an expression (group relabelled to 0)
+            e = []
+            for (r, c, v) in hnnz:
+                if r == ii:
+                    e += expr(t2, coef=v, group=c)
+            return e
+
+        def optm_left(a2, aa, prods):  # ApplyOpTMLeftGen(h, a2, aa) = sum_g aa_g^T (h a2)_g
+            for g in range(d * d):
+                oe = []
+                for t2, coef in a2:
+                    oe += scale(op_group(t2, g), coef)
+                if oe:
+                    prods.append((expr(aa, group=g, t=True), oe, _bm))
+
+        def mps2(ea, eb, materialize=mat):  # two-site product A_i B_j -> group i*d + j
+            return materialize([(ea, eb, lambda ga, gb: ga * d + gb)], d * d)[0]
+
+        HBL = []
+        for n in range(Ns):
+            prods = []
+            if n == 0:
+                hlb = mat([(expr(self.HL[Ns - 1]), expr(Bin[0]), _right_group)], d)[0]
+                prods.append((expr(self.AL[0], t=True), expr(hlb), _same_group))
+                a2 = [(mps2(ALe(Ns - 1), expr(Bin[0])), 1.0), (mps2(expr(Bin[Ns - 1]), ARe(0)), ck)]
+                aa = mps2(ALe(Ns - 1), ALe(0))
+            else:
+                w1 = mat([(expr(HBL[-1]), ARe(n), _right_group)], d)[0]
+                w2 = mat([(expr(self.HL[n - 1]), expr(Bin[n]), _right_group)], d)[0]
+                prods.append((expr(self.AL[n], t=True), expr(w1) + expr(w2), _same_group))
+                a2 = [(mps2(ALe(n - 1), expr(Bin[n])), 1.0), (mps2(expr(Bin[n - 1]), ARe(n)), 1.0)]
+                aa = mps2(ALe(n - 1), ALe(n))
+            optm_left(a2, aa, prods)
+            HBL.append(mat(prods, 1, force_complex=True, slot=RHS if n == Ns - 1 else SCR)[0])
+        self.HBL = HBL
+        # right-hand sides of the two solves: ABR[0] and HBL[N-1], both in RHS
+        self.rhs_r, self.rhs_l = ABR[0], HBL[Ns - 1]
+        # the solutions of (1 - kfac T_R^{AL,AR}) EBR = ABR[0] and (1 - ck T_L^{AR,AL}) EHBL =
+        # HBL[N-1] live in ES: EBR [re | im], EHBL [re | im], same structure as the rhs
+        nr, nl = self.rhs_r[0].nelem(), self.rhs_l[0].nelem()
+
+        def in_es(t, base):
+            n = t.nelem()
+            shift = lambda blocks, b0: {k: (v[0], v[1], v[2], b0 + (v[3] - min(x[3] for x in blocks.values())))
+                                        for k, v in blocks.items()}
+            return (Tensor(ES, shift(t.blocks, base), 1), Tensor(ES, shift(t.blocks, base + n), 1))
+
+        EBR, EHBL = in_es(self.rhs_r[0], 0), in_es(self.rhs_l[0], 2 * nr)
+        self.Bin, self.EBR, self.EHBL = Bin, EBR, EHBL
+        self.es_size = 2 * (nr + nl)
+        self.nr, self.nl = nr, nl
+        # ---- program B: per-bond sums of the solutions, the output terms, X_out = NL^T B_out ----
+        prog_a.closed = True
+        prog_b = Program(prog_a.sizes)
+        prog_b.sizes[ES] = self.es_size
+        matb = prog_b.materialize
+        ABRtot = [None] * Ns
+        ABRtot[0] = expr(EBR, coef=kf)
+        E = EBR
+        for n in range(Ns - 1, 0, -1):
+            w = matb([(ALe(n), expr(E), _left_group)], d)[0]
+            E = matb([(expr(w), ARe(n, t=True), _same_group)], 1, force_complex=True)[0]
+            ABRtot[n] = expr(ABR[n]) + expr(E, coef=kf)
+        self.bouts = []  # B_out[n] (scratch), kept for inspection
+        HBLtot = [None] * Ns
+        HBLtot[Ns - 1] = expr(EHBL, coef=ck)
+        E = EHBL
+        for n in range(Ns - 1):
+            w = matb([(expr(E), ARe(n), _right_group)], d)[0]
+            E = matb([(expr(self.AL[n], t=True), expr(w), _same_group)], 1, force_complex=True)[0]
+            HBLtot[n] = expr(HBL[n]) + expr(E, coef=ck)
+
+        def contract(prods, n, left2=None, right2=None, coef=1.0):
+            """+= coef sum_k AL[n-1][k]^T (h left2)[k d + s] + sum_k (h right2)[s d + k] AR[n+1][k]^T."""
+            for s in range(d):
+                for k in range(d):
+                    if left2 is not None:
+                        oe = op_group(left2, k * d + s)
+                        if oe:
+                            prods.append((expr(self.AL[P(n - 1)], group=k, t=True), scale(oe, coef),
+                                          lambda ga, gb, s=s: s))
+                    if right2 is not None:
+                        oe = op_group(right2, s * d + k)
+                        if oe:
+                            prods.append((oe, expr(self.AR[P(n + 1)], group=k, t=True), lambda ga, gb, s=s: s))
+
+        for n in range(Ns):
+            prods = [(expr(self.HL[P(n - 1)]), expr(Bin[n]), _right_group),
+                     (expr(Bin[n]), expr(self.HR[P(n + 1)]), _left_group)]
+            # h on B and the output site
+            contract(prods, n, mps2(ALe(P(n - 1)), expr(Bin[n]), matb), mps2(expr(Bin[n]), ARe(P(n + 1)), matb))
+            # B left of the output site
+            prods.append((HBLtot[P(n - 1)], ARe(n), _right_group))
+            contract(prods, n, mps2(expr(Bin[P(n - 1)]), ARe(n), matb), None, ck if n == 0 else 1.0)
+            # B right of the output site
+            alabr2 = matb([(ALe(P(n + 1)), ABRtot[P(n + 2)], _left_group)], d, force_complex=True)[0]
+            atmp = expr(Bin[P(n + 1)]) + expr(alabr2)
+            if n == Ns - 1:
+                atmp = scale(atmp, kf)
+            alabr = matb([(ALe(n), ABRtot[P(n + 1)], _left_group)], d, force_complex=True)[0]
+            prods.append((expr(self.HL[P(n - 1)]), expr(alabr), _right_group))
+            a2d = mps2(ALe(P(n - 1)), expr(alabr), matb)
+            a2e = matb([(ALe(n), atmp, lambda ga, gb: ga * d + gb)], d * d, force_complex=True)[0]
+            contract(prods, n, a2d, a2e)
+            bout = matb(prods, d, force_complex=True)[0]
+            self.bouts.append(bout)
+            # X_out[n] = sum_s NL[n]_s^T B_out[n]_s, into the output's X structure
+            matb([(expr(self.NL[n], t=True), expr(bout), _same_group)], 1, target=self.Y[n])
+
+        self.prog_a, self.prog_b = prog_a, prog_b
+        self.sizes = {k: max(prog_a.sizes.get(k, 0), prog_b.sizes.get(k, 0)) for k in range(6)}
+        self.sizes[ES] = self.es_size
+        self.structs = (AL, AR)
+
+    def rhs_planes(self):
+        """(offset of re, offset of im, length) of the two right-hand sides in RHS."""
+        lo = lambda t: min(v[3] for v in t.blocks.values())
+        return ((lo(self.rhs_r[0]), lo(self.rhs_r[1]), self.nr), (lo(self.rhs_l[0]), lo(self.rhs_l[1]), self.nl))
+
+
+class HeffGPU:
+    """ApplyHeff on the device: the two programs of HeffProgram around two imps_invert_e_fac
+    solves on mixed transfer-matrix plans."""
+
+    def __init__(self, ctx, AL, AR, NL, HLtot, HRtot, hnnz, d, xdims, kfac, tol=1e-14, maxit=0):
+        import torch
+        self.torch, self.ctx, self.d = torch, ctx, d
+        self.tol, self.maxit = tol, maxit
+        pr = HeffProgram(AL, AR, NL, HLtot, HRtot, hnnz, d, xdims, kfac)
+        self.pr = pr
+        self.kfac, self.NS, self.xoff, self.mtot = pr.kfac, pr.NS, pr.xoff, pr.mtot
+        self.sizes, self.nr, self.nl = pr.sizes, pr.nr, pr.nl
+        Ns, ns_ = pr.NS, pr.nsym
+        lay_mps = lambda A: B.Layout([(s, tuple(qi), tuple(bm[qi][0]), bm[qi][1].shape[0], bm[qi][1].shape[1])
+                                      for s, bm in enumerate(A) for qi in sorted(bm)], ns_)
+        lay_t = lambda t: B.Layout([(0, k[1], v[0], v[1], v[2]) for k, v in sorted(t.blocks.items())], ns_)
+        self.lay_AL = [lay_mps(a) for a in AL]
+        self.lay_AR = [lay_mps(a) for a in AR]
+        self.lay_r, self.lay_l = lay_t(pr.rhs_r[0]), lay_t(pr.rhs_l[0])
+        self.plan_r = B.plan_tm_mixed(ctx, self.lay_AL, self.lay_AR, 1, self.lay_r, self.lay_r)
+        self.plan_l = B.plan_tm_mixed(ctx, self.lay_AR, self.lay_AL, 0, self.lay_l, self.lay_l)
+        self.AL, self.AR = pr.AL, pr.AR
+        dev = lambda n: torch.zeros(max(int(n), 1), dtype=torch.float64, device="cuda")
+        self.buf = {k: dev(self.sizes.get(k, 0)) for k in range(6)}
+        self.buf[OPS].copy_(torch.from_numpy(pr.ops_vec))
+        self.plan_a = self._plan(pr.prog_a)
+        self.plan_b = self._plan(pr.prog_b)
+        A_ = lambda lst, k: self._op_view(lst[k])
+        for k in range(Ns):
+            self.plan_r.bind(2 + k, A_(self.AL, k))
+            self.plan_r.bind(2 + Ns + k, A_(self.AR, k))
+            self.plan_l.bind(2 + k, A_(self.AR, k))
+            self.plan_l.bind(2 + Ns + k, A_(self.AL, k))
+        self.stats = {"gmres_iters": 0}
+
+    def _op_view(self, ct):
+        t = ct[0]
+        offs = [v[3] for v in t.blocks.values()]
+        lo, n = min(offs), t.nelem()
+        return self.buf[OPS][lo:lo + n]
+
+    def _plan(self, prog):
+        nouts, outs, terms, alphas = prog.tables()
+        sizes = np.array([max(int(self.sizes.get(k, 0)), 1) for k in range(6)], np.int64)
+        h = C.c_void_p()
+        N.call("imps_plan_program", self.ctx.handle, 6, sizes.ctypes.data_as(N.P_i64), len(nouts),
+               nouts.ctypes.data_as(N.P_i32), outs.ctypes.data_as(N.P_i64), terms.ctypes.data_as(N.P_i64),
+               alphas.ctypes.data_as(N.P_dbl), C.byref(h))
+        plan = B.Plan(self.ctx, h, "program")
+        for k in range(6):
+            plan.bind(k, self.buf[k])
+        return plan
+
+    def x_to_planes(self, xs):
+        """Per-site complex vectors (XDims order) -> the XS slot."""
+        torch = self.torch
+        for (xo, n), x in zip(self.xoff, xs):
+            x = np.asarray(x, np.complex128)
+            self.buf[XS][xo:xo + n].copy_(torch.from_numpy(x.real.copy()))
+            self.buf[XS][xo + n:xo + 2 * n].copy_(torch.from_numpy(x.imag.copy()))
+
+    def y_from_planes(self):
+        out = []
+        for (xo, n) in self.xoff:
+            re = self.buf[OUT][xo:xo + n].cpu().numpy()
+            im = self.buf[OUT][xo + n:xo + 2 * n].cpu().numpy()
+            out.append(re + 1j * im)
+        return out
+
+    def apply(self):
+        """Y = H_eff X on the device buffers (XS -> OUT)."""
+        self.plan_a.run()
+        nr, nl = self.nr, self.nl
+        rhs, es = self.buf[RHS], self.buf[ES]
+        (off_r, off_ri, _), (off_l, off_li, _) = self.pr.rhs_planes()
+        it, _, conv_r = ops.InvertE_fac(self.plan_r, rhs[off_r:off_r + nr], rhs[off_ri:off_ri + nr], self.kfac,
+                                        es[0:nr], es[nr:2 * nr], self.tol, self.maxit)
+        self.stats["gmres_iters"] += it
+        it, _, conv_l = ops.InvertE_fac(self.plan_l, rhs[off_l:off_l + nl], rhs[off_li:off_li + nl],
+                                        self.kfac.conjugate(), es[2 * nr:2 * nr + nl], es[2 * nr + nl:2 * nr + 2 * nl],
+                                        self.tol, self.maxit)
+        self.stats["gmres_iters"] += it
+        self.plan_b.run()
+        return conv_r and conv_l

@@ -107,6 +107,15 @@ int imps_plan_tm(imps_ctx* ctx, int nsites, const imps_layout* const* A, int dir
  * Slots: 0 in, 1 out, 2.. A[k], 2+nsites.. B[k]. */
 int imps_plan_tm_mixed(imps_ctx* ctx, int nsites, const imps_layout* const* A, const imps_layout* const* B,
                        int dir, const imps_layout* in, const imps_layout* out, imps_plan** plan);
+/* A grouped-GEMM program from explicit tables (all slots external, bound with
+ * imps_plan_bind, executed in stage order by imps_plan_run).  stage_nouts[s] output blocks per
+ * stage; per output block 7 int64 (c_slot, c_off, c_ld, M, N, accumulate, nterms) followed in
+ * `terms` by its nterms terms of 9 int64 (a_slot, a_off, a_ld, a_trans, b_slot, b_off, b_ld,
+ * b_trans, k) with `alphas`: C (+)= sum alpha op(A) op(B).  Output blocks of one stage must not
+ * overlap.  Every region is bounds-checked against the slot sizes (IMPS_ERR_BAD_TABLE). */
+int imps_plan_program(imps_ctx* ctx, int nslots, const int64_t* slot_nelem, int nstages,
+                      const int32_t* stage_nouts, const int64_t* outs, const int64_t* terms,
+                      const double* alphas, imps_plan** plan);
 /* ReducedOp (MPSBlockUtilities.hpp:37-74).  Slots: 0 A, 1 out (derived layout 0). */
 int imps_plan_redop(imps_ctx* ctx, const imps_layout* A, int d, int nnz, const int32_t* hrow,
                     const int32_t* hcol, const double* hval, int dir, imps_plan** out);

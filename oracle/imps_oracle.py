@@ -591,6 +591,178 @@ def InvertE_proj_fac(Avec, Bvec, x, L, R, direction, fac, tol=1e-14, maxit=0, y0
     return bm_from_vec(y, sizes), flag
 
 
+# ----------------------------------------------------------------------------------------------
+# excitation ansatz: effective Hamiltonian on X (Excitations/Excitations_helpers.hpp:20-228)
+# ----------------------------------------------------------------------------------------------
+
+
+def mps_mul_bm(A, X):
+    """MPSBlockMat * BlockMat: [A_s X]."""
+    return [bm_mul(a, X) for a in A]
+
+
+def bm_mul_mps(X, A):
+    """BlockMat * MPSBlockMat: [X A_s]."""
+    return [bm_mul(X, a) for a in A]
+
+
+def mps_add(A, B):
+    """MPSBlockMat + MPSBlockMat (sector-wise, inserting missing sectors)."""
+    out = [{q: (qo, M.copy()) for q, (qo, M) in a.items()} for a in A]
+    for o, b in zip(out, B):
+        bm_iadd(o, b)
+    return out
+
+
+def mps_scale(A, a):
+    return [bm_scale(x, a) for x in A]
+
+
+def bm_add(X, Y):
+    return bm_iadd({q: (qo, M.copy()) for q, (qo, M) in X.items()}, Y)
+
+
+def ApplyOpTMLeftGen(hnnz, A, B):
+    """TMBlockFunctions.hpp:825-830: ApplyTMmixedLeft(ApplyOperator(A, O), B)."""
+    return ApplyTMmixedLeft(ApplyOperator(A, hnnz), B)
+
+
+def HeffConstants(AL, AR, L, R, hnnz, tol=1e-14, rng=None):
+    """Excitations_helpers.hpp:258-331 (h with E0 already subtracted): the environments HLtot[n]
+    (left of the bond right of site n) and HRtot[n] (right of the bond left of site n)."""
+    N = len(AL)
+    P = lambda x: (x + N) % N
+    HL = [ApplyOpTMLeftDiag(hnnz, mps_mul_mps(AL[N - 1], AL[0]))]
+    for n in range(1, N):
+        HL.append(bd_add(ApplyOpTMLeftDiag(hnnz, mps_mul_mps(AL[n - 1], AL[n])), ApplyTMLeft(AL[n], HL[-1])))
+    HR = [None] * N
+    HR[N - 1] = ApplyOpTMRightDiag(hnnz, mps_mul_mps(AR[N - 1], AR[0]))
+    for n in range(N - 2, -1, -1):
+        HR[n] = bd_add(ApplyOpTMRightDiag(hnnz, mps_mul_mps(AR[n], AR[n + 1])), ApplyTMRight(AR[n], HR[n + 1]))
+    HLtot, HRtot = [None] * N, [None] * N
+    eyeR = bd_eye({q: M.shape[1] for q, M in R.items()})
+    EHL = [None] * N
+    EHL[N - 1], _ = InvertE_proj(AL, HL[N - 1], eyeR, R, "l", tol, rng=rng)
+    HLtot[N - 1] = EHL[N - 1]
+    for n in range(N - 1):
+        EHL[n] = ApplyTMLeft(AL[n], EHL[P(n - 1)])
+        HLtot[n] = bd_add(HL[n], EHL[n])
+    eyeL = bd_eye({q: M.shape[1] for q, M in L.items()})
+    EHR = [None] * N
+    EHR[0], _ = InvertE_proj(AR, HR[0], L, eyeL, "r", tol, rng=rng)
+    HRtot[0] = EHR[0]
+    for n in range(N - 1, 0, -1):
+        EHR[n] = ApplyTMRight(AR[n], EHR[P(n + 1)])
+        HRtot[n] = bd_add(EHR[n], HR[n])
+    return HLtot, HRtot
+
+
+def XDims(NL, AR, K):
+    """Excitations_helpers.hpp:641-678: sectors of X_n: NL[n] right keys q with AR[n+1] left keys
+    q + K (both non-empty)."""
+    N = len(NL)
+    out = []
+    for n in range(N):
+        ml = {}
+        for bm in NL[n]:
+            for qi, (qo, M) in bm.items():
+                ml.setdefault(qo, M.shape[1])
+        mr = {}
+        for bm in AR[(n + 1) % N]:
+            for qi, (qo, M) in bm.items():
+                mr.setdefault(qi, M.shape[0])
+        dims = []
+        for q in sorted(ml):
+            qk = kadd(q, K)
+            if qk in mr and ml[q] > 0 and mr[qk] > 0:
+                dims.append((q, qk, ml[q], mr[qk]))
+        out.append(dims)
+    return out
+
+
+def ApplyHeff(Xin, kfac, AL, AR, NL, hnnz, d, HLtot, HRtot, LM=None, RM=None, tol=1e-14, rng=None):
+    """Effective Hamiltonian of the excitation ansatz applied to X (Excitations_helpers.hpp:20-211):
+    B_n = NL_n X_n; the terms with B right of, on top of and left of the output site; the
+    infinite sums closed by the factored environment solves EBR (right, fac = kfac) and EHBL
+    (left, fac = conj(kfac)), projected when LM and RM are given.  Returns Xout (list of
+    BlockMats; the caller keeps the sectors of its X structure)."""
+    N = len(Xin)
+    ck = np.conj(kfac)
+    P = lambda x: (x + N) % N
+    proj = LM is not None and RM is not None
+    Bin = [mps_mul_bm(NL[n], Xin[n]) for n in range(N)]
+    # B overlapping AR to the right within the unit cell (:64-72)
+    ABR = [None] * N
+    ABR[N - 1] = ApplyTMmixedRight(Bin[N - 1], AR[N - 1])
+    for n in range(N - 1, 0, -1):
+        ABR[n - 1] = ApplyTMmixedRight(mps_add(Bin[n - 1], mps_mul_bm(AL[n - 1], ABR[n])), AR[n - 1])
+    # all unit cells to the right (:75-89), then per bond (:91-99): ABRtot[0] = kfac E,
+    # ABRtot[n] = ABR[n] + kfac T_n...T_{N-1} E
+    if proj:
+        E, _ = InvertE_proj_fac(AL, AR, ABR[0], LM, RM, "r", kfac, tol, rng=rng)
+    else:
+        E, _ = InvertE_fac(AL, AR, ABR[0], "r", kfac, tol, rng=rng)
+    ABRtot = [None] * N
+    ABRtot[0] = bm_scale(E, kfac)
+    for n in range(N - 1, 0, -1):
+        E = ApplyTMmixedRightX(AL[n], AR[n], E)
+        ABRtot[n] = bm_add(ABR[n], bm_scale(E, kfac))
+    # H left of or on B within the unit cell, one step into the cell to the left (:104-115)
+    HBL = [bm_add(ApplyTMmixedLeft(bd_mul_mps(HLtot[N - 1], Bin[0]), AL[0]),
+                  ApplyOpTMLeftGen(hnnz, mps_add(mps_mul_mps(AL[N - 1], Bin[0]),
+                                                 mps_scale(mps_mul_mps(Bin[N - 1], AR[0]), ck)),
+                                   mps_mul_mps(AL[N - 1], AL[0])))]
+    for n in range(1, N):
+        HBL.append(bm_add(ApplyTMmixedLeft(mps_add(bm_mul_mps(HBL[-1], AR[n]), bd_mul_mps(HLtot[n - 1], Bin[n])),
+                                           AL[n]),
+                          ApplyOpTMLeftGen(hnnz, mps_add(mps_mul_mps(AL[n - 1], Bin[n]),
+                                                         mps_mul_mps(Bin[n - 1], AR[n])),
+                                           mps_mul_mps(AL[n - 1], AL[n]))))
+    # all unit cells to the left (:118-132), then per bond (:134-140): HBLtot[n] = HBL[n] +
+    # conj(kfac) T_n...T_0 E for n < N-1, HBLtot[N-1] = conj(kfac) E
+    if proj:
+        E, _ = InvertE_proj_fac(AR, AL, HBL[-1], bm_t(LM), bm_t(RM), "l", ck, tol, rng=rng)
+    else:
+        E, _ = InvertE_fac(AR, AL, HBL[-1], "l", ck, tol, rng=rng)
+    HBLtot = [None] * N
+    HBLtot[N - 1] = bm_scale(E, ck)
+    for n in range(N - 1):
+        E = ApplyTMmixedLeftX(AR[n], AL[n], E)
+        HBLtot[n] = bm_add(HBL[n], bm_scale(E, ck))
+
+    Bout = [mps_add(bd_mul_mps(HLtot[P(n - 1)], Bin[n]), mps_mul_bd(Bin[n], HRtot[P(n + 1)])) for n in range(N)]
+
+    def contract(n, left2=None, right2=None, scale=1.0):
+        """Bout[n][s] += scale * sum_k AL[n-1][k]^T left2[k*d+s] + sum_k right2[s*d+k] AR[n+1][k]^T."""
+        for s_ in range(d):
+            for k in range(d):
+                if left2 is not None:
+                    bm_iadd(Bout[n][s_], bm_scale(bm_mul(bm_t(AL[P(n - 1)][k]), left2[k * d + s_]), scale))
+                if right2 is not None:
+                    bm_iadd(Bout[n][s_], bm_mul(right2[s_ * d + k], bm_t(AR[P(n + 1)][k])))
+
+    # h acting on B and the output site (:146-167)
+    for n in range(N):
+        contract(n, ApplyOperator(mps_mul_mps(AL[P(n - 1)], Bin[n]), hnnz),
+                 ApplyOperator(mps_mul_mps(Bin[n], AR[P(n + 1)]), hnnz))
+    # B left of the output site (:170-198)
+    for n in range(N):
+        for s_ in range(d):
+            bm_iadd(Bout[n][s_], bm_mul(HBLtot[P(n - 1)], AR[n][s_]))
+        contract(n, ApplyOperator(mps_mul_mps(Bin[P(n - 1)], AR[n]), hnnz), None, ck if n == 0 else 1.0)
+    # B right of the output site (:203-224)
+    for n in range(N):
+        Atmp = mps_add(Bin[P(n + 1)], mps_mul_bm(AL[P(n + 1)], ABRtot[P(n + 2)]))
+        if n == N - 1:
+            Atmp = mps_scale(Atmp, kfac)
+        ALABR = mps_mul_bm(AL[n], ABRtot[P(n + 1)])
+        Bout[n] = mps_add(Bout[n], bd_mul_mps(HLtot[P(n - 1)], ALABR))
+        contract(n, ApplyOperator(mps_mul_mps(AL[P(n - 1)], ALABR), hnnz),
+                 ApplyOperator(mps_mul_mps(AL[n], Atmp), hnnz))
+    # back to X (:227)
+    return [ApplyTMmixedLeft(Bout[n], NL[n]) for n in range(N)]
+
+
 def ApplyOperator(A, hnnz):
     """MPSBlockUtilities.hpp:17-34: out[ii] += h * in[jj]."""
     out = [dict() for _ in A]

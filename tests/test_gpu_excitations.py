@@ -94,3 +94,23 @@ def test_invert_e_fac_matches_oracle(cuda_ctx, state, direction, K, p):
 def test_invert_e_proj_fac_matches_oracle(cuda_ctx, state, direction):
     yg, yo = _solve_pair(cuda_ctx, state, direction, (0,), 0.9 * np.exp(0.4j), proj=True)
     assert np.linalg.norm(yg - yo) / np.linalg.norm(yo) < 1e-9
+
+
+@pytest.mark.parametrize("K,p", [((2,), 0.6), ((-2,), 2.4)])
+def test_heff_apply_matches_oracle(cuda_ctx, K, p):
+    """ApplyHeff (Excitations_helpers.hpp:20-228) compiled into grouped-GEMM programs around the
+    two factored solves, against the oracle's restatement on the same state and X."""
+    from imps_cpp_tools_gb300.excitations import HeffGPU
+    from tests.test_oracle_excitations import excitation_setup, rand_x
+    e = excitation_setup(K)
+    kfac = np.exp(1j * p)
+    H = HeffGPU(cuda_ctx, e["AL"], e["AR"], e["NL"], e["HLtot"], e["HRtot"], e["h"], e["d"], e["xdims"], kfac,
+                tol=1e-13)
+    X = rand_x(e["xdims"], np.random.default_rng(12))
+    H.x_to_planes([O.bm_vec(x) for x in X])
+    assert H.apply()
+    got = H.y_from_planes()
+    ref = O.ApplyHeff(X, kfac, e["AL"], e["AR"], e["NL"], e["h"], e["d"], e["HLtot"], e["HRtot"], tol=1e-13)
+    for n, dims in enumerate(e["xdims"]):
+        refv = np.concatenate([ref[n][qi][1].reshape(-1, order="F") for (qi, _, _, _) in dims])
+        assert np.linalg.norm(got[n] - refv) / np.linalg.norm(refv) < 1e-9, n

@@ -65,3 +65,105 @@ def test_invert_e_fac_solves_its_equation(state):
     assert flag >= 0
     res = O.bm_vec(y) - fac * O.bm_vec(O.ApplyTMmixedRightUC(AL, AR, y)) - O.bm_vec(x)
     assert np.linalg.norm(res) < 1e-11 * np.linalg.norm(O.bm_vec(x))
+
+
+def excitation_setup(K, seed=3):
+    """A random left/right-canonical two-site XXZ state (the oracle's randMPS_LR), h shifted by
+    its energy density E0, its environments (HeffConstants) and null spaces, and the X sector
+    structure for charge K."""
+    from imps_cpp_tools_gb300 import models
+    st = T.random_state("xxz", B0, seed=seed, J=1.0, Delta=-1.0)
+    AL, AR, C, d = st["AL"], st["AR"], st["C"], st["d"]
+    C0 = C[-1]  # bond 0
+    R = O.bd_mul(C0, O.bd_t(C0))
+    L = O.bd_mul(O.bd_t(C0), C0)
+    _, _, h = models.build_model("xxz", J=1.0, Delta=-1.0)
+    hn = O.sparse_nnz(h)
+    HL0 = O.ApplyOpTMLeftDiag(hn, O.mps_mul_mps(AL[1], AL[0]))
+    HL1 = O.bd_add(O.ApplyOpTMLeftDiag(hn, O.mps_mul_mps(AL[0], AL[1])), O.ApplyTMLeft(AL[1], HL0))
+    E0 = O.bd_trace(O.bd_mul(HL1, R)) / 2
+    hs = O.sparse_nnz(h - E0 * np.eye(h.shape[0]))
+    HLtot, HRtot = O.HeffConstants(AL, AR, L, R, hs, tol=1e-13)
+    NL = [O.Nullspace(AL[n], "l") for n in range(2)]
+    xd = O.XDims(NL, AR, K)
+    return dict(AL=AL, AR=AR, NL=NL, d=d, h=hs, HLtot=HLtot, HRtot=HRtot, xdims=xd, E0=E0)
+
+
+def rand_x(xdims, rng):
+    return [{qi: (qo, rng.standard_normal((ml, mr)) + 1j * rng.standard_normal((ml, mr)))
+             for (qi, qo, ml, mr) in dims} for dims in xdims]
+
+
+def x_inner(X, Y, xdims):
+    return sum(np.vdot(X[n][qi][1], Y[n][qi][1]) for n, dims in enumerate(xdims) for (qi, _, _, _) in dims)
+
+
+@pytest.mark.parametrize("K,p", [((2,), 0.6), ((-2,), 2.4)])
+def test_heff_is_hermitian(K, p):
+    """The excitation effective Hamiltonian (with E0 subtracted and exact environments) is
+    Hermitian in the X inner product: <Y, H X> = <H Y, X>."""
+    e = excitation_setup(K)
+    rng = np.random.default_rng(11)
+    X, Y = rand_x(e["xdims"], rng), rand_x(e["xdims"], rng)
+    kfac = np.exp(1j * p)
+    args = (kfac, e["AL"], e["AR"], e["NL"], e["h"], e["d"], e["HLtot"], e["HRtot"])
+    HX = O.ApplyHeff(X, *args, tol=1e-13)
+    HY = O.ApplyHeff(Y, *args, tol=1e-13)
+    a, b = x_inner(Y, HX, e["xdims"]), x_inner(HY, X, e["xdims"])
+    assert abs(a - b) < 1e-10 * abs(a), (a, b)
+
+
+def run_tables(stages, bufs):
+    """Execute grouped-GEMM program stages with numpy (the device engine's semantics)."""
+    def mat(slot, off, ld, rows, cols):
+        idx = off + np.arange(rows)[:, None] + np.arange(cols)[None, :] * ld
+        return bufs[slot][idx]
+    for stage in stages:
+        res = []
+        for (cs, coff, cld, M, Nn, acc, tl) in stage:
+            Cm = np.zeros((M, Nn))
+            for (sa, oa, la, ta, sb, ob, lb, tb, k, alpha) in tl:
+                A = mat(sa, oa, la, k, M).T if ta else mat(sa, oa, la, M, k)
+                Bm = mat(sb, ob, lb, Nn, k).T if tb else mat(sb, ob, lb, k, Nn)
+                Cm += alpha * (A @ Bm)
+            res.append((cs, coff, cld, M, Nn, acc, Cm))
+        for (cs, coff, cld, M, Nn, acc, Cm) in res:
+            if M and Nn:
+                idx = coff + np.arange(M)[:, None] + np.arange(Nn)[None, :] * cld
+                bufs[cs][idx] = bufs[cs][idx] + Cm if acc else Cm
+
+
+@pytest.mark.parametrize("K,p", [((2,), 0.6), ((-2,), 2.4)])
+def test_heff_program_tables_match_oracle(K, p):
+    """The host compilation of ApplyHeff (imps_cpp_tools_gb300.excitations.HeffProgram), executed
+    table by table with numpy and the oracle's InvertE_fac for the two solves, reproduces the
+    oracle's ApplyHeff: a check of the sector matching and term expansion without a GPU."""
+    from imps_cpp_tools_gb300 import excitations as EX
+    e = excitation_setup(K)
+    kfac = np.exp(1j * p)
+    pr = EX.HeffProgram(e["AL"], e["AR"], e["NL"], e["HLtot"], e["HRtot"], e["h"], e["d"], e["xdims"], kfac)
+    bufs = {k: np.zeros(max(int(pr.sizes.get(k, 0)), 1)) for k in range(6)}
+    bufs[EX.OPS][:pr.ops_vec.size] = pr.ops_vec
+    X = rand_x(e["xdims"], np.random.default_rng(12))
+    for (xo, n), x in zip(pr.xoff, X):
+        v = O.bm_vec(x)
+        bufs[EX.XS][xo:xo + n], bufs[EX.XS][xo + n:xo + 2 * n] = v.real, v.imag
+    run_tables(pr.prog_a.stages, bufs)
+
+    def to_bm(t_re, t_im, slot):
+        return {k[1]: (qo, (bufs[slot][o1:o1 + r * c] + 1j * bufs[slot][t_im.blocks[k][3]:t_im.blocks[k][3] + r * c])
+                       .reshape(c, r).T) for k, (qo, r, c, o1) in t_re.blocks.items()}
+
+    xr, xl = to_bm(*pr.rhs_r, EX.RHS), to_bm(*pr.rhs_l, EX.RHS)
+    yr, _ = O.InvertE_fac(e["AL"], e["AR"], xr, "r", kfac, tol=1e-13)
+    yl, _ = O.InvertE_fac(e["AR"], e["AL"], xl, "l", np.conj(kfac), tol=1e-13)
+    vr, vl = O.bm_vec(yr), O.bm_vec(yl)
+    nr, nl = pr.nr, pr.nl
+    bufs[EX.ES][:nr], bufs[EX.ES][nr:2 * nr] = vr.real, vr.imag
+    bufs[EX.ES][2 * nr:2 * nr + nl], bufs[EX.ES][2 * nr + nl:2 * nr + 2 * nl] = vl.real, vl.imag
+    run_tables(pr.prog_b.stages, bufs)
+    ref = O.ApplyHeff(X, kfac, e["AL"], e["AR"], e["NL"], e["h"], e["d"], e["HLtot"], e["HRtot"], tol=1e-13)
+    for n, ((xo, nn), dims) in enumerate(zip(pr.xoff, e["xdims"])):
+        got = bufs[EX.OUT][xo:xo + nn] + 1j * bufs[EX.OUT][xo + nn:xo + 2 * nn]
+        refv = np.concatenate([ref[n][qi][1].reshape(-1, order="F") for (qi, _, _, _) in dims])
+        assert np.linalg.norm(got - refv) / np.linalg.norm(refv) < 1e-9, n
