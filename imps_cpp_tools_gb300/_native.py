@@ -14,6 +14,8 @@ from . import build as _build
 c_int, c_i64, c_dbl, c_vp = C.c_int, C.c_int64, C.c_double, C.c_void_p
 P_i32 = C.POINTER(C.c_int32)
 P_i64 = C.POINTER(C.c_int64)
+# imps_apply_fn: int (*)(void* user, const double* in, double* out)
+APPLY_FN = C.CFUNCTYPE(C.c_int, C.c_void_p, C.c_void_p, C.c_void_p)
 P_dbl = C.POINTER(C.c_double)
 P_int = C.POINTER(C.c_int)
 
@@ -77,6 +79,8 @@ _PROTOS = {
     "imps_invert_e_proj": (c_int, [c_vp, c_vp, c_vp, c_vp, c_int, c_vp, c_int, c_dbl, c_int, c_int,
                                    P_int, P_dbl]),
     "imps_tm_dominant": (c_int, [c_vp, c_vp, c_vp, c_int, c_dbl, c_int, P_dbl, P_int]),
+    "imps_eigs_rs_op": (c_int, [c_vp, c_i64, APPLY_FN, c_vp, c_vp, c_int, c_int, c_dbl, c_int, c_int, P_dbl,
+                                c_vp, P_int]),
     "imps_plan_program": (c_int, [c_vp, c_int, P_i64, c_int, P_i32, P_i64, P_i64, P_dbl, C.POINTER(c_vp)]),
     "imps_plan_tm_mixed": (c_int, [c_vp, c_int, C.POINTER(c_vp), C.POINTER(c_vp), c_int, c_vp, c_vp,
                                    C.POINTER(c_vp)]),

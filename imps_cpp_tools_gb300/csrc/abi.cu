@@ -752,23 +752,27 @@ int imps_dot(imps_ctx* c, const double* x, const double* y, int64_t n, double* r
   return IMPS_OK;
 }
 
-// ---- Lanczos: eigs_rs(nev=1, "SA") ----
-int imps_eigs_rs(imps_plan* p, double* x, int mem, double tol, int ncv, int maxit, double* eval,
-                 int* n_applies) {
-  if (!p || !x || (p->P.kind != PLAN_HAC && p->P.kind != PLAN_HC)) return IMPS_ERR_BAD_ARG;
-  imps_ctx* c = p->ctx;
+// ---- Lanczos: eigs_rs("SA") for the nev lowest eigenpairs of a symmetric operator ----
+using DevApply = std::function<int(const double* in, double* out)>;
+
+// p (optional): the plan whose precision the ladder may switch; op applies the operator on
+// device vectors; x: start vector (mem), on return the normalised lowest Ritz vector;
+// evecs (device, n x nev, optional): the nev Ritz vectors; evals (host, nev).
+static int eigs_impl(imps_ctx* c, imps_plan* p, int64_t n, const DevApply& op, double* x, int mem, int nev,
+                     double tol, int ncv, int maxit, double* evals, double* evecs, int* n_applies) {
   cudaStream_t st = c->stream;
-  const int64_t n = p->P.slots[p->P.n_in].nelem;
-  if (n < 2) return IMPS_ERR_BAD_ARG;
-  int m = ncv > 0 ? ncv : 20;  // eigs.cpp:4, 390: max(std_ncv, 2*nev) capped at N
+  if (n < 2 || nev < 1 || nev > 16 || nev >= n) return IMPS_ERR_BAD_ARG;
+  int m = ncv > 0 ? ncv : std::max(20, 2 * nev);  // eigs.cpp:4, 390: max(std_ncv, 2*nev) capped at N
   if (m > n) m = (int)n;
   if (m > kMaxCols - 2) m = kMaxCols - 2;
+  if (m < nev + 3) m = (int)std::min<int64_t>(nev + 3, n);
   if (m < 2) m = 2;
   // maxit counts restart cycles, as ARPACK's IPARAM(3) (eigs.cpp:384, 399)
   if (maxit <= 0) maxit = (int)std::min<int64_t>(n, 100000);
   const int64_t max_applies = (int64_t)maxit * m;
   const int ld = m + 1;
-  const int kk = std::max(1, std::min(m / 2, m - 3));  // Ritz vectors kept at a thick restart
+  const int kk = std::max(nev, std::max(1, std::min(m / 2, m - 3)));  // Ritz vectors kept at a thick restart
+  if (kk >= m) return IMPS_ERR_BAD_ARG;
   RC(arena_reserve(c, round256(n * 8) * (m + 4 + kk) + round256((size_t)ld * ld * 8) +
                           round256((size_t)m * kk * 8) + 4096));
   Bump bp{c->arena};
@@ -788,7 +792,7 @@ int imps_eigs_rs(imps_plan* p, double* x, int mem, double tol, int ncv, int maxi
   // (alpha_j = h_j, beta_j = |w_j|), exact up to rounding because the basis is kept
   // orthonormal and a thick restart re-tridiagonalises the kept block (arrow_tridiag).
   std::vector<double> H((size_t)ld * ld, 0.0);
-  std::vector<double> ta(m + 1, 0.0), tb(m + 1, 0.0), z(m, 0.0);
+  std::vector<double> ta(m + 1, 0.0), tb(m + 1, 0.0), z(m, 0.0), thv(nev, 0.0), Zv((size_t)m * nev, 0.0);
   std::vector<double> th(kk), Z((size_t)m * kk), sv(kk), Q((size_t)kk * kk), qa(kk), qb(kk),
       Wr((size_t)m * kk);
   int applies = 0;
@@ -834,12 +838,22 @@ int imps_eigs_rs(imps_plan* p, double* x, int mem, double tol, int ncv, int maxi
       }
       jpulled = j + 1;
       const int k = j + 1;
-      tri_lowest_pairs(k, ta.data(), tb.data(), 1, &theta, z.data());
+      const int nw = std::min(nev, k);
+      tri_lowest_pairs(k, ta.data(), tb.data(), nw, thv.data(), Zv.data());
+      theta = thv[0];
       if (!std::isfinite(theta)) return IMPS_ERR_NAN;
-      const double res = std::fabs(tb[k - 1] * z[k - 1]);
+      std::copy(Zv.begin(), Zv.begin() + k, z.begin());
+      // every wanted Ritz pair must pass the test (ARPACK counts nconv >= nev)
+      double res = 0.0;
+      bool all = nw == nev;
+      for (int i = 0; i < nw; ++i) {
+        const double ri = std::fabs(tb[k - 1] * Zv[(size_t)(k - 1) + (size_t)i * k]);
+        res = std::max(res, i == 0 ? ri : 0.0);
+        all = all && ri <= tol_eff * std::max(std::fabs(thv[i]), eps23);
+      }
       last_res = res;
       kfinal = k;
-      if (res <= tol_eff * std::max(std::fabs(theta), eps23) || pin_flags[0]) {
+      if (all || pin_flags[0]) {
         status = IMPS_OK;
         return 1;
       }
@@ -854,7 +868,7 @@ int imps_eigs_rs(imps_plan* p, double* x, int mem, double tol, int ncv, int maxi
     };
     while (!done) {
       for (int j = jstart; j < m; ++j) {
-        if (!(pre_applied && j == jstart)) RC(apply_dev(p, V + (size_t)j * n, w));
+        if (!(pre_applied && j == jstart)) RC(op(V + (size_t)j * n, w));
         pre_applied = false;
         ++applies;
         ++used;
@@ -872,7 +886,7 @@ int imps_eigs_rs(imps_plan* p, double* x, int mem, double tol, int ncv, int maxi
         // restart point: the first apply of the next cycle (on the residual direction v_m)
         // runs on the device while the host evaluates the check and computes the restart
         if (j == m - 1) {
-          RC(apply_dev(p, V + (size_t)m * n, w));
+          RC(op(V + (size_t)m * n, w));
           pre_applied = true;
         }
         const int r = evaluate(j);
@@ -910,10 +924,16 @@ int imps_eigs_rs(imps_plan* p, double* x, int mem, double tol, int ncv, int maxi
     }
     // the staging buffer is reused below: wait for the rotation upload to be consumed
     CK(cudaStreamSynchronize(st));
-    // Ritz vector x = V[:, 0..k-1] z
+    // Ritz vectors: x = V[:, 0..k-1] z (lowest); all nev into evecs
     std::copy(z.begin(), z.begin() + kfinal, c->hpin);
     CK(cudaMemcpyAsync(tmp, c->hpin, kfinal * 8, cudaMemcpyHostToDevice, st));
     RC(kr_gemv(V, n, kfinal, tmp, xr, n, st));
+    if (evecs && kfinal >= nev) {
+      CK(cudaStreamSynchronize(st));
+      std::copy(Zv.begin(), Zv.begin() + (size_t)kfinal * nev, c->hpin);
+      CK(cudaMemcpyAsync(Wrot, c->hpin, (size_t)kfinal * nev * 8, cudaMemcpyHostToDevice, st));
+      RC(kr_basis_rotate(V, n, kfinal, Wrot, nev, evecs, n, n, st));
+    }
     CK(cudaStreamSynchronize(st));
     return status;
   };
@@ -923,16 +943,16 @@ int imps_eigs_rs(imps_plan* p, double* x, int mem, double tol, int ncv, int maxi
   // that floor runs on the tensor cores (FP64 applies finish only if the mixed run stalls); a
   // tolerance below it runs in FP64 from the start — a mixed run followed by an FP64 run that
   // restarts from its Ritz vector costs more than the FP64 run alone.
-  const int prec_saved = p->prec;
-  const bool mixed = p->prec == IMPS_PREC_BF16X6 && tol >= kMixedEigTol;
-  p->prec = mixed ? IMPS_PREC_BF16X6 : IMPS_PREC_FP64;
+  const int prec_saved = p ? p->prec : IMPS_PREC_FP64;
+  const bool mixed = p && p->prec == IMPS_PREC_BF16X6 && tol >= kMixedEigTol;
+  if (p) p->prec = mixed ? IMPS_PREC_BF16X6 : IMPS_PREC_FP64;
   int status = lanczos(tol, max_applies, mixed);
   const int applies_mixed = mixed ? applies : 0;
   if (status >= 0 && mixed && status != IMPS_OK && applies < max_applies) {
     p->prec = IMPS_PREC_FP64;
     status = lanczos(tol, std::max<int64_t>(max_applies - applies, m), false);
   }
-  p->prec = prec_saved;
+  if (p) p->prec = prec_saved;
   if (status < 0) return status;
   // normalise
   RC(kr_multidot(c->ws, xr, n, 1, xr, n, tmp, 0, nrm, st));
@@ -943,13 +963,35 @@ int imps_eigs_rs(imps_plan* p, double* x, int mem, double tol, int ncv, int maxi
     RC(kr_scale_inv(xr, nrm, x, n, bflag, st));
   }
   CK(cudaStreamSynchronize(st));
-  if (eval) *eval = theta;
+  if (evals) {
+    evals[0] = theta;
+    for (int i = 1; i < nev; ++i) evals[i] = thv[i];
+  }
   if (n_applies) *n_applies = applies;
   if (debug_on())
     fprintf(stderr,
             "[imps eigs_rs] n=%lld prec=%d applies=%d (split-bf16 %d) theta=%.15g res=%.3e tol=%.1e status=%d\n",
-            (long long)n, p->prec, applies, applies_mixed, theta, last_res, tol, status);
+            (long long)n, prec_saved, applies, applies_mixed, theta, last_res, tol, status);
   return status;
+}
+
+int imps_eigs_rs(imps_plan* p, double* x, int mem, double tol, int ncv, int maxit, double* eval,
+                 int* n_applies) {
+  if (!p || !x || (p->P.kind != PLAN_HAC && p->P.kind != PLAN_HC)) return IMPS_ERR_BAD_ARG;
+  const int64_t n = p->P.slots[p->P.n_in].nelem;
+  DevApply op = [p](const double* in, double* out) { return apply_dev(p, in, out); };
+  return eigs_impl(p->ctx, p, n, op, x, mem, 1, tol, ncv, maxit, eval, nullptr, n_applies);
+}
+
+int imps_eigs_rs_op(imps_ctx* c, int64_t n, imps_apply_fn fn, void* user, double* x, int mem, int nev, double tol,
+                    int ncv, int maxit, double* evals, double* evecs, int* n_applies) {
+  if (!c || !fn || !x || !evals) return IMPS_ERR_BAD_ARG;
+  if (c->device < 0) return IMPS_ERR_NO_DEVICE;
+  DevApply op = [fn, user](const double* in, double* out) {
+    const int rc = fn(user, in, out);
+    return rc < 0 ? rc : IMPS_OK;
+  };
+  return eigs_impl(c, nullptr, n, op, x, mem, nev, tol, ncv, maxit, evals, evecs, n_applies);
 }
 
 // ---- device GMRES (generic operator) ----

@@ -469,3 +469,32 @@ class HeffGPU:
         self.stats["gmres_iters"] += it
         self.plan_b.run()
         return conv_r and conv_l
+
+
+class ExcitationsGPU:
+    """Excitation energies of the ansatz (Excitations_main.cpp:255-297): for each momentum, the
+    nev lowest eigenvalues of H_eff (eigs_n "SR" in the reference; H_eff is Hermitian, so here
+    the device Lanczos on its real form over the [re | im] planes of X)."""
+
+    def __init__(self, ctx, AL, AR, NL, HLtot, HRtot, hnnz, d, xdims, tol=1e-14):
+        self.ctx, self.args, self.tol = ctx, (AL, AR, NL, HLtot, HRtot, hnnz, d, xdims), tol
+        self.applies = 0
+
+    def energies(self, kfac, nev=4, eig_tol=1e-10, ncv=0, seed=1):
+        import torch
+        H = HeffGPU(self.ctx, *self.args, kfac, tol=self.tol)
+        n = 2 * H.mtot
+        xs, out = H.buf[XS], H.buf[OUT]
+
+        def apply(pin, pout):
+            N.call("imps_axpby", self.ctx.handle, 1.0, C.c_void_p(pin), 0.0, C.c_void_p(xs.data_ptr()), n)
+            if not H.apply():
+                raise RuntimeError("environment solve did not converge")
+            N.call("imps_axpby", self.ctx.handle, 1.0, C.c_void_p(out.data_ptr()), 0.0, C.c_void_p(pout), n)
+
+        g = torch.Generator(device="cpu").manual_seed(seed)
+        x = torch.randn(n, generator=g, dtype=torch.float64).to("cuda")
+        ev, na, conv = ops.eigs_rs_op(self.ctx, n, apply, x, nev=nev, tol=eig_tol, ncv=ncv)
+        self.applies += na
+        return ev, conv
+

@@ -48,6 +48,27 @@ def eigs_rs(plan, x, tol, ncv=0, maxit=0):
     return ev.value, na.value, st == 0
 
 
+def eigs_rs_op(ctx, n, apply, x, nev=1, tol=1e-12, ncv=0, maxit=0, evecs=None):
+    """eigs_rs(fun, N, vals, vecs, nev, "SA", tol, x0) (eigs.cpp:369-494) for an operator given as a
+    Python callable apply(in_ptr, out_ptr) on device pointers (enqueues work on the context's
+    stream).  x: device start vector, on return the lowest Ritz vector; evecs: optional device
+    (nev, n) tensor receiving the Ritz vectors.  Returns (eigenvalues, applies, converged)."""
+    ev = (C.c_double * nev)()
+    na = C.c_int()
+
+    def cb(user, pin, pout):
+        try:
+            apply(pin, pout)
+            return 0
+        except Exception:  # a failing apply aborts the solve with an error status
+            return -3
+
+    fn = N.APPLY_FN(cb)
+    st = N.call("imps_eigs_rs_op", ctx.handle, int(n), fn, None, _dptr(x), N.MEM_DEVICE, int(nev), float(tol), int(ncv),
+                int(maxit), ev, None if evecs is None else _dptr(evecs), C.byref(na))
+    return [ev[i] for i in range(nev)], na.value, st == 0
+
+
 def InvertE_fac(plan, x_re, x_im, fac, y_re, y_im, tol, maxit=0, krylov=0):
     """InvertE_fac(A, B, x, dir, fac) (InvEBlockFunctions.hpp:413-451) for the mixed TM ``plan``:
     (1 - fac T) y = x with complex x, y as real / imaginary device planes (y holds y0 on entry).

@@ -167,6 +167,16 @@ int imps_tm_proj_apply(imps_plan* tm, const double* in, const double* rho_in,
  * entry and the normalised eigenvector on exit.  ncv = 0 selects max(20, 2) capped at n. */
 int imps_eigs_rs(imps_plan* op, double* x, int mem, double tol, int ncv, int maxit,
                  double* eval, int* n_applies);
+/* Operator given by the caller for imps_eigs_rs_op: out = A in on device vectors of length n,
+ * enqueued on the context's stream; return < 0 to abort the solve. */
+typedef int (*imps_apply_fn)(void* user, const double* in, double* out);
+/* eigs_rs(fun, N, vals, vecs, nev, "SA", tol, x0) (eigs.cpp:369-494) for a symmetric operator
+ * given as a callback: the nev lowest eigenpairs by the device thick-restart Lanczos.  x holds
+ * x0 on entry and the normalised lowest Ritz vector on exit; evals (host, nev); evecs (device,
+ * n x nev column-major, optional).  A complex Hermitian operator is passed in its real form on
+ * [re; im] (every eigenvalue twice; a Lanczos run from one start vector finds each once). */
+int imps_eigs_rs_op(imps_ctx* ctx, int64_t n, imps_apply_fn fn, void* user, double* x, int mem, int nev,
+                    double tol, int ncv, int maxit, double* evals, double* evecs, int* n_applies);
 /* InvertE_proj (InvEBlockFunctions.hpp:201-266) on a TM plan: solves
  *  dir l: y (1 - T + |R)(L|) = x (1 - |R)(L|),  dir r: (1 - T + |R)(L|) y = (1 - |R)(L|) x
  * with restarted GMRES (Krylov size `krylov`, 0 = 40); y holds y0 on entry (NULL = zeros). */

@@ -114,3 +114,35 @@ def test_heff_apply_matches_oracle(cuda_ctx, K, p):
     for n, dims in enumerate(e["xdims"]):
         refv = np.concatenate([ref[n][qi][1].reshape(-1, order="F") for (qi, _, _, _) in dims])
         assert np.linalg.norm(got[n] - refv) / np.linalg.norm(refv) < 1e-9, n
+
+
+def test_excitation_energies_match_oracle(cuda_ctx):
+    """The 4 lowest eigenvalues of H_eff at one momentum (Excitations_main.cpp:270-279, eigs_n
+    "SR"): the device Lanczos on the real form of H_eff against ARPACK (scipy) on the oracle's
+    ApplyHeff."""
+    from scipy.sparse.linalg import LinearOperator, eigsh
+    from imps_cpp_tools_gb300.excitations import ExcitationsGPU
+    from tests.test_oracle_excitations import excitation_setup
+    dims0 = {(-2,): 3, (0,): 5, (2,): 3}
+    e = excitation_setup((2,), dims0=dims0)
+    kfac = np.exp(0.9j)
+    ex = ExcitationsGPU(cuda_ctx, e["AL"], e["AR"], e["NL"], e["HLtot"], e["HRtot"], e["h"], e["d"], e["xdims"],
+                        tol=1e-13)
+    ev, conv = ex.energies(kfac, nev=4, eig_tol=1e-10)
+    assert conv
+    sizes = [[(qi, qo, ml, mr) for (qi, qo, ml, mr) in dims] for dims in e["xdims"]]
+    lens = [sum(ml * mr for (_, _, ml, mr) in dims) for dims in sizes]
+    mtot = sum(lens)
+
+    def hop(v):
+        parts, pos = [], 0
+        for dims, ln in zip(sizes, lens):
+            parts.append(O.bm_from_vec(v[pos:pos + ln], dims))
+            pos += ln
+        out = O.ApplyHeff(parts, kfac, e["AL"], e["AR"], e["NL"], e["h"], e["d"], e["HLtot"], e["HRtot"], tol=1e-13)
+        return np.concatenate([np.concatenate([out[n][qi][1].reshape(-1, order="F") for (qi, _, _, _) in dims])
+                               for n, dims in enumerate(sizes)])
+
+    op = LinearOperator((mtot, mtot), matvec=hop, dtype=np.complex128)
+    ref = np.sort(eigsh(op, k=4, which="SA", tol=1e-11, return_eigenvectors=False))
+    assert np.abs(np.sort(ev) - ref).max() < 1e-8 * max(1.0, np.abs(ref).max()), (ev, ref)

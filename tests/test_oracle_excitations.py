@@ -67,12 +67,12 @@ def test_invert_e_fac_solves_its_equation(state):
     assert np.linalg.norm(res) < 1e-11 * np.linalg.norm(O.bm_vec(x))
 
 
-def excitation_setup(K, seed=3):
+def excitation_setup(K, seed=3, dims0=None):
     """A random left/right-canonical two-site XXZ state (the oracle's randMPS_LR), h shifted by
     its energy density E0, its environments (HeffConstants) and null spaces, and the X sector
     structure for charge K."""
     from imps_cpp_tools_gb300 import models
-    st = T.random_state("xxz", B0, seed=seed, J=1.0, Delta=-1.0)
+    st = T.random_state("xxz", dims0 or B0, seed=seed, J=1.0, Delta=-1.0)
     AL, AR, C, d = st["AL"], st["AR"], st["C"], st["d"]
     C0 = C[-1]  # bond 0
     R = O.bd_mul(C0, O.bd_t(C0))
