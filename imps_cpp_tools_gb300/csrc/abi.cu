@@ -31,6 +31,10 @@ struct imps_ctx {
   int* dflag = nullptr;     // 16 device flags
   char* arena = nullptr;
   size_t arena_bytes = 0;
+  // a second arena for solvers whose operator is a caller's callback: the callback may run
+  // solvers of its own on this context, which take the first arena
+  char* arena_cb = nullptr;
+  size_t arena_cb_bytes = 0;
   // pinned staging of solver convergence data (projected-matrix columns + flags), so that the
   // device-to-host copies are asynchronous and a check can be evaluated while the next
   // Krylov step runs
@@ -170,12 +174,14 @@ int run_stages(imps_plan* p, std::vector<Stage>& stages) {
 }
 
 // ---- arena (per-context scratch, grows; never shrinks) ----
-int arena_reserve(imps_ctx* c, size_t bytes) {
-  if (bytes <= c->arena_bytes) return IMPS_OK;
-  if (c->arena) { cudaStreamSynchronize(c->stream); cudaFree(c->arena); c->arena = nullptr; c->arena_bytes = 0; }
+int arena_reserve(imps_ctx* c, size_t bytes, bool callback_arena = false) {
+  char*& a = callback_arena ? c->arena_cb : c->arena;
+  size_t& ab = callback_arena ? c->arena_cb_bytes : c->arena_bytes;
+  if (bytes <= ab) return IMPS_OK;
+  if (a) { cudaStreamSynchronize(c->stream); cudaFree(a); a = nullptr; ab = 0; }
   size_t nb = std::max(bytes, (size_t)1 << 20);
-  CK(cudaMalloc(&c->arena, nb));
-  c->arena_bytes = nb;
+  CK(cudaMalloc(&a, nb));
+  ab = nb;
   return IMPS_OK;
 }
 
@@ -282,6 +288,7 @@ int imps_ctx_destroy(imps_ctx* c) {
   if (c->hpin) cudaFreeHost(c->hpin);
   if (c->ev_check) cudaEventDestroy(c->ev_check);
   if (c->arena) cudaFree(c->arena);
+  if (c->arena_cb) cudaFree(c->arena_cb);
   if (c->own) cudaStreamDestroy(c->own);
   delete c;
   return IMPS_OK;
@@ -773,9 +780,10 @@ static int eigs_impl(imps_ctx* c, imps_plan* p, int64_t n, const DevApply& op, d
   const int ld = m + 1;
   const int kk = std::max(nev, std::max(1, std::min(m / 2, m - 3)));  // Ritz vectors kept at a thick restart
   if (kk >= m) return IMPS_ERR_BAD_ARG;
+  const bool cb_arena = p == nullptr;  // operator is a callback: keep clear of its solvers
   RC(arena_reserve(c, round256(n * 8) * (m + 4 + kk) + round256((size_t)ld * ld * 8) +
-                          round256((size_t)m * kk * 8) + 4096));
-  Bump bp{c->arena};
+                          round256((size_t)m * kk * 8) + 4096, cb_arena));
+  Bump bp{cb_arena ? c->arena_cb : c->arena};
   double* V = bp.take((size_t)n * (m + 1));
   double* Wk = bp.take((size_t)n * kk);
   double* w = bp.take(n);
