@@ -93,6 +93,7 @@ _PROTOS = {
     "imps_plan_decomp": (c_int, [c_vp, c_vp, c_int, C.POINTER(c_vp)]),
     "imps_sector_qr": (c_int, [c_vp, c_vp, c_vp, c_vp, c_int]),
     "imps_sector_svd": (c_int, [c_vp, c_vp, c_vp, c_vp, c_vp, c_int]),
+    "imps_sector_nullspace": (c_int, [c_vp, c_vp, c_vp, c_int]),
     "imps_sector_colscale": (c_int, [c_vp, c_vp, c_vp, c_dbl, c_int]),
     "imps_bd_trace_prod": (c_int, [c_vp, c_vp, c_vp, c_vp, P_dbl]),
     "imps_absmax": (c_int, [c_vp, c_vp, c_i64, P_dbl]),

@@ -310,4 +310,6 @@ def plan_decomp(ctx, A, direction):
     p = Plan(ctx, h, "decomp")
     p.rlayout = p.derived(1)
     p.nsv = sum(b[3] for b in p.rlayout.blocks)
+    if direction in ("l", 0):
+        p.nslayout = p.derived(2)  # left null space (Nullspace(A, l))
     return p

@@ -593,6 +593,7 @@ int imps_plan_destroy(imps_plan* p) {
     cudaFree(p->dc->d_ent); cudaFree(p->dc->d_mats); cudaFree(p->dc->dA); cudaFree(p->dc->dQ);
     cudaFree(p->dc->dR); cudaFree(p->dc->dV2); cudaFree(p->dc->dS); cudaFree(p->dc->dW);
     cudaFree(p->dc->dstatus);
+    cudaFree(p->dc->dNS); cudaFree(p->dc->d_nent);
     delete p->dc;
   }
   delete p;
@@ -1363,6 +1364,7 @@ int imps_plan_decomp(imps_ctx* ctx, const imps_layout* A, int dir, imps_plan** o
   p->P.kind = PLAN_DECOMP;
   p->P.derived.push_back(A->L);
   p->P.derived.push_back(D->rlayout);
+  p->P.derived.push_back(D->nslayout);  // left null space (dir l; empty for dir r)
   p->dc = D;
   *out = p;
   if (ctx->device < 0) return IMPS_OK;
@@ -1384,7 +1386,28 @@ int imps_plan_decomp(imps_ctx* ctx, const imps_layout* A, int dir, imps_plan** o
   RC(alloc(&D->dV2, D->r_elems));
   RC(alloc(&D->dS, D->s_elems));
   RC(alloc(&D->dW, D->w_elems));
+  RC(alloc(&D->dNS, D->ns_elems));
+  if (!D->nent.empty()) {
+    CK(cudaMalloc(&D->d_nent, D->nent.size() * sizeof(GatherEntry)));
+    CK(cudaMemcpy(D->d_nent, D->nent.data(), D->nent.size() * sizeof(GatherEntry), cudaMemcpyHostToDevice));
+  }
   CK(cudaMalloc(&D->dstatus, sizeof(int)));
+  return IMPS_OK;
+}
+
+// Nullspace(A, l) (MPSBlockUtilities.hpp:247-300): N_L with A_s^T-orthogonal, orthonormal columns
+// per right sector; layout: derived layout 2 of the plan.  A must be left-isometric (full
+// column rank per sector); the basis is the Householder complement (the reference's SVD basis
+// spans the same space).
+int imps_sector_nullspace(imps_plan* p, const double* A, double* NL, int mem) {
+  if (!p || p->P.kind != PLAN_DECOMP || !A || !NL || mem != IMPS_MEM_DEVICE) return IMPS_ERR_BAD_ARG;
+  if (p->ctx->device < 0) return IMPS_ERR_NO_DEVICE;
+  DecompPlan* D = p->dc;
+  if (D->dir != 0 || !D->tall) return IMPS_ERR_UNSUPPORTED;
+  cudaStream_t st = p->ctx->stream;
+  RC(dc_gather(D->d_ent, (int)D->ent.size(), A, D->dA, st));
+  RC(dc_nullspace(D->d_mats, (int)D->mats.size(), D->dA, D->dNS, st));
+  RC(dc_scatter(D->d_nent, (int)D->nent.size(), D->dNS, NL, st));
   return IMPS_OK;
 }
 

@@ -64,16 +64,10 @@ __global__ void scatter_kernel(const imps::GatherEntry* __restrict__ ent, int ne
   }
 }
 
-// Householder QR of the M x N matrix A (in place, column-major, ld = M), K = min(M,N).
-// Outputs Q (M x K, ld M) and R (K x N, ld K) with diag(R) >= 0.
-__global__ void __launch_bounds__(DT) qr_kernel(const imps::DenseMat* __restrict__ mats,
-                                                double* __restrict__ A, double* __restrict__ Q,
-                                                double* __restrict__ R, int transpose_out) {
-  __shared__ double sh[32];
-  __shared__ double tau_s[512];
-  const imps::DenseMat mt = mats[blockIdx.x];
-  const int M = mt.M, N = mt.N, K = min(M, N);
-  double* a = A + mt.a_off;
+// Householder QR of the M x N matrix a (in place, column-major, ld = M), K = min(M, N):
+// reflectors below the diagonal, R on and above it, tau_s[k] their scalars.
+__device__ void householder(double* a, int M, int N, double* tau_s, double* sh) {
+  const int K = min(M, N);
   const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5, nw = blockDim.x >> 5;
   for (int k = 0; k < K; ++k) {
     double p = 0.0;
@@ -107,6 +101,41 @@ __global__ void __launch_bounds__(DT) qr_kernel(const imps::DenseMat* __restrict
     }
     __syncthreads();
   }
+}
+
+// Apply H_0 ... H_{K-1} (reflectors of `a`) to the M x P matrix c (ld M), backwards.
+__device__ void apply_reflectors(const double* a, int M, int K, const double* tau_s, double* c, int P) {
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5, nw = blockDim.x >> 5;
+  for (int k = K - 1; k >= 0; --k) {
+    const double tau = tau_s[k];
+    if (tau != 0.0) {
+      const double* v = a + (int64_t)k * M;
+      for (int j = warp; j < P; j += nw) {
+        double* cj = c + (int64_t)j * M;
+        double w = 0.0;
+        for (int i = k + 1 + lane; i < M; i += 32) w += v[i] * cj[i];
+        w = wsum(w) + cj[k];
+        const double tw = tau * w;
+        if (lane == 0) cj[k] -= tw;
+        for (int i = k + 1 + lane; i < M; i += 32) cj[i] -= tw * v[i];
+      }
+    }
+    __syncthreads();
+  }
+}
+
+// Householder QR of the M x N matrix A (in place, column-major, ld = M), K = min(M,N).
+// Outputs Q (M x K, ld M) and R (K x N, ld K) with diag(R) >= 0.
+__global__ void __launch_bounds__(DT) qr_kernel(const imps::DenseMat* __restrict__ mats,
+                                                double* __restrict__ A, double* __restrict__ Q,
+                                                double* __restrict__ R, int transpose_out) {
+  __shared__ double sh[32];
+  __shared__ double tau_s[512];
+  const imps::DenseMat mt = mats[blockIdx.x];
+  const int M = mt.M, N = mt.N, K = min(M, N);
+  double* a = A + mt.a_off;
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5, nw = blockDim.x >> 5;
+  householder(a, M, N, tau_s, sh);
   // R (K x N) and the sign of its diagonal
   double* q = Q + mt.q_off;
   double* r = R + mt.r_off;
@@ -145,6 +174,27 @@ __global__ void __launch_bounds__(DT) qr_kernel(const imps::DenseMat* __restrict
     const int j = (int)(t / M);
     q[t] *= sgn[j];
   }
+}
+
+// Left null space of the M x N matrix A (M > N, full column rank; dir l of Nullspace,
+// MPSBlockUtilities.hpp:247-300): the last M - N columns of the full Householder Q,
+// NS = H_0 ... H_{N-1} [0; I_{M-N}] (M x (M - N), orthonormal, orthogonal to A's columns).
+__global__ void __launch_bounds__(DT) nullspace_kernel(const imps::DenseMat* __restrict__ mats,
+                                                       double* __restrict__ A, double* __restrict__ NS) {
+  __shared__ double sh[32];
+  __shared__ double tau_s[512];
+  const imps::DenseMat mt = mats[blockIdx.x];
+  const int M = mt.M, N = mt.N, P = M - N;
+  if (P <= 0) return;
+  double* a = A + mt.a_off;
+  double* ns = NS + mt.ns_off;
+  householder(a, M, N, tau_s, sh);
+  for (int64_t t = threadIdx.x; t < (int64_t)M * P; t += blockDim.x) {
+    const int i = (int)(t % M), j = (int)(t / M);
+    ns[t] = (i == N + j) ? 1.0 : 0.0;
+  }
+  __syncthreads();
+  apply_reflectors(a, M, min(M, N), tau_s, ns, P);
 }
 
 // One-sided Jacobi SVD of the M x N matrix held in U (in place, M >= N): on exit U holds the
@@ -314,6 +364,13 @@ int dc_scatter(const GatherEntry* d_ent, int nent, const double* dense, double* 
 int dc_qr(const DenseMat* d_mats, int nmat, double* A, double* Q, double* R, int transpose_r, cudaStream_t st) {
   if (nmat > 0) imps::count_launch();
   if (nmat > 0) qr_kernel<<<nmat, DT, 0, st>>>(d_mats, A, Q, R, transpose_r);
+  return cudaGetLastError() == cudaSuccess ? IMPS_OK : IMPS_ERR_CUDA;
+}
+
+int dc_nullspace(const DenseMat* d_mats, int nmat, double* A, double* NS, cudaStream_t st) {
+  if (nmat <= 0) return IMPS_OK;
+  imps::count_launch();
+  nullspace_kernel<<<nmat, DT, 0, st>>>(d_mats, A, NS);
   return cudaGetLastError() == cudaSuccess ? IMPS_OK : IMPS_ERR_CUDA;
 }
 

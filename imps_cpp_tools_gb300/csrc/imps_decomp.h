@@ -26,6 +26,7 @@ struct DenseMat {
   int64_t r_off;  // R (K x N) / V (N x N) / DiagIso
   int64_t s_off;  // singular values (N)
   int64_t w_off;  // scratch (N + M*N)
+  int64_t ns_off; // null space (M x (M - N)), dir l only
   int32_t M, N;
 };
 
@@ -36,6 +37,13 @@ struct DecompPlan {
   int64_t dense_elems = 0, r_elems = 0, s_elems = 0, w_elems = 0;
   bool tall = true;  // every sector has M >= N
   Layout rlayout;    // R / DiagIso BlockDiag layout over the sectors
+  // left null space (dir l, Nullspace(A, l), MPSBlockUtilities.hpp:247-300): per physical
+  // index s the blocks (Qin -> q) of A whose right sector q has M > N, with M - N columns
+  Layout nslayout;
+  std::vector<GatherEntry> nent;  // dense null-space rows -> N_L blocks
+  int64_t ns_elems = 0;
+  GatherEntry* d_nent = nullptr;
+  double* dNS = nullptr;
   GatherEntry* d_ent = nullptr;
   DenseMat* d_mats = nullptr;
   double* dA = nullptr;  // dense input (overwritten by QR / holds U for SVD)
@@ -56,5 +64,6 @@ int dc_svd(const DenseMat* d_mats, int nmat, double* U, double* S, double* V, do
            cudaStream_t st);
 int dc_colscale(const DenseMat* d_mats, int nmat, double* X, const double* S, double power, cudaStream_t st);
 int dc_transpose_sq(const DenseMat* d_mats, int nmat, const double* X, double* Y, cudaStream_t st);
+int dc_nullspace(const DenseMat* d_mats, int nmat, double* A, double* NS, cudaStream_t st);
 
 }  // namespace imps

@@ -72,6 +72,57 @@ int build_decomp(DecompPlan& D, const Layout& A, int dir) {
   }
   D.rlayout.nelem = r;
   layout_index(D.rlayout);
+  // null space of the stacked sector matrices (dir l): block rows follow the gather order
+  if (dir == 0) {
+    std::map<Key, int> sec_index;
+    int si = 0;
+    for (auto& kv : secs) sec_index[kv.first] = si++;
+    int64_t ns = 0;
+    for (DenseMat& mt : D.mats) {
+      mt.ns_off = ns;
+      ns += (int64_t)mt.M * std::max(mt.M - mt.N, 0);
+    }
+    D.ns_elems = ns;
+    // row position of each block of A inside its stacked sector matrix
+    std::map<int, int> row0;
+    for (auto& kv : secs) {
+      int pos = 0;
+      for (int b : kv.second.blocks) { row0[b] = pos; pos += A.blocks[b].rows; }
+    }
+    D.nslayout = Layout();
+    D.nslayout.nsym = A.nsym;
+    int64_t off = 0;
+    int maxg = 0;
+    for (int b = 0; b < (int)A.blocks.size(); ++b) {  // A's (group, qin) order
+      const Block& B = A.blocks[b];
+      const DenseMat& mt = D.mats[sec_index[B.qout]];
+      const int nul = mt.M - mt.N;
+      if (nul <= 0) continue;
+      Block nb;
+      nb.qin = B.qin;
+      nb.qout = B.qout;
+      nb.rows = B.rows;
+      nb.cols = nul;
+      nb.group = B.group;
+      nb.off = off;
+      D.nslayout.blocks.push_back(nb);
+      GatherEntry e{};
+      e.src_off = off;
+      e.dst_off = mt.ns_off;
+      e.rows = B.rows;
+      e.cols = nul;
+      e.r0 = row0[b];
+      e.c0 = 0;
+      e.dst_ld = std::max(mt.M, 1);
+      e.transpose = 0;
+      D.nent.push_back(e);
+      off += (int64_t)B.rows * nul;
+      maxg = std::max(maxg, B.group);
+    }
+    D.nslayout.nelem = off;
+    D.nslayout.ngroups = A.ngroups;
+    layout_index(D.nslayout);
+  }
   D.dense_elems = a;
   D.r_elems = r;
   D.s_elems = sv;

@@ -128,6 +128,13 @@ def svd(dec, A, U=None, S=None, V=None):
     return st == 0
 
 
+def Nullspace(plan, A, NL):
+    """Nullspace(A, l) (MPSBlockUtilities.hpp:247-300) with a dir-l decomposition plan: NL in the
+    plan's derived layout 2."""
+    N.call("imps_sector_nullspace", plan.handle, _dptr(A), _dptr(NL), N.MEM_DEVICE)
+    return NL
+
+
 def colscale(dec, X, S, power):
     """X_q[:, j] *= S_q[j]**power on square sector blocks (BlockDiagMat << BlockLam)."""
     N.call("imps_sector_colscale", dec.handle, _dptr(X), _dptr(S), float(power), N.MEM_DEVICE)

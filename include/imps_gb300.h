@@ -232,6 +232,10 @@ int imps_plan_decomp(imps_ctx* ctx, const imps_layout* A, int dir, imps_plan** o
  * (MPSBlockUtilities.hpp:181-244, BlockObj.hpp:2422-2459, helpers.hpp:181-195).  Device
  * pointers only; every sector needs stacked dimension >= sector dimension. */
 int imps_sector_qr(imps_plan* dec, const double* A, double* Q, double* R, int mem);
+/* Nullspace(A, l) (MPSBlockUtilities.hpp:247-300) on a dir-l decomposition plan of a
+ * left-isometric A: N_L (layout: imps_plan_derived_layout(plan, 2)) with orthonormal columns
+ * orthogonal to A's, per right sector (sectors without a null space omitted).  Device memory. */
+int imps_sector_nullspace(imps_plan* plan, const double* A, double* NL, int mem);
 /* svd(S, DiagIso, MPS, dir) (MPSBlockUtilities.hpp:78-153): U = MPSIso (A's layout), S =
  * singular values per sector concatenated in sector order (descending), Viso = DiagIso
  * (V^T for dir l, U for dir r).  Any output may be NULL.  One-sided Jacobi, FP64. */

@@ -146,3 +146,57 @@ def test_excitation_energies_match_oracle(cuda_ctx):
     op = LinearOperator((mtot, mtot), matvec=hop, dtype=np.complex128)
     ref = np.sort(eigsh(op, k=4, which="SA", tol=1e-11, return_eigenvectors=False))
     assert np.abs(np.sort(ev) - ref).max() < 1e-8 * max(1.0, np.abs(ref).max()), (ev, ref)
+
+
+def _mps_from_vec(v, layout):
+    """Device-layout vector -> map-of-blocks MPS (list over s of {qin: (qout, M)})."""
+    ng = max(b[0] for b in layout.blocks) + 1 if layout.blocks else 1
+    out = [dict() for _ in range(ng)]
+    pos = 0
+    for (g, qi, qo, r, c) in layout.blocks:
+        out[g][tuple(qi)] = (tuple(qo), np.array(v[pos:pos + r * c]).reshape(c, r).T.copy())
+        pos += r * c
+    return out
+
+
+def test_nullspace_on_device(cuda_ctx, state):
+    """Nullspace(A, l) on the device: orthonormal columns per right sector, orthogonal to A."""
+    ns = len(state["I2K"][0])
+    for A in state["AL"]:
+        plan = B.plan_decomp(cuda_ctx, B.Layout(T.mps_blocks(A), ns), "l")
+        NLd = dev(np.zeros(plan.nslayout.nelem))
+        ops.Nullspace(plan, dev(O.mps_vec(A)), NLd)
+        NL = _mps_from_vec(host(NLd), plan.nslayout)
+        NL += [dict() for _ in range(len(A) - len(NL))]
+        G = O.ApplyTMmixedLeft(NL, NL)  # sum_s NL_s^T NL_s per sector
+        for q, (qo, M) in G.items():
+            assert np.abs(M - np.eye(M.shape[0])).max() < 1e-12
+        X = O.ApplyTMmixedLeft(NL, A)  # sum_s A_s^T NL_s
+        assert max((np.abs(M).max() for (_, M) in X.values()), default=0.0) < 1e-12
+
+
+def test_excitation_energies_with_device_nullspace(cuda_ctx):
+    """Excitation energies do not depend on the null-space basis: the device N_L gives the same
+    4 lowest energies as the oracle's (SVD-based) N_L."""
+    from imps_cpp_tools_gb300.excitations import ExcitationsGPU
+    from tests.test_oracle_excitations import excitation_setup
+    dims0 = {(-2,): 3, (0,): 5, (2,): 3}
+    e = excitation_setup((2,), dims0=dims0)
+    ns = 1
+    NLd = []
+    for A in e["AL"]:
+        plan = B.plan_decomp(cuda_ctx, B.Layout(T.mps_blocks(A), ns), "l")
+        v = dev(np.zeros(plan.nslayout.nelem))
+        ops.Nullspace(plan, dev(O.mps_vec(A)), v)
+        m = _mps_from_vec(host(v), plan.nslayout)
+        NLd.append(m + [dict() for _ in range(len(A) - len(m))])
+    xd = O.XDims(NLd, e["AR"], (2,))
+    assert [[(q, qo, a, b) for (q, qo, a, b) in dd] for dd in xd] == e["xdims"]
+    kfac = np.exp(0.9j)
+    args = (e["AL"], e["AR"])
+    ev_dev, c1 = ExcitationsGPU(cuda_ctx, *args, NLd, e["HLtot"], e["HRtot"], e["h"], e["d"], xd,
+                                tol=1e-13).energies(kfac, nev=4, eig_tol=1e-10)
+    ev_ora, c2 = ExcitationsGPU(cuda_ctx, *args, e["NL"], e["HLtot"], e["HRtot"], e["h"], e["d"], e["xdims"],
+                                tol=1e-13).energies(kfac, nev=4, eig_tol=1e-10)
+    assert c1 and c2
+    assert np.abs(np.array(ev_dev) - np.array(ev_ora)).max() < 1e-8

@@ -156,3 +156,21 @@ def test_bad_dims_rejected(host_ctx):
     with pytest.raises(N.ImpsError) as ex:
         B.plan_hac(host_ctx, ac, e, er, empty, empty, 1)
     assert ex.value.status == -2
+
+
+def test_nullspace_layout_matches_oracle_structure():
+    """The null-space layout of a dir-l decomposition plan has the sectors and dimensions of
+    the reference's Nullspace(A, l) (MPSBlockUtilities.hpp:247-300), in std::map order."""
+    from imps_cpp_tools_gb300 import blocks as B
+    from oracle import imps_oracle as O
+    from tests import imps_testlib as T
+    st = T.random_state("xxz", {(-4,): 3, (-2,): 8, (0,): 10, (2,): 8, (4,): 3}, seed=3, J=1.0, Delta=-1.0)
+    ns = len(st["I2K"][0])
+    ctx = B.Context(-1)
+    for A in st["AL"]:
+        plan = B.plan_decomp(ctx, B.Layout(T.mps_blocks(A), ns), "l")
+        NL = O.Nullspace(A, "l")
+        ref = [(s, tuple(qi), tuple(NL[s][qi][0]), NL[s][qi][1].shape[0], NL[s][qi][1].shape[1])
+               for s in range(len(NL)) for qi in sorted(NL[s]) if NL[s][qi][1].shape[1] > 0]
+        got = [(b[0], tuple(b[1]), tuple(b[2]), b[3], b[4]) for b in plan.nslayout.blocks]
+        assert got == ref
