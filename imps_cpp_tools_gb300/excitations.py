@@ -506,3 +506,92 @@ class ExcitationsGPU:
                 out.append(v)
         return out[:nev], conv and len(out) >= nev
 
+
+# ------------------------------------------------------------------------------------------------
+# inputs of the excitation ansatz from a converged two-site VUMPS state on the device
+# ------------------------------------------------------------------------------------------------
+
+def _blocks(layout):
+    return [(g, tuple(qi), tuple(qo), r, c) for (g, qi, qo, r, c) in layout.blocks]
+
+
+def mps_to_host(vec, layout, d):
+    """Device vector in an MPS layout -> list over s of {qin: (qout, matrix)}."""
+    v = vec.detach().cpu().numpy()
+    out, pos = [dict() for _ in range(d)], 0
+    for (g, qi, qo, r, c) in _blocks(layout):
+        out[g][qi] = (qo, v[pos:pos + r * c].reshape(c, r).T.copy())
+        pos += r * c
+    return out
+
+
+def bd_to_host(vec, layout):
+    v = vec.detach().cpu().numpy()
+    out, pos = {}, 0
+    for (g, qi, qo, r, c) in _blocks(layout):
+        out[qi] = v[pos:pos + r * c].reshape(c, r).T.copy()
+        pos += r * c
+    return out
+
+
+def xdims_from_layouts(ns_layout, ar_layout, K):
+    """XDims (Excitations_helpers.hpp:641-678): X_n maps the right sectors q of N_L[n] to the
+    left sectors q + K of AR[n+1]."""
+    ml, mr = {}, {}
+    for (g, qi, qo, r, c) in _blocks(ns_layout):
+        ml.setdefault(qo, c)
+    for (g, qi, qo, r, c) in _blocks(ar_layout):
+        mr.setdefault(qi, r)
+    dims = []
+    for q in sorted(ml):
+        qk = _kadd(q, K)
+        if qk in mr and ml[q] > 0 and mr[qk] > 0:
+            dims.append((q, qk, ml[q], mr[qk]))
+    return dims
+
+
+def excitation_inputs(v, K, tol=1e-13):
+    """AL, AR, N_L, HLtot, HRtot (HeffConstants, Excitations_helpers.hpp:258-331), h - E0 and
+    XDims for charge K, from a converged VumpsGPU state (sites n: bond n -> n + 1; C[b] on bond
+    b), every contraction and solve on the device; host copies as map-of-blocks structures."""
+    from . import ops as _ops
+    ctx, d, torch = v.ctx, v.d, v.torch
+    AL, AR = v.AL, v.AR
+    E0 = float(np.mean(v.energy()))
+    eye0 = v._eye(0)
+    # left: HL[0] = OpTM(AL1 AL0) on bond 1, HL[1] = OpTM(AL0 AL1) + T_L(AL1, HL[0]) on bond 0
+    HL0 = v._optm(True, 1, AL, v._z(v.LB[1]))
+    HL1 = v._get_hl(0)
+    R0 = v._tm_dominant(("R", 0), AL, v._cct(0, right=True), 1e-15)
+    EHL1 = v._invert_e(("L", 0), AL, HL1, eye0, R0, "l", None, tol)
+    EHL0 = v._tm(("L1", 0), AL, EHL1, v._z(v.LB[1]))
+    # right: HR[1] = OpTM(AR1 AR0) on bond 1, HR[0] = OpTM(AR0 AR1) + T_R(AR0, HR[1]) on bond 0
+    HR1 = v._optm(False, 1, AR, v._z(v.LB[1]))
+    HR0 = v._get_hr(0)
+    L0 = v._tm_dominant(("L", 0), AR, v._cct(0, right=False), 1e-15)
+    EHR0 = v._invert_e(("R", 0), AR, HR0, L0, eye0, "r", None, tol)
+    EHR1 = v._tm(("R1", 1), AR, EHR0, v._z(v.LB[1]))
+    # h - E0: for isometric tensors OpTM(h - E0) = OpTM(h) - E0 1 along each chain
+    eye1 = v._eye(1)
+    HLtot = [_ops.axpby(ctx, 1.0, EHL0, 1.0, _ops.axpby(ctx, -E0, eye1, 1.0, HL0.clone())), EHL1]
+    HRtot = [EHR0, _ops.axpby(ctx, 1.0, EHR1, 1.0, _ops.axpby(ctx, -E0, eye1, 1.0, HR1.clone()))]
+    # N_L on the device
+    NL, nsl = [], []
+    for n in range(2):
+        plan = v.dec_ac_l[n]
+        out = torch.zeros(max(plan.nslayout.nelem, 1), dtype=torch.float64, device="cuda")
+        _ops.Nullspace(plan, AL[n], out)
+        NL.append(mps_to_host(out, plan.nslayout, d))
+        nsl.append(plan.nslayout)
+    hs = [(r, c, val - (E0 if r == c else 0.0)) for (r, c, val) in v.hnnz]
+    diag = {r for (r, c, _) in v.hnnz if r == c}
+    hs += [(i, i, -E0) for i in range(d * d) if i not in diag]
+    hs.sort(key=lambda t: (t[1], t[0]))
+    xd = [xdims_from_layouts(nsl[n], v.LA[(n + 1) % 2], tuple(K)) for n in range(2)]
+    host = dict(AL=[mps_to_host(AL[n], v.LA[n], d) for n in range(2)],
+                AR=[mps_to_host(AR[n], v.LA[n], d) for n in range(2)], NL=NL,
+                HLtot=[bd_to_host(HLtot[0], v.LB[1]), bd_to_host(HLtot[1], v.LB[0])],
+                HRtot=[bd_to_host(HRtot[0], v.LB[0]), bd_to_host(HRtot[1], v.LB[1])],
+                h=hs, d=d, xdims=xd, E0=E0)
+    return host
+

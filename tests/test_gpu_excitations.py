@@ -200,3 +200,53 @@ def test_excitation_energies_with_device_nullspace(cuda_ctx):
                                 tol=1e-13).energies(kfac, nev=4, eig_tol=1e-10)
     assert c1 and c2
     assert np.abs(np.array(ev_dev) - np.array(ev_ora)).max() < 1e-8
+
+
+def test_excitations_from_converged_vumps_state(cuda_ctx):
+    """The whole excitation pipeline from a converged GPU VUMPS state (HeffConstants, N_L and
+    XDims on the device / from layouts), against the oracle's HeffConstants and ARPACK on the
+    oracle's H_eff for the same state."""
+    from scipy.sparse.linalg import LinearOperator, eigsh
+    from imps_cpp_tools_gb300.excitations import ExcitationsGPU, excitation_inputs
+    from imps_cpp_tools_gb300.vumps import VumpsGPU
+    b0 = {(-2,): 3, (0,): 5, (2,): 3}
+    from imps_cpp_tools_gb300 import models
+    dimvec = models.make_dims(b0, 2, models.build_model("xxz", J=1.0, Delta=-1.0)[1])
+    v = VumpsGPU(cuda_ctx, "xxz", dimvec=dimvec, seed=5, InvETol=1e-13, J=1.0, Delta=-1.0)
+    for _ in range(200):
+        E, F, _ = v.sweep()
+        if F.max() < 1e-11:
+            break
+    assert F.max() < 1e-10
+    inp = excitation_inputs(v, (2,), tol=1e-13)
+    # HeffConstants against the oracle on the same (downloaded) state
+    C0 = O.bd_from_vec(v.C[0].cpu().numpy(), [(tuple(b[1]), b[3]) for b in v.LB[0].blocks])
+    R = O.bd_mul(C0, O.bd_t(C0))
+    L = O.bd_mul(O.bd_t(C0), C0)
+    HLo, HRo = O.HeffConstants(inp["AL"], inp["AR"], L, R, inp["h"], tol=1e-13)
+    for got, ref in ((inp["HLtot"], HLo), (inp["HRtot"], HRo)):
+        for n in range(2):
+            for q in ref[n]:
+                assert np.abs(got[n][q] - ref[n][q]).max() < 1e-8 * max(1.0, np.abs(ref[n][q]).max())
+    kfac = np.exp(1.1j)
+    ex = ExcitationsGPU(cuda_ctx, inp["AL"], inp["AR"], inp["NL"], inp["HLtot"], inp["HRtot"], inp["h"], inp["d"],
+                        inp["xdims"], tol=1e-13)
+    ev, conv = ex.energies(kfac, nev=3, eig_tol=1e-10)
+    assert conv
+    sizes = inp["xdims"]
+    lens = [sum(ml * mr for (_, _, ml, mr) in dd) for dd in sizes]
+
+    def hop(x):
+        parts, pos = [], 0
+        for dd, ln in zip(sizes, lens):
+            parts.append(O.bm_from_vec(x[pos:pos + ln], dd))
+            pos += ln
+        out = O.ApplyHeff(parts, kfac, inp["AL"], inp["AR"], inp["NL"], inp["h"], inp["d"], inp["HLtot"],
+                          inp["HRtot"], tol=1e-13)
+        return np.concatenate([np.concatenate([out[n][qi][1].reshape(-1, order="F") for (qi, _, _, _) in dd])
+                               for n, dd in enumerate(sizes)])
+
+    mtot = sum(lens)
+    ref = np.sort(eigsh(LinearOperator((mtot, mtot), matvec=hop, dtype=np.complex128), k=3, which="SA",
+                        tol=1e-11, return_eigenvectors=False))
+    assert np.abs(np.sort(ev) - ref).max() < 1e-8 * max(1.0, np.abs(ref).max()), (ev, ref)
