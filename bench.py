@@ -11,6 +11,8 @@ same sweeps from the same initial state and is reported beside it, with the ener
 of the two after the last sweep.
 
 --mode hac times H_AC applies only (ApplyHAvec; a step = 20 applies).
+--mode excitations converges the XXZ D=256 ground state and times the 4 lowest excitation
+energies in the Sz = +1 sector at --steps momenta (H_eff compiled into grouped-GEMM programs).
 --mode krylov times one bounded thick-restart Lanczos solve (eigs_rs, ncv 64, at most 8 restart
 cycles; FP64 at an unreachable tolerance, split-BF16 at its 2e-7 floor) on the synthetic H_AC,
 next to the same number of bare applies: the difference is the per-iteration
@@ -464,13 +466,65 @@ def run_krylov(args):
                       "launches_per_iteration": launches / na}), flush=True)
 
 
+def run_excitations(args):
+    """Excitation energies on a converged ground state (Excitations_main.cpp:255-297): XXZ D=256
+    (17 U(1) sectors, dims ~exp(-q^2/10)) converged by VumpsGPU to |grad| < 1e-10 (at most 120
+    sweeps), then for a sample of momenta p in [0, pi] the 4 lowest energies of H_eff in the
+    Sz = +1 sector (charge label K = 2) by the device Lanczos on H_eff's real form."""
+    import torch
+    from imps_cpp_tools_gb300 import blocks as B
+    from imps_cpp_tools_gb300 import configs
+    from imps_cpp_tools_gb300.excitations import ExcitationsGPU, HeffGPU, excitation_inputs
+    from imps_cpp_tools_gb300.vumps import VumpsGPU
+    ctx = B.Context(0)
+    ctx.set_stream(torch.cuda.current_stream())
+    model, fn, params = configs.WORKLOADS["xxz_d256"]
+    t0 = time.perf_counter()
+    v = VumpsGPU(ctx, model, dims0=fn(), seed=1, tolmin=1e-12, InvETol=1e-12, **params)
+    nsw = 0
+    for nsw in range(1, 121):
+        E, F, _ = v.sweep()
+        if F.max() < 1e-10:
+            break
+    torch.cuda.synchronize()
+    t_gs = time.perf_counter() - t0
+    t0 = time.perf_counter()
+    inp = excitation_inputs(v, (2,), tol=1e-12)
+    torch.cuda.synchronize()
+    t_inp = time.perf_counter() - t0
+    ex = ExcitationsGPU(ctx, inp["AL"], inp["AR"], inp["NL"], inp["HLtot"], inp["HRtot"], inp["h"], inp["d"],
+                        inp["xdims"], tol=1e-12)
+    ps = np.linspace(0.0, np.pi, max(args.steps, 1) + 2)[1:-1]
+    rows, t_tot, applies0 = [], 0.0, 0
+    for p in ps:
+        # compile + solve; the compile (host sector matching) is reported separately
+        tc = time.perf_counter()
+        HeffGPU(ctx, *ex.args, np.exp(1j * p), tol=1e-12)
+        t_compile = time.perf_counter() - tc
+        a0 = ex.applies
+        tq = time.perf_counter()
+        ev, conv = ex.energies(np.exp(1j * p), nev=4, eig_tol=1e-10)
+        torch.cuda.synchronize()
+        dt = time.perf_counter() - tq
+        t_tot += dt
+        rows.append({"p": float(p), "energies": [float(x) for x in ev], "converged": bool(conv), "s": dt,
+                     "compile_s": t_compile, "heff_applies": ex.applies - a0})
+    napp = sum(r["heff_applies"] for r in rows)
+    mtot = sum(r * c for dd in inp["xdims"] for (_, _, r, c) in dd)
+    print(json.dumps({"mode": "excitations", "workload": "XXZ D=256 ground state (VumpsGPU, %d sweeps, |grad| "
+                      "%.1e), K = Sz +1, 4 lowest states" % (nsw, float(F.max())), "mtot": mtot,
+                      "ground_state_s": t_gs, "inputs_s": t_inp, "momenta": rows,
+                      "s_per_momentum": t_tot / max(len(rows), 1), "ms_per_heff_apply": 1e3 * t_tot / max(napp, 1),
+                      "E0": inp["E0"]}), flush=True)
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
     ap.add_argument("--steps", type=int, default=47)
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
-    ap.add_argument("--mode", default="vumps", choices=["vumps", "hac", "krylov"])
+    ap.add_argument("--mode", default="vumps", choices=["vumps", "hac", "krylov", "excitations"])
     ap.add_argument("--workload", default="xxz_d512")
     ap.add_argument("--precision", default="bf16x6", choices=["fp64", "bf16x6"])
     ap.add_argument("--no-cpu", action="store_true")
@@ -482,6 +536,8 @@ def main():
         run_hac(args)
     elif args.mode == "krylov":
         run_krylov(args)
+    elif args.mode == "excitations":
+        run_excitations(args)
     else:
         run_vumps(args)
 
