@@ -25,6 +25,7 @@ STATUS = {0: "ok", 1: "not converged", -1: "bad argument", -2: "inconsistent sec
           -9: "problem exceeds the fixed scratch of the no-allocation entry point"}
 
 MEM_HOST, MEM_DEVICE = 0, 1
+WHICH = {"LM": 0, "LR": 1, "SR": 2}
 DIR_LEFT, DIR_RIGHT = 0, 1
 PREC_FP64, PREC_BF16X6 = 0, 1
 
@@ -81,6 +82,9 @@ _PROTOS = {
     "imps_tm_dominant": (c_int, [c_vp, c_vp, c_vp, c_int, c_dbl, c_int, P_dbl, P_int]),
     "imps_eigs_rs_op": (c_int, [c_vp, c_i64, APPLY_FN, c_vp, c_vp, c_int, c_int, c_dbl, c_int, c_int, P_dbl,
                                 c_vp, P_int]),
+    "imps_eigs_n": (c_int, [c_vp, c_vp, c_int, c_int, c_int, c_dbl, c_int, c_int, P_dbl, c_vp, c_vp, P_int]),
+    "imps_eigs_n_op": (c_int, [c_vp, c_i64, APPLY_FN, c_vp, c_vp, c_int, c_int, c_int, c_dbl, c_int, c_int,
+                               P_dbl, c_vp, c_vp, P_int]),
     "imps_plan_program": (c_int, [c_vp, c_int, P_i64, c_int, P_i32, P_i64, P_i64, P_dbl, C.POINTER(c_vp)]),
     "imps_plan_tm_mixed": (c_int, [c_vp, c_int, C.POINTER(c_vp), C.POINTER(c_vp), c_int, c_vp, c_vp,
                                    C.POINTER(c_vp)]),

@@ -18,6 +18,7 @@
 #include "imps_internal.h"
 #include "imps_krylov.h"
 #include "imps_tc.h"
+#include "imps_nonsym.h"
 #include "imps_tridiag.h"
 
 using namespace imps;
@@ -1001,6 +1002,243 @@ int imps_eigs_rs_op(imps_ctx* c, int64_t n, imps_apply_fn fn, void* user, double
     return rc < 0 ? rc : IMPS_OK;
   };
   return eigs_impl(c, nullptr, n, op, x, mem, nev, tol, ncv, maxit, evals, evecs, n_applies);
+}
+
+// ---- Arnoldi: eigs_n for the nev wanted eigenpairs of a real nonsymmetric operator ----
+// Restart of Krylov-Schur type (Stewart, SIAM J. Matrix Anal. Appl. 23 (2001) 601): at the end
+// of a cycle the kept Ritz vectors of the projected matrix G = V^T A V span an invariant
+// subspace of G; with an orthonormal basis Q of it (real and imaginary parts of complex pairs)
+// the kept basis is V Q, the kept block Q^T G Q and the coupling row h_m Q[m-1, :] to the
+// residual direction v_m, which becomes the next basis vector.  The full CGS2 columns keep
+// G = V^T A V exact up to rounding.  Convergence as ARPACK's dnconv (used by dnaupd):
+// |h_m y[m-1]| <= tol max(eps^(2/3), |theta|) for each of the nev wanted Ritz pairs.
+static int eign_impl(imps_ctx* c, imps_plan* p, int64_t n, const DevApply& op, const double* x0, int mem,
+                     int nev, int which, double tol, int ncv, int maxit, double* evals, double* evecs_re,
+                     double* evecs_im, int* n_applies) {
+  cudaStream_t st = c->stream;
+  if (n < 3 || nev < 1 || nev > 32 || nev > n - 2 || which < 0 || which > 2 || !evals) return IMPS_ERR_BAD_ARG;
+  int m = ncv > 0 ? ncv : std::max(20, 2 * nev + 1);  // eigs.cpp: NCV = min(max(20, 2 NEV + 1), N)
+  if (m > n) m = (int)n;
+  if (m > kMaxCols - 2) m = kMaxCols - 2;
+  if (m < nev + 2) return IMPS_ERR_BAD_ARG;  // dnaupd needs NCV - NEV >= 2
+  if (maxit <= 0) maxit = (int)std::min<int64_t>(n, 100000);  // restart cycles (eigs.cpp: MAXIT = N)
+  if (tol <= 0.0) tol = kEps;                                   // dnaupd: TOL <= 0 means machine precision
+  const int ld = m + 1;
+  const bool cb_arena = p == nullptr;
+  RC(arena_reserve(c, round256(n * 8) * (2 * (size_t)m + 3) + round256((size_t)ld * ld * 8) +
+                          round256((size_t)m * m * 8) + 4096, cb_arena));
+  Bump bp{cb_arena ? c->arena_cb : c->arena};
+  double* V = bp.take((size_t)n * (m + 1));
+  double* Wk = bp.take((size_t)n * m);
+  double* w = bp.take(n);
+  double* Hd = bp.take((size_t)ld * ld);
+  double* Qd = bp.take((size_t)m * m);
+  double* tmp = bp.take(ld);
+  double* nrm = c->dscal + 8;
+  int* bflag = c->dflag;
+  int* pin_flags = (int*)(c->hpin + kPinDoubles);
+  // the operator runs in FP64 unless the tolerance is above the split-BF16 floor
+  const int prec_saved = p ? p->prec : IMPS_PREC_FP64;
+  if (p && tol < kMixedEigTol) p->prec = IMPS_PREC_FP64;
+  struct Restore {
+    imps_plan* p;
+    int prec;
+    ~Restore() { if (p) p->prec = prec; }
+  } restore{p, prec_saved};
+
+  if (x0) {
+    CK(cudaMemcpyAsync(w, x0, n * 8, mem == IMPS_MEM_HOST ? cudaMemcpyHostToDevice : cudaMemcpyDeviceToDevice, st));
+  } else {
+    RC(kr_fill_random(w, n, 0x5EED0F1A4D0C0DEull, st));  // dnaupd starts from a random vector
+  }
+  CK(cudaMemsetAsync(bflag, 0, sizeof(int), st));
+  RC(kr_multidot(c->ws, w, n, 1, w, n, tmp, 0, nrm, st));
+  RC(kr_scale_inv(w, nrm, V, n, bflag, st));
+
+  std::vector<double> G((size_t)m * m, 0.0), Gs((size_t)m * m), wr(m), wi(m), Qh((size_t)m * m), B((size_t)m * m);
+  std::vector<imps::cplx> Y((size_t)m * m);  // Ritz vectors of G, column i for order[i]
+  std::vector<int> order;
+  const double eps23 = std::cbrt(kEps * kEps);
+  int kept = 0, applies = 0, cycles = 0, status = IMPS_WARN_NOT_CONVERGED, k = m;
+  double hm = 0.0, worst = 0.0;
+  while (true) {
+    for (int j = kept; j < m; ++j) {
+      RC(op(V + (size_t)j * n, w));
+      ++applies;
+      RC(kr_cgs2_step(c->ws, V, n, j + 1, w, n, Hd + (size_t)j * ld, tmp, V + (size_t)(j + 1) * n, bflag, st));
+    }
+    ++cycles;
+    CK(cudaMemcpyAsync(c->hpin, Hd + (size_t)kept * ld, (size_t)(m - kept) * ld * 8, cudaMemcpyDeviceToHost, st));
+    CK(cudaMemcpyAsync(pin_flags + 1, c->ws.err, sizeof(int), cudaMemcpyDeviceToHost, st));
+    CK(cudaStreamSynchronize(st));
+    if (pin_flags[1]) {  // a grid-barrier wait of the CGS2 step ran out: report, re-arm
+      CK(cudaMemsetAsync(c->ws.err, 0, sizeof(int), st));
+      return IMPS_ERR_TIMEOUT;
+    }
+    double gscale = 0.0;
+    for (int j = kept; j < m; ++j) {
+      const double* hc = c->hpin + (size_t)(j - kept) * ld;
+      for (int i = 0; i < m; ++i) G[i + (size_t)j * m] = i <= j + 1 && i < m ? hc[i] : 0.0;
+    }
+    hm = c->hpin[(size_t)(m - 1 - kept) * ld + m];
+    for (double g : G) {
+      if (!std::isfinite(g)) return IMPS_ERR_NAN;
+      gscale = std::max(gscale, std::fabs(g));
+    }
+    if (!std::isfinite(hm)) return IMPS_ERR_NAN;
+    // breakdown: an exactly invariant Krylov subspace of size k < m (later columns are void)
+    k = m;
+    for (int j = kept; j + 1 < m; ++j)
+      if (!(std::fabs(G[j + 1 + (size_t)j * m]) > 1e-14 * gscale)) {
+        k = j + 1;
+        break;
+      }
+    if (k < m) hm = 0.0;
+    for (int j = 0; j < k; ++j)
+      for (int i = 0; i < k; ++i) Gs[i + (size_t)j * k] = G[i + (size_t)j * m];
+    if (!imps::dense_eigvals(k, Gs.data(), wr.data(), wi.data())) return IMPS_ERR_NAN;
+    order = imps::order_ritz(k, wr.data(), wi.data(), which);
+    // kept set (real dimension), never splitting a conjugate pair
+    const int target = std::min(k, std::max(nev + 1, std::min(m - 2, nev + (m - nev) / 2)));
+    int nk = 0, nsel = 0;  // real dimension kept, Ritz values selected
+    while (nsel < k && nk < target) {
+      const int i = order[nsel];
+      nk += wi[i] != 0.0 ? 2 : 1;
+      nsel += wi[i] != 0.0 ? 2 : 1;
+    }
+    nsel = std::max(nsel, std::min(k, nev + (wi[order[std::min(nev, k) - 1]] > 0.0 ? 1 : 0)));
+    for (int s = 0; s < nsel; ++s) {
+      const int i = order[s];
+      imps::cplx* y = Y.data() + (size_t)s * m;
+      if (wi[i] < 0.0 && s > 0 && order[s - 1] >= 0 && wi[order[s - 1]] == -wi[i] && wr[order[s - 1]] == wr[i]) {
+        for (int r = 0; r < k; ++r) y[r] = std::conj(Y[(size_t)(s - 1) * m + r]);
+      } else {
+        imps::dense_eigvec(k, Gs.data(), gscale * k, imps::cplx(wr[i], wi[i]), y);
+      }
+    }
+    // convergence of the nev wanted pairs
+    int nconv = 0;
+    worst = 0.0;
+    for (int s = 0; s < std::min(nev, k); ++s) {
+      const int i = order[s];
+      const double res = std::fabs(hm) * std::abs(Y[(size_t)s * m + (k - 1)]);
+      worst = std::max(worst, res);
+      if (res <= tol * std::max(eps23, std::hypot(wr[i], wi[i]))) ++nconv;
+    }
+    if (nconv >= nev && k >= nev) {
+      status = IMPS_OK;
+      break;
+    }
+    if (k < m || cycles >= maxit) break;
+    // restart: orthonormal real basis of the kept invariant subspace (two MGS passes)
+    int q = 0;
+    for (int s = 0; s < nsel && q < m - 1; ++s) {
+      const int i = order[s];
+      if (wi[i] < 0.0) continue;  // the conjugate partner adds nothing new
+      for (int part = 0; part < (wi[i] > 0.0 ? 2 : 1); ++part) {
+        double* col = Qh.data() + (size_t)q * m;
+        for (int r = 0; r < k; ++r) col[r] = part ? Y[(size_t)s * m + r].imag() : Y[(size_t)s * m + r].real();
+        double n0 = 0.0;
+        for (int r = 0; r < k; ++r) n0 += col[r] * col[r];
+        n0 = std::sqrt(n0);
+        for (int pass = 0; pass < 2; ++pass)
+          for (int t = 0; t < q; ++t) {
+            const double* qt = Qh.data() + (size_t)t * m;
+            double d = 0.0;
+            for (int r = 0; r < k; ++r) d += qt[r] * col[r];
+            for (int r = 0; r < k; ++r) col[r] -= d * qt[r];
+          }
+        double n1 = 0.0;
+        for (int r = 0; r < k; ++r) n1 += col[r] * col[r];
+        n1 = std::sqrt(n1);
+        if (!(n1 > 1e-8 * n0)) continue;  // dependent (a defective cluster): drop
+        for (int r = 0; r < k; ++r) col[r] /= n1;
+        ++q;
+        if (q >= m - 1) break;
+      }
+    }
+    if (q < 1) break;
+    // kept block B = Q^T G Q and coupling row g = h_m Q[m-1, :]
+    for (int b = 0; b < q; ++b) {
+      std::vector<double> gq(k, 0.0);
+      const double* qb = Qh.data() + (size_t)b * m;
+      for (int j = 0; j < k; ++j)
+        for (int i = 0; i < k; ++i) gq[i] += G[i + (size_t)j * m] * qb[j];
+      for (int a = 0; a < q; ++a) {
+        const double* qa = Qh.data() + (size_t)a * m;
+        double acc = 0.0;
+        for (int i = 0; i < k; ++i) acc += qa[i] * gq[i];
+        B[a + (size_t)b * q] = acc;
+      }
+    }
+    for (int b = 0; b < q; ++b)
+      for (int r = 0; r < k; ++r) c->hpin[r + (size_t)b * k] = Qh[r + (size_t)b * m];
+    CK(cudaMemcpyAsync(Qd, c->hpin, (size_t)k * q * 8, cudaMemcpyHostToDevice, st));
+    RC(kr_basis_rotate(V, n, k, Qd, q, Wk, n, n, st));
+    CK(cudaMemcpyAsync(V, Wk, (size_t)q * n * 8, cudaMemcpyDeviceToDevice, st));
+    CK(cudaMemcpyAsync(V + (size_t)q * n, V + (size_t)m * n, n * 8, cudaMemcpyDeviceToDevice, st));
+    std::fill(G.begin(), G.end(), 0.0);
+    for (int b = 0; b < q; ++b) {
+      for (int a = 0; a < q; ++a) G[a + (size_t)b * m] = B[a + (size_t)b * q];
+      G[q + (size_t)b * m] = hm * Qh[(size_t)(k - 1) + (size_t)b * m];
+    }
+    kept = q;
+  }
+  // the staging buffer is reused below: wait for any rotation upload to be consumed
+  CK(cudaStreamSynchronize(st));
+  const int nout = std::min(nev, k);
+  for (int s = 0; s < nev; ++s) {
+    evals[2 * s] = s < nout ? wr[order[s]] : std::numeric_limits<double>::quiet_NaN();
+    evals[2 * s + 1] = s < nout ? wi[order[s]] : std::numeric_limits<double>::quiet_NaN();
+  }
+  if (evecs_re && nout > 0) {
+    for (int part = 0; part < 2; ++part) {
+      double* dst = part ? evecs_im : evecs_re;
+      if (!dst) continue;
+      for (int s = 0; s < nout; ++s)
+        for (int r = 0; r < k; ++r) {
+          const imps::cplx y = Y[(size_t)s * m + r];
+          c->hpin[r + (size_t)s * k] = part ? y.imag() : y.real();
+        }
+      CK(cudaMemcpyAsync(Qd, c->hpin, (size_t)k * nout * 8, cudaMemcpyHostToDevice, st));
+      if (mem == IMPS_MEM_HOST) {
+        RC(kr_basis_rotate(V, n, k, Qd, nout, Wk, n, n, st));
+        CK(cudaMemcpyAsync(dst, Wk, (size_t)nout * n * 8, cudaMemcpyDeviceToHost, st));
+      } else {
+        RC(kr_basis_rotate(V, n, k, Qd, nout, dst, n, n, st));
+      }
+      CK(cudaStreamSynchronize(st));
+    }
+  }
+  if (n_applies) *n_applies = applies;
+  if (debug_on())
+    fprintf(stderr, "[imps eigs_n] n=%lld which=%d nev=%d ncv=%d applies=%d cycles=%d theta0=%.15g%+.3gi res=%.3e status=%d\n",
+            (long long)n, which, nev, m, applies, cycles, evals[0], evals[1], worst, status);
+  return status;
+}
+
+int imps_eigs_n(imps_plan* p, const double* x0, int mem, int nev, int which, double tol, int ncv, int maxit,
+                double* evals, double* evecs_re, double* evecs_im, int* n_applies) {
+  if (!p || !evals) return IMPS_ERR_BAD_ARG;
+  const int kd = p->P.kind;
+  if (kd != PLAN_TM && !is_mixed_tm(p) && kd != PLAN_HAC && kd != PLAN_HC) return IMPS_ERR_BAD_ARG;
+  if (p->ctx->device < 0) return IMPS_ERR_NO_DEVICE;
+  const int64_t n = p->P.slots[p->P.n_in].nelem;
+  if (p->P.slots[p->P.n_out].nelem != n) return IMPS_ERR_BAD_ARG;
+  DevApply op = [p](const double* in, double* out) { return apply_dev(p, in, out); };
+  return eign_impl(p->ctx, p, n, op, x0, mem, nev, which, tol, ncv, maxit, evals, evecs_re, evecs_im, n_applies);
+}
+
+int imps_eigs_n_op(imps_ctx* c, int64_t n, imps_apply_fn fn, void* user, const double* x0, int mem, int nev,
+                   int which, double tol, int ncv, int maxit, double* evals, double* evecs_re, double* evecs_im,
+                   int* n_applies) {
+  if (!c || !fn || !evals) return IMPS_ERR_BAD_ARG;
+  if (c->device < 0) return IMPS_ERR_NO_DEVICE;
+  DevApply op = [fn, user](const double* in, double* out) {
+    const int rc = fn(user, in, out);
+    return rc < 0 ? rc : IMPS_OK;
+  };
+  return eign_impl(c, nullptr, n, op, x0, mem, nev, which, tol, ncv, maxit, evals, evecs_re, evecs_im, n_applies);
 }
 
 // ---- device GMRES (generic operator) ----

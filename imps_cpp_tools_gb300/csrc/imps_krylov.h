@@ -36,6 +36,7 @@ int kr_basis_rotate(const double* V, int64_t ldv, int m, const double* W, int kk
                     int64_t ldo, int64_t n, cudaStream_t st);
 int kr_scale_inv(const double* x, const double* nrm, double* y, int64_t n, int* flag, cudaStream_t st);
 int kr_axpby(double a, const double* x, double b, double* y, int64_t n, cudaStream_t st);
+int kr_fill_random(double* x, int64_t n, uint64_t seed, cudaStream_t st);
 int kr_proj_epilogue(const double* x, const double* t, const double* s, const double* rho, double* y,
                      int64_t n, cudaStream_t st);
 int kr_trace_prod(const KrylovWs& ws, const double* X, const double* R, const int64_t* boff,

@@ -631,6 +631,17 @@ __global__ void sign_first_kernel(const double* __restrict__ x, double* __restri
   if (threadIdx.x == 0 && blockIdx.x == 0) *s = x[0] < 0.0 ? -1.0 : 1.0;
 }
 
+// x[i] uniform in [-1, 1) from splitmix64(seed + i): a reproducible start vector
+__global__ void fill_random_kernel(double* __restrict__ x, int64_t n, uint64_t seed) {
+  for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x) {
+    uint64_t z = seed + 0x9E3779B97F4A7C15ull * (uint64_t)(i + 1);
+    z = (z ^ (z >> 30)) * 0xBF58476D1CE4E5B9ull;
+    z = (z ^ (z >> 27)) * 0x94D049BB133111EBull;
+    z ^= z >> 31;
+    x[i] = (double)(z >> 11) * (2.0 / 9007199254740992.0) - 1.0;
+  }
+}
+
 int grid_for(int64_t n) {
   int64_t g = (n + 255) / 256;
   if (g > 152 * 8) g = 152 * 8;
@@ -719,6 +730,12 @@ int kr_cgs2_step(const KrylovWs& ws, const double* V, int64_t ldv, int nc, doubl
 int kr_scale_inv(const double* x, const double* nrm, double* y, int64_t n, int* flag, cudaStream_t st) {
   imps::count_launch();
   scale_inv_kernel<<<grid_for(n), 256, 0, st>>>(x, nrm, y, n, flag);
+  return IMPS_OK;
+}
+
+int kr_fill_random(double* x, int64_t n, uint64_t seed, cudaStream_t st) {
+  imps::count_launch();
+  fill_random_kernel<<<grid_for(n), 256, 0, st>>>(x, n, seed);
   return IMPS_OK;
 }
 

@@ -387,9 +387,11 @@ class HeffProgram:
 
 class HeffGPU:
     """ApplyHeff on the device: the two programs of HeffProgram around two imps_invert_e_fac
-    solves on mixed transfer-matrix plans."""
+    solves on mixed transfer-matrix plans; with LM and RM (the dominant eigenmatrices of the
+    mixed TM, LRoverlaps) the solves are the projected imps_invert_e_proj_fac ones
+    (Excitations_helpers.hpp:83, 124: EBR with (LM, RM), EHBL with (LM^T, RM^T))."""
 
-    def __init__(self, ctx, AL, AR, NL, HLtot, HRtot, hnnz, d, xdims, kfac, tol=1e-14, maxit=0):
+    def __init__(self, ctx, AL, AR, NL, HLtot, HRtot, hnnz, d, xdims, kfac, tol=1e-14, maxit=0, LM=None, RM=None):
         import torch
         self.torch, self.ctx, self.d = torch, ctx, d
         self.tol, self.maxit = tol, maxit
@@ -419,6 +421,16 @@ class HeffGPU:
             self.plan_l.bind(2 + k, A_(self.AR, k))
             self.plan_l.bind(2 + Ns + k, A_(self.AL, k))
         self.stats = {"gmres_iters": 0}
+        self.proj = LM is not None and RM is not None
+        if self.proj:
+            # (rho_in, rho_out) of InvEfun_proj_fac: the EBR solve (dir r) takes (L, R) = (LM, RM),
+            # the EHBL solve (dir l) (R, L) = (RM^T, LM^T); rho_out pairs with x's blocks, rho_in
+            # with the transposed structure (InvEBlockFunctions.hpp:104-108)
+            tdev = lambda v: torch.from_numpy(np.ascontiguousarray(v, np.float64)).to("cuda")
+            bt = lambda X: {qo: (qi, M.T.copy()) for qi, (qo, M) in X.items()}
+            self.proj_r = (tdev(_rho_vec(self.lay_r, LM, inside=True)), tdev(_rho_vec(self.lay_r, RM, inside=False)))
+            self.proj_l = (tdev(_rho_vec(self.lay_l, bt(LM), inside=False)),
+                           tdev(_rho_vec(self.lay_l, bt(RM), inside=True)))
 
     def _op_view(self, ct):
         t = ct[0]
@@ -460,12 +472,18 @@ class HeffGPU:
         nr, nl = self.nr, self.nl
         rhs, es = self.buf[RHS], self.buf[ES]
         (off_r, off_ri, _), (off_l, off_li, _) = self.pr.rhs_planes()
-        it, _, conv_r = ops.InvertE_fac(self.plan_r, rhs[off_r:off_r + nr], rhs[off_ri:off_ri + nr], self.kfac,
-                                        es[0:nr], es[nr:2 * nr], self.tol, self.maxit)
-        self.stats["gmres_iters"] += it
-        it, _, conv_l = ops.InvertE_fac(self.plan_l, rhs[off_l:off_l + nl], rhs[off_li:off_li + nl],
-                                        self.kfac.conjugate(), es[2 * nr:2 * nr + nl], es[2 * nr + nl:2 * nr + 2 * nl],
-                                        self.tol, self.maxit)
+        xr, xl = (rhs[off_r:off_r + nr], rhs[off_ri:off_ri + nr]), (rhs[off_l:off_l + nl], rhs[off_li:off_li + nl])
+        yr, yl = (es[0:nr], es[nr:2 * nr]), (es[2 * nr:2 * nr + nl], es[2 * nr + nl:2 * nr + 2 * nl])
+        ck = self.kfac.conjugate()
+        if self.proj:
+            it, _, conv_r = ops.InvertE_proj_fac(self.plan_r, *xr, *self.proj_r, "r", self.kfac, *yr, self.tol,
+                                                 self.maxit)
+            self.stats["gmres_iters"] += it
+            it, _, conv_l = ops.InvertE_proj_fac(self.plan_l, *xl, *self.proj_l, "l", ck, *yl, self.tol, self.maxit)
+        else:
+            it, _, conv_r = ops.InvertE_fac(self.plan_r, *xr, self.kfac, *yr, self.tol, self.maxit)
+            self.stats["gmres_iters"] += it
+            it, _, conv_l = ops.InvertE_fac(self.plan_l, *xl, ck, *yl, self.tol, self.maxit)
         self.stats["gmres_iters"] += it
         self.plan_b.run()
         return conv_r and conv_l
@@ -476,13 +494,24 @@ class ExcitationsGPU:
     nev lowest eigenvalues of H_eff (eigs_n "SR" in the reference; H_eff is Hermitian, so here
     the device Lanczos on its real form over the [re | im] planes of X)."""
 
-    def __init__(self, ctx, AL, AR, NL, HLtot, HRtot, hnnz, d, xdims, tol=1e-14):
+    def __init__(self, ctx, AL, AR, NL, HLtot, HRtot, hnnz, d, xdims, tol=1e-14, LM=None, RM=None):
         self.ctx, self.args, self.tol = ctx, (AL, AR, NL, HLtot, HRtot, hnnz, d, xdims), tol
+        self.LM, self.RM = LM, RM
+        qi, qo = next((b[0], b[1]) for dd in xdims for b in dd)
+        self.K = tuple(b - a for a, b in zip(qi, qo))
         self.applies = 0
 
-    def energies(self, kfac, nev=4, eig_tol=1e-10, ncv=0, seed=1):
+    def projected(self, p):
+        """Excitations_main.cpp:263-268: the dominant subspace of the mixed TM is projected out of
+        the environment solves only at K = 0 and momentum p = 0 (|p| < 10 InvETol)."""
+        return self.LM is not None and all(k == 0 for k in self.K) and abs(p) < 10 * self.tol
+
+    def energies(self, kfac, nev=4, eig_tol=1e-10, ncv=0, seed=1, p=None):
+        """The nev lowest energies at kfac = e^{ip} (p: the momentum, default arg(kfac))."""
         import torch
-        H = HeffGPU(self.ctx, *self.args, kfac, tol=self.tol)
+        p = float(np.angle(kfac)) if p is None else float(p)
+        LM, RM = (self.LM, self.RM) if self.projected(p) else (None, None)
+        H = HeffGPU(self.ctx, *self.args, kfac, tol=self.tol, LM=LM, RM=RM)
         n = 2 * H.mtot
         xs, out = H.buf[XS], H.buf[OUT]
 
@@ -505,6 +534,95 @@ class ExcitationsGPU:
             if not out or abs(v - out[-1]) > 10 * eig_tol * max(abs(v), 1.0):
                 out.append(v)
         return out[:nev], conv and len(out) >= nev
+
+
+# ------------------------------------------------------------------------------------------------
+# dominant eigenmatrices of the mixed transfer matrix (EigsBlockFunctions.hpp:282-391,
+# Excitations_helpers.hpp:915-946)
+# ------------------------------------------------------------------------------------------------
+
+def _rho_vec(lay, M, inside):
+    """Vector of the BlockMat M paired block by block with the X layout ``lay``: rho_out blocks have
+    X's structure (key qin), rho_in blocks the transposed one (key qout)."""
+    parts = []
+    for (_, qi, qo, r, c) in _blocks(lay):
+        key, other, shape = (qo, qi, (c, r)) if inside else (qi, qo, (r, c))
+        if key not in M or tuple(M[key][0]) != other or M[key][1].shape != shape:
+            raise ValueError("LM/RM sectors do not match the environment structure")
+        parts.append(np.asarray(M[key][1], np.float64).reshape(-1, order="F"))
+    return np.concatenate(parts) if parts else np.zeros(0)
+
+
+def _mps_layout(A, nsym):
+    return B.Layout([(s, tuple(qi), tuple(bm[qi][0]), bm[qi][1].shape[0], bm[qi][1].shape[1])
+                     for s, bm in enumerate(A) for qi in sorted(bm)], nsym)
+
+
+def _mps_vec(A):
+    return np.concatenate([np.asarray(bm[qi][1], np.float64).reshape(-1, order="F") for bm in A for qi in sorted(bm)])
+
+
+def _mps_ml(A):
+    out = {}
+    for bm in A:
+        for qi, (qo, M) in bm.items():
+            out.setdefault(tuple(qi), M.shape[0])
+    return out
+
+
+def tm_mixed_eigs(ctx, A, Bm, direction, K, nev, mode="LM", tol=1e-14, ncv=0):
+    """TMmixedEigs(A, B, V, dir, K, nev, mode, tol) (EigsBlockFunctions.hpp:282-391) on the device:
+    the nev leading eigenpairs of the mixed unit-cell TM (ApplyTMmixedLeft/Right(A, B, X) over
+    the sites) in the charge sector K, by the device Arnoldi (imps_eigs_n) on a mixed-TM plan.
+    Sectors (q, q + K) for q in GetMl of A (dir r) or of B (dir l).  A, B: lists over sites of
+    host MPS tensors.  Returns (complex eigenvalues sorted by |lambda| (LM) or Re lambda (LR)
+    descending, the eigenvectors as complex BlockMats, the sector sizes, applies, converged)."""
+    import torch
+    if mode not in ("LM", "LR"):
+        raise ValueError("TMmixedEigs: wrong mode " + mode)
+    K = tuple(int(k) for k in K)
+    nsym = len(K)
+    diml, dimr = _mps_ml(A[0]), _mps_ml(Bm[0])
+    if direction == "l":
+        diml, dimr = dimr, diml
+    sizes = [(q, _kadd(q, K), diml[q], dimr[_kadd(q, K)]) for q in sorted(diml) if _kadd(q, K) in dimr]
+    if not sizes:
+        raise ValueError("TMmixedEigs: no TM eigenvalues for this quantum number")
+    lay = B.Layout([(0, qi, qo, ml, mr) for (qi, qo, ml, mr) in sizes], nsym)
+    lay_a, lay_b = [_mps_layout(a, nsym) for a in A], [_mps_layout(b, nsym) for b in Bm]
+    plan = B.plan_tm_mixed(ctx, lay_a, lay_b, 0 if direction == "l" else 1, lay, lay)
+    tdev = lambda v: torch.from_numpy(v).to("cuda")
+    ops_a, ops_b = [tdev(_mps_vec(a)) for a in A], [tdev(_mps_vec(b)) for b in Bm]
+    ns = len(A)
+    for k in range(ns):
+        plan.bind(2 + k, ops_a[k])
+        plan.bind(2 + ns + k, ops_b[k])
+    n = lay.nelem
+    ere = torch.zeros((nev, n), dtype=torch.float64, device="cuda")
+    eim = torch.zeros((nev, n), dtype=torch.float64, device="cuda")
+    vals, na, conv = ops.eigs_n(plan, nev, mode, tol, ncv=ncv, evecs_re=ere, evecs_im=eim)
+    vr, vi = ere.cpu().numpy(), eim.cpu().numpy()
+    V = []
+    for i in range(nev):
+        v = vr[i] + 1j * vi[i]
+        X, pos = {}, 0
+        for (qi, qo, ml, mr) in sizes:
+            X[qi] = (qo, v[pos:pos + ml * mr].reshape(mr, ml).T.copy())
+            pos += ml * mr
+        V.append(X)
+    return vals, V, sizes, na, conv
+
+
+def LRoverlaps(ctx, AL, AR, K, nev, OLtol=1e-14):
+    """LRoverlaps(LM, RM, AL, AR, K, nev, OLtol) (Excitations_helpers.hpp:915-946) on the device:
+    the dominant left (sector -K) and right (sector K) eigenmatrices of the mixed TM of AL and
+    AR, as real BlockMats, and the overlap OL = (Re OL_L + Re OL_R) / 2.  Returns
+    (LM, RM, OL, OL_L eigenvalues, OL_R eigenvalues, converged)."""
+    K = tuple(int(k) for k in K)
+    vl, VL, _, _, cl = tm_mixed_eigs(ctx, AL, AR, "l", tuple(-k for k in K), nev, "LM", OLtol)
+    vr, VR, _, _, cr = tm_mixed_eigs(ctx, AL, AR, "r", K, nev, "LM", OLtol)
+    real = lambda X: {qi: (qo, np.real(M).copy()) for qi, (qo, M) in X.items()}
+    return real(VL[0]), real(VR[0]), 0.5 * (vl[0].real + vr[0].real), vl, vr, cl and cr
 
 
 # ------------------------------------------------------------------------------------------------
@@ -588,10 +706,16 @@ def excitation_inputs(v, K, tol=1e-13):
     hs += [(i, i, -E0) for i in range(d * d) if i not in diag]
     hs.sort(key=lambda t: (t[1], t[0]))
     xd = [xdims_from_layouts(nsl[n], v.LA[(n + 1) % 2], tuple(K)) for n in range(2)]
-    host = dict(AL=[mps_to_host(AL[n], v.LA[n], d) for n in range(2)],
-                AR=[mps_to_host(AR[n], v.LA[n], d) for n in range(2)], NL=NL,
+    ALh = [mps_to_host(AL[n], v.LA[n], d) for n in range(2)]
+    ARh = [mps_to_host(AR[n], v.LA[n], d) for n in range(2)]
+    # overlap of AL and AR and the dominant mixed-TM eigenmatrices (Excitations_main.cpp:174-178);
+    # AR[0] *= sign(OL) makes the overlap positive (it leaves HRtot unchanged)
+    LM, RM, OL, _, _, _ = LRoverlaps(ctx, ALh, ARh, K, 2, 1e-14)
+    if OL < 0:
+        ARh[0] = [{qi: (qo, -M) for qi, (qo, M) in bm.items()} for bm in ARh[0]]
+    host = dict(AL=ALh, AR=ARh, NL=NL,
                 HLtot=[bd_to_host(HLtot[0], v.LB[1]), bd_to_host(HLtot[1], v.LB[0])],
                 HRtot=[bd_to_host(HRtot[0], v.LB[0]), bd_to_host(HRtot[1], v.LB[1])],
-                h=hs, d=d, xdims=xd, E0=E0)
+                h=hs, d=d, xdims=xd, E0=E0, LM=LM, RM=RM, OL=OL)
     return host
 

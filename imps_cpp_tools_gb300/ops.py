@@ -8,6 +8,8 @@ from __future__ import annotations
 
 import ctypes as C
 
+import numpy as np
+
 from . import _native as N
 from .blocks import _dptr
 
@@ -67,6 +69,47 @@ def eigs_rs_op(ctx, n, apply, x, nev=1, tol=1e-12, ncv=0, maxit=0, evecs=None):
     st = N.call("imps_eigs_rs_op", ctx.handle, int(n), fn, None, _dptr(x), N.MEM_DEVICE, int(nev), float(tol), int(ncv),
                 int(maxit), ev, None if evecs is None else _dptr(evecs), C.byref(na))
     return [ev[i] for i in range(nev)], na.value, st == 0
+
+
+def _eigs_n_result(ev, nev, na, st):
+    vals = np.array([complex(ev[2 * i], ev[2 * i + 1]) for i in range(nev)])
+    return vals, na.value, st == 0
+
+
+def eigs_n(plan, nev=1, which="LM", tol=1e-14, x0=None, ncv=0, maxit=0, evecs_re=None, evecs_im=None):
+    """eigs_n(fun, N, vals, vecs, nev, whch, tol, x0) (eigs.cpp:193-342) for the square operator of
+    ``plan`` (TM, mixed TM, H_AC, H_C) by the device Arnoldi.  x0: optional device start vector;
+    evecs_re / evecs_im: optional device (nev, n) tensors receiving the Ritz vectors.  Returns
+    (complex eigenvalues sorted by ``which``, applies, converged)."""
+    ev = (C.c_double * (2 * nev))()
+    na = C.c_int()
+    st = N.call("imps_eigs_n", plan.handle, None if x0 is None else _dptr(x0), N.MEM_DEVICE, int(nev),
+                N.WHICH[which], float(tol), int(ncv), int(maxit), ev,
+                None if evecs_re is None else _dptr(evecs_re), None if evecs_im is None else _dptr(evecs_im),
+                C.byref(na))
+    return _eigs_n_result(ev, nev, na, st)
+
+
+def eigs_n_op(ctx, n, apply, nev=1, which="LM", tol=1e-14, x0=None, ncv=0, maxit=0, evecs_re=None,
+              evecs_im=None):
+    """eigs_n for an operator given as a Python callable apply(in_ptr, out_ptr) on device
+    pointers, as eigs_rs_op."""
+    ev = (C.c_double * (2 * nev))()
+    na = C.c_int()
+
+    def cb(user, pin, pout):
+        try:
+            apply(pin, pout)
+            return 0
+        except Exception:  # a failing apply aborts the solve with an error status
+            return -3
+
+    fn = N.APPLY_FN(cb)
+    st = N.call("imps_eigs_n_op", ctx.handle, int(n), fn, None, None if x0 is None else _dptr(x0), N.MEM_DEVICE,
+                int(nev), N.WHICH[which], float(tol), int(ncv), int(maxit), ev,
+                None if evecs_re is None else _dptr(evecs_re), None if evecs_im is None else _dptr(evecs_im),
+                C.byref(na))
+    return _eigs_n_result(ev, nev, na, st)
 
 
 def InvertE_fac(plan, x_re, x_im, fac, y_re, y_im, tol, maxit=0, krylov=0):

@@ -177,6 +177,24 @@ typedef int (*imps_apply_fn)(void* user, const double* in, double* out);
  * [re; im] (every eigenvalue twice; a Lanczos run from one start vector finds each once). */
 int imps_eigs_rs_op(imps_ctx* ctx, int64_t n, imps_apply_fn fn, void* user, double* x, int mem, int nev,
                     double tol, int ncv, int maxit, double* evals, double* evecs, int* n_applies);
+/* eigs_n(fun, N, vals, vecs, nev, whch, tol, x0) (eigs.cpp:193-342, real nonsymmetric
+ * operator, ARPACK dnaupd/dneupd) on the device: Arnoldi with CGS2 orthogonalisation and a
+ * Krylov-Schur restart, convergence as dnaupd (Ritz estimate <= tol max(eps^(2/3), |theta|)),
+ * ncv = 0: min(max(20, 2 nev + 1), N), maxit = 0: N restart cycles.  which: IMPS_WHICH_LM
+ * (largest modulus), IMPS_WHICH_LR (largest real part), IMPS_WHICH_SR (smallest real part).
+ * evals (host, 2 nev doubles: re, im interleaved as std::complex) sorted by `which`, conjugate
+ * pairs adjacent (+im first); evecs_re / evecs_im (mem, n x nev column-major, either may be
+ * NULL): the Ritz vectors, unit 2-norm, largest-modulus component real and positive.  x0 (mem,
+ * n) or NULL for a fixed pseudo-random start.  imps_eigs_n takes any square plan (TM, mixed
+ * TM, H_AC, H_C); imps_eigs_n_op an operator callback as imps_eigs_rs_op. */
+#define IMPS_WHICH_LM 0
+#define IMPS_WHICH_LR 1
+#define IMPS_WHICH_SR 2
+int imps_eigs_n(imps_plan* op, const double* x0, int mem, int nev, int which, double tol, int ncv, int maxit,
+                double* evals, double* evecs_re, double* evecs_im, int* n_applies);
+int imps_eigs_n_op(imps_ctx* ctx, int64_t n, imps_apply_fn fn, void* user, const double* x0, int mem, int nev,
+                   int which, double tol, int ncv, int maxit, double* evals, double* evecs_re, double* evecs_im,
+                   int* n_applies);
 /* InvertE_proj (InvEBlockFunctions.hpp:201-266) on a TM plan: solves
  *  dir l: y (1 - T + |R)(L|) = x (1 - |R)(L|),  dir r: (1 - T + |R)(L|) y = (1 - |R)(L|) x
  * with restarted GMRES (Krylov size `krylov`, 0 = 40); y holds y0 on entry (NULL = zeros). */

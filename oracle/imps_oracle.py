@@ -944,6 +944,80 @@ def TMDominantEig(MPSarr, dims, direction, tol=1e-14, x0=None):
     return float(np.real(vals[0])), V
 
 
+def mps_ml(A):
+    """MPSBlockMat::GetMl (MPSBlockMat.hpp:281-304): left charge -> left dimension over all s."""
+    out = {}
+    for bm in A:
+        for qi, (qo, M) in bm.items():
+            out.setdefault(qi, M.shape[0])
+    return out
+
+
+def mps_mr(A):
+    """MPSBlockMat::GetMr (MPSBlockMat.hpp:306-323)."""
+    out = {}
+    for bm in A:
+        for qi, (qo, M) in bm.items():
+            out.setdefault(qo, M.shape[1])
+    return out
+
+
+def eigs_n(fun, N, nev, which="LM", tol=1e-14, x0=None, ncv=0, maxit=0):
+    """eigs.cpp:193-342: dnaupd/dneupd (real nonsymmetric) with ncv = min(max(20, 2 nev + 1), N)
+    and maxit = N; returns (complex eigenvalues, complex eigenvectors as columns)."""
+    from scipy.sparse.linalg import LinearOperator, eigs
+    if ncv <= 0:
+        ncv = min(max(20, 2 * nev + 1), N)
+    maxit = N if maxit <= 0 else min(maxit, N)
+    op = LinearOperator((N, N), matvec=lambda v: fun(np.real(np.asarray(v).ravel())), dtype=np.float64)
+    if x0 is None:
+        x0 = np.random.default_rng(0).standard_normal(N)  # eigs.cpp: RESID = randn
+    return eigs(op, k=nev, which=which, tol=tol, v0=x0, ncv=ncv, maxiter=maxit)
+
+
+def TMmixedEigs(A, B, direction, K, nev, mode="LM", tol=1e-14, x0=None):
+    """EigsBlockFunctions.hpp:282-391: the nev leading eigenpairs of the mixed unit-cell TM in the
+    charge sector K.  Sectors (q, q + K) for q in diml with q + K in dimr, where diml, dimr =
+    GetMl of A, B (swapped for dir l); TMMult over the vectorisation; eigs_n, then sorted by
+    |lambda| (LM) or Re lambda (LR) descending.  Returns (vals, [complex BlockMats])."""
+    if mode not in ("LM", "LR"):
+        raise ValueError("TMmixedEigs: wrong mode " + mode)
+    diml, dimr = mps_ml(A[0]), mps_ml(B[0])
+    if mps_mr(A[-1]) != diml or mps_mr(B[-1]) != dimr:
+        raise ValueError("left and right end of A, B need to have same dimensions")
+    if direction == "l":
+        diml, dimr = dimr, diml
+    sizes = [(q, kadd(q, K), diml[q], dimr[kadd(q, K)]) for q in sorted(diml) if kadd(q, K) in dimr]
+    if not sizes:
+        raise ValueError("TMmixedEigs: no TM eigenvalues for this quantum number")
+    D_tot = sum(ml * mr for (_, _, ml, mr) in sizes)
+    if direction == "l":
+        f = lambda v: bm_vec(ApplyTMmixedLeftUC(A, B, bm_from_vec(v, sizes)))
+    else:
+        f = lambda v: bm_vec(ApplyTMmixedRightUC(A, B, bm_from_vec(v, sizes)))
+    v0 = bm_vec(x0) if x0 is not None and bm_sizes(x0) == sizes else None
+    vals, vecs = eigs_n(f, D_tot, nev, mode, tol, v0)
+    order = np.argsort(-np.abs(vals), kind="stable") if mode == "LM" else np.argsort(-vals.real, kind="stable")
+    vals, vecs = vals[order], vecs[:, order]
+    V = [bm_from_vec(vecs[:, i], sizes) for i in range(len(vals))]
+    return vals, V, sizes
+
+
+def bm_real(X):
+    """BlockMat<KT,Real>(BlockMat<KT,Complex>) (BlockObj.hpp:612-629): the real part."""
+    return {qi: (qo, np.real(M).copy()) for qi, (qo, M) in X.items()}
+
+
+def LRoverlaps(AL, AR, K, nev, OLtol=1e-14):
+    """Excitations_helpers.hpp:915-946: the dominant left (charge -K) and right (charge K)
+    eigenmatrices LM, RM of the mixed TMs of AL and AR (real parts) and the overlap
+    OL = (Re OL_L + Re OL_R) / 2.  Returns (LM, RM, OL, OLLv, OLRv)."""
+    OLLv, VL, _ = TMmixedEigs(AL, AR, "l", tuple(-k for k in K), nev, "LM", OLtol)
+    OLRv, VR, _ = TMmixedEigs(AL, AR, "r", tuple(K), nev, "LM", OLtol)
+    LM, RM = bm_real(VL[0]), bm_real(VR[0])
+    return LM, RM, 0.5 * (OLLv[0].real + OLRv[0].real), OLLv, OLRv
+
+
 # ----------------------------------------------------------------------------------------------
 # per-sector decompositions (helpers.hpp:181-195, MPSBlockUtilities.hpp:78-340, BlockObj.hpp:2422-2541)
 # ----------------------------------------------------------------------------------------------

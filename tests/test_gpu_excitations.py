@@ -219,6 +219,8 @@ def test_excitations_from_converged_vumps_state(cuda_ctx):
             break
     assert F.max() < 1e-10
     inp = excitation_inputs(v, (2,), tol=1e-13)
+    # the overlap of the K = +-2 sectors only sets the sign of AR[0] (Excitations_main.cpp:177-178)
+    assert 0.0 < abs(inp["OL"]) < 1.0
     # HeffConstants against the oracle on the same (downloaded) state
     C0 = O.bd_from_vec(v.C[0].cpu().numpy(), [(tuple(b[1]), b[3]) for b in v.LB[0].blocks])
     R = O.bd_mul(C0, O.bd_t(C0))
@@ -243,6 +245,153 @@ def test_excitations_from_converged_vumps_state(cuda_ctx):
             pos += ln
         out = O.ApplyHeff(parts, kfac, inp["AL"], inp["AR"], inp["NL"], inp["h"], inp["d"], inp["HLtot"],
                           inp["HRtot"], tol=1e-13)
+        return np.concatenate([np.concatenate([out[n][qi][1].reshape(-1, order="F") for (qi, _, _, _) in dd])
+                               for n, dd in enumerate(sizes)])
+
+    mtot = sum(lens)
+    ref = np.sort(eigsh(LinearOperator((mtot, mtot), matvec=hop, dtype=np.complex128), k=3, which="SA",
+                        tol=1e-11, return_eigenvectors=False))
+    assert np.abs(np.sort(ev) - ref).max() < 1e-8 * max(1.0, np.abs(ref).max()), (ev, ref)
+    # K = 0, p = 0: the projected case from the same state; the overlap of AL and AR is +-1 and,
+    # the state being a variational minimum, H_eff - E0 is positive on the ansatz space
+    inp0 = excitation_inputs(v, (0,), tol=1e-13)
+    assert abs(abs(inp0["OL"]) - 1.0) < 1e-8
+    ex0 = ExcitationsGPU(cuda_ctx, inp0["AL"], inp0["AR"], inp0["NL"], inp0["HLtot"], inp0["HRtot"], inp0["h"],
+                         inp0["d"], inp0["xdims"], tol=1e-13, LM=inp0["LM"], RM=inp0["RM"])
+    ev0, conv0 = ex0.energies(1.0 + 0j, nev=2, eig_tol=1e-10)
+    assert conv0 and ev0[0] > -1e-6, ev0
+
+
+def _dense_op(ctx, M):
+    """Device callback applying the dense matrix M (the context shares torch's stream)."""
+    import ctypes as C
+    import torch
+    from imps_cpp_tools_gb300 import _native as N
+    Md = torch.tensor(M, dtype=torch.float64, device="cuda")
+    n = M.shape[0]
+    xin = torch.zeros(n, dtype=torch.float64, device="cuda")
+    keep = {}
+
+    def apply(pin, pout):
+        N.call("imps_axpby", ctx.handle, 1.0, C.c_void_p(pin), 0.0, C.c_void_p(xin.data_ptr()), n)
+        keep["y"] = Md @ xin
+        N.call("imps_axpby", ctx.handle, 1.0, C.c_void_p(keep["y"].data_ptr()), 0.0, C.c_void_p(pout), n)
+    return apply
+
+
+@pytest.mark.parametrize("which,want", [("LM", [3.0, 2.5 + 1j, 2.5 - 1j, -2.6]),
+                                        ("LR", [3.0, 2.5 + 1j, 2.5 - 1j, 1.5]),
+                                        ("SR", [-2.6, -1.9, -1.2 + 0.5j, -1.2 - 0.5j])])
+def test_eigs_n_dense_spectrum(cuda_ctx, which, want):
+    """eigs_n (eigs.cpp:193-342) by the device Arnoldi on a real nonsymmetric matrix with a known
+    spectrum (real eigenvalues and conjugate pairs): values in the requested order, unit-norm
+    eigenvectors with small residuals."""
+    import torch
+    rng = np.random.default_rng(3)
+    n = 300
+    D = np.zeros((n, n))
+    specials = [3.0, -2.6, 1.5, -1.9]
+    for i, l in enumerate(specials):
+        D[i, i] = l
+    for i, (a, b) in enumerate([(2.5, 1.0), (-1.2, 0.5)]):
+        j = 4 + 2 * i
+        D[j:j + 2, j:j + 2] = [[a, b], [-b, a]]
+    D[8:, 8:] = np.diag(rng.uniform(-1.0, 1.0, n - 8))
+    X = np.eye(n) + 0.1 * rng.standard_normal((n, n))
+    M = X @ D @ np.linalg.inv(X)
+    nev = 4
+    ere = torch.zeros((nev, n), dtype=torch.float64, device="cuda")
+    eim = torch.zeros((nev, n), dtype=torch.float64, device="cuda")
+    vals, na, conv = ops.eigs_n_op(cuda_ctx, n, _dense_op(cuda_ctx, M), nev=nev, which=which, tol=1e-13,
+                                   ncv=30, evecs_re=ere, evecs_im=eim)
+    assert conv and na > 0
+    assert np.abs(vals - np.array(want)).max() < 1e-10, vals
+    V = host(ere) + 1j * host(eim)
+    for i in range(nev):
+        assert abs(np.linalg.norm(V[i]) - 1.0) < 1e-12
+        assert np.linalg.norm(M @ V[i] - vals[i] * V[i]) < 1e-9 * np.linalg.norm(M, 2)
+
+
+@pytest.mark.parametrize("direction", ["l", "r"])
+@pytest.mark.parametrize("K", [(0,), (2,)])
+def test_tm_mixed_eigs_matches_arpack(cuda_ctx, state, direction, K):
+    """TMmixedEigs (EigsBlockFunctions.hpp:282-391): the device Arnoldi on the mixed-TM plan
+    against ARPACK (scipy, the library eigs.cpp drives) on the oracle's mixed TM."""
+    from imps_cpp_tools_gb300.excitations import tm_mixed_eigs
+    AL, AR = state["AL"], state["AR"]
+    vg, Vg, sg, na, conv = tm_mixed_eigs(cuda_ctx, AL, AR, direction, K, 3, "LM", 1e-13)
+    vo, Vo, so = O.TMmixedEigs(AL, AR, direction, K, 3, "LM", 1e-13)
+    assert conv and sg == so
+    for a in vg:  # each device eigenvalue has an ARPACK partner (conjugate pairs may swap)
+        assert np.abs(vo - a).min() < 1e-10 * max(1.0, abs(a)), (vg, vo)
+    j = int(np.argmin(np.abs(vo - vg[0])))  # the partner (conjugates may be listed either way)
+    a, b = O.bm_vec(Vg[0]), O.bm_vec(Vo[j])
+    assert abs(abs(np.vdot(a, b)) / (np.linalg.norm(a) * np.linalg.norm(b)) - 1.0) < 1e-9
+    res = O.bm_vec(O.ApplyTMmixedLeftUC(AL, AR, Vg[0]) if direction == "l" else
+                   O.ApplyTMmixedRightUC(AL, AR, Vg[0])) - vg[0] * a
+    assert np.linalg.norm(res) < 1e-11
+
+
+def test_lroverlaps_on_device(cuda_ctx, state):
+    """LRoverlaps (Excitations_helpers.hpp:915-946): overlap and dominant eigenmatrices against
+    the oracle's (real parts; the eigenvectors' sign is free)."""
+    from imps_cpp_tools_gb300.excitations import LRoverlaps
+    AL, AR = state["AL"], state["AR"]
+    LM, RM, OL, vl, vr, conv = LRoverlaps(cuda_ctx, AL, AR, (0,), 2)
+    LMo, RMo, OLo, _, _ = O.LRoverlaps(AL, AR, (0,), 2)
+    assert conv and abs(OL - OLo) < 1e-12
+    for X, Y in ((LM, LMo), (RM, RMo)):
+        a, b = O.bm_vec(X), O.bm_vec(Y)
+        assert min(np.abs(a - b).max(), np.abs(a + b).max()) < 1e-10
+
+
+def _proj_setup():
+    from tests.test_oracle_excitations import excitation_setup
+    e = excitation_setup((0,), dims0={(-2,): 3, (0,): 5, (2,): 3})
+    LM, RM, OL, _, _ = O.LRoverlaps(e["AL"], e["AR"], (0,), 2)
+    return e, LM, RM
+
+
+def test_projected_heff_apply_matches_oracle(cuda_ctx):
+    """p = 0, K = 0: ApplyHeff with the projected environment solves (InvertE_proj_fac with LM,
+    RM) on the device against the oracle."""
+    from imps_cpp_tools_gb300.excitations import HeffGPU
+    from tests.test_oracle_excitations import rand_x
+    e, LM, RM = _proj_setup()
+    H = HeffGPU(cuda_ctx, e["AL"], e["AR"], e["NL"], e["HLtot"], e["HRtot"], e["h"], e["d"], e["xdims"], 1.0 + 0j,
+                tol=1e-13, LM=LM, RM=RM)
+    X = rand_x(e["xdims"], np.random.default_rng(13))
+    H.x_to_planes([O.bm_vec(x) for x in X])
+    assert H.apply()
+    got = H.y_from_planes()
+    ref = O.ApplyHeff(X, 1.0 + 0j, e["AL"], e["AR"], e["NL"], e["h"], e["d"], e["HLtot"], e["HRtot"], LM=LM, RM=RM,
+                      tol=1e-13)
+    for n, dims in enumerate(e["xdims"]):
+        refv = np.concatenate([ref[n][qi][1].reshape(-1, order="F") for (qi, _, _, _) in dims])
+        assert np.linalg.norm(got[n] - refv) / np.linalg.norm(refv) < 1e-9, n
+
+
+def test_projected_energies_match_oracle(cuda_ctx):
+    """The excitation energies at p = 0, K = 0 (the projected case of Excitations_main.cpp:
+    263-279) against ARPACK on the oracle's projected H_eff."""
+    from scipy.sparse.linalg import LinearOperator, eigsh
+    from imps_cpp_tools_gb300.excitations import ExcitationsGPU
+    e, LM, RM = _proj_setup()
+    ex = ExcitationsGPU(cuda_ctx, e["AL"], e["AR"], e["NL"], e["HLtot"], e["HRtot"], e["h"], e["d"], e["xdims"],
+                        tol=1e-13, LM=LM, RM=RM)
+    assert ex.projected(0.0) and not ex.projected(0.3)
+    ev, conv = ex.energies(1.0 + 0j, nev=3, eig_tol=1e-10)
+    assert conv
+    sizes = e["xdims"]
+    lens = [sum(ml * mr for (_, _, ml, mr) in dd) for dd in sizes]
+
+    def hop(x):
+        parts, pos = [], 0
+        for dd, ln in zip(sizes, lens):
+            parts.append(O.bm_from_vec(x[pos:pos + ln], dd))
+            pos += ln
+        out = O.ApplyHeff(parts, 1.0 + 0j, e["AL"], e["AR"], e["NL"], e["h"], e["d"], e["HLtot"], e["HRtot"], LM=LM,
+                          RM=RM, tol=1e-13)
         return np.concatenate([np.concatenate([out[n][qi][1].reshape(-1, order="F") for (qi, _, _, _) in dd])
                                for n, dd in enumerate(sizes)])
 

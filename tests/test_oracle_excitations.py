@@ -167,3 +167,45 @@ def test_heff_program_tables_match_oracle(K, p):
         got = bufs[EX.OUT][xo:xo + nn] + 1j * bufs[EX.OUT][xo + nn:xo + 2 * nn]
         refv = np.concatenate([ref[n][qi][1].reshape(-1, order="F") for (qi, _, _, _) in dims])
         assert np.linalg.norm(got - refv) / np.linalg.norm(refv) < 1e-9, n
+
+
+def test_lroverlaps_dominant_eigenmatrices(state):
+    """LRoverlaps at K = 0 (Excitations_helpers.hpp:915-946): for AL C = C AR the dominant left
+    and right eigenmatrices of the mixed TM of AL and AR are C^T and C (bond 0), overlap 1; the
+    eigen-relations hold for the oracle's ARPACK eigenpairs."""
+    AL, AR, C0 = state["AL"], state["AR"], state["C"][-1]
+    LM, RM, OL, OLLv, OLRv = O.LRoverlaps(AL, AR, (0,), 3)
+    assert abs(abs(OL) - 1.0) < 1e-12 and abs(OLLv[0].imag) < 1e-12 and abs(OLRv[0].imag) < 1e-12
+    assert np.all(np.abs(OLLv[1:]) <= np.abs(OLLv[0]) + 1e-12)
+    res_l = O.bm_add(O.ApplyTMmixedLeftUC(AL, AR, LM), O.bm_scale(LM, -OLLv[0].real))
+    res_r = O.bm_add(O.ApplyTMmixedRightUC(AL, AR, RM), O.bm_scale(RM, -OLRv[0].real))
+    assert np.linalg.norm(O.bm_vec(res_l)) < 1e-12 and np.linalg.norm(O.bm_vec(res_r)) < 1e-12
+    Cm = {q: (q, M) for q, M in C0.items()}
+    for X, ref in [(LM, O.bm_t(Cm)), (RM, Cm)]:
+        a, b = O.bm_vec(X), O.bm_vec(ref)
+        assert abs(abs(a @ b) - np.linalg.norm(a) * np.linalg.norm(b)) < 1e-11
+
+
+def test_lroverlaps_charge_offset_sectors(state):
+    """K != 0: the left problem runs in sector -K, the right one in K; sizes follow XDims-style
+    pairing (q, q + K) and the leading overlaps are below 1 in modulus."""
+    AL, AR = state["AL"], state["AR"]
+    vl, VL, sl = O.TMmixedEigs(AL, AR, "l", (-2,), 2, "LM", 1e-13)
+    vr, VR, sr = O.TMmixedEigs(AL, AR, "r", (2,), 2, "LM", 1e-13)
+    assert all(qo == (q[0] - 2,) for (q, qo, _, _) in sl) and all(qo == (q[0] + 2,) for (q, qo, _, _) in sr)
+    assert abs(vl[0]) < 1 - 1e-6 and abs(abs(vl[0]) - abs(vr[0])) < 1e-10
+
+
+def test_projected_heff_is_hermitian():
+    """p = 0, K = 0: ApplyHeff with the projected environment solves (LM, RM from LRoverlaps) is
+    Hermitian in the X inner product."""
+    e = excitation_setup((0,))
+    LM, RM, OL, _, _ = O.LRoverlaps(e["AL"], e["AR"], (0,), 2)
+    assert OL > 0
+    rng = np.random.default_rng(5)
+    X, Y = rand_x(e["xdims"], rng), rand_x(e["xdims"], rng)
+    args = (1.0 + 0j, e["AL"], e["AR"], e["NL"], e["h"], e["d"], e["HLtot"], e["HRtot"])
+    HX = O.ApplyHeff(X, *args, LM=LM, RM=RM, tol=1e-13)
+    HY = O.ApplyHeff(Y, *args, LM=LM, RM=RM, tol=1e-13)
+    a, b = x_inner(Y, HX, e["xdims"]), x_inner(HY, X, e["xdims"])
+    assert abs(a - b) < 1e-10 * abs(a), (a, b)
