@@ -1669,7 +1669,13 @@ int imps_sector_svd(imps_plan* p, const double* A, double* U, double* S, double*
   cudaStream_t st = p->ctx->stream;
   CK(cudaMemsetAsync(D->dstatus, 0, sizeof(int), st));
   RC(dc_gather(D->d_ent, (int)D->ent.size(), A, D->dA, st));
-  RC(dc_svd(D->d_mats, (int)D->mats.size(), D->dA, S ? S : D->dS, D->dR, D->dW, D->dstatus, st));
+  int maxN = 0;
+  int64_t maxMN = 0;
+  for (const DenseMat& m : D->mats) {
+    maxN = std::max(maxN, (int)m.N);
+    maxMN = std::max(maxMN, (int64_t)m.M * m.N);
+  }
+  RC(dc_svd(D->d_mats, (int)D->mats.size(), maxN, maxMN, D->dA, S ? S : D->dS, D->dR, D->dW, D->dstatus, st));
   if (U) RC(dc_scatter(D->d_ent, (int)D->ent.size(), D->dA, U, st));
   if (Viso) {
     if (D->dir == 0) RC(dc_transpose_sq(D->d_mats, (int)D->mats.size(), D->dR, Viso, st));  // V^T

@@ -60,8 +60,13 @@ int build_decomp(DecompPlan& D, const Layout& A, int dir);
 int dc_gather(const GatherEntry* d_ent, int nent, const double* src, double* dense, cudaStream_t st);
 int dc_scatter(const GatherEntry* d_ent, int nent, const double* dense, double* dst, cudaStream_t st);
 int dc_qr(const DenseMat* d_mats, int nmat, double* A, double* Q, double* R, int transpose_r, cudaStream_t st);
-int dc_svd(const DenseMat* d_mats, int nmat, double* U, double* S, double* V, double* W, int* status,
-           cudaStream_t st);
+// Largest sector dimension N handled by the shared-memory SVD (R and V, N x N each, in shared
+// memory); larger sectors use the global-memory Jacobi kernel.
+constexpr int kJacobiMaxN = 118;
+// Largest N of the mixed-precision SVD (R, V and an FP32 / scratch square in shared memory).
+constexpr int kMixedMaxN = 96;
+int dc_svd(const DenseMat* d_mats, int nmat, int maxN, int64_t maxMN, double* U, double* S, double* V, double* W,
+           int* status, cudaStream_t st);
 int dc_colscale(const DenseMat* d_mats, int nmat, double* X, const double* S, double power, cudaStream_t st);
 int dc_transpose_sq(const DenseMat* d_mats, int nmat, const double* X, double* Y, cudaStream_t st);
 int dc_nullspace(const DenseMat* d_mats, int nmat, double* A, double* NS, cudaStream_t st);
