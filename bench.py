@@ -323,11 +323,14 @@ def run_vumps(args):
     stream = torch.cuda.current_stream()
     ctx.set_stream(stream)
 
-    # plain FP64 path and the chosen split-BF16 path, from the same seeded initial state
-    r64 = _run_vumps(torch, "fp64", args.steps, args.warmup, stream)
+    # the headline precision (timed with clocks and end to end) and the other one for comparison,
+    # from the same seeded initial state
+    other = "bf16x6" if args.precision == "fp64" else "fp64"
+    roth = _run_vumps(torch, other, args.steps, args.warmup, stream)
     if ws > 1:
         dist.barrier()
     rmx = _run_vumps(torch, args.precision, args.steps, args.warmup, stream, ClockSampler(local), e2e=True)
+    r64, rsp = (rmx, roth) if args.precision == "fp64" else (roth, rmx)
     t_step = float(np.mean(rmx["times"]))
     t_wall = float(np.mean(rmx["walls"]))
     if ws > 1:
@@ -335,11 +338,11 @@ def run_vumps(args):
         dist.all_reduce(tt, op=dist.ReduceOp.MAX)
         t_step, t_wall = (float(x) for x in tt.tolist())
     value = ws / t_step  # replicas: every rank runs its own sweeps
-    E64, Emx = r64["E"], rmx["E"]
+    E64, Emx = r64["E"], rsp["E"]
     dE = float(abs(Emx.mean() - E64.mean()))
 
     # H_AC TFLOP/s on the final-state plans (site 0)
-    v64, vmx = r64["v"], rmx["v"]
+    v64, vmx = r64["v"], rsp["v"]
     n = v64.LA[0].nelem
     flops = v64.flops_hac[0]
     t_hac64 = _time_hac_applies(torch, v64.p_hac[0], n, stream)
@@ -360,10 +363,18 @@ def run_vumps(args):
                                 "frac": flops / t_hac64 / 1e12 / fp64_peak,
                                 "peak_source": "dense FP64 matmul measured in this run"}}
     else:
+        # the FP64 grouped GEMM dominates the timed sweeps (every solve below the split-BF16
+        # floor runs on it); GB300 has no FP64 tensor rate, so its roof is the FP64 pipe, taken
+        # as the dense FP64 matmul rate measured in this run
         achieved = flops / t_hac64 / 1e12
         roof = {"bound": "tensor", "achieved": achieved, "peak": fp64_peak, "unit": "TFLOP/s",
                 "frac": achieved / fp64_peak, "traffic": NCU_TRAFFIC_BYTES["fp64"],
-                "peak_source": "dense FP64 matmul measured in this run", "kernel": "grouped_gemm_f64 (H_AC apply)"}
+                "peak_source": "dense FP64 matmul (torch, cuBLAS DGEMM 4096^3) measured in this run; the FP64 "
+                               "pipe, not a tensor pipe, bounds this kernel on GB300",
+                "kernel": "grouped_gemm_f64 (H_AC apply; the dominant kernel of the timed sweeps)",
+                "split_bf16_engine": {"achieved_fp64_equivalent_tflops": flops / t_hacmx / 1e12,
+                                      "tensor_tflops": 6 * flops / t_hacmx / 1e12, "tensor_peak": bf16_peak,
+                                      "tensor_frac": 6 * flops / t_hacmx / 1e12 / bf16_peak}}
 
     e2e = {"value": ws / t_wall, "unit": "sweeps/s", "h2d_bytes_per_step": rmx["h2d"],
            "d2h_bytes_per_step": rmx["h2d"] + 16, "ms_per_step": 1e3 * t_wall,
@@ -392,9 +403,13 @@ def run_vumps(args):
                        "parallelism": f"replicas x{ws}"},
             "fp64": {"sweeps_per_s": 1.0 / float(np.mean(r64["times"])), "ms_per_step": 1e3 * float(np.mean(r64["times"])),
                      "energy": float(E64.mean()), "grad_norm": float(r64["F"].max()), "counts": r64["counts"]},
-            "mixed": {"sweeps_per_s": 1.0 / t_step, "energy": float(Emx.mean()),
-                      "grad_norm": float(rmx["F"].max()), "counts": rmx["counts"]},
-            "dE_mixed_vs_fp64": dE, "speedup_mixed_vs_fp64": float(np.mean(r64["times"])) / t_step,
+            "mixed": {"sweeps_per_s": 1.0 / float(np.mean(rsp["times"])), "energy": float(Emx.mean()),
+                      "grad_norm": float(rsp["F"].max()), "counts": rsp["counts"],
+                      "note": "split-BF16 applies serve only solves with tol >= 2e-7 (their linearity floor); "
+                              "below it the precision ladder runs FP64, which at this tolerance schedule is every "
+                              "solve, so the two arms take the same path"},
+            "dE_mixed_vs_fp64": dE,
+            "speedup_mixed_vs_fp64": float(np.mean(r64["times"])) / float(np.mean(rsp["times"])),
             "h_ac": h_ac, "roofline": roof, "cpu_baseline": cpu, "e2e": e2e, "gpu_launches": rmx["launches"],
             "clocks": rmx["clocks"]}
     if rank == 0:
@@ -526,7 +541,7 @@ def main():
     ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
     ap.add_argument("--mode", default="vumps", choices=["vumps", "hac", "krylov", "excitations"])
     ap.add_argument("--workload", default="xxz_d512")
-    ap.add_argument("--precision", default="bf16x6", choices=["fp64", "bf16x6"])
+    ap.add_argument("--precision", default="fp64", choices=["fp64", "bf16x6"])
     ap.add_argument("--no-cpu", action="store_true")
     args = ap.parse_args()
     args.warmup = max(args.warmup, 3)

@@ -101,24 +101,43 @@ std::vector<HNnz> make_h(int nnz, const int32_t* r, const int32_t* c, const doub
 }
 
 int upload_stage(Stage& S) {
-  // tile size: minimise the estimated makespan of the FP64-pipe-bound kernel, i.e. the larger
-  // of the heaviest single tile (one CTA cannot be split across SMs) and the total work
-  // spread over the 152 SMs
-  auto makespan = [&](int T) {
+  // tile size and split-K: minimise the estimated makespan of the FP64-pipe-bound kernel, the
+  // larger of the heaviest tile's share (a tile's K chunks split over `splits` CTAs) and the
+  // total padded work spread over the 152 SMs
+  constexpr int kSMs = 152, kMaxSplits = 8;
+  auto plan_for = [&](int T, int* splits_out) {
     int64_t crit = 0, total = 0;
+    int max_chunks = 0;
     for (const OutBlock& o : S.outs) {
       int64_t k = 0;
-      for (int t = o.t0; t < o.t1; ++t) k += S.terms[t].k;
+      int ch = 0;
+      for (int t = o.t0; t < o.t1; ++t) {
+        k += S.terms[t].k;
+        ch += (S.terms[t].k + 15) / 16;
+      }
       crit = std::max(crit, (int64_t)std::min(T, o.M) * std::min(T, o.N) * k);
       total += (int64_t)((o.M + T - 1) / T * T) * ((o.N + T - 1) / T * T) * k;
+      max_chunks = std::max(max_chunks, ch);
     }
-    return std::max(crit, total / 152);
+    const int64_t spread = std::max<int64_t>(total / kSMs, 1);
+    int sp = (int)std::min<int64_t>((crit + spread - 1) / spread, kMaxSplits);
+    sp = std::max(1, std::min(sp, max_chunks / (T == 16 ? 4 : 2)));  // at least one chunk per K group
+    *splits_out = sp;
+    return std::max(crit / sp, spread);
   };
-  const int T = makespan(16) <= makespan(32) ? 16 : 32;
+  int s16 = 1, s32 = 1;
+  const int64_t m16 = plan_for(16, &s16), m32 = plan_for(32, &s32);
+  const int T = m16 <= m32 ? 16 : 32;
   finalize_tiles(S, T, T);
+  S.splits = T == 16 ? s16 : s32;
   if (!S.tiles.empty()) {
     CK(cudaMalloc(&S.d_tiles, S.tiles.size() * sizeof(Tile)));
     CK(cudaMemcpy(S.d_tiles, S.tiles.data(), S.tiles.size() * sizeof(Tile), cudaMemcpyHostToDevice));
+    if (S.splits > 1) {
+      CK(cudaMalloc(&S.d_ws, S.tiles.size() * S.splits * (size_t)T * T * sizeof(double)));
+      CK(cudaMalloc(&S.d_cnt, S.tiles.size() * sizeof(int)));
+      CK(cudaMemset(S.d_cnt, 0, S.tiles.size() * sizeof(int)));
+    }
   }
   if (!S.terms.empty()) {
     CK(cudaMalloc(&S.d_terms, S.terms.size() * sizeof(Term)));
@@ -168,7 +187,8 @@ int run_stages(imps_plan* p, std::vector<Stage>& stages) {
     if (tc) {
       RC(tc_run_stage(p->tc, S, sl, p->ctx->stream));
     } else {
-      RC(imps_launch_grouped_f64(S.d_tiles, (int)S.tiles.size(), S.d_terms, sl, S.tile_m, p->ctx->stream));
+      RC(imps_launch_grouped_f64(S.d_tiles, (int)S.tiles.size(), S.d_terms, sl, S.tile_m, S.splits, S.d_ws,
+                                 S.d_cnt, p->ctx->stream));
     }
   }
   return IMPS_OK;
@@ -579,6 +599,8 @@ int imps_plan_destroy(imps_plan* p) {
     for (Stage& S : *v) {
       if (S.d_tiles) cudaFree(S.d_tiles);
       if (S.d_terms) cudaFree(S.d_terms);
+      if (S.d_ws) cudaFree(S.d_ws);
+      if (S.d_cnt) cudaFree(S.d_cnt);
     }
   cudaFree(p->stage_in);
   cudaFree(p->stage_out);

@@ -88,6 +88,11 @@ struct Stage {
   void* d_terms = nullptr;
   int64_t flops = 0;  // useful flops: sum over terms of 2*M*N*K
   int tile_m = 32, tile_n = 32;
+  // split-K over CTAs (FP64 engine): `splits` CTAs per tile write partial tiles to d_ws and the
+  // last one to finish (ticket in d_cnt, reset by it) sums them in a fixed order
+  int splits = 1;
+  double* d_ws = nullptr;
+  int* d_cnt = nullptr;
 };
 
 enum SlotKind { SLOT_EXTERNAL = 0, SLOT_INTERNAL = 1 };
@@ -148,4 +153,4 @@ void finalize_tiles(Stage& S, int tm, int tn);
 // ----- kernel launchers (kernels_f64.cu) -----
 struct imps_dslots { double* p[imps::kMaxSlots]; };
 int imps_launch_grouped_f64(const void* d_tiles, int ntiles, const void* d_terms, imps_dslots slots,
-                            int tile_m, void* stream);
+                            int tile_m, int splits, double* ws, int* cnt, void* stream);

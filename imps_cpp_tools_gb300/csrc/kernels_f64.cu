@@ -1,10 +1,13 @@
 // FP64 kernels for the block-sparse hot path on sm_103a.
 //
 //  * grouped_gemm_f64: output-stationary grouped GEMM over the planner's tile/term tables.
-//    One CTA per output tile; every term of the tile is accumulated in registers (split over
-//    K groups inside the CTA, summed in a fixed order) and the tile is written once
-//    (deterministic, no atomics, no separate zero-fill: the first write also performs the
-//    reference's memset of `out`, VUMPS_helpers.hpp:69).
+//    `splits` CTAs per output tile (split-K: each takes an equal share of the tile's K chunks,
+//    over all of its terms in order); inside a CTA the chunks are dealt to K groups whose
+//    partial tiles are summed in a fixed order.  With one split the tile is written directly;
+//    otherwise every CTA stores its partial tile and the last CTA of the tile to finish (an
+//    atomic ticket after a memory fence; nobody waits) sums the partials in split order and
+//    writes the tile.  Deterministic for a given plan; no separate zero-fill: the first write
+//    also performs the reference's memset of `out`, VUMPS_helpers.hpp:69.
 //  * Krylov BLAS-1 (reductions without atomics: fixed-grid partials + one finishing block).
 #include <cuda_runtime.h>
 
@@ -32,14 +35,24 @@ __device__ __forceinline__ void group_sync(int id, int nthreads) {
 template <int TM, int TN, int RM, int RN, int KS>
 __global__ void __launch_bounds__((TM / RM) * (TN / RN) * KS)
 grouped_gemm_f64_kernel(const Tile* __restrict__ tiles, const Term* __restrict__ terms,
-                        imps_dslots slots) {
+                        imps_dslots slots, int splits, double* __restrict__ ws, int* __restrict__ cnt) {
   constexpr int NT = (TM / RM) * (TN / RN);
   constexpr int TX = TN / RN;  // threads along n
   constexpr int AS = TK * (TM + 1), BS = TK * (TN + 1);
   constexpr int STAGE = KS * (AS + BS);
   constexpr int RED = (KS - 1) * NT * RM * RN;
   __shared__ double smem[STAGE > RED ? STAGE : RED];
-  const Tile tl = tiles[blockIdx.x];
+  __shared__ int last;
+  const int tile_id = blockIdx.x / splits, part = blockIdx.x - tile_id * splits;
+  const Tile tl = tiles[tile_id];
+  // this CTA's chunk range [c_lo, c_hi) of the tile's chunk sequence
+  int c_lo = 0, c_hi = 1 << 30;
+  if (splits > 1) {
+    int nch = 0;
+    for (int t = tl.t0; t < tl.t1; ++t) nch += (terms[t].k + TK - 1) / TK;
+    c_lo = (int)((int64_t)nch * part / splits);
+    c_hi = (int)((int64_t)nch * (part + 1) / splits);
+  }
   const int g = threadIdx.x / NT;
   const int tid = threadIdx.x - g * NT;
   const int tx = tid % TX, ty = tid / TX;
@@ -52,13 +65,18 @@ grouped_gemm_f64_kernel(const Tile* __restrict__ tiles, const Term* __restrict__
     for (int j = 0; j < RN; ++j) acc[i][j] = 0.0;
 
   int chunk = 0;
-  for (int t = tl.t0; t < tl.t1; ++t) {
+  for (int t = tl.t0; t < tl.t1 && chunk < c_hi; ++t) {
     const Term tm = terms[t];
+    const int nk = (tm.k + TK - 1) / TK;
+    if (chunk + nk <= c_lo) {  // wholly before this split's range
+      chunk += nk;
+      continue;
+    }
     const double* __restrict__ A = slots.p[tm.a_slot] + tm.a_off;
     const double* __restrict__ B = slots.p[tm.b_slot] + tm.b_off;
     const double alpha = tm.alpha;
     for (int k0 = 0; k0 < tm.k; k0 += TK, ++chunk) {
-      if (chunk % KS != g) continue;
+      if (chunk < c_lo || chunk >= c_hi || (chunk - c_lo) % KS != g) continue;
       // A tile: rows m0..m0+TM, cols k0..k0+TK of op(A)
       for (int e = tid; e < TM * TK; e += NT) {
         int m, k;
@@ -104,12 +122,36 @@ grouped_gemm_f64_kernel(const Tile* __restrict__ tiles, const Term* __restrict__
         for (int j = 0; j < RN; ++j) red[(((g - 1) * NT + tid) * RM + i) * RN + j] = acc[i][j];
     }
     __syncthreads();
-    if (g > 0) return;
+    if (g > 0) return;  // only group 0 (its own named barrier below) goes on
     for (int q = 1; q < KS; ++q)
 #pragma unroll
       for (int i = 0; i < RM; ++i)
 #pragma unroll
         for (int j = 0; j < RN; ++j) acc[i][j] += red[(((q - 1) * NT + tid) * RM + i) * RN + j];
+  }
+  if (splits > 1) {
+    // partial tile -> workspace; the last CTA of the tile sums all partials in split order
+    double* wp = ws + ((int64_t)tile_id * splits + part) * (TM * TN);
+#pragma unroll
+    for (int i = 0; i < RM; ++i)
+#pragma unroll
+      for (int j = 0; j < RN; ++j) wp[(ty + i * (TM / RM)) * TN + tx + j * TX] = acc[i][j];
+    __threadfence();
+    group_sync(1, NT);
+    if (tid == 0) last = atomicAdd(cnt + tile_id, 1) == splits - 1;
+    group_sync(1, NT);
+    if (!last) return;
+    __threadfence();
+#pragma unroll
+    for (int i = 0; i < RM; ++i)
+#pragma unroll
+      for (int j = 0; j < RN; ++j) {
+        const int e = (ty + i * (TM / RM)) * TN + tx + j * TX;
+        double sum = 0.0;
+        for (int q = 0; q < splits; ++q) sum += __ldcg(ws + ((int64_t)tile_id * splits + q) * (TM * TN) + e);
+        acc[i][j] = sum;
+      }
+    if (tid == 0) cnt[tile_id] = 0;  // re-armed for the next launch of this stage
   }
   double* __restrict__ C = slots.p[tl.c_slot] + tl.c_off;
 #pragma unroll
@@ -129,17 +171,18 @@ grouped_gemm_f64_kernel(const Tile* __restrict__ tiles, const Term* __restrict__
 }  // namespace
 
 int imps_launch_grouped_f64(const void* d_tiles, int ntiles, const void* d_terms, imps_dslots slots,
-                            int tile_m, void* stream) {
+                            int tile_m, int splits, double* ws, int* cnt, void* stream) {
   if (ntiles <= 0) return IMPS_OK;
+  if (splits < 1 || (splits > 1 && (!ws || !cnt))) return IMPS_ERR_BAD_ARG;
   cudaStream_t st = (cudaStream_t)stream;
+  const int grid = ntiles * splits;
+  imps::count_launch();
   if (tile_m == 16) {
-    imps::count_launch();
-    grouped_gemm_f64_kernel<16, 16, 2, 2, 4><<<ntiles, 256, 0, st>>>((const Tile*)d_tiles,
-                                                                    (const Term*)d_terms, slots);
+    grouped_gemm_f64_kernel<16, 16, 2, 2, 4><<<grid, 256, 0, st>>>((const Tile*)d_tiles, (const Term*)d_terms,
+                                                                  slots, splits, ws, cnt);
   } else {
-    imps::count_launch();
-    grouped_gemm_f64_kernel<32, 32, 2, 4, 2><<<ntiles, 256, 0, st>>>((const Tile*)d_tiles,
-                                                                     (const Term*)d_terms, slots);
+    grouped_gemm_f64_kernel<32, 32, 2, 4, 2><<<grid, 256, 0, st>>>((const Tile*)d_tiles, (const Term*)d_terms,
+                                                                   slots, splits, ws, cnt);
   }
   return cudaGetLastError() == cudaSuccess ? IMPS_OK : IMPS_ERR_CUDA;
 }

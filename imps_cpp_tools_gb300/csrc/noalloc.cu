@@ -169,7 +169,7 @@ extern "C" int imps_tm_apply_noalloc(const imps_layout* A, const imps_layout* in
   sl.p[SY] = dY;
   sl.p[SA] = const_cast<double*>(dA);
   sl.p[SW] = d_scratch[dev];
-  int rc = imps_launch_grouped_f64(dimg->tiles[0], s1.ntiles, dimg->terms[0], sl, kTile, stream);
+  int rc = imps_launch_grouped_f64(dimg->tiles[0], s1.ntiles, dimg->terms[0], sl, kTile, 1, nullptr, nullptr, stream);
   if (rc) return rc;
-  return imps_launch_grouped_f64(dimg->tiles[1], s2.ntiles, dimg->terms[1], sl, kTile, stream);
+  return imps_launch_grouped_f64(dimg->tiles[1], s2.ntiles, dimg->terms[1], sl, kTile, 1, nullptr, nullptr, stream);
 }
