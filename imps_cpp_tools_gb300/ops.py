@@ -198,6 +198,13 @@ def norm_inf(ctx, x):
     return r.value
 
 
+def dot(ctx, x, y):
+    """x^T y of two device vectors (fixed-order reduction)."""
+    r = C.c_double()
+    N.call("imps_dot", ctx.handle, _dptr(x), _dptr(y), int(x.numel()), C.byref(r))
+    return r.value
+
+
 def axpby(ctx, a, x, b, y):
     """y = a*x + b*y on the device."""
     N.call("imps_axpby", ctx.handle, float(a), _dptr(x), float(b), _dptr(y), y.numel())

@@ -1019,6 +1019,177 @@ def LRoverlaps(AL, AR, K, nev, OLtol=1e-14):
 
 
 # ----------------------------------------------------------------------------------------------
+# energy density of a uniform two-site MPS and its gradient (adjoint check).  The reference has
+# no gradient of its own beyond the tangent-space residual H_AC AC - AL H_C C
+# (VUMPS_helpers.hpp:135-177); these restate the energy of MeasureObservables
+# (MPSBlockUtilities.hpp:1017-1091) for a general, non-isometric unit cell and differentiate it.
+# ----------------------------------------------------------------------------------------------
+
+
+def bd_dot(X, Y):
+    """(X|Y) = sum_q tr(X_q^T Y_q)."""
+    return float(sum(np.sum(X[q] * Y[q]) for q in X if q in Y))
+
+
+def bd_scale(X, a):
+    return {q: a * M for q, M in X.items()}
+
+
+def mps_dot(A, B):
+    return float(sum(np.sum(M * B[s][qi][1]) for s, bm in enumerate(A) for qi, (qo, M) in bm.items()
+                     if qi in B[s]))
+
+
+def opTM_left(A0, A1, l, hnnz):
+    """sum_st (A0 A1)_st^T l (h A0 A1)_st: the two-site term E(l) carried from bond 0 to bond 2."""
+    AA = mps_mul_mps(A0, A1)
+    HA = ApplyOperator(AA, hnnz)
+    out = {}
+    for a, b in zip(AA, HA):
+        for qi, (qo, M) in a.items():
+            if qi in b and qi in l:
+                c = M.T @ l[qi] @ b[qi][1]
+                out[qo] = out[qo] + c if qo in out else c
+    return out
+
+
+def opTM_right(A0, A1, r, hnnz):
+    """sum_st (h A0 A1)_st r (A0 A1)_st^T: the two-site term carried from bond 2 to bond 0."""
+    AA = mps_mul_mps(A0, A1)
+    HA = ApplyOperator(AA, hnnz)
+    out = {}
+    for a, b in zip(AA, HA):
+        for qi, (qo, M) in a.items():
+            if qi in b and qo in r:
+                c = b[qi][1] @ r[qo] @ M.T
+                out[qi] = out[qi] + c if qi in out else c
+    return out
+
+
+def _dense_map(f, sizes):
+    n = sum(m * m for _, m in sizes)
+    M = np.zeros((n, n))
+    for i in range(n):
+        e = np.zeros(n)
+        e[i] = 1.0
+        M[:, i] = bd_vec(f(bd_from_vec(e, sizes)))
+    return M
+
+
+def energy_uniform(A, hnnz):
+    """Energy density of the uniform MPS of the unit cell A = [A0, A1] (any, not necessarily
+    isometric): e = (N0 / lam + N1 / lam^2) / (2 (l|r)) with lam, l, r the dominant eigenvalue and
+    fixed points of the unit-cell TM (dense eigendecomposition: small bonds only), N0 the bond
+    (0,1) term between l and r, N1 the bond (1,2) term between l1 = T_0(l) and r1 = T~_1(r)."""
+    A0, A1 = A
+    sizes = sorted(mps_ml(A0).items())
+    w, V = np.linalg.eig(_dense_map(lambda X: ApplyTMLeftUC(A, X), sizes))
+    i = int(np.argmax(w.real))
+    lam = float(w[i].real)
+    l = bd_from_vec(np.real(V[:, i]), sizes)
+    w2, V2 = np.linalg.eig(_dense_map(lambda X: ApplyTMRightUC(A, X), sizes))
+    r = bd_from_vec(np.real(V2[:, int(np.argmax(w2.real))]), sizes)
+    l1, r1 = ApplyTMLeft(A0, l), ApplyTMRight(A1, r)
+    N0 = bd_dot(l, opTM_right(A0, A1, r, hnnz))
+    N1 = bd_dot(l1, opTM_right(A1, A0, r1, hnnz))
+    return (N0 / lam + N1 / lam ** 2) / (2.0 * bd_dot(l, r))
+
+
+def _redop_env(A, env, hnnz, d, direction):
+    """ReducedOp (MPSBlockUtilities.hpp:37-74) with an environment inserted, as BlockMats (a pair
+    i0 != j0 carries a charge offset): direction "r" gives W[i0][j0] = sum h_(i0 i1),(j0 j1)
+    A[j1] env A[i1]^T, "l" gives V[i1][j1] = sum h A[i0]^T env A[j0]."""
+    W = [[None] * d for _ in range(d)]
+    for (rr, cc, h) in hnnz:
+        i0, i1 = num2ditvec(rr, d)
+        j0, j1 = num2ditvec(cc, d)
+        if direction == "r":
+            c, a, b = bm_mul(bm_mul_bd(A[j1], env), bm_t(A[i1])), i0, j0
+        else:
+            c, a, b = bm_mul(bm_mul_bd(bm_t(A[i0]), env), A[j0]), i1, j1
+        W[a][b] = bm_iadd(W[a][b] if W[a][b] is not None else {}, bm_scale(c, h))
+    return W
+
+
+def invert_e_proj_scipy(MPSarr, x, L, R, direction, tol=1e-14):
+    """The projected system of InvertE_proj (InvEBlockFunctions.hpp:201-266) solved with scipy's
+    restarted GMRES: test infrastructure for bonds where the restated unrestarted GMRES is slow."""
+    from scipy.sparse.linalg import LinearOperator, gmres as sp_gmres
+    dims = bd_sizes(x)
+    n = sum(m * m for _, m in dims)
+    if direction == "l":
+        b = bd_vec(x) - bd_trace(bd_mul(x, R)) * bd_vec(L)
+        f = lambda v: InvEfun_proj(v, lambda X: ApplyTMLeftUC(MPSarr, X), R, L, dims)
+    else:
+        b = bd_vec(x) - bd_trace(bd_mul(L, x)) * bd_vec(R)
+        f = lambda v: InvEfun_proj(v, lambda X: ApplyTMRightUC(MPSarr, X), L, R, dims)
+    op = LinearOperator((n, n), matvec=lambda v: f(np.asarray(v).ravel()), dtype=np.float64)
+    y, info = sp_gmres(op, b, rtol=tol, atol=0.0, restart=120, maxiter=200)
+    return bd_from_vec(y, dims), info
+
+
+def energy_gradient(AL, R, hnnz, tol=1e-14, solver=None):
+    """Gradient of energy_uniform with respect to every entry of a left-isometric unit cell AL
+    (lam = 1, l = l1 = 1, r = R with tr R = 1), by the adjoint method:
+      * direct two-site terms: H_AC-type contractions with the ReducedOp environments W, V, W', V';
+      * the dependence of r1 = T~_1(r) and l1 = T_0(l) on A (TM adjoints: left TM
+        (Y|dT(X)) -> X A Y^T + X^T A Y, right TM (Y|dT~(X)) -> Y A X^T + Y^T A X);
+      * the eigenvalue, dlam = (r1|dT_0(l)) + (r|dT_1(l1)), weighted by -(N0 + 2 N1) / 2;
+      * the fixed points through the implicit function theorem: g_l = de/dl, g_r = de/dr (both
+        orthogonal to the null directions by scale invariance), z_l = (1 - T~ + |r)(l|)^-1 (-g_l)
+        and z_r = (1 - T + |l)(r|)^-1 (-g_r): GMRES on the transposed transfer matrices
+        (InvertE_proj with the roles of the two directions exchanged), then
+        -(z_l|dT(l)) - (z_r|dT~(r)) through the TM adjoints.
+    solver: optional replacement of InvertE_proj with the same signature (a faster library
+    GMRES for large bonds; the solution of the projected system does not depend on it).
+    Returns ([G0, G1] as MPS structures, e)."""
+    A0, A1 = AL
+    d = len(A0)
+    I0, I1 = bd_eye(mps_ml(A0)), bd_eye(mps_ml(A1))
+    r = bd_scale(R, 1.0 / bd_trace(R))
+    r1 = ApplyTMRight(A1, r)
+    N0 = bd_dot(I0, opTM_right(A0, A1, r, hnnz))
+    N1 = bd_dot(I1, opTM_right(A1, A0, r1, hnnz))
+    E2, E2l = N0 + N1, N0 + 2.0 * N1
+    Et1 = opTM_right(A1, A0, r1, hnnz)          # bond 1
+    E1l = opTM_left(A1, A0, I1, hnnz)           # bond 1
+    gl = bd_scale(bd_add(bd_add(opTM_right(A0, A1, r, hnnz), ApplyTMRight(A0, Et1)), bd_scale(r, -E2)), 0.5)
+    gr = bd_scale(bd_add(bd_add(opTM_left(A0, A1, I0, hnnz), ApplyTMLeft(A1, E1l)), bd_scale(I0, -E2)), 0.5)
+    solve = solver or InvertE_proj
+    zl, _ = solve(AL, bd_scale(gl, -1.0), I0, r, "r", tol)
+    zr, _ = solve(AL, bd_scale(gr, -1.0), I0, r, "l", tol)
+    W = _redop_env(A1, r, hnnz, d, "r")    # bond 1
+    V = _redop_env(A0, I0, hnnz, d, "l")   # bond 1
+    Wp = _redop_env(A0, r1, hnnz, d, "r")  # bond 0 (= 2)
+    Vp = _redop_env(A1, I1, hnnz, d, "l")  # bond 0 (= 2)
+    T1zl = ApplyTMRight(A1, zl)            # bond 1
+    T0zr = ApplyTMLeft(A0, zr)             # bond 1
+    G0, G1 = [], []
+    for s in range(d):
+        g = {}
+        for sp in range(d):
+            if W[s][sp] is not None:
+                bm_iadd(g, bm_mul(A0[sp], W[s][sp]))
+            if Vp[s][sp] is not None:
+                bm_iadd(g, bm_mul_bd(bm_mul(Vp[s][sp], A0[sp]), r1))
+        Y1 = bd_add(bd_add(Et1, bd_scale(r1, -E2l)), bd_scale(T1zl, -2.0))
+        bm_iadd(g, bm_mul_bd(A0[s], Y1))
+        bm_iadd(g, bm_scale(bm_mul_bd(bd_mul_bm(zr, A0[s]), r1), -2.0))
+        G0.append(g)
+    for t in range(d):
+        g = {}
+        for tp in range(d):
+            if V[t][tp] is not None:
+                bm_iadd(g, bm_mul_bd(bm_mul(V[t][tp], A1[tp]), r))
+            if Wp[t][tp] is not None:
+                bm_iadd(g, bm_mul(A1[tp], Wp[t][tp]))
+        bm_iadd(g, bm_mul_bd(bd_mul_bm(bd_add(E1l, bd_scale(T0zr, -2.0)), A1[t]), r))
+        bm_iadd(g, bm_mul_bd(A1[t], bd_add(bd_scale(r, -E2l), bd_scale(zl, -2.0))))
+        G1.append(g)
+    return [G0, G1], 0.5 * E2
+
+
+# ----------------------------------------------------------------------------------------------
 # per-sector decompositions (helpers.hpp:181-195, MPSBlockUtilities.hpp:78-340, BlockObj.hpp:2422-2541)
 # ----------------------------------------------------------------------------------------------
 
