@@ -533,13 +533,71 @@ def run_excitations(args):
                       "E0": inp["E0"]}), flush=True)
 
 
+def run_adjoint(args):
+    """The adjoint check's shapes: dE/dA_L and dE/dcouplings of the energy density at the
+    left-isometric unit cell of a VUMPS state (a few sweeps from the seeded random start) for
+    XXZ D=256 with Delta = 0.5, 1.0, 1.5 (antiferromagnetic sign convention of the reference:
+    Delta = -0.5, -1, -1.5) and Hubbard D=256 with U = 2, 4.  Per case: device gradient
+    evaluations timed with CUDA events over `steps` repetitions after `warmup`, the gradient's
+    difference from the oracle, and the oracle (numpy, all host threads) timed on one evaluation."""
+    import torch
+    from imps_cpp_tools_gb300 import blocks as B
+    from imps_cpp_tools_gb300 import configs
+    from imps_cpp_tools_gb300.adjoint import CouplingGradientGPU, EnergyGradientGPU
+    from imps_cpp_tools_gb300.excitations import bd_to_host, mps_to_host
+    from imps_cpp_tools_gb300.vumps import VumpsGPU
+    from oracle import imps_oracle as O  # the checker and the CPU baseline leg
+    ctx = B.Context(0)
+    stream = torch.cuda.current_stream()
+    ctx.set_stream(stream)
+    cases = [("xxz_d256", {"Delta": -0.5}), ("xxz_d256", {"Delta": -1.0}), ("xxz_d256", {"Delta": -1.5}),
+             ("hubbard_d256", {"U": 2.0}), ("hubbard_d256", {"U": 4.0})]
+    rows = []
+    for name, over in cases:
+        model, fn, params = configs.WORKLOADS[name]
+        params = {**params, **over}
+        v = VumpsGPU(ctx, model, dims0=fn(), seed=1, **params)
+        for _ in range(3):
+            v.sweep()
+        R = bd_to_host(v.C[0], v.LB[0])
+        R = O.bd_mul(R, O.bd_t(R))
+        Rd = torch.from_numpy(O.bd_vec(R)).to("cuda")
+        g = EnergyGradientGPU(ctx, v.LA, v.LB, v.hnnz, v.d, tol=1e-11)
+        cg = CouplingGradientGPU(ctx, v.LA, v.LB, model, v.d, **params)
+        for _ in range(args.warmup):
+            g(v.AL[0], v.AL[1], Rd)
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        torch.cuda.synchronize()
+        it0 = g.stats["gmres_iters"]
+        e0.record(stream)
+        for _ in range(max(args.steps, 1)):
+            G0, G1, e, _, conv = g(v.AL[0], v.AL[1], Rd)
+        e1.record(stream)
+        torch.cuda.synchronize()
+        ms = e0.elapsed_time(e1) / max(args.steps, 1)
+        dcoup = cg(v.AL[0], v.AL[1], Rd)
+        AL = [mps_to_host(v.AL[n], v.LA[n], v.d) for n in range(2)]
+        tc = time.perf_counter()
+        Gref, eref = O.energy_gradient(AL, R, v.hnnz, tol=1e-11, solver=O.invert_e_proj_scipy)
+        t_cpu = time.perf_counter() - tc
+        err = max(float(np.linalg.norm(G0.cpu().numpy() - O.mps_vec(Gref[0])) / np.linalg.norm(O.mps_vec(Gref[0]))),
+                  float(np.linalg.norm(G1.cpu().numpy() - O.mps_vec(Gref[1])) / np.linalg.norm(O.mps_vec(Gref[1]))))
+        rows.append({"workload": name, "params": params, "energy": e, "converged": bool(conv),
+                     "ms_per_gradient": ms, "gradients_per_s": 1e3 / ms,
+                     "gmres_iters_per_gradient": (g.stats["gmres_iters"] - it0) / max(args.steps, 1),
+                     "dE_dcouplings": dcoup, "rel_diff_vs_oracle": err, "oracle_s_per_gradient": t_cpu})
+    print(json.dumps({"mode": "adjoint", "metric": "energy-density gradients/s (dE/dA_L via TM/H_AC adjoints + "
+                      "transposed-GMRES fixed-point adjoint)", "cpu_cores": os.cpu_count(), "cases": rows}),
+          flush=True)
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
     ap.add_argument("--steps", type=int, default=47)
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
-    ap.add_argument("--mode", default="vumps", choices=["vumps", "hac", "krylov", "excitations"])
+    ap.add_argument("--mode", default="vumps", choices=["vumps", "hac", "krylov", "excitations", "adjoint"])
     ap.add_argument("--workload", default="xxz_d512")
     ap.add_argument("--precision", default="fp64", choices=["fp64", "bf16x6"])
     ap.add_argument("--no-cpu", action="store_true")
@@ -551,6 +609,8 @@ def main():
         run_hac(args)
     elif args.mode == "krylov":
         run_krylov(args)
+    elif args.mode == "adjoint":
+        run_adjoint(args)
     elif args.mode == "excitations":
         run_excitations(args)
     else:
