@@ -43,8 +43,14 @@ TOLMIN = 1e-12  # floor of the eigensolver tolerance schedule and the GMRES tole
 # (profiles/tc_gemm_hac_xxz_d512.md: tc_gemm 5.26 MB + pack 0.40 MB;
 # profiles/grouped_gemm_f64_hac_xxz_d512.md: 2.36 MB), cold caches
 NCU_TRAFFIC_BYTES = {"bf16x6": 5.66e6, "fp64": 2.36e6}
-WORKLOAD_DESC = ("XXZ D=512 (21 U(1) sectors, dims ~exp(-q^2/18)), 2-site VUMPS sweep, tolerance schedule "
-                 "min(max(prec/100, 1e-12), 1e-6) (VUMPS_main.cpp:177), GMRES tol 1e-12, expansion off")
+_SCHEDULE = ("2-site VUMPS sweep, tolerance schedule min(max(prec/100, 1e-12), 1e-6) (VUMPS_main.cpp:177), "
+             "GMRES tol 1e-12, expansion off")
+WORKLOAD_DESCS = {
+    "xxz_d512": "XXZ D=512 (21 U(1) sectors, dims ~exp(-q^2/18)), " + _SCHEDULE,
+    "hubbard_d1024": "Fermi-Hubbard t=1, U=4, half filling, D=1024 (60 U(1)xU(1) (N, Sz) sectors, dims "
+                     "~exp(-(dN^2+4Sz^2)/8)), " + _SCHEDULE,
+}
+_WORKLOAD = ["xxz_d512"]  # the VUMPS workload of this run (--workload)
 
 
 def _peaks():
@@ -129,9 +135,14 @@ def _fp64_peak_tflops(torch):
 
 
 def _xxz_params():
+    """(model, bond dims, couplings) of the VUMPS workload of this run (default XXZ D=512)."""
     from imps_cpp_tools_gb300 import configs
-    model, fn, params = configs.WORKLOADS["xxz_d512"]
+    model, fn, params = configs.WORKLOADS[_WORKLOAD[0]]
     return model, fn(), params
+
+
+def _workload_desc():
+    return WORKLOAD_DESCS.get(_WORKLOAD[0], _WORKLOAD[0] + ", " + _SCHEDULE)
 
 
 # ------------------------------------------------------------------------------------------------
@@ -143,12 +154,14 @@ def _xxz_params():
 # Lanczos solves per site update), unit-cell transfer-matrix applies (GMRES iterations of the
 # environment and fixed-point solves).  The reference arm weights its CPU operator times with
 # these; the GPU arm uses the counts of its own timed sweeps.
-REF_COUNTS_PER_SWEEP = {"hac": 373.4, "hc": 554.9, "tm": 311.7}
+REF_COUNTS_BY_WORKLOAD = {"xxz_d512": {"hac": 373.4, "hc": 554.9, "tm": 311.7},
+                          # --workload hubbard_d1024 --steps 37 --warmup 3
+                          "hubbard_d1024": {"hac": 618.6, "hc": 1129.1, "tm": 293.6}}
 
 
 def cpu_op_times(budget_per_op=2.0, seed=1):
     """CPU time of one H_AC apply (ApplyHAvec), one H_C apply (ApplyHCvec) and one unit-cell
-    transfer-matrix apply (ApplyTMLeftUC) of the numpy restatement on XXZ D=512 operands of the
+    transfer-matrix apply (ApplyTMLeftUC) of the numpy restatement on operands of the VUMPS
     workload's sector structure (values seeded random: the cost does not depend on them), all
     host threads.  Each is repeated until budget_per_op seconds (at least twice)."""
     from imps_cpp_tools_gb300 import models
@@ -210,17 +223,17 @@ def run_reference(args):
     for i in range(args.warmup + args.steps):
         times, reps = cpu_op_times(budget_per_op=0.5)
         if i >= args.warmup:
-            per.append(cpu_sweep_model(REF_COUNTS_PER_SWEEP, times))
+            per.append(cpu_sweep_model(REF_COUNTS_BY_WORKLOAD[_WORKLOAD[0]], times))
     value = 1.0 / float(np.mean(per))
     cores = os.cpu_count()
     sample = ("per step: H_AC, H_C and unit-cell TM applies of the numpy restatement of the reference's "
-              "operators on XXZ D=512 operands (>= 2 applies each, 0.5 s per operator), weighted by the "
-              f"per-sweep operator counts of the FP64 path {REF_COUNTS_PER_SWEEP}; orthogonalisation and "
+              f"operators on {_WORKLOAD[0]} operands (>= 2 applies each, 0.5 s per operator), weighted by the "
+              f"per-sweep operator counts of the FP64 path {REF_COUNTS_BY_WORKLOAD[_WORKLOAD[0]]}; orthogonalisation and "
               "decompositions excluded (lower bound on the CPU sweep time); all host threads")
     line = {"impl": "reference", "metric": METRIC, "value": value, "unit": "sweeps/s", "n_gpus": ws,
             "steps": len(per), "warmup": args.warmup, "ms_per_step": 1e3 * float(np.mean(per)),
             "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic",
-            "config": {"workload": WORKLOAD_DESC, "implementation": "numpy restatement of the reference's operators"},
+            "config": {"workload": _workload_desc(), "implementation": "numpy restatement of the reference's operators"},
             "cpu_baseline": {"value": value, "unit": "sweeps/s", "cores": cores, "kind": "port", "sample": sample},
             "e2e": {"value": value, "unit": "sweeps/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
     print(json.dumps(line), flush=True)
@@ -389,7 +402,7 @@ def run_vumps(args):
         times, reps = cpu_op_times()
         t_cpu = cpu_sweep_model(counts, times)
         cpu = {"value": 1.0 / t_cpu, "unit": "sweeps/s", "cores": os.cpu_count(), "kind": "port",
-               "sample": "H_AC, H_C and unit-cell TM applies of the numpy restatement on XXZ D=512 operands "
+               "sample": f"H_AC, H_C and unit-cell TM applies of the numpy restatement on {_WORKLOAD[0]} operands "
                          f"({reps} applies), weighted by the per-sweep operator counts of the timed GPU sweeps "
                          f"{ {k: round(v, 1) for k, v in counts.items()} }; orthogonalisation and decompositions "
                          "excluded (lower bound on the CPU sweep time); all host threads",
@@ -398,7 +411,7 @@ def run_vumps(args):
             "warmup": args.warmup, "ms_per_step": t_step * 1e3, "higher_is_better": True, "scaling": "weak",
             "vs_baseline": None, "dtype": "bf16x6->f32 applies, f64 Krylov/decompositions" if args.precision == "bf16x6"
             else "f64", "data": "synthetic",
-            "config": {"workload": WORKLOAD_DESC, "precision": args.precision, "seed": 1,
+            "config": {"workload": _workload_desc(), "precision": args.precision, "seed": 1,
                        "l2": "working set (~40 MB) is L2-resident by design; H_AC timing flushes L2 (512 MB write)",
                        "parallelism": f"replicas x{ws}"},
             "fp64": {"sweeps_per_s": 1.0 / float(np.mean(r64["times"])), "ms_per_step": 1e3 * float(np.mean(r64["times"])),
@@ -603,6 +616,10 @@ def main():
     ap.add_argument("--no-cpu", action="store_true")
     args = ap.parse_args()
     args.warmup = max(args.warmup, 3)
+    if args.mode in ("vumps",) or args.impl == "reference":
+        if args.workload not in WORKLOAD_DESCS:
+            raise SystemExit(f"--workload for the VUMPS bench: one of {sorted(WORKLOAD_DESCS)}")
+        _WORKLOAD[0] = args.workload
     if args.impl == "reference":
         run_reference(args)
     elif args.mode == "hac":

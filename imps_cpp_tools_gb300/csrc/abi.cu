@@ -40,6 +40,9 @@ struct imps_ctx {
   // device-to-host copies are asynchronous and a check can be evaluated while the next
   // Krylov step runs
   double* hpin = nullptr;   // kPinDoubles doubles, then 16 ints
+  // the GMRES core's own staging (its solves run inside eigensolver callbacks, between an
+  // eigensolver's staging and its check)
+  double* hpin_g = nullptr;  // kPinDoubles doubles, then 16 ints
   cudaEvent_t ev_check = nullptr;
 };
 constexpr size_t kPinDoubles = (size_t)(imps::kMaxCols + 1) * (imps::kMaxCols + 1);
@@ -293,6 +296,7 @@ int imps_ctx_create(int device, imps_ctx** out) {
   c->ws.sync = c->ws.counter + 1;  // counter[0]: last-block reductions; [1], [2]: grid barrier
   c->ws.err = c->dflag + 4;
   CK(cudaMallocHost(&c->hpin, kPinDoubles * sizeof(double) + 16 * sizeof(int)));
+  CK(cudaMallocHost(&c->hpin_g, kPinDoubles * sizeof(double) + 16 * sizeof(int)));
   CK(cudaEventCreateWithFlags(&c->ev_check, cudaEventDisableTiming));
   *out = c;
   return IMPS_OK;
@@ -307,6 +311,7 @@ int imps_ctx_destroy(imps_ctx* c) {
   cudaFree(c->dscal);
   cudaFree(c->dflag);
   if (c->hpin) cudaFreeHost(c->hpin);
+  if (c->hpin_g) cudaFreeHost(c->hpin_g);
   if (c->ev_check) cudaEventDestroy(c->ev_check);
   if (c->arena) cudaFree(c->arena);
   if (c->arena_cb) cudaFree(c->arena_cb);
@@ -1280,15 +1285,12 @@ static int gmres_dev(imps_ctx* c, int64_t n, const DevOp& A, bool mixed, const d
   double* V = bp.take((size_t)n * (m + 1));
   double* w = bp.take(n);
   double* t = bp.take(n);
-  double* Hc = bp.take(ld);
+  double* Hd = bp.take((size_t)ld * m);  // Hessenberg columns (CGS2 projections), column j at j*ld
   double* tmp = bp.take(ld);
-  double* cs = bp.take(ld);
-  double* sn = bp.take(ld);
-  double* gam = bp.take(ld);
-  double* R = bp.take((size_t)ld * ld);
   double* ys = bp.take(ld);
-  double* dsc = c->dscal;  // 0: trace, 1: |r|, 2: |b|, 3: resid
+  double* dsc = c->dscal;  // 0: trace, 1: |r|, 2: |b|
   int* bflag = c->dflag + 1;
+  int* pin_flags = (int*)(c->hpin_g + kPinDoubles);
   // |b|
   RC(kr_multidot(c->ws, b, n, 1, b, n, tmp, 0, dsc + 2, st));
   double bnorm = 0.0;
@@ -1304,7 +1306,10 @@ static int gmres_dev(imps_ctx* c, int64_t n, const DevOp& A, bool mixed, const d
     if (relres) *relres = 0.0;
     return IMPS_OK;
   }
-  std::vector<double> Rh((size_t)ld * ld), gh(ld), yh(ld);
+  // Givens rotations of the Hessenberg columns (IterativeSolvers.hpp:79-85, 103-115), on the
+  // host at the residual checks: the columns of the steps since the last check arrive in one
+  // copy, so the device runs no serial rotation kernel per iteration
+  std::vector<double> Rh((size_t)ld * ld), gh(ld), yh(ld), csh(ld), snh(ld), col(ld + 1);
   // Mixed precision: every restart recomputes the true residual with the FP64 engine and the
   // inner Krylov cycle (split-BF16 applies) only has to reduce it by kMixedInnerTol, i.e.
   // restarted GMRES acts as iterative refinement with FP64 residuals.
@@ -1334,40 +1339,63 @@ static int gmres_dev(imps_ctx* c, int64_t n, const DevOp& A, bool mixed, const d
     inner_hit = false;
     CK(cudaMemsetAsync(bflag, 0, sizeof(int), st));
     RC(kr_scale_inv(w, dsc + 1, V, n, bflag, st));
-    CK(cudaMemsetAsync(gam, 0, ld * 8, st));
-    CK(cudaMemcpyAsync(gam, dsc + 1, 8, cudaMemcpyDeviceToDevice, st));
-    int kdim = 0;
+    std::fill(gh.begin(), gh.end(), 0.0);
+    gh[0] = rn;
+    int kdim = 0, jpulled = 0;
     for (int j = 0; j < m && it < maxit; ++j) {
       double* vj = V + (size_t)j * n;
       RC(A(vj, w, false));
       ++it;
-      RC(kr_cgs2_step(c->ws, V, n, j + 1, w, n, Hc, tmp, V + (size_t)(j + 1) * n, nullptr, st));
-      RC(kr_givens(Hc, j, cs, sn, gam, R, ld, dsc + 3, bflag, st));
+      RC(kr_cgs2_step(c->ws, V, n, j + 1, w, n, Hd + (size_t)j * ld, tmp, V + (size_t)(j + 1) * n, nullptr, st));
       kdim = j + 1;
       if ((j + 1) % 4 == 0 || j == m - 1 || it >= maxit) {
-        double res = 0.0;
-        int brk = 0, terr = 0;
-        CK(cudaMemcpyAsync(&res, dsc + 3, 8, cudaMemcpyDeviceToHost, st));
-        CK(cudaMemcpyAsync(&brk, bflag, sizeof(int), cudaMemcpyDeviceToHost, st));
-        CK(cudaMemcpyAsync(&terr, c->ws.err, sizeof(int), cudaMemcpyDeviceToHost, st));
+        CK(cudaMemcpyAsync(c->hpin_g, Hd + (size_t)jpulled * ld, (size_t)(j + 1 - jpulled) * ld * 8,
+                           cudaMemcpyDeviceToHost, st));
+        CK(cudaMemcpyAsync(pin_flags, c->ws.err, sizeof(int), cudaMemcpyDeviceToHost, st));
         CK(cudaStreamSynchronize(st));
-        if (terr) {
+        if (pin_flags[0]) {  // a grid-barrier wait of the CGS2 step ran out: report, re-arm
           CK(cudaMemsetAsync(c->ws.err, 0, sizeof(int), st));
           return IMPS_ERR_TIMEOUT;
         }
-        if (!std::isfinite(res)) return IMPS_ERR_NAN;
-        if (brk) { kdim = j; break; }  // invariant subspace
+        double res = 0.0;
+        bool brk = false;
+        for (int q = jpulled; q <= j; ++q) {
+          const double* hc = c->hpin_g + (size_t)(q - jpulled) * ld;
+          for (int i = 0; i <= q + 1; ++i) col[i] = hc[i];
+          for (int i = 0; i < q; ++i) {
+            const double h1 = col[i], h2 = col[i + 1];
+            col[i] = csh[i] * h1 + snh[i] * h2;
+            col[i + 1] = -snh[i] * h1 + csh[i] * h2;
+          }
+          const double hqq = col[q], hq1 = col[q + 1];
+          const double beta = std::sqrt(hqq * hqq + hq1 * hq1);
+          if (!std::isfinite(beta)) return IMPS_ERR_NAN;
+          if (!(beta >= 2e-16)) {  // flag -2 of the reference: column q adds nothing
+            brk = true;
+            kdim = q;
+            break;
+          }
+          const double habs = std::fabs(hqq);
+          const double phase = habs > 0.0 ? hqq / habs : 1.0;
+          snh[q] = phase * hq1 / beta;
+          csh[q] = habs / beta;
+          col[q] = phase * beta;
+          gh[q + 1] = -snh[q] * gh[q];
+          gh[q] *= csh[q];
+          for (int i = 0; i <= q; ++i) Rh[i + (size_t)q * ld] = col[i];
+          res = std::fabs(gh[q + 1]);
+        }
+        jpulled = j + 1;
+        if (brk) break;  // invariant subspace
         if (res < std::max(tol * bnorm, mixed ? kMixedInnerTol * rn : 0.0)) {
           inner_hit = true;
           break;
         }
       }
     }
-    // y += V[:, :kdim] * R^{-1} gamma
+    // y += V[:, :kdim] * R^{-1} gamma (R and gamma are on the host; checks pulled every column
+    // up to kdim, since a cycle ends only at a check)
     if (kdim > 0) {
-      CK(cudaMemcpyAsync(Rh.data(), R, (size_t)ld * kdim * 8, cudaMemcpyDeviceToHost, st));
-      CK(cudaMemcpyAsync(gh.data(), gam, kdim * 8, cudaMemcpyDeviceToHost, st));
-      CK(cudaStreamSynchronize(st));
       for (int i = kdim - 1; i >= 0; --i) {
         double s = gh[i];
         for (int q = i + 1; q < kdim; ++q) s -= Rh[i + (size_t)q * ld] * yh[q];

@@ -48,7 +48,4 @@ int kr_segsq(const KrylovWs& ws, const double* X, const int64_t* soff, const int
              double* out, cudaStream_t st);
 int kr_absmax(const KrylovWs& ws, const double* x, int64_t n, double* out, cudaStream_t st);
 int kr_sign_of_first(const double* x, double* s, cudaStream_t st);
-int kr_givens(double* Hcol, int j, double* cs, double* sn, double* gamma, double* R, int ldr,
-              double* res, int* breakdown, cudaStream_t st);
-
 }  // namespace imps

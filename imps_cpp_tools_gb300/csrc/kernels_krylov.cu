@@ -497,7 +497,9 @@ __global__ void proj_epilogue_kernel(const double* __restrict__ x, const double*
 
 // sum over blocks q of trace(X_q * R_q) = sum_{i,j} X_q[i + j m] * R_q[j + i m]
 // sum_b tr(X_b R_b): X_b is rows x cols at boff[b], R_b the cols x rows block at the same
-// offset (blocks paired in order; bcols == nullptr: square blocks)
+// offset (blocks paired in order; bcols == nullptr: square blocks).  Each CTA takes whole
+// blocks (warps over columns, lanes over rows: no index division, X read coalesced); the
+// partial sums are combined in a fixed order by the last CTA to finish.
 __global__ void __launch_bounds__(RB) trace_prod_kernel(const double* __restrict__ X,
                                                         const double* __restrict__ R,
                                                         const int64_t* __restrict__ boff,
@@ -508,17 +510,15 @@ __global__ void __launch_bounds__(RB) trace_prod_kernel(const double* __restrict
                                                         double* __restrict__ out) {
   __shared__ double sh[32];
   __shared__ bool last;
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5, nw = RB / 32;
   double acc = 0.0;
-  // flatten (block, element) pairs with a grid-stride loop over blocks x elements
-  for (int b = 0; b < nb; ++b) {
+  for (int b = blockIdx.x; b < nb; b += gridDim.x) {
     const int m = bdim[b];
     const int nc = bcols ? bcols[b] : m;
-    const int64_t o = boff[b];
-    const int64_t mm = (int64_t)m * nc;
-    for (int64_t e = (int64_t)blockIdx.x * RB + threadIdx.x; e < mm; e += (int64_t)gridDim.x * RB) {
-      const int64_t i = e % m, j = e / m;
-      acc = fma(X[o + e], R[o + j + i * nc], acc);
-    }
+    const double* __restrict__ x = X + boff[b];
+    const double* __restrict__ r = R + boff[b];
+    for (int j = warp; j < nc; j += nw)
+      for (int i = lane; i < m; i += 32) acc = fma(x[i + (int64_t)j * m], r[j + (int64_t)i * nc], acc);
   }
   acc = block_sum(acc, sh);
   if (threadIdx.x == 0) partials[blockIdx.x] = acc;
@@ -591,40 +591,6 @@ __global__ void __launch_bounds__(RB) absmax_kernel(const double* __restrict__ x
     __syncthreads();
   }
   if (threadIdx.x == 0) { *out = sh[0]; *counter = 0u; }
-}
-
-// One GMRES step of the reference's Givens update (IterativeSolvers.hpp:77-116), run by a
-// single thread on the device.  Hcol holds column j (j+2 entries, already orthogonalised,
-// Hcol[j+1] = |w|).  Applies rotations 0..j-1, forms rotation j, updates gamma, writes
-// |gamma[j+1]| to *res and stores the rotated column into R (column-major, ld = ldr).
-__global__ void givens_kernel(double* __restrict__ Hcol, int j, double* __restrict__ cs,
-                              double* __restrict__ sn, double* __restrict__ gamma,
-                              double* __restrict__ R, int ldr, double* __restrict__ res,
-                              int* __restrict__ breakdown) {
-  if (threadIdx.x != 0 || blockIdx.x != 0) return;
-  for (int i = 0; i < j; ++i) {
-    const double h1 = Hcol[i], h2 = Hcol[i + 1];
-    Hcol[i] = cs[i] * h1 + sn[i] * h2;
-    Hcol[i + 1] = -sn[i] * h1 + cs[i] * h2;
-  }
-  const double hjj = Hcol[j], hj1 = Hcol[j + 1];
-  const double beta = sqrt(hjj * hjj + hj1 * hj1);
-  if (!(beta >= 2e-16)) {  // flag -2 of the reference
-    *breakdown = 1;
-    *res = 0.0;
-    for (int i = 0; i <= j; ++i) R[i + (int64_t)j * ldr] = Hcol[i];
-    return;
-  }
-  const double habs = fabs(hjj);
-  const double phase = habs > 0.0 ? hjj / habs : 1.0;
-  sn[j] = phase * hj1 / beta;
-  cs[j] = habs / beta;
-  Hcol[j] = phase * beta;
-  Hcol[j + 1] = 0.0;
-  gamma[j + 1] = -sn[j] * gamma[j];
-  gamma[j] *= cs[j];
-  for (int i = 0; i <= j; ++i) R[i + (int64_t)j * ldr] = Hcol[i];
-  *res = fabs(gamma[j + 1]);
 }
 
 __global__ void sign_first_kernel(const double* __restrict__ x, double* __restrict__ s) {
@@ -755,7 +721,8 @@ int kr_proj_epilogue(const double* x, const double* t, const double* s, const do
 int kr_trace_prod(const KrylovWs& ws, const double* X, const double* R, const int64_t* boff,
                   const int32_t* bdim, int nb, double* out, cudaStream_t st, const int32_t* bcols) {
   imps::count_launch();
-  trace_prod_kernel<<<32, RB, 0, st>>>(X, R, boff, bdim, bcols, nb, ws.partials, ws.counter, out);
+  const int grid = std::max(1, std::min(nb, RB));  // the finishing CTA sums <= RB partials
+  trace_prod_kernel<<<grid, RB, 0, st>>>(X, R, boff, bdim, bcols, nb, ws.partials, ws.counter, out);
   return IMPS_OK;
 }
 
@@ -795,13 +762,6 @@ int kr_absmax(const KrylovWs& ws, const double* x, int64_t n, double* out, cudaS
   if (grid < 1) grid = 1;
   imps::count_launch();
   absmax_kernel<<<grid, RB, 0, st>>>(x, n, ws.partials, ws.counter, out);
-  return IMPS_OK;
-}
-
-int kr_givens(double* Hcol, int j, double* cs, double* sn, double* gamma, double* R, int ldr,
-              double* res, int* breakdown, cudaStream_t st) {
-  imps::count_launch();
-  givens_kernel<<<1, 32, 0, st>>>(Hcol, j, cs, sn, gamma, R, ldr, res, breakdown);
   return IMPS_OK;
 }
 
