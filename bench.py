@@ -41,8 +41,8 @@ L2_FLUSH_BYTES = 512 << 20
 TOLMIN = 1e-12  # floor of the eigensolver tolerance schedule and the GMRES tolerance
 # DRAM bytes (read + write) of one H_AC apply from one ncu capture of `bench.py --mode hac`
 # (profiles/tc_gemm_hac_xxz_d512.md: tc_gemm 5.26 MB + pack 0.40 MB;
-# profiles/grouped_gemm_f64_hac_xxz_d512.md: 2.36 MB), cold caches
-NCU_TRAFFIC_BYTES = {"bf16x6": 5.66e6, "fp64": 2.36e6}
+# profiles/grouped_gemm_f64_hac_xxz_d512.md: 2.38 MB), cold caches
+NCU_TRAFFIC_BYTES = {"bf16x6": 5.66e6, "fp64": 2.38e6}
 _SCHEDULE = ("2-site VUMPS sweep, tolerance schedule min(max(prec/100, 1e-12), 1e-6) (VUMPS_main.cpp:177), "
              "GMRES tol 1e-12, expansion off")
 WORKLOAD_DESCS = {
