@@ -82,6 +82,8 @@ _PROTOS = {
     "imps_tm_dominant": (c_int, [c_vp, c_vp, c_vp, c_int, c_dbl, c_int, P_dbl, P_int]),
     "imps_eigs_rs_op": (c_int, [c_vp, c_i64, APPLY_FN, c_vp, c_vp, c_int, c_int, c_dbl, c_int, c_int, P_dbl,
                                 c_vp, P_int]),
+    "imps_sector_svd_batch": (c_int, [c_int, C.POINTER(c_vp), C.POINTER(c_vp), C.POINTER(c_vp), C.POINTER(c_vp),
+                                      C.POINTER(c_vp), c_int]),
     "imps_eigs_n": (c_int, [c_vp, c_vp, c_int, c_int, c_int, c_dbl, c_int, c_int, P_dbl, c_vp, c_vp, P_int]),
     "imps_eigs_n_op": (c_int, [c_vp, c_i64, APPLY_FN, c_vp, c_vp, c_int, c_int, c_int, c_dbl, c_int, c_int,
                                P_dbl, c_vp, c_vp, P_int]),

@@ -1737,6 +1737,45 @@ int imps_sector_svd(imps_plan* p, const double* A, double* U, double* S, double*
   return status ? IMPS_WARN_NOT_CONVERGED : IMPS_OK;
 }
 
+int imps_sector_svd_batch(int np, imps_plan* const* plans, const double* const* A, double* const* U,
+                          double* const* S, double* const* Viso, int mem) {
+  if (np < 1 || np > kSvdSets || !plans || !A || mem != IMPS_MEM_DEVICE) return IMPS_ERR_BAD_ARG;
+  imps_ctx* c = plans[0] ? plans[0]->ctx : nullptr;
+  if (!c) return IMPS_ERR_BAD_ARG;
+  if (c->device < 0) return IMPS_ERR_NO_DEVICE;
+  cudaStream_t st = c->stream;
+  SvdSets sets{};
+  sets.nsets = np;
+  int maxN = 0;
+  int64_t maxMN = 0;
+  for (int k = 0; k < np; ++k) {
+    imps_plan* p = plans[k];
+    if (!p || p->P.kind != PLAN_DECOMP || p->ctx != c || !A[k] || !p->dc->tall) return IMPS_ERR_BAD_ARG;
+    DecompPlan* D = p->dc;
+    for (const DenseMat& m : D->mats) {
+      maxN = std::max(maxN, (int)m.N);
+      maxMN = std::max(maxMN, (int64_t)m.M * m.N);
+    }
+    RC(dc_gather(D->d_ent, (int)D->ent.size(), A[k], D->dA, st));
+    sets.s[k] = SvdSet{D->d_mats, D->dA, (S && S[k]) ? S[k] : D->dS, D->dR, D->dW, (int)D->mats.size()};
+  }
+  int* status = plans[0]->dc->dstatus;
+  CK(cudaMemsetAsync(status, 0, sizeof(int), st));
+  RC(dc_svd_sets(sets, maxN, maxMN, status, st));
+  for (int k = 0; k < np; ++k) {
+    DecompPlan* D = plans[k]->dc;
+    if (U && U[k]) RC(dc_scatter(D->d_ent, (int)D->ent.size(), D->dA, U[k], st));
+    if (Viso && Viso[k]) {
+      if (D->dir == 0) RC(dc_transpose_sq(D->d_mats, (int)D->mats.size(), D->dR, Viso[k], st));
+      else CK(cudaMemcpyAsync(Viso[k], D->dR, D->r_elems * 8, cudaMemcpyDeviceToDevice, st));
+    }
+  }
+  int stat = 0;
+  CK(cudaMemcpyAsync(&stat, status, sizeof(int), cudaMemcpyDeviceToHost, st));
+  CK(cudaStreamSynchronize(st));
+  return stat ? IMPS_WARN_NOT_CONVERGED : IMPS_OK;
+}
+
 int imps_sector_colscale(imps_plan* p, double* X, const double* S, double power, int mem) {
   if (!p || p->P.kind != PLAN_DECOMP || !X || !S || mem != IMPS_MEM_DEVICE) return IMPS_ERR_BAD_ARG;
   if (p->ctx->device < 0) return IMPS_ERR_NO_DEVICE;

@@ -453,14 +453,21 @@ __device__ int jacobi_sweeps(T* B, T* V, int N, int ld, double tol, int max_swee
 // |<b_p, b_q>| <= N eps |b_p| |b_q| for all pairs.  Outputs as svd_kernel: U (M x N) left
 // singular vectors, S descending, V (N x N) right singular vectors.
 template <bool MIXED>
-__global__ void __launch_bounds__(JT) svd_pjac_kernel(const imps::DenseMat* __restrict__ mats,
-                                                      double* __restrict__ U, double* __restrict__ S,
-                                                      double* __restrict__ V, double* __restrict__ Wk,
-                                                      int a_smem, int max_sweeps, int* __restrict__ status) {
+__global__ void __launch_bounds__(JT) svd_pjac_kernel(const imps::SvdSets sets, int a_smem, int max_sweeps,
+                                                      int* __restrict__ status) {
   extern __shared__ double smem[];
   __shared__ double sh[32];
   __shared__ int flag, sel;
-  const imps::DenseMat mt = mats[blockIdx.x];
+  int bi = blockIdx.x, ks = 0;
+  while (ks + 1 < sets.nsets && bi >= sets.s[ks].n) {
+    bi -= sets.s[ks].n;
+    ++ks;
+  }
+  const imps::DenseMat mt = sets.s[ks].mats[bi];
+  double* __restrict__ U = sets.s[ks].U;
+  double* __restrict__ S = sets.s[ks].S;
+  double* __restrict__ V = sets.s[ks].V;
+  double* __restrict__ Wk = sets.s[ks].W;
   const int M = mt.M, N = mt.N;
   if (N <= 0 || M < N) return;
   const int ld = N | 1;  // odd: lanes owning different columns hit different banks
@@ -643,12 +650,27 @@ int dc_nullspace(const DenseMat* d_mats, int nmat, double* A, double* NS, cudaSt
 
 int dc_svd(const DenseMat* d_mats, int nmat, int maxN, int64_t maxMN, double* U, double* S, double* V, double* W,
            int* status, cudaStream_t st) {
+  SvdSets sets{};
+  sets.nsets = 1;
+  sets.s[0] = SvdSet{d_mats, U, S, V, W, nmat};
+  return dc_svd_sets(sets, maxN, maxMN, status, st);
+}
+
+int dc_svd_sets(const SvdSets& sets, int maxN, int64_t maxMN, int* status, cudaStream_t st) {
+  if (sets.nsets < 1 || sets.nsets > kSvdSets) return IMPS_ERR_BAD_ARG;
+  int nmat = 0;
+  for (int k = 0; k < sets.nsets; ++k) nmat += sets.s[k].n;
   if (nmat <= 0) return IMPS_OK;
-  imps::count_launch();
-  if (maxN > kJacobiMaxN) {
-    svd_kernel<<<nmat, DT, 0, st>>>(d_mats, U, S, V, W, 40, status);
+  if (maxN > kJacobiMaxN) {  // global-memory fallback, one launch per set
+    for (int k = 0; k < sets.nsets; ++k) {
+      if (sets.s[k].n <= 0) continue;
+      imps::count_launch();
+      svd_kernel<<<sets.s[k].n, DT, 0, st>>>(sets.s[k].mats, sets.s[k].U, sets.s[k].S, sets.s[k].V, sets.s[k].W,
+                                             40, status);
+    }
     return cudaGetLastError() == cudaSuccess ? IMPS_OK : IMPS_ERR_CUDA;
   }
+  imps::count_launch();
   constexpr size_t kSmemMax = 226 * 1024;  // dynamic part; the static flags and sums take < 1 KB
   const bool mixed = maxN <= kMixedMaxN;
   const int64_t ld = maxN | 1;
@@ -665,8 +687,8 @@ int dc_svd(const DenseMat* d_mats, int nmat, int maxN, int64_t maxMN, double* U,
       return IMPS_ERR_CUDA;
     attr_set = true;
   }
-  if (mixed) svd_pjac_kernel<true><<<nmat, JT, bytes, st>>>(d_mats, U, S, V, W, a_smem, 20, status);
-  else svd_pjac_kernel<false><<<nmat, JT, bytes, st>>>(d_mats, U, S, V, W, a_smem, 30, status);
+  if (mixed) svd_pjac_kernel<true><<<nmat, JT, bytes, st>>>(sets, a_smem, 20, status);
+  else svd_pjac_kernel<false><<<nmat, JT, bytes, st>>>(sets, a_smem, 30, status);
   return cudaGetLastError() == cudaSuccess ? IMPS_OK : IMPS_ERR_CUDA;
 }
 

@@ -67,6 +67,19 @@ constexpr int kJacobiMaxN = 118;
 constexpr int kMixedMaxN = 96;
 int dc_svd(const DenseMat* d_mats, int nmat, int maxN, int64_t maxMN, double* U, double* S, double* V, double* W,
            int* status, cudaStream_t st);
+// Up to kSvdSets independent sector SVDs (e.g. the two polar steps of a site update) in one
+// launch: set k's sectors are CTAs [sum_{j<k} n_j, sum_{j<=k} n_j).
+constexpr int kSvdSets = 4;
+struct SvdSet {
+  const DenseMat* mats;
+  double *U, *S, *V, *W;
+  int n;
+};
+struct SvdSets {
+  SvdSet s[kSvdSets];
+  int nsets;
+};
+int dc_svd_sets(const SvdSets& sets, int maxN, int64_t maxMN, int* status, cudaStream_t st);
 int dc_colscale(const DenseMat* d_mats, int nmat, double* X, const double* S, double power, cudaStream_t st);
 int dc_transpose_sq(const DenseMat* d_mats, int nmat, const double* X, double* Y, cudaStream_t st);
 int dc_nullspace(const DenseMat* d_mats, int nmat, double* A, double* NS, cudaStream_t st);

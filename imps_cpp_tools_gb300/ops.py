@@ -171,6 +171,16 @@ def svd(dec, A, U=None, S=None, V=None):
     return st == 0
 
 
+def svd_batch(decs, As, Us=None, Ss=None, Vs=None):
+    """Several independent svd(S, DiagIso, MPS, dir) in one launch (imps_sector_svd_batch), e.g.
+    the two polar steps of a site update.  Returns True if every one converged."""
+    n = len(decs)
+    arr = lambda ts: (C.c_void_p * n)(*[None if t is None else _dptr(t) for t in (ts or [None] * n)])
+    hs = (C.c_void_p * n)(*[d.handle.value for d in decs])
+    st = N.call("imps_sector_svd_batch", n, hs, arr(As), arr(Us), arr(Ss), arr(Vs), N.MEM_DEVICE)
+    return st == 0
+
+
 def Nullspace(plan, A, NL):
     """Nullspace(A, l) (MPSBlockUtilities.hpp:247-300) with a dir-l decomposition plan: NL in the
     plan's derived layout 2."""

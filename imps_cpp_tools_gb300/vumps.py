@@ -295,15 +295,15 @@ class VumpsGPU:
             self.dosvd = False
         ALnew, ARnew = self._z(self.LA[n]), self._z(self.LA[n])
         if self.dosvd:
-            # polar: AL = U V^T of AC CR^T ; AR = U V^T of CL^T AC  (VUMPS_main.cpp:213-220)
+            # polar: AL = U V^T of AC CR^T ; AR = U V^T of CL^T AC  (VUMPS_main.cpp:213-220); the
+            # two independent SVDs share one launch
             X = self._mul(self.p_mul_r_t[n], AC, CR, self._z(self.LA[n]))
+            X2 = self._mul(self.p_mul_l_t[n], AC, CL, self._z(self.LA[n]))
             U, V = self._z(self.LA[n]), self._z(self.dec_ac_l[n].rlayout)
-            ops.svd(self.dec_ac_l[n], X, U, None, V)
+            U2, V2 = self._z(self.LA[n]), self._z(self.dec_ac_r[n].rlayout)
+            ops.svd_batch([self.dec_ac_l[n], self.dec_ac_r[n]], [X, X2], [U, U2], None, [V, V2])
             self._mul(self.p_mul_r[n], U, V, ALnew)
-            X = self._mul(self.p_mul_l_t[n], AC, CL, self._z(self.LA[n]))
-            U, V = self._z(self.LA[n]), self._z(self.dec_ac_r[n].rlayout)
-            ops.svd(self.dec_ac_r[n], X, U, None, V)
-            self._mul(self.p_mul_l[n], U, V, ARnew)
+            self._mul(self.p_mul_l[n], U2, V2, ARnew)
         else:
             # QR scheme (VUMPS_main.cpp:221-234)
             QL, Rt = self._z(self.LA[n]), self._z(self.dec_ac_l[n].rlayout)

@@ -256,8 +256,15 @@ int imps_sector_qr(imps_plan* dec, const double* A, double* Q, double* R, int me
 int imps_sector_nullspace(imps_plan* plan, const double* A, double* NL, int mem);
 /* svd(S, DiagIso, MPS, dir) (MPSBlockUtilities.hpp:78-153): U = MPSIso (A's layout), S =
  * singular values per sector concatenated in sector order (descending), Viso = DiagIso
- * (V^T for dir l, U for dir r).  Any output may be NULL.  One-sided Jacobi, FP64. */
+ * (V^T for dir l, U for dir r).  Any output may be NULL.  Column-pivoted QR, then one-sided
+ * Jacobi on R^T (first sweeps in FP32, finished and tested in FP64); FP64 results. */
 int imps_sector_svd(imps_plan* dec, const double* A, double* U, double* S, double* Viso, int mem);
+/* Several independent sector SVDs (each as imps_sector_svd, on its own decomposition plan of
+ * one context; at most 4) in one launch: the two polar steps of a site update,
+ * svd(AC CR^T, l) and svd(CL^T AC, r) (VUMPS_main.cpp:213-220), fill twice the SMs of one.
+ * Arrays of np pointers; entries of U, S, Viso may be NULL. */
+int imps_sector_svd_batch(int np, imps_plan* const* plans, const double* const* A, double* const* U,
+                          double* const* S, double* const* Viso, int mem);
 /* X_q[:, j] *= S_q[j]^power on a BlockDiagMat decomposition plan (BlockDiagMat << BlockLam,
  * BlockObj.hpp:2316), e.g. U * sqrt(S) in randMPS_LR (MPSBlockUtilities.hpp:1116-1118) */
 int imps_sector_colscale(imps_plan* dec, double* X, const double* S, double power, int mem);
