@@ -305,7 +305,7 @@ __global__ void __launch_bounds__(CT) cgs2_coop_kernel(const double* __restrict_
                                                       double* __restrict__ partials, unsigned int* sync,
                                                       int* err) {
   __shared__ double wsm[COOP_SUB];
-  __shared__ double h1[imps::kMaxCols + 1];
+  __shared__ double h1[imps::kMaxCols];
   __shared__ double h2[imps::kMaxCols + 1];
   __shared__ double sh[32];
   __shared__ double beta;
@@ -319,69 +319,40 @@ __global__ void __launch_bounds__(CT) cgs2_coop_kernel(const double* __restrict_
   bool ok = true;
   for (int t = threadIdx.x; t < len; t += blockDim.x) wsm[t] = w[base + t];
   __syncthreads();
-  // pass 1: h1 = V^T w, and |w|^2 as column nc of the same partials
+  // pass 1: h1 = V^T w
   block_dots(Vb, ldv, nc, wsm, len, P0, G);
-  {
-    double n0 = 0.0;
-    for (int t = threadIdx.x; t < len; t += blockDim.x) n0 = fma(wsm[t], wsm[t], n0);
-    n0 = block_sum(n0, sh);
-    if (threadIdx.x == 0) P0[(int64_t)nc * G + blockIdx.x] = n0;
-  }
   ok = grid_barrier(sync, (unsigned)G, err, ok);
-  if (ok) reduce_partials(P0, G, nc + 1, h1);  // h1[nc] = |w|^2
+  if (ok) reduce_partials(P0, G, nc, h1);
   __syncthreads();
-  // DGKS test, as ARPACK's dsaitr / dnaitr: re-orthogonalise only if the projection removed
-  // enough of w that |w1| <= 0.717 |w|.  Otherwise one pass is orthogonal to working precision
-  // and |w1|^2 = |w|^2 - |h1|^2 loses at most a factor 2 of relative accuracy.  Every block
-  // holds the same reduced values, so all take the same branch.
-  __shared__ bool once;
-  if (threadIdx.x == 0) {
-    double s1 = 0.0;
-    for (int c = 0; c < nc; ++c) s1 = fma(h1[c], h1[c], s1);
-    const double r2 = h1[nc] - s1;
-    once = ok && r2 > 0.514089 * h1[nc];  // 0.717^2
-    if (once) beta = sqrt(r2);
-  }
-  __syncthreads();
-  if (once) {
-    update_rows(Vb, ldv, nc, h1, wsm, len);
-    for (int c = threadIdx.x; c <= nc; c += blockDim.x) h2[c] = 0.0;
-    __syncthreads();
-  }
   // pass 2: w -= V h1; h2 = V^T w
-  if (ok && !once) {
+  if (ok) {
     update_rows(Vb, ldv, nc, h1, wsm, len);
     __syncthreads();
     block_dots(Vb, ldv, nc, wsm, len, P1, G);
   }
-  __shared__ bool pyth;
-  if (!once) {
-    // |w|^2 before the second update rides along as column nc of the same partials
-    {
-      double n1 = 0.0;
-      if (ok)
-        for (int t = threadIdx.x; t < len; t += blockDim.x) n1 = fma(wsm[t], wsm[t], n1);
-      n1 = block_sum(n1, sh);
-      if (threadIdx.x == 0) P1[(int64_t)nc * G + blockIdx.x] = n1;
-    }
-    ok = grid_barrier(sync, 2u * G, err, ok);
-    if (ok) reduce_partials(P1, G, nc + 1, h2);  // h2[nc] = |w1|^2
-    __syncthreads();
-    // pass 3: w -= V h2; beta = |w|.  V orthonormal: |w2|^2 = |w1|^2 - |h2|^2 exactly, and the
-    // second-pass coefficients are tiny unless w1 nearly lies in span(V); then (identically in
-    // every block, which all hold the same reduced values) the norm is reduced explicitly.
-    if (threadIdx.x == 0) {
-      double s2 = 0.0;
-      for (int c = 0; c < nc; ++c) s2 = fma(h2[c], h2[c], s2);
-      pyth = s2 <= 0.1 * h2[nc];
-      if (pyth) beta = sqrt(h2[nc] - s2);
-    }
-    __syncthreads();
-    if (ok) update_rows(Vb, ldv, nc, h2, wsm, len);
-    __syncthreads();
-  } else if (threadIdx.x == 0) {
-    pyth = true;
+  // |w|^2 before the second update rides along as column nc of the same partials
+  {
+    double n1 = 0.0;
+    if (ok)
+      for (int t = threadIdx.x; t < len; t += blockDim.x) n1 = fma(wsm[t], wsm[t], n1);
+    n1 = block_sum(n1, sh);
+    if (threadIdx.x == 0) P1[(int64_t)nc * G + blockIdx.x] = n1;
   }
+  ok = grid_barrier(sync, 2u * G, err, ok);
+  if (ok) reduce_partials(P1, G, nc + 1, h2);  // h2[nc] = |w1|^2
+  __syncthreads();
+  // pass 3: w -= V h2; beta = |w|.  V orthonormal: |w2|^2 = |w1|^2 - |h2|^2 exactly, and the
+  // second-pass coefficients are tiny unless w1 nearly lies in span(V); then (identically in
+  // every block, which all hold the same reduced values) the norm is reduced explicitly.
+  __shared__ bool pyth;
+  if (threadIdx.x == 0) {
+    double s2 = 0.0;
+    for (int c = 0; c < nc; ++c) s2 = fma(h2[c], h2[c], s2);
+    pyth = s2 <= 0.1 * h2[nc];
+    if (pyth) beta = sqrt(h2[nc] - s2);
+  }
+  __syncthreads();
+  if (ok) update_rows(Vb, ldv, nc, h2, wsm, len);
   __syncthreads();
   if (!pyth) {
     double nacc = 0.0;
