@@ -506,8 +506,10 @@ class ExcitationsGPU:
         the environment solves only at K = 0 and momentum p = 0 (|p| < 10 InvETol)."""
         return self.LM is not None and all(k == 0 for k in self.K) and abs(p) < 10 * self.tol
 
-    def energies(self, kfac, nev=4, eig_tol=1e-10, ncv=0, seed=1, p=None):
-        """The nev lowest energies at kfac = e^{ip} (p: the momentum, default arg(kfac))."""
+    def energies(self, kfac, nev=4, eig_tol=1e-10, ncv=64, seed=1, p=None):
+        """The nev lowest energies at kfac = e^{ip} (p: the momentum, default arg(kfac)).  ncv: the
+        Lanczos basis (eigs.cpp's default is 20; with each H_eff apply costing two GMRES
+        solves, 64 needs ~half the applies at XXZ D=256, with the same energies)."""
         import torch
         p = float(np.angle(kfac)) if p is None else float(p)
         LM, RM = (self.LM, self.RM) if self.projected(p) else (None, None)

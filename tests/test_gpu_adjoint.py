@@ -66,3 +66,44 @@ def test_energy_gradient_from_vumps_state_xxz_d256(cuda_ctx):
     assert conv and abs(e - eref) < 1e-11 * abs(eref)
     for got, ref in ((host(G0), O.mps_vec(Gref[0])), (host(G1), O.mps_vec(Gref[1]))):
         assert np.linalg.norm(got - ref) <= 1e-8 * np.linalg.norm(ref)
+
+
+def test_autograd_wrapper(cuda_ctx):
+    """The gradient as the backward of a torch.autograd.Function (test harness only): autograd's
+    gradient of e with respect to both site tensors equals the device gradient, and its
+    directional derivative matches central differences of the oracle's energy."""
+    import torch
+    from imps_cpp_tools_gb300.adjoint import EnergyGradientGPU
+    model, dims0, params = CASES[1]
+    st = _state(model, dims0, params)
+    AL, R, hnnz, d = st["AL"], st["R"], st["hnnz"], st["d"]
+    LA, LB = _layouts(st)
+    g = EnergyGradientGPU(cuda_ctx, LA, LB, hnnz, d, tol=1e-13)
+
+    class Energy(torch.autograd.Function):
+        @staticmethod
+        def forward(fctx, A0, A1):
+            G0, G1, e, _, _ = g(A0.detach(), A1.detach(), dev(O.bd_vec(R)))
+            fctx.save_for_backward(G0.clone(), G1.clone())
+            return torch.tensor(e, dtype=torch.float64, device=A0.device)
+
+        @staticmethod
+        def backward(fctx, ge):
+            G0, G1 = fctx.saved_tensors
+            return ge * G0, ge * G1
+
+    A0 = dev(O.mps_vec(AL[0])).requires_grad_(True)
+    A1 = dev(O.mps_vec(AL[1])).requires_grad_(True)
+    e = Energy.apply(A0, A1)
+    e.backward()
+    Gref, eref = O.energy_gradient(AL, R, hnnz, tol=1e-14)
+    assert abs(float(e) - eref) < 1e-12
+    assert np.linalg.norm(host(A0.grad) - O.mps_vec(Gref[0])) <= 1e-9 * np.linalg.norm(O.mps_vec(Gref[0]))
+    rng = np.random.default_rng(2)
+    D = [[{q: (qo, rng.standard_normal(M.shape)) for q, (qo, M) in bm.items()} for bm in A] for A in AL]
+    pert = lambda s: [[{q: (qo, M + s * D[n][k][q][1]) for q, (qo, M) in bm.items()} for k, bm in enumerate(A)]
+                      for n, A in enumerate(AL)]
+    eps = 1e-6
+    fd = (O.energy_uniform(pert(eps), hnnz) - O.energy_uniform(pert(-eps), hnnz)) / (2 * eps)
+    an = float(host(A0.grad) @ O.mps_vec(D[0]) + host(A1.grad) @ O.mps_vec(D[1]))
+    assert abs(fd - an) <= 1e-6 * abs(fd)
