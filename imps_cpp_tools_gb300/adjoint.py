@@ -30,7 +30,7 @@ import numpy as np
 from . import _native as N
 from . import blocks as B
 from . import ops
-from .excitations import ES, OPS, OUT, RHS, SCR, Program, Tensor, _left_group, _same_group, expr
+from .excitations import ES, OPS, OUT, RHS, SCR, Program, Tensor, _left_group, _right_group, _same_group, expr
 
 
 def _layout_tensor(prog, slot, lay, ngroups):
@@ -103,7 +103,7 @@ class EnergyGradientProgram:
         # right-hand sides (before the -E2/2 r and -E2/2 1 corrections):
         # g_l = (E~0(r) + T~_0(E~1(r1))) / 2, g_r = (E0(1) + T_1(E1(1))) / 2 on bond 0
         self.A0Et1 = mat([(expr(A0), expr(self.Et1), _left_group)], d)[0]
-        self.E1lA1 = mat([(expr(self.E1l), expr(A1), _right_group_d)], d)[0]
+        self.E1lA1 = mat([(expr(self.E1l), expr(A1), _right_group)], d)[0]
         self.gl, self.gl_off = target(RHS, LB[0], 1)
         mat([(expr(self.G0a, coef=0.5), expr(A0, t=True), _same_group),
              (expr(self.A0Et1, coef=0.5), expr(A0, t=True), _same_group)], 1, target=self.gl)
@@ -120,10 +120,10 @@ class EnergyGradientProgram:
         A1yl = matb([(expr(A1), expr(self.yl), _left_group)], d)[0]
         self.T1yl, _ = _layout_tensor(pb, SCR, LB[1], 1)
         matb([(expr(A1yl), expr(A1, t=True), _same_group)], 1, target=self.T1yl)
-        yrA0 = matb([(expr(self.yr), expr(A0), _right_group_d)], d)[0]
+        yrA0 = matb([(expr(self.yr), expr(A0), _right_group)], d)[0]
         self.T0yr, _ = _layout_tensor(pb, SCR, LB[1], 1)
         matb([(expr(A0, t=True), expr(yrA0), _same_group)], 1, target=self.T0yr)
-        T0yrA1 = matb([(expr(self.T0yr), expr(A1), _right_group_d)], d)[0]
+        T0yrA1 = matb([(expr(self.T0yr), expr(A1), _right_group)], d)[0]
         # z_l = -y_l, z_r = -y_r: the -2 (z ...) terms enter with +2
         self.G0, self.g0_off = _layout_tensor(pb, OUT, LA[0], d)
         matb(self._w_right(A0, self.W) + [
@@ -145,10 +145,6 @@ class EnergyGradientProgram:
         d = self.d
         return [(expr(A, group=sp), expr(W, group=s * d + sp), (lambda ga, gb, g=s: g))
                 for s in range(d) for sp in range(d)]
-
-
-def _right_group_d(ga, gb):
-    return gb
 
 
 class EnergyGradientGPU:

@@ -18,7 +18,6 @@ Only U(1)^k charges are restated (all configurations use U(1) or U(1)xU(1)).
 from __future__ import annotations
 
 import math
-from functools import reduce
 
 import numpy as np
 
