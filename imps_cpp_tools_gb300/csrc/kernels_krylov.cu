@@ -497,9 +497,12 @@ __global__ void proj_epilogue_kernel(const double* __restrict__ x, const double*
 
 // sum over blocks q of trace(X_q * R_q) = sum_{i,j} X_q[i + j m] * R_q[j + i m]
 // sum_b tr(X_b R_b): X_b is rows x cols at boff[b], R_b the cols x rows block at the same
-// offset (blocks paired in order; bcols == nullptr: square blocks).  Each CTA takes whole
-// blocks (warps over columns, lanes over rows: no index division, X read coalesced); the
-// partial sums are combined in a fixed order by the last CTA to finish.
+// offset (blocks paired in order; bcols == nullptr: square blocks).  A flat grid-stride loop
+// over all elements (about one per thread: the loads are independent, so the transposed R
+// reads do not form a latency chain); each element finds its block by binary search over the
+// block offsets, cached in shared memory.  Partial sums are combined in a fixed order by the
+// last CTA to finish (gridDim.x <= RB).
+constexpr int kTraceCache = 1024;
 __global__ void __launch_bounds__(RB) trace_prod_kernel(const double* __restrict__ X,
                                                         const double* __restrict__ R,
                                                         const int64_t* __restrict__ boff,
@@ -508,17 +511,40 @@ __global__ void __launch_bounds__(RB) trace_prod_kernel(const double* __restrict
                                                         double* __restrict__ partials,
                                                         unsigned int* __restrict__ counter,
                                                         double* __restrict__ out) {
+  __shared__ int64_t so[kTraceCache];
+  __shared__ int32_t sm[kTraceCache], sc[kTraceCache];
   __shared__ double sh[32];
   __shared__ bool last;
-  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5, nw = RB / 32;
+  const bool cached = nb <= kTraceCache;
+  if (cached)
+    for (int b = threadIdx.x; b < nb; b += blockDim.x) {
+      so[b] = boff[b];
+      sm[b] = bdim[b];
+      sc[b] = bcols ? bcols[b] : bdim[b];
+    }
+  __syncthreads();
+  auto off = [&](int b) -> int64_t { return cached ? so[b] : boff[b]; };
+  auto rows = [&](int b) -> int { return cached ? sm[b] : bdim[b]; };
+  auto cols = [&](int b) -> int { return cached ? sc[b] : (bcols ? bcols[b] : bdim[b]); };
   double acc = 0.0;
-  for (int b = blockIdx.x; b < nb; b += gridDim.x) {
-    const int m = bdim[b];
-    const int nc = bcols ? bcols[b] : m;
-    const double* __restrict__ x = X + boff[b];
-    const double* __restrict__ r = R + boff[b];
-    for (int j = warp; j < nc; j += nw)
-      for (int i = lane; i < m; i += 32) acc = fma(x[i + (int64_t)j * m], r[j + (int64_t)i * nc], acc);
+  if (nb > 0) {
+    const int64_t ntot = off(nb - 1) + (int64_t)rows(nb - 1) * cols(nb - 1);
+    for (int64_t e = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; e < ntot;
+         e += (int64_t)gridDim.x * blockDim.x) {
+      // the last block starting at or before e (a later block at the same offset is the one
+      // that is not empty)
+      int lo = 0, hi = nb - 1;
+      while (lo < hi) {
+        const int mid = (lo + hi + 1) >> 1;
+        if (off(mid) <= e) lo = mid;
+        else hi = mid - 1;
+      }
+      const int m = rows(lo), nc = cols(lo);
+      const int64_t o = off(lo);
+      const int t = (int)(e - o);
+      const int i = t % m, j = t / m;
+      acc = fma(X[e], R[o + j + (int64_t)i * nc], acc);
+    }
   }
   acc = block_sum(acc, sh);
   if (threadIdx.x == 0) partials[blockIdx.x] = acc;
@@ -721,7 +747,7 @@ int kr_proj_epilogue(const double* x, const double* t, const double* s, const do
 int kr_trace_prod(const KrylovWs& ws, const double* X, const double* R, const int64_t* boff,
                   const int32_t* bdim, int nb, double* out, cudaStream_t st, const int32_t* bcols) {
   imps::count_launch();
-  const int grid = std::max(1, std::min(nb, RB));  // the finishing CTA sums <= RB partials
+  constexpr int grid = 128;  // <= RB: the finishing CTA sums the partials of every CTA
   trace_prod_kernel<<<grid, RB, 0, st>>>(X, R, boff, bdim, bcols, nb, ws.partials, ws.counter, out);
   return IMPS_OK;
 }
