@@ -154,7 +154,7 @@ def _workload_desc():
 # Lanczos solves per site update), unit-cell transfer-matrix applies (GMRES iterations of the
 # environment and fixed-point solves).  The reference arm weights its CPU operator times with
 # these; the GPU arm uses the counts of its own timed sweeps.
-REF_COUNTS_BY_WORKLOAD = {"xxz_d512": {"hac": 373.4, "hc": 554.9, "tm": 311.7},
+REF_COUNTS_BY_WORKLOAD = {"xxz_d512": {"hac": 281.6, "hc": 448.4, "tm": 293.0},
                           # --workload hubbard_d1024 --steps 37 --warmup 3
                           "hubbard_d1024": {"hac": 618.6, "hc": 1129.1, "tm": 293.6}}
 
