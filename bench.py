@@ -156,7 +156,7 @@ def _workload_desc():
 # these; the GPU arm uses the counts of its own timed sweeps.
 REF_COUNTS_BY_WORKLOAD = {"xxz_d512": {"hac": 281.6, "hc": 448.4, "tm": 293.0},
                           # --workload hubbard_d1024 --steps 37 --warmup 3
-                          "hubbard_d1024": {"hac": 618.6, "hc": 1129.1, "tm": 293.6}}
+                          "hubbard_d1024": {"hac": 570.5, "hc": 1029.8, "tm": 296.3}}
 
 
 def cpu_op_times(budget_per_op=2.0, seed=1):
