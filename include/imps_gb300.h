@@ -197,7 +197,7 @@ int imps_eigs_n_op(imps_ctx* ctx, int64_t n, imps_apply_fn fn, void* user, const
                    int* n_applies);
 /* InvertE_proj (InvEBlockFunctions.hpp:201-266) on a TM plan: solves
  *  dir l: y (1 - T + |R)(L|) = x (1 - |R)(L|),  dir r: (1 - T + |R)(L|) y = (1 - |R)(L|) x
- * with restarted GMRES (Krylov size `krylov`, 0 = 40); y holds y0 on entry (NULL = zeros). */
+ * with restarted GMRES (Krylov size `krylov`, 0 = 80); y holds y0 on entry (NULL = zeros). */
 int imps_invert_e_proj(imps_plan* tm, const double* x, const double* L, const double* R,
                        int dir, double* y, int mem, double tol, int maxit, int krylov,
                        int* iters, double* relres);

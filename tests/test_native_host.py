@@ -174,3 +174,30 @@ def test_nullspace_layout_matches_oracle_structure():
                for s in range(len(NL)) for qi in sorted(NL[s]) if NL[s][qi][1].shape[1] > 0]
         got = [(b[0], tuple(b[1]), tuple(b[2]), b[3], b[4]) for b in plan.nslayout.blocks]
         assert got == ref
+
+
+def _build_cpp_host(tmp_path):
+    """Compile and link the C++ host program over the C ABI (include/imps_gb300.hpp)."""
+    import shutil
+    import subprocess
+    from pathlib import Path
+    gxx, nvcc = shutil.which("g++"), shutil.which("nvcc")
+    if gxx is None or nvcc is None:
+        pytest.skip("g++ or the CUDA toolkit not available")
+    cuda = Path(nvcc).resolve().parent.parent
+    N.load()
+    lib = Path(N.lib_path()).parent
+    root = Path(__file__).resolve().parent.parent
+    exe = tmp_path / "cpp_host_check"
+    cmd = [gxx, "-std=c++17", "-O2", "-I", str(root / "include"), "-I", str(cuda / "include"),
+           str(root / "tests" / "native" / "cpp_host_check.cpp"), "-L", str(lib), "-limps_gb300",
+           "-L", str(cuda / "lib64"), "-lcudart", f"-Wl,-rpath,{lib}", f"-Wl,-rpath,{cuda / 'lib64'}", "-o", str(exe)]
+    subprocess.run(cmd, check=True)
+    return exe
+
+
+def test_cpp_host_program_builds(tmp_path):
+    """The C++ host interface (RAII handles and the reference-named functors) compiles and
+    links against the in-tree library; tests/test_gpu_cpp_host.py runs it."""
+    assert _build_cpp_host(tmp_path).exists()
+
