@@ -6,9 +6,11 @@ reference's sign convention), two-site unit cell, U(1) Sz sectors q=-10..10 with
 tolerance schedule tol = min(max(prec/100, tolmin), tolmax) (VUMPS_main.cpp:37-38, 177) with
 tolmin = GMRES tolerance = 1e-12, bond expansion off.  A step is one VUMPS sweep (both site
 updates of VUMPS_main.cpp:165-354); the default 3 warm-up + 47 timed steps are the 50 sweeps
-of the workload.  The headline value is the split-BF16 (tcgen05) path; the FP64 path runs the
-same sweeps from the same initial state and is reported beside it, with the energy difference
-of the two after the last sweep.
+of the workload.  The headline value is the FP64 path (--precision fp64, the default); the
+split-BF16 (tcgen05) path runs the same sweeps from the same initial state and is reported
+beside it, with the energy difference of the two after the last sweep.  Under torchrun every
+rank runs its own replica of the sweeps (the path does not shard); the step time is the maximum
+over ranks and the value N / that time.
 
 --mode hac times H_AC applies only (ApplyHAvec; a step = 20 applies).
 --mode excitations converges the XXZ D=256 ground state and times the 4 lowest excitation
@@ -113,6 +115,14 @@ class ClockSampler:
 
 def _dist():
     return int(os.environ.get("WORLD_SIZE", "1")), int(os.environ.get("RANK", "0")), int(os.environ.get("LOCAL_RANK", "0"))
+
+
+def _max_over_ranks(dist, values, device):
+    """Element-wise maximum of `values` over all ranks: the slowest replica sets the step time."""
+    import torch
+    t = torch.tensor([float(x) for x in values], dtype=torch.float64, device=device)
+    dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    return [float(x) for x in t.tolist()]
 
 
 def _fp64_peak_tflops(torch):
@@ -347,9 +357,7 @@ def run_vumps(args):
     t_step = float(np.mean(rmx["times"]))
     t_wall = float(np.mean(rmx["walls"]))
     if ws > 1:
-        tt = torch.tensor([t_step, t_wall], device="cuda", dtype=torch.float64)
-        dist.all_reduce(tt, op=dist.ReduceOp.MAX)
-        t_step, t_wall = (float(x) for x in tt.tolist())
+        t_step, t_wall = _max_over_ranks(dist, [t_step, t_wall], "cuda")
     value = ws / t_step  # replicas: every rank runs its own sweeps
     E64, Emx = r64["E"], rsp["E"]
     dE = float(abs(Emx.mean() - E64.mean()))
