@@ -379,3 +379,62 @@ class VumpsGPU:
     def host_state(self):
         t = lambda x: x.cpu().numpy()
         return {"AL": [t(a) for a in self.AL], "AR": [t(a) for a in self.AR], "C": [t(c) for c in self.C]}
+
+    # ------------------------------------------------------------------ state files
+    def imps_state(self):
+        """The state in the arrangement saveIMPS writes at the end of VUMPS_main.cpp (:368-403,
+        AR shifted back at :368): ALvec[n] = AL(n), ARvec[n] = AR(n), Cvec[n] = the C right of
+        site n (C[n+1] here) and Lamvec[n] its singular values (svd(C), VUMPS_main.cpp:207-208),
+        computed by the device sector SVD."""
+        from . import imps_io
+        torch = self.torch
+        h = self.host_state()
+        AL = [imps_io.flat_to_mps(h["AL"][n], self.LA[n], self.d) for n in range(2)]
+        AR = [imps_io.flat_to_mps(h["AR"][n], self.LA[n], self.d) for n in range(2)]
+        Cv, Lam = [], []
+        for n in range(2):
+            b = (n + 1) % 2
+            Cv.append(imps_io.flat_to_bd(h["C"][b], self.LB[b]))
+            S = torch.zeros(self.dec_b_l[b].nsv, dtype=torch.float64, device="cuda")
+            ops.svd(self.dec_b_l[b], self.C[b], self._z(self.LB[b]), S, None)
+            Lam.append(imps_io.lam_from_flat(S.cpu().numpy(), self.LB[b]))
+        return imps_io.IMPSState(Lam, Cv, AL, AR)
+
+    def save_imps(self, name, ending="bin", folder="."):
+        """saveIMPS(Lamvec, Cvec, ALvec, ARvec, folder/name) (VUMPS_main.cpp:403); returns the path."""
+        from . import imps_io
+        s = self.imps_state()
+        return imps_io.saveIMPS(s.Lam, s.C, s.AL, s.AR, name, ending, folder)
+
+    @classmethod
+    def from_imps(cls, ctx, model, state, **kw):
+        """A driver started from a state file (a path, or an ``imps_io.IMPSState``), as
+        Excitations_main.cpp:84-101 loads one: the bond dimensions come from the file's centre
+        matrices, and the isometries must carry exactly the sectors the model's I2K gives for
+        them ("AL not compatible with I2K from model" otherwise).  Unit cells of two sites."""
+        import torch
+        from . import imps_io
+        st = imps_io.loadIMPS(state) if isinstance(state, (str, bytes)) or hasattr(state, "__fspath__") else state
+        if not (len(st.AL) == len(st.AR) == len(st.C) == 2):
+            raise imps_io.IMPSFormatError(f"unit cell of {len(st.AL)} sites; this driver runs two-site cells")
+        d, I2K, _ = models.build_model(model, **kw)  # reads only the model's own parameters
+        # Cvec[n] is the C right of site n, i.e. on bond n + 1
+        dimvec = [imps_io.bond_dims(st.C[(b + 1) % 2]) for b in range(2)]
+        nsym = len(I2K[0])
+        for key, arr in (("AL", st.AL), ("AR", st.AR)):
+            for n, A in enumerate(arr):
+                if A.d != d or A.nsites != 1:
+                    raise imps_io.IMPSFormatError(f"{key}({n}): d = {A.d}, {A.nsites} site(s); the model has d = {d}")
+        if any(len(q) != nsym for b in range(2) for q in dimvec[b]):
+            raise imps_io.IMPSFormatError(f"keys of the state do not have the model's {nsym} quantum number(s)")
+        init = {"AL": [], "AR": [], "C": []}
+        for n in range(2):
+            lay = B.Layout.mps(I2K, dimvec[n], dimvec[1 - n])
+            for key, A in (("AL", st.AL[n]), ("AR", st.AR[n])):
+                try:
+                    init[key].append(torch.from_numpy(imps_io.mps_to_flat(A, lay)))
+                except imps_io.IMPSFormatError as e:
+                    raise imps_io.IMPSFormatError(f"{key}({n}) not compatible with I2K from model: {e}") from None
+        for b in range(2):
+            init["C"].append(torch.from_numpy(imps_io.bd_to_flat(st.C[(b + 1) % 2], B.Layout.blockdiag(dimvec[b]))))
+        return cls(ctx, model, dimvec=dimvec, init_state=init, **kw)
