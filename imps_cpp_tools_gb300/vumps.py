@@ -1,6 +1,6 @@
-"""VUMPS driver on the GPU: the loop of VUMPS/VUMPS_main.cpp:97-354 (two-site unit cell,
-bond expansion disabled) with every contraction, eigensolve, linear solve and decomposition
-on the device through the C ABI.
+"""VUMPS driver on the GPU: the loop of VUMPS/VUMPS_main.cpp:97-354 (two-site unit cell;
+bond expansion by ExpandFromH when mmax is given) with every contraction, eigensolve, linear
+solve and decomposition on the device through the C ABI.
 
 Indices.  Site n (n = 0, 1) maps bond n -> bond n+1 (mod 2).  C[b] is the centre matrix on
 bond b (the reference's Cvec[n] is the C right of site n, i.e. C[n+1]).  The reference
@@ -21,7 +21,8 @@ class VumpsGPU:
     def __init__(self, ctx, model, dims0=None, dimvec=None, seed=1, InvETol=5e-15, InvEfac=2.0,
                  fixed_tol=None, tolmin=5e-16, tolmax=1e-6, trueLR=True, svdthresh=5e-7, precision="fp64",
                  init_state=None, lanczos_maxit=300, gmres_maxit=4000, lanczos_ncv=96, eig_margin=0.1,
-                 mixed_tm=False, verbose=False, **params):
+                 mixed_tm=False, verbose=False, mmax=None, dmmax=20, expand_pause=5, expand_thresh=1e-5,
+                 lamthresh=1e-12, **params):
         import torch
         self.torch = torch
         self.verbose = verbose
@@ -45,7 +46,14 @@ class VumpsGPU:
         self.mixed_tm = mixed_tm
         self.precision = precision
         self.rng = np.random.default_rng(seed)
-        self.stats = {"lanczos_applies": 0, "gmres_iters": 0, "hac_applies": 0, "hc_applies": 0}
+        self.stats = {"lanczos_applies": 0, "gmres_iters": 0, "hac_applies": 0, "hc_applies": 0, "expansions": 0}
+        # bond expansion (ExpandFromH at VUMPS_main.cpp:270-308), off unless mmax (the largest total
+        # bond dimension, per site or one for both) is given; defaults of VUMPS_main.cpp:31-35
+        self.mmax = None if mmax is None else ([int(mmax)] * 2 if np.isscalar(mmax) else [int(x) for x in mmax])
+        self.dmmax, self.expand_pause = int(dmmax), int(expand_pause)
+        self.expand_thresh, self.lamthresh = expand_thresh, lamthresh
+        self.expand_ct = [0, 0]
+        self.exp_prec = 1.0
         d, hnnz = self.d, self.hnnz
         self.LA = [B.Layout.mps(self.I2K, dimvec[n], dimvec[1 - n]) for n in range(2)]
         self.LB = [B.Layout.blockdiag(dimvec[b]) for b in range(2)]
@@ -343,6 +351,11 @@ class VumpsGPU:
         HAR = self._get_hr(n)
         y0 = self.EHR0[m]
         self.EHR = self._invert_e(("R", n), self.AR, HAR, Lm, self._eye(l), "r", y0, gtol)
+        if self.mmax is not None and self._expand_now(n) and self._expand(n):
+            # EHL on the grown bond (VUMPS_main.cpp:301); EHL1, EHR and the bond-n objects keep
+            # their values (AL(n+1) only gained zero rows)
+            EHLtmp = ops.axpby(ctx, 1.0, self._optm(True, m, self.AL, self._z(self.LB[r])), 1.0,
+                               self._tm(("L1", n), self.AL, self.EHL, self._z(self.LB[r])))
         self.EHL = EHLtmp
         self.EHR1 = ops.axpby(ctx, 1.0, self._tm(("R1", m), self.AR, self.EHR, self._z(self.LB[r])), 1.0,
                               self._optm(False, m, self.AR, self._z(self.LB[r])))
@@ -355,6 +368,7 @@ class VumpsGPU:
         import time
         t0 = time.perf_counter()
         s0 = dict(self.stats)
+        self.exp_prec = float(np.max(self.prec))  # VUMPS_main.cpp:168
         for n in range(2):
             self.site_update(n)
         self.E = self.energy()
@@ -379,6 +393,79 @@ class VumpsGPU:
     def host_state(self):
         t = lambda x: x.cpu().numpy()
         return {"AL": [t(a) for a in self.AL], "AR": [t(a) for a in self.AR], "C": [t(c) for c in self.C]}
+
+    # ------------------------------------------------------------------ bond expansion
+    def _lam(self, b):
+        """Singular values of C[b] per sector (svd(C), VUMPS_main.cpp:207-208), device SVD."""
+        from . import imps_io
+        S = self.torch.zeros(self.dec_b_l[b].nsv, dtype=self.torch.float64, device="cuda")
+        ops.svd(self.dec_b_l[b], self.C[b], self._z(self.LB[b]), S, None)
+        return imps_io.lam_from_flat(S.cpu().numpy(), self.LB[b])
+
+    def _expand_now(self, n):
+        """The expansion test of VUMPS_main.cpp:272-277 for the bond right of site n: enough site
+        updates since the last one, the previous sweep converged below expand_thresh, room below
+        mmax, and some sector whose smallest singular value is above lamthresh."""
+        r = 1 - n
+        mr_tot = sum(self.LB[r].dims().values())
+        now = self.expand_ct[n] >= self.expand_pause and self.exp_prec < self.expand_thresh and mr_tot < self.mmax[n]
+        if now:
+            lam = self._lam(r)
+            now = max(float(v.min()) for v in lam.values() if len(v)) > self.lamthresh
+        if not now:
+            self.expand_ct[n] += 1
+        return now
+
+    def _expand(self, n):
+        """ExpandFromH(H, I2K, AL(n), AR(n+1), C[n+1], min(dmmax, mmax - m_tot)) and the zero
+        padding of AR(n) (VUMPS_main.cpp:282-299), then every plan rebuilt for the grown bond.
+        Returns False if nothing was added."""
+        from . import expand
+        r = m = 1 - n
+        self.expand_ct[n] = 0
+        mr_tot = sum(self.LB[r].dims().values())
+        res = expand.expand_from_h(self.ctx, self.I2K, self.hnnz, self.LA[n], self.AL[n], self.LA[m], self.AR[m],
+                                   self.LB[r], self.C[r], min(self.dmmax, self.mmax[n] - mr_tot))
+        if res is None or sum(res["dm"].values()) == 0:
+            return False
+        oldLA, oldLB = list(self.LA), list(self.LB)
+        dimvec = list(self.dimvec)
+        dimvec[r] = res["dims"]
+        self.dimvec = dimvec
+        self.LA = [B.Layout.mps(self.I2K, dimvec[k], dimvec[1 - k]) for k in range(2)]
+        self.LB = [B.Layout.blockdiag(dimvec[b]) for b in range(2)]
+        if self.LA[n].blocks != res["LA"].blocks or self.LA[m].blocks != res["LR"].blocks:
+            raise RuntimeError("expanded layouts differ from the driver's")
+        # AR(n) (right index on the grown bond) is padded with zeros as in the reference; AL(n+1)
+        # (left index there) gains zero rows and is replaced at its own site update
+        na, nm, nb = self.LA[n].nelem, self.LA[m].nelem, self.LB[r].nelem
+        self.AR[n] = expand.relayout(self.ctx, oldLA[n], self.LA[n], self.AR[n])[:na]
+        self.AL[m] = expand.relayout(self.ctx, oldLA[m], self.LA[m], self.AL[m])[:nm]
+        self.AL[n], self.AR[m], self.C[r] = res["AL"][:na], res["AR"][:nm], res["C"][:nb]
+        if self.EHR0[n] is not None:  # initial guess of the next right-environment solve on that bond
+            self.EHR0[n] = expand.relayout(self.ctx, oldLB[r], self.LB[r], self.EHR0[n])[:nb]
+        self._build_plans()
+        self.stats["expansions"] += 1
+        if self.verbose:
+            import sys
+            print(f"[vumps] expanded bond {r}: +{sum(res['dm'].values())} -> {sum(res['dims'].values())}",
+                  file=sys.stderr, flush=True)
+        return True
+
+    def keep_running(self, thresh=1e-14):
+        """run_IDMRG (VUMPS_main.cpp:331-340): the gradient is above thresh, or (with expansion
+        on) some bond below its mmax has a sector whose smallest singular value exceeds
+        lamthresh."""
+        if float(np.max(self.F)) > thresh:
+            return True
+        if self.mmax is None:
+            return False
+        too_large, too_small = [], []
+        for n in range(2):
+            b = (n + 1) % 2  # Lamvec[n] belongs to the C right of site n
+            too_large.append(any(float(v.min()) > self.lamthresh for v in self._lam(b).values() if len(v)))
+            too_small.append(sum(self.LB[b].dims().values()) < self.mmax[n])
+        return any(too_large) and any(too_small)
 
     # ------------------------------------------------------------------ state files
     def imps_state(self):

@@ -1311,6 +1311,128 @@ def Nullspace(A, direction):
     return NS
 
 
+def GetDenseSplitMat(phi, I2K):
+    """MPSBlockMat::GetDenseSplitMat / GetDoubleSecData (MPSBlockMat.hpp:533-620) for a two-site
+    tensor phi[sl*d + sr]: per centre charge c = ql + I2K[sl], the dense matrix with row spans
+    per left physical index sl (its block ql = c - I2K[sl]) and column spans per right index sr,
+    both in increasing index order.  Returns {c: (dense, [(sl, ql, start, rows)],
+    [(sr, qr, start, cols)])}."""
+    d = len(I2K)
+    secs = {}
+    for s, bm in enumerate(phi):
+        sl, sr = divmod(s, d)
+        for ql, (qr, M) in bm.items():
+            c = kadd(ql, I2K[sl])
+            e = secs.setdefault(c, {"left": {}, "right": {}, "blocks": []})
+            e["left"][sl] = (ql, M.shape[0])
+            e["right"][sr] = (qr, M.shape[1])
+            e["blocks"].append((sl, sr, M))
+    out = {}
+    for c in sorted(secs):
+        e = secs[c]
+        lsp, rsp, pos = {}, {}, 0
+        for sl in sorted(e["left"]):
+            ql, m = e["left"][sl]
+            lsp[sl] = (ql, pos, m)
+            pos += m
+        ml = pos
+        pos = 0
+        for sr in sorted(e["right"]):
+            qr, m = e["right"][sr]
+            rsp[sr] = (qr, pos, m)
+            pos += m
+        D = np.zeros((ml, pos))
+        for sl, sr, M in e["blocks"]:
+            _, r0, rm = lsp[sl]
+            _, c0, cm = rsp[sr]
+            D[r0:r0 + rm, c0:c0 + cm] = M
+        out[c] = (D, [(sl, q, a, m) for sl, (q, a, m) in sorted(lsp.items())],
+                  [(sr, q, a, m) for sr, (q, a, m) in sorted(rsp.items())])
+    return out
+
+
+def ExpandFromH(hnnz, I2K, AL, AR, C, dmmax):
+    """ExpandFromH (MPSBlockUtilities.hpp:409-601): grow the bond between AL and AR by the
+    dominant directions of H acting on AL C AR outside the current tangent space.
+
+    phi = ApplyOperator(AL C AR, H); for every centre charge c already on the bond, the
+    projection M[c] = sum_{sl,sr} NL[sl]^T phi[sl,sr] NR[sr]^T onto the null spaces (skipped
+    if either null space is empty); for a charge not yet on the bond, the whole dense block of
+    phi.  The singular values of all M[c] compete for dmmax new states (largest first; ties
+    keep charge order, the reference's std::sort leaves their order unspecified).  New
+    columns NL U (or U for a new charge) are appended to AL, new rows V^T NR (or V^T) to AR,
+    and C is padded with zeros, so AL C AR is unchanged.  Returns (AL, AR, C, dm) with dm =
+    {c: states added} for every charge considered."""
+    d = len(I2K)
+    phi = ApplyOperator(mps_mul_mps(mps_mul_bd(AL, C), AR), hnnz)
+    dense = GetDenseSplitMat(phi, I2K)
+    NL = Nullspace(AL, "l")
+    NR = Nullspace(AR, "r")
+    M = {}
+    for sl in range(d):
+        for sr in range(d):
+            for ql, (qr, P) in phi[sl * d + sr].items():
+                if ql not in NL[sl]:
+                    continue
+                c, nl = NL[sl][ql]
+                if c not in NR[sr]:
+                    continue
+                qr2, nr = NR[sr][c]
+                assert qr2 == qr
+                M[c] = M.get(c, 0.0) + nl.T @ P @ nr.T
+    svds = []
+    for c, (D, lsp, rsp) in dense.items():
+        isnew = c not in C
+        if isnew:
+            X = D
+        elif c in M:
+            X = M[c]
+        else:
+            continue  # no null space on one side: the sector is already full rank
+        U, lam, Vt = np.linalg.svd(X, full_matrices=False)
+        svds.append({"c": c, "new": isnew, "U": U, "lam": lam, "V": Vt.T, "lsp": lsp, "rsp": rsp, "dm": 0})
+    dmtot = sum(len(e["lam"]) for e in svds)
+    if dmtot > dmmax:
+        allv = [(-float(x), i) for i, e in enumerate(svds) for x in e["lam"]]
+        for _, i in sorted(allv, key=lambda t: t[0])[:dmmax]:
+            svds[i]["dm"] += 1
+    else:
+        for e in svds:
+            e["dm"] = len(e["lam"])
+    AL = [dict(bm) for bm in AL]
+    AR = [dict(bm) for bm in AR]
+    C = dict(C)
+    dm = {}
+    for e in svds:
+        c, k = e["c"], e["dm"]
+        dm[c] = k
+        if k == 0:
+            continue
+        m0 = C[c].shape[0] if c in C else 0
+        Cn = np.zeros((m0 + k, m0 + k))
+        if m0:
+            Cn[:m0, :m0] = C[c]
+        C[c] = Cn
+        U, V = e["U"][:, :k], e["V"][:, :k]
+        if e["new"]:
+            for (sl, ql, r0, m) in e["lsp"]:
+                AL[sl][ql] = (c, U[r0:r0 + m, :].copy())
+            for (sr, qr, c0, m) in e["rsp"]:
+                AR[sr][c] = (qr, V[c0:c0 + m, :].T.copy())
+        else:
+            for sl in range(d):
+                for ql, (c2, nl) in NL[sl].items():
+                    if c2 == c:
+                        q2, A0 = AL[sl][ql]
+                        AL[sl][ql] = (c, np.hstack([A0, nl @ U]))
+            for sr in range(d):
+                if c in NR[sr]:
+                    qr, nr = NR[sr][c]
+                    q2, A0 = AR[sr][c]
+                    AR[sr][c] = (qr, np.vstack([A0, V.T @ nr]))
+    return AL, AR, C, dm
+
+
 def norm_scaled_bm(X):
     """helpers.hpp:146 norm(x)/sqrt(x.size()) on a BlockMat (Frobenius over all blocks)."""
     n = sum(M.size for (_, M) in X.values())
