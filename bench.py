@@ -15,6 +15,8 @@ over ranks and the value N / that time.
 --mode hac times H_AC applies only (ApplyHAvec; a step = 20 applies).
 --mode excitations converges the XXZ D=256 ground state and times the 4 lowest excitation
 energies in the Sz = +1 sector at --steps momenta (H_eff compiled into grouped-GEMM programs).
+--mode expand times one bond expansion (ExpandFromH, dmmax 20) at the XXZ D=512 and Hubbard
+D=1024 starts against the oracle on the same state.
 --mode krylov times one bounded thick-restart Lanczos solve (eigs_rs, ncv 64, at most 8 restart
 cycles; FP64 at an unreachable tolerance, split-BF16 at its 2e-7 floor) on the synthetic H_AC,
 next to the same number of bare applies: the difference is the per-iteration
@@ -612,13 +614,55 @@ def run_adjoint(args):
           flush=True)
 
 
+def run_expand(args):
+    """ExpandFromH (MPSBlockUtilities.hpp:409-601) at the bond right of site 0 of the seeded
+    XXZ D=512 and Hubbard D=1024 starts, dmmax 20 (VUMPS_main.cpp:31): device wall time per
+    expansion (host bookkeeping, planning and the device programs, null spaces and SVDs,
+    synchronised), the oracle (numpy, all host threads) on the same state, and whether both
+    add the same states per charge."""
+    import torch
+    from imps_cpp_tools_gb300 import blocks as B
+    from imps_cpp_tools_gb300 import configs
+    from imps_cpp_tools_gb300 import expand as E
+    from imps_cpp_tools_gb300.excitations import bd_to_host, mps_to_host
+    from imps_cpp_tools_gb300.vumps import VumpsGPU
+    from oracle import imps_oracle as O  # the checker and the CPU baseline leg
+    ctx = B.Context(0)
+    ctx.set_stream(torch.cuda.current_stream())
+    rows = []
+    for name in ("xxz_d512", "hubbard_d1024"):
+        model, fn, params = configs.WORKLOADS[name]
+        v = VumpsGPU(ctx, model, dims0=fn(), seed=1, **params)
+        call = (ctx, v.I2K, v.hnnz, v.LA[0], v.AL[0], v.LA[1], v.AR[1], v.LB[1], v.C[1], 20)
+        for _ in range(args.warmup):
+            E.expand_from_h(*call)
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        for _ in range(max(args.steps, 1)):
+            res = E.expand_from_h(*call)
+        torch.cuda.synchronize()
+        ms = 1e3 * (time.perf_counter() - t0) / max(args.steps, 1)
+        AL = mps_to_host(v.AL[0], v.LA[0], v.d)
+        AR = mps_to_host(v.AR[1], v.LA[1], v.d)
+        Cb = bd_to_host(v.C[1], v.LB[1])
+        tc = time.perf_counter()
+        _, _, _, dmo = O.ExpandFromH(v.hnnz, v.I2K, AL, AR, Cb, 20)
+        t_cpu = time.perf_counter() - tc
+        same = {q: k for q, k in res["dm"].items() if k} == {q: k for q, k in dmo.items() if k}
+        rows.append({"workload": name, "bond_dim": sum(v.LB[1].dims().values()), "added": sum(res["dm"].values()),
+                     "ms_per_expansion": ms, "oracle_s_per_expansion": t_cpu, "same_states_as_oracle": same,
+                     "svd_converged": bool(res["converged"])})
+    print(json.dumps({"mode": "expand", "metric": "ExpandFromH wall time per expansion (ms)", "dmmax": 20,
+                      "cpu_cores": os.cpu_count(), "cases": rows}), flush=True)
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
     ap.add_argument("--steps", type=int, default=47)
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
-    ap.add_argument("--mode", default="vumps", choices=["vumps", "hac", "krylov", "excitations", "adjoint"])
+    ap.add_argument("--mode", default="vumps", choices=["vumps", "hac", "krylov", "excitations", "adjoint", "expand"])
     ap.add_argument("--workload", default="xxz_d512")
     ap.add_argument("--precision", default="fp64", choices=["fp64", "bf16x6"])
     ap.add_argument("--no-cpu", action="store_true")
@@ -636,6 +680,8 @@ def main():
         run_krylov(args)
     elif args.mode == "adjoint":
         run_adjoint(args)
+    elif args.mode == "expand":
+        run_expand(args)
     elif args.mode == "excitations":
         run_excitations(args)
     else:
