@@ -93,6 +93,36 @@ def fhub_h(t=1.0, U=4.0, V=0.0, mu=0.0, hz=0.0):
             - 0.5 * hz * (np.kron(sz, one) + np.kron(one, sz)))
 
 
+def observables(model, names):
+    """GetObservables (Models.cpp:95-147 for the XYZ models, 575-632 for Fermi-Hubbard): the
+    one-site operators named in ``names`` as (name, d x d matrix) pairs, in the order given.
+    An unknown name is skipped with the reference's message ("operator X not defined")."""
+    import sys
+    if model == "xxz":
+        sx = np.array([[0.0, 0.5], [0.5, 0.0]])
+        syi = np.array([[0.0, -0.5], [0.5, 0.0]])
+        sz = np.diag([0.5, -0.5])
+        table = {"sx": sx, "syi": syi, "sz": sz, "sp": sx - syi, "sm": sx + syi, "rx": 2 * sx, "rz": 2 * sz}
+    elif model == "fhub":
+        cup = np.zeros((4, 4)); cup[0, 2] = 1.0; cup[1, 3] = 1.0
+        cdo = np.zeros((4, 4)); cdo[0, 1] = 1.0; cdo[2, 3] = -1.0
+        nup, ndo = np.diag([0.0, 0.0, 1.0, 1.0]), np.diag([0.0, 1.0, 0.0, 1.0])
+        rx = np.zeros((4, 4))
+        for r, c, v in ((0, 0, 1.0), (1, 2, 1.0), (2, 1, 1.0), (3, 3, -1.0)):
+            rx[r, c] = v
+        table = {"cup": cup, "cdo": cdo, "cupd": cup.T.copy(), "cdod": cdo.T.copy(), "nup": nup, "ndo": ndo,
+                 "sz": 0.5 * (nup - ndo), "n": nup + ndo, "rx": rx, "rz": np.diag([1.0, -1.0, 1.0, -1.0])}
+    else:
+        raise ValueError(f"unknown model {model}")
+    out = []
+    for name in names:
+        if name not in table:
+            print(f"operator {name} not defined", file=sys.stderr)
+            continue
+        out.append((name, table[name]))
+    return out
+
+
 def h_nonzeros(h):
     """Nonzeros (row, col, value) in armadillo SpMat iteration order (column-major)."""
     out = []

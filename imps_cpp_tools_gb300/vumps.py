@@ -27,6 +27,7 @@ class VumpsGPU:
         self.torch = torch
         self.verbose = verbose
         self.ctx = ctx
+        self._model = model
         self.d, self.I2K, h = models.build_model(model, **params)
         self.hnnz = models.h_nonzeros(h)
         if dimvec is None:
@@ -389,6 +390,83 @@ class VumpsGPU:
             Lk = self._cct(k, right=False)
             E.append(ops.bd_trace_prod(self.ctx, self.LB[k], Lk, X))
         return np.array(E)
+
+    @staticmethod
+    def first_block_sectors(LA, I2K, O, keys):
+        """The left-bond sectors q (of ``keys``) at which the first block that
+        ApplyTMmixedRight(ApplyOperator(A, O), A) creates (physical index order, TMBlockFunctions.hpp:
+        445-473) is charge-diagonal, for a one-site O that mixes entries of different charge shifts.
+        The reference's BlockMat holds one block per incoming charge and std::map::emplace_hint
+        drops a later block with another outgoing charge, so at the other sectors every diagonal
+        contribution is lost and the trace (BlockObj.hpp:1340-1350) sees none of them."""
+        d = len(I2K)
+        out = set()
+        for q in keys:
+            first = None
+            for r in range(d):
+                for c in range(d):
+                    if O[r, c] == 0.0 or LA.find(c, q) < 0:
+                        continue
+                    qb = tuple(a + b - e for a, b, e in zip(q, I2K[c], I2K[r]))
+                    if LA.find(r, qb) < 0:
+                        continue
+                    first = tuple(I2K[c]) == tuple(I2K[r])
+                    break
+                if first is not None:
+                    break
+            if first:
+                out.add(tuple(q))
+        return out
+
+    def measure(self, obs):
+        """MeasureObservables(obs, AR, L) (MPSBlockUtilities.hpp:1017-1073, dir r) as the driver
+        calls it (VUMPS_main.cpp:344): for every operator, tr(L[n-1] OpTM_R(O, AR(n)...)) at both
+        sites, in the reference's output order (its AR array is rotated by one, so entry 0
+        belongs to site 1).  obs: names of GetObservables or (name, matrix) pairs, one-site
+        (d x d) or two-site (d^2 x d^2).  The trace of a BlockMat sums only blocks with equal
+        charges (BlockObj.hpp:1340-1350), so the charge-changing entries of O contribute exactly
+        zero; the charge-conserving rest runs through the operator transfer matrix plans, a
+        one-site O as O x 1 on AR(n) AR(n+1) (AR(n+1) right-isometric).  A one-site O with entries
+        of both kinds (Fermi-Hubbard "rx") is traced over ``first_block_sectors`` only, as the
+        reference's map insertion leaves it.  Returns {name: values}."""
+        d = self.d
+        if obs and isinstance(obs[0], str):
+            obs = models.observables(self._model, obs)
+        charge = lambda s: tuple(self.I2K[s])
+        out = {}
+        for name, O in obs:
+            O = np.asarray(O, dtype=np.float64)
+            O1 = None
+            if O.shape == (d, d):
+                cons1 = np.array([[charge(r) == charge(c) for c in range(d)] for r in range(d)])
+                if np.any(O[cons1] != 0.0) and np.any(O[~cons1] != 0.0):
+                    O1 = O
+                O = np.kron(O, np.eye(d))
+            elif O.shape != (d * d, d * d):
+                raise ValueError(f"operator {name}: shape {O.shape}, expected ({d}, {d}) or ({d * d}, {d * d})")
+            q2 = [tuple(a + b for a, b in zip(charge(s1), charge(s2))) for s1 in range(d) for s2 in range(d)]
+            keep = np.array([[q2[r] == q2[c] for c in range(d * d)] for r in range(d * d)])
+            if O1 is None and np.any(O[keep] != 0.0) and np.any(O[~keep] != 0.0):
+                raise NotImplementedError(f"two-site operator {name} mixes charge-conserving and charge-changing "
+                                          "entries")
+            hnnz = models.h_nonzeros(np.where(keep, O, 0.0))
+            vals = []
+            for k in (1, 0):
+                if not hnnz:
+                    vals.append(0.0)
+                    continue
+                p = B.plan_optm(self.ctx, self.LA[k], self.LA[1 - k], d, hnnz, 1, self.LB[k])
+                X = self._z(self.LB[k])
+                p.bind(0, self.AR[k]); p.bind(1, self.AR[1 - k]); p.bind(2, X); p.run()
+                L = self._cct(k, right=False)
+                if O1 is not None:
+                    sel = self.first_block_sectors(self.LA[k], self.I2K, O1, [b[1] for b in self.LB[k].blocks])
+                    for (_, q, _, m, _), o in zip(self.LB[k].blocks, self.LB[k].offsets):
+                        if tuple(q) not in sel:
+                            L[o:o + m * m].zero_()
+                vals.append(ops.bd_trace_prod(self.ctx, self.LB[k], L, X))
+            out[name] = np.array(vals)
+        return out
 
     def host_state(self):
         t = lambda x: x.cpu().numpy()

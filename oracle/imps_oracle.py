@@ -471,8 +471,10 @@ def ApplyTMmixedRight(A, B):
                 c = MA @ MB.T
                 if qi in out and out[qi][0] == qbi:
                     out[qi] = (qbi, out[qi][1] + c)
-                else:
+                elif qi not in out:
                     out[qi] = (qbi, c)
+                # else: std::map::emplace_hint keeps the block already there (same incoming,
+                # other outgoing charge) and drops this one (TMBlockFunctions.hpp:466-468)
     return out
 
 
@@ -489,8 +491,9 @@ def ApplyTMmixedLeft(A, B):
                 c = MB.T @ MA
                 if qb in out and out[qb][0] == qa:
                     out[qb] = (qa, out[qb][1] + c)
-                else:
+                elif qb not in out:
                     out[qb] = (qa, c)
+                # else: dropped, as emplace_hint does (TMBlockFunctions.hpp:324-327)
     return out
 
 
@@ -1485,6 +1488,31 @@ def shift(arr, k):
     """MPSBlockUtilities.hpp:1154-1169 (shift(arr,-1) rotates left by one)."""
     k %= len(arr)
     return arr[-k:] + arr[:-k] if k else list(arr)
+
+
+def MeasureObservables(obs, A, L):
+    """MeasureObservables (MPSBlockUtilities.hpp:1017-1073) with dir = r (A = AR, L given): for
+    every (name, O) with O acting on NS sites (d^NS x d^NS),
+    val[n] = trace(L[n-1] ApplyOpTMRightGen(O, A[n] ... A[n+NS-1])) with ApplyOpTMRightGen =
+    ApplyTMmixedRight(ApplyOperator(A, O), A) (TMBlockFunctions.hpp:851-856) and the BlockMat
+    trace over blocks with equal charges only (BlockObj.hpp:1340-1350)."""
+    N = len(A)
+    d = len(A[0])
+    out = {}
+    for name, O in obs:
+        O = np.asarray(O, dtype=np.float64)
+        NS = int(round(math.log(O.shape[0]) / math.log(d)))
+        hnnz = [(r, c, float(O[r, c])) for c in range(O.shape[1]) for r in range(O.shape[0]) if O[r, c] != 0.0]
+        vals = []
+        for n in range(N):
+            At = A[n]
+            for k in range(1, NS):
+                At = mps_mul_mps(At, A[(n + k) % N])
+            X = ApplyTMmixedRight(ApplyOperator(At, hnnz), At)
+            Lm = L[(n - 1) % N]
+            vals.append(float(sum(np.trace(Lm[qi] @ M) for qi, (qo, M) in X.items() if qi == qo and qi in Lm)))
+        out[name] = np.array(vals)
+    return out
 
 
 def energy_right(hnnz, ARvec, Lvec):
