@@ -3,7 +3,8 @@
 Restates, for the GB300 driver, the pieces of MPShelpers/src/Models.cpp and
 include/Block/ItoKey.hpp that define the inputs of the hot path: the two-site Hamiltonian h
 (as its nonzeros in armadillo SpMat iteration order), the physical-index -> charge map I2K,
-validpath and MakeDims.  Only U(1)^k charges occur in the supported models.
+validpath and MakeDims.  Only U(1)^k charges occur in the supported models (XXZ,
+Fermi-Hubbard, Bose-Hubbard).
 """
 from __future__ import annotations
 
@@ -36,6 +37,17 @@ def fhub_i2k(N=2, QN=(2, 0)):
     a1, a0 = N // divn, -(n // divn)
     b1, b0 = N // divm, -((N + m) // divm)
     return [(a0, b0 + b1), (a0 + a1, b0), (a0 + a1, b0 + 2 * b1), (a0 + 2 * a1, b0 + b1)]
+
+
+def bhub_i2k(N=2, QN=(2,), d=4):
+    """BoseHubbardModel::GetdQ + GetI2K (Models.cpp:825-862): n = QN[0] bosons per N-site cell,
+    charge of level i = (i N - n) / gcd(N, n)."""
+    n = QN[0]
+    if n < 1 or n >= N * d:
+        raise ValueError(f"0 < n < {N * d}")
+    div = math.gcd(N, n)
+    first, second = N // div, -(n // div)
+    return [(second + i * first,) for i in range(d)]
 
 
 def validpath(N, I2K):
@@ -93,9 +105,10 @@ def fhub_h(t=1.0, U=4.0, V=0.0, mu=0.0, hz=0.0):
             - 0.5 * hz * (np.kron(sz, one) + np.kron(one, sz)))
 
 
-def observables(model, names):
-    """GetObservables (Models.cpp:95-147 for the XYZ models, 575-632 for Fermi-Hubbard): the
-    one-site operators named in ``names`` as (name, d x d matrix) pairs, in the order given.
+def observables(model, names, d=4):
+    """GetObservables (Models.cpp:95-147 for the XYZ models, 575-632 for Fermi-Hubbard, 782-823
+    for Bose-Hubbard with d levels): the one-site operators named in ``names`` as
+    (name, d x d matrix) pairs, in the order given.
     An unknown name is skipped with the reference's message ("operator X not defined")."""
     import sys
     if model == "xxz":
@@ -112,6 +125,11 @@ def observables(model, names):
             rx[r, c] = v
         table = {"cup": cup, "cdo": cdo, "cupd": cup.T.copy(), "cdod": cdo.T.copy(), "nup": nup, "ndo": ndo,
                  "sz": 0.5 * (nup - ndo), "n": nup + ndo, "rx": rx, "rz": np.diag([1.0, -1.0, 1.0, -1.0])}
+    elif model == "bhub":
+        b, n = bhub_ops(d)
+        nmax = np.zeros((d, d))
+        nmax[d - 1, d - 1] = 1.0
+        table = {"b": b, "b2": b @ b, "n": n, "nmax": nmax}
     else:
         raise ValueError(f"unknown model {model}")
     out = []
@@ -121,6 +139,25 @@ def observables(model, names):
             continue
         out.append((name, table[name]))
     return out
+
+
+def bhub_ops(d=4):
+    """Annihilator b and number operator n of BoseHubbardModel::MakeOps (Models.cpp:768-779)."""
+    b = np.zeros((d, d))
+    n = np.zeros((d, d))
+    for i in range(1, d):
+        b[i - 1, i] = math.sqrt(i)
+        n[i, i] = i
+    return b, n
+
+
+def bhub_h(d=4, t=1.0, U=4.0, mu=0.0):
+    """BoseHubbardModel::MakeOps (Models.cpp:768-779): -t (b b^+ + b^+ b) plus the on-site
+    0.5 U n (n - 1) - mu n shared equally by the two sites."""
+    b, n = bhub_ops(d)
+    one = np.eye(d)
+    onsite = 0.5 * U * n @ (n - one) - mu * n
+    return -t * (np.kron(b, b.T) + np.kron(b.T, b)) + 0.5 * (np.kron(onsite, one) + np.kron(one, onsite))
 
 
 def h_nonzeros(h):
@@ -134,10 +171,15 @@ def h_nonzeros(h):
 
 
 def build_model(name, **params):
-    """Return (d, I2K, h) for 'xxz' (U(1), QN=[0]) or 'fhub' (U(1)xU(1), QN=[2,0], N=2)."""
+    """Return (d, I2K, h) for 'xxz' (U(1), QN=[0]), 'fhub' (U(1)xU(1), QN=[2,0]) or 'bhub'
+    (U(1), n bosons per cell, d levels per site), all with N = 2 sites per unit cell."""
     if name == "xxz":
         return 2, xxz_i2k(2, (0,)), xxz_h(params.get("J", 1.0), params.get("Delta", -1.0), params.get("hz", 0.0))
     if name == "fhub":
         return 4, fhub_i2k(2, (2, 0)), fhub_h(params.get("t", 1.0), params.get("U", 4.0), params.get("V", 0.0),
                                               params.get("mu", 0.0), params.get("hz", 0.0))
+    if name == "bhub":
+        d = int(params.get("d", 4))
+        return d, bhub_i2k(2, (int(params.get("n", 2)),), d), bhub_h(d, params.get("t", 1.0), params.get("U", 4.0),
+                                                                      params.get("mu", 0.0))
     raise ValueError(f"unknown model {name}")

@@ -431,7 +431,7 @@ class VumpsGPU:
         reference's map insertion leaves it.  Returns {name: values}."""
         d = self.d
         if obs and isinstance(obs[0], str):
-            obs = models.observables(self._model, obs)
+            obs = models.observables(self._model, obs, d=self.d)
         charge = lambda s: tuple(self.I2K[s])
         out = {}
         for name, O in obs:

@@ -65,6 +65,38 @@ def fhub_i2k(N, QN):
     return [(a0, b0 + b1), (a0 + a1, b0), (a0 + a1, b0 + 2 * b1), (a0 + 2 * a1, b0 + b1)]
 
 
+def bhub_dQ(N, QN):
+    """BoseHubbardModel::GetdQ (Models.cpp:825-838): (N / g, -n / g) with g = gcd(N, n)."""
+    n = QN[0]
+    if n < 1:
+        raise ValueError("n must be positive")
+    g = math.gcd(N, n)
+    return N // g, -(n // g)
+
+
+def bhub_i2k(N, QN, d):
+    """BoseHubbardModel::GetI2K (Models.cpp:855-862): level i -> dQ.second + i dQ.first."""
+    first, second = bhub_dQ(N, QN)
+    return [(second + i * first,) for i in range(d)]
+
+
+def bhub_h(d, t=1.0, U=4.0, mu=0.0):
+    """BoseHubbardModel::MakeOps (Models.cpp:768-779), element by element."""
+    D = d * d
+    h = np.zeros((D, D))
+    for i0 in range(d):
+        for i1 in range(d):
+            r = i0 * d + i1
+            # on-site part shared by the two sites: 0.5 (U/2 n(n-1) - mu n) on each
+            h[r, r] += 0.5 * (0.5 * U * i0 * (i0 - 1) - mu * i0) + 0.5 * (0.5 * U * i1 * (i1 - 1) - mu * i1)
+            # b (x) b^+ moves a boson from site 0 to site 1, b^+ (x) b from 1 to 0
+            if i0 >= 1 and i1 + 1 < d:
+                h[(i0 - 1) * d + i1 + 1, r] += -t * math.sqrt(i0) * math.sqrt(i1 + 1)
+            if i1 >= 1 and i0 + 1 < d:
+                h[(i0 + 1) * d + i1 - 1, r] += -t * math.sqrt(i1) * math.sqrt(i0 + 1)
+    return h
+
+
 def _path_iter(N, key, I2K, zero):
     if N == 1:
         for j, k in enumerate(I2K):

@@ -13,21 +13,31 @@ from tests.test_expand import FHUB0
 pytestmark = pytest.mark.gpu
 
 
-@pytest.mark.parametrize("model", ["xxz", "fhub"])
+BH = {(-2,): 1, (-1,): 3, (0,): 4, (1,): 3, (2,): 1}
+NAMES = {"xxz": ["sx", "syi", "sz", "sp", "sm", "rx", "rz"],
+         "fhub": ["cup", "cdo", "cupd", "cdod", "nup", "ndo", "sz", "n", "rx", "rz"],
+         "bhub": ["b", "b2", "n", "nmax"]}
+PARAMS = {"xxz": {"J": 1.0, "Delta": -1.0}, "fhub": {"t": 1.0, "U": 4.0}, "bhub": {"d": 4, "t": 0.3, "U": 2.0, "n": 2}}
+
+
+@pytest.mark.parametrize("model", ["xxz", "fhub", "bhub"])
 def test_observables_match_oracle(cuda_ctx, model):
-    params = {"J": 1.0, "Delta": -1.0} if model == "xxz" else {"t": 1.0, "U": 4.0}
+    params = PARAMS[model]
     d, I2K, h = models.build_model(model, **params)
-    dims0 = {(-4,): 2, (-2,): 4, (0,): 6, (2,): 4, (4,): 2} if model == "xxz" else FHUB0
-    v = VumpsGPU(cuda_ctx, model, dimvec=models.make_dims(dims0, 2, I2K), seed=3, **params)
+    if model == "bhub":
+        dimvec = [BH, BH]
+    else:
+        dims0 = {(-4,): 2, (-2,): 4, (0,): 6, (2,): 4, (4,): 2} if model == "xxz" else FHUB0
+        dimvec = models.make_dims(dims0, 2, I2K)
+    v = VumpsGPU(cuda_ctx, model, dimvec=dimvec, seed=3, **params)
     for _ in range(4):
         v.sweep()
-    names = ["sx", "syi", "sz", "sp", "sm", "rx", "rz"] if model == "xxz" else \
-        ["cup", "cdo", "cupd", "cdod", "nup", "ndo", "sz", "n", "rx", "rz"]
+    names = NAMES[model]
     got = v.measure(names)
     AR = [mps_to_host(v.AR[n], v.LA[n], d) for n in range(2)]
     Cb = [bd_to_host(v.C[b], v.LB[b]) for b in range(2)]
     L = [O.bd_mul(O.bd_t(Cb[(m + 1) % 2]), Cb[(m + 1) % 2]) for m in range(2)]  # left of site m + 1
-    ref = O.MeasureObservables(models.observables(model, names), AR, L)
+    ref = O.MeasureObservables(models.observables(model, names, d=d), AR, L)
     for n in names:
         # device order: entry 0 is site 1, entry 1 site 0
         assert np.allclose(got[n], ref[n][::-1], atol=1e-12, rtol=0), (n, got[n], ref[n])

@@ -28,9 +28,13 @@ def _pair(cuda_ctx, model, dimvec, seed, fixed_tol=1e-12, **params):
     return ora, gpu
 
 
+BH = {(-2,): 1, (-1,): 3, (0,): 4, (1,): 3, (2,): 1}
+
+
 @pytest.mark.parametrize("model,dimvec,params", [
     ("xxz", [B0, B1], {"J": 1.0, "Delta": -1.0}),
     ("fhub", None, {"t": 1.0, "U": 4.0}),
+    ("bhub", [BH, BH], {"d": 4, "t": 0.3, "U": 2.0, "n": 2}),
 ])
 def test_vumps_sweeps_match_oracle(cuda_ctx, model, dimvec, params):
     if dimvec is None:

@@ -170,3 +170,30 @@ def test_heisenberg_bethe_ansatz():
     e0 = 0.25 - math.log(2)
     assert abs(E.mean() - e0) < 2e-4
     assert F.max() < 1e-3
+
+
+def test_bose_hubbard_model():
+    """BoseHubbardModel (Models.cpp:739-862): the package's h, I2K and GetObservables against
+    the oracle's element-wise restatement; h conserves the boson number; and the oracle's VUMPS
+    at unit filling (n = 2 per two-site cell) in the Mott regime follows strong-coupling
+    perturbation theory, e0 = -4 t^2 / U + O(t^4 / U^3): the remainder scales as t^4."""
+    for d in (3, 4, 5):
+        assert np.array_equal(models.bhub_h(d, 0.7, 3.0, 0.4), O.bhub_h(d, 0.7, 3.0, 0.4))
+        assert models.bhub_i2k(2, (2,), d) == O.bhub_i2k(2, [2], d)
+    d, I2K, h = models.build_model("bhub", d=4, t=0.3, U=2.0, n=2)
+    q = [tuple(a + b for a, b in zip(I2K[s1], I2K[s2])) for s1 in range(d) for s2 in range(d)]
+    assert all(q[r] == q[c] for r in range(d * d) for c in range(d * d) if h[r, c] != 0.0)
+    names = [n for n, _ in models.observables("bhub", ["b", "b2", "n", "nmax"], d=4)]
+    assert names == ["b", "b2", "n", "nmax"]
+    rem = []
+    for t in (0.05, 0.1):
+        bd = {(-2,): 1, (-1,): 3, (0,): 4, (1,): 3, (2,): 1}
+        v = O.VUMPS(O.bhub_h(4, t, 1.0, 0.0), 4, O.bhub_i2k(2, [2], 4), bd, dimvec=[bd, bd], seed=2)
+        for _ in range(40):
+            E, F, _ = v.sweep()
+            if F.max() < 1e-10:
+                break
+        assert F.max() < 1e-9 and abs(E[0] - E[1]) < 1e-9
+        rem.append(E.mean() + 4 * t * t)
+    assert 0 < rem[0] < 5e-5
+    assert 14.0 < rem[1] / rem[0] < 18.0
