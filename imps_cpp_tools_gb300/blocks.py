@@ -76,10 +76,12 @@ class Layout:
     @classmethod
     def mps(cls, I2K, dl, dr):
         """MPSBlockMat(I2K, ml, mr) sector structure (MPSBlockMat.hpp:221-236)."""
+        from . import charges
+        per = charges.periods_of(I2K)
         blocks = []
         for s, sh in enumerate(I2K):
             for ql in sorted(dl):
-                qr = tuple(a + b for a, b in zip(ql, sh))
+                qr = charges.add(ql, sh, per)
                 if qr in dr:
                     blocks.append((s, ql, qr, dl[ql], dr[qr]))
         return cls(blocks, len(I2K[0]))

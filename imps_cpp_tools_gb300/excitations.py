@@ -25,7 +25,7 @@ import numpy as np
 
 from . import _native as N
 from . import blocks as B
-from . import ops
+from . import charges, ops
 
 OPS, XS, OUT, SCR, ES, RHS = range(6)
 
@@ -572,7 +572,7 @@ def _mps_ml(A):
     return out
 
 
-def tm_mixed_eigs(ctx, A, Bm, direction, K, nev, mode="LM", tol=1e-14, ncv=0):
+def tm_mixed_eigs(ctx, A, Bm, direction, K, nev, mode="LM", tol=1e-14, ncv=0, periods=None):
     """TMmixedEigs(A, B, V, dir, K, nev, mode, tol) (EigsBlockFunctions.hpp:282-391) on the device:
     the nev leading eigenpairs of the mixed unit-cell TM (ApplyTMmixedLeft/Right(A, B, X) over
     the sites) in the charge sector K, by the device Arnoldi (imps_eigs_n) on a mixed-TM plan.
@@ -587,7 +587,8 @@ def tm_mixed_eigs(ctx, A, Bm, direction, K, nev, mode="LM", tol=1e-14, ncv=0):
     diml, dimr = _mps_ml(A[0]), _mps_ml(Bm[0])
     if direction == "l":
         diml, dimr = dimr, diml
-    sizes = [(q, _kadd(q, K), diml[q], dimr[_kadd(q, K)]) for q in sorted(diml) if _kadd(q, K) in dimr]
+    kk = (lambda q: charges.add(q, K, periods)) if periods else (lambda q: _kadd(q, K))
+    sizes = [(q, kk(q), diml[q], dimr[kk(q)]) for q in sorted(diml) if kk(q) in dimr]
     if not sizes:
         raise ValueError("TMmixedEigs: no TM eigenvalues for this quantum number")
     lay = B.Layout([(0, qi, qo, ml, mr) for (qi, qo, ml, mr) in sizes], nsym)
@@ -615,14 +616,15 @@ def tm_mixed_eigs(ctx, A, Bm, direction, K, nev, mode="LM", tol=1e-14, ncv=0):
     return vals, V, sizes, na, conv
 
 
-def LRoverlaps(ctx, AL, AR, K, nev, OLtol=1e-14):
+def LRoverlaps(ctx, AL, AR, K, nev, OLtol=1e-14, periods=None):
     """LRoverlaps(LM, RM, AL, AR, K, nev, OLtol) (Excitations_helpers.hpp:915-946) on the device:
     the dominant left (sector -K) and right (sector K) eigenmatrices of the mixed TM of AL and
     AR, as real BlockMats, and the overlap OL = (Re OL_L + Re OL_R) / 2.  Returns
     (LM, RM, OL, OL_L eigenvalues, OL_R eigenvalues, converged)."""
     K = tuple(int(k) for k in K)
-    vl, VL, _, _, cl = tm_mixed_eigs(ctx, AL, AR, "l", tuple(-k for k in K), nev, "LM", OLtol)
-    vr, VR, _, _, cr = tm_mixed_eigs(ctx, AL, AR, "r", K, nev, "LM", OLtol)
+    mK = charges.neg(K, periods) if periods else tuple(-k for k in K)
+    vl, VL, _, _, cl = tm_mixed_eigs(ctx, AL, AR, "l", mK, nev, "LM", OLtol, periods=periods)
+    vr, VR, _, _, cr = tm_mixed_eigs(ctx, AL, AR, "r", K, nev, "LM", OLtol, periods=periods)
     real = lambda X: {qi: (qo, np.real(M).copy()) for qi, (qo, M) in X.items()}
     return real(VL[0]), real(VR[0]), 0.5 * (vl[0].real + vr[0].real), vl, vr, cl and cr
 
@@ -654,7 +656,7 @@ def bd_to_host(vec, layout):
     return out
 
 
-def xdims_from_layouts(ns_layout, ar_layout, K):
+def xdims_from_layouts(ns_layout, ar_layout, K, periods=None):
     """XDims (Excitations_helpers.hpp:641-678): X_n maps the right sectors q of N_L[n] to the
     left sectors q + K of AR[n+1]."""
     ml, mr = {}, {}
@@ -664,7 +666,7 @@ def xdims_from_layouts(ns_layout, ar_layout, K):
         mr.setdefault(qi, r)
     dims = []
     for q in sorted(ml):
-        qk = _kadd(q, K)
+        qk = charges.add(q, K, periods) if periods else _kadd(q, K)
         if qk in mr and ml[q] > 0 and mr[qk] > 0:
             dims.append((q, qk, ml[q], mr[qk]))
     return dims
@@ -707,12 +709,13 @@ def excitation_inputs(v, K, tol=1e-13):
     diag = {r for (r, c, _) in v.hnnz if r == c}
     hs += [(i, i, -E0) for i in range(d * d) if i not in diag]
     hs.sort(key=lambda t: (t[1], t[0]))
-    xd = [xdims_from_layouts(nsl[n], v.LA[(n + 1) % 2], tuple(K)) for n in range(2)]
+    per = charges.periods_of(v.I2K)
+    xd = [xdims_from_layouts(nsl[n], v.LA[(n + 1) % 2], tuple(K), per) for n in range(2)]
     ALh = [mps_to_host(AL[n], v.LA[n], d) for n in range(2)]
     ARh = [mps_to_host(AR[n], v.LA[n], d) for n in range(2)]
     # overlap of AL and AR and the dominant mixed-TM eigenmatrices (Excitations_main.cpp:174-178);
     # AR[0] *= sign(OL) makes the overlap positive (it leaves HRtot unchanged)
-    LM, RM, OL, _, _, _ = LRoverlaps(ctx, ALh, ARh, K, 2, 1e-14)
+    LM, RM, OL, _, _, _ = LRoverlaps(ctx, ALh, ARh, K, 2, 1e-14, periods=per)
     if OL < 0:
         ARh[0] = [{qi: (qo, -M) for qi, (qo, M) in bm.items()} for bm in ARh[0]]
     host = dict(AL=ALh, AR=ARh, NL=NL,

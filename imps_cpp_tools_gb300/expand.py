@@ -31,15 +31,7 @@ import numpy as np
 
 from . import _native as N
 from . import blocks as B
-from . import ops
-
-
-def _kadd(a, b):
-    return tuple(x + y for x, y in zip(a, b))
-
-
-def _ksub(a, b):
-    return tuple(x - y for x, y in zip(a, b))
+from . import charges, ops
 
 
 class _Program:
@@ -132,8 +124,10 @@ def expand_from_h(ctx, I2K, hnnz, LA, AL, LR, AR, LC, Cc, dmmax):
     dec_l = B.plan_decomp(ctx, LA, "l")
     NL = _zeros(dec_l.nslayout.nelem)
     ops.Nullspace(dec_l, AL, NL)
-    negI2K = [tuple(-x for x in s) for s in I2K]
-    LT = B.Layout.mps(negI2K, dR, dc)
+    per = charges.periods_of(I2K)
+    _kadd = lambda a, b: charges.add(a, b, per)
+    _ksub = lambda a, b: charges.sub(a, b, per)
+    LT = B.Layout.mps(charges.negated(I2K), dR, dc)
     ART = _zeros(LT.nelem)
     for (s, qc, qr, mc, mqr), off in zip(LR.blocks, LR.offsets):
         i = LT.find(s, qr)

@@ -3,8 +3,8 @@
 Restates, for the GB300 driver, the pieces of MPShelpers/src/Models.cpp and
 include/Block/ItoKey.hpp that define the inputs of the hot path: the two-site Hamiltonian h
 (as its nonzeros in armadillo SpMat iteration order), the physical-index -> charge map I2K,
-validpath and MakeDims.  Only U(1)^k charges occur in the supported models (XXZ,
-Fermi-Hubbard, Bose-Hubbard).
+validpath and MakeDims, for U(1) (XXZ, Fermi-Hubbard, Bose-Hubbard) and Z(N) charges (quantum
+Ising, quantum Potts; charges.py holds the group arithmetic).
 """
 from __future__ import annotations
 
@@ -13,8 +13,11 @@ import math
 import numpy as np
 
 
-def _kadd(a, b):
-    return tuple(x + y for x, y in zip(a, b))
+from . import charges
+
+
+def _kadd(a, b, periods=None):
+    return charges.add(a, b, periods) if periods else tuple(x + y for x, y in zip(a, b))
 
 
 def xxz_i2k(N=2, QN=(0,), d=2):
@@ -50,16 +53,28 @@ def bhub_i2k(N=2, QN=(2,), d=4):
     return [(second + i * first,) for i in range(d)]
 
 
+def qim_i2k():
+    """QuantumIsingModel::GetI2K (Models.cpp:371-375): the Z(2) parity of sz, [0, 1]."""
+    return charges.I2K([(0,), (1,)], (2,))
+
+
+def potts_i2k(q):
+    """QuantumPottsModel::GetI2K (Models.cpp:498-504): level i -> i in Z(q)."""
+    return charges.I2K([(i,) for i in range(q)], (q,))
+
+
 def validpath(N, I2K):
     """ItoKey.hpp:126-165: indices j_1..j_N with sum I2K[j] = 0, first-found depth-first order."""
+    per = charges.periods_of(I2K)
+
     def it(n, key):
         if n == 1:
             for j, k in enumerate(I2K):
-                if _kadd(key, k) == I2K[0]:
+                if _kadd(key, k, per) == I2K[0]:
                     return [j]
             return None
         for j, k in enumerate(I2K):
-            p = it(n - 1, _kadd(key, k))
+            p = it(n - 1, _kadd(key, k, per))
             if p is not None:
                 return p + [j]
         return None
@@ -76,7 +91,7 @@ def make_dims(dmap0, N, I2K):
     for k in range(N):
         out.append(dict(cur))
         sh = I2K[path[N - k - 1]]
-        cur = {_kadd(q, sh): m for q, m in cur.items()}
+        cur = {_kadd(q, sh, charges.periods_of(I2K)): m for q, m in cur.items()}
     return out
 
 
@@ -106,12 +121,12 @@ def fhub_h(t=1.0, U=4.0, V=0.0, mu=0.0, hz=0.0):
 
 
 def observables(model, names, d=4):
-    """GetObservables (Models.cpp:95-147 for the XYZ models, 575-632 for Fermi-Hubbard, 782-823
-    for Bose-Hubbard with d levels): the one-site operators named in ``names`` as
-    (name, d x d matrix) pairs, in the order given.
+    """GetObservables (Models.cpp:95-147 for the XYZ models incl. quantum Ising, 436-468 for
+    Potts with q = d, 575-632 for Fermi-Hubbard, 782-823 for Bose-Hubbard with d levels): the
+    one-site operators named in ``names`` as (name, d x d matrix) pairs, in the order given.
     An unknown name is skipped with the reference's message ("operator X not defined")."""
     import sys
-    if model == "xxz":
+    if model in ("xxz", "qim"):
         sx = np.array([[0.0, 0.5], [0.5, 0.0]])
         syi = np.array([[0.0, -0.5], [0.5, 0.0]])
         sz = np.diag([0.5, -0.5])
@@ -125,6 +140,9 @@ def observables(model, names, d=4):
             rx[r, c] = v
         table = {"cup": cup, "cdo": cdo, "cupd": cup.T.copy(), "cdod": cdo.T.copy(), "nup": nup, "ndo": ndo,
                  "sz": 0.5 * (nup - ndo), "n": nup + ndo, "rx": rx, "rz": np.diag([1.0, -1.0, 1.0, -1.0])}
+    elif model == "potts":
+        X, Z = potts_ops(d)
+        table = {"X": X, "Z": Z}
     elif model == "bhub":
         b, n = bhub_ops(d)
         nmax = np.zeros((d, d))
@@ -139,6 +157,38 @@ def observables(model, names, d=4):
             continue
         out.append((name, table[name]))
     return out
+
+
+def qim_h(J=1.0, h=1.0):
+    """QuantumIsingModel = XYZAbstractModel(QIM, J, 0, 0, h, 2) (Models.cpp:323-330, 91):
+    -J sx sx - h/2 (sz 1 + 1 sz) with spin-1/2 operators."""
+    sx = np.array([[0.0, 0.5], [0.5, 0.0]])
+    sz = np.diag([0.5, -0.5])
+    one = np.eye(2)
+    return -J * np.kron(sx, sx) - 0.5 * h * (np.kron(sz, one) + np.kron(one, sz))
+
+
+def potts_ops(q):
+    """X (cyclic shift, X(i-1, i) = 1, X(q-1, 0) = 1) and Z = diag(q - 1, -1, ..., -1) of
+    QuantumPottsModel::MakeOps (Models.cpp:405-418)."""
+    X = np.zeros((q, q))
+    X[q - 1, 0] = 1.0
+    for i in range(1, q):
+        X[i - 1, i] = 1.0
+    Z = -np.eye(q)
+    Z[0, 0] = q - 1
+    return X, Z
+
+
+def potts_h(q=3, h=1.0):
+    """QuantumPottsModel::MakeOps (Models.cpp:405-425): -h/2 (Z 1 + 1 Z) - sum_k X^k X^(q-k)."""
+    X, Z = potts_ops(q)
+    one = np.eye(q)
+    H = -0.5 * h * (np.kron(Z, one) + np.kron(one, Z))
+    P = [np.linalg.matrix_power(X, k) for k in range(1, q)]
+    for i in range(q - 1):
+        H -= np.kron(P[i], P[q - 2 - i])
+    return H
 
 
 def bhub_ops(d=4):
@@ -171,13 +221,19 @@ def h_nonzeros(h):
 
 
 def build_model(name, **params):
-    """Return (d, I2K, h) for 'xxz' (U(1), QN=[0]), 'fhub' (U(1)xU(1), QN=[2,0]) or 'bhub'
-    (U(1), n bosons per cell, d levels per site), all with N = 2 sites per unit cell."""
+    """Return (d, I2K, h) for 'xxz' (U(1), QN=[0]), 'fhub' (U(1)xU(1), QN=[2,0]), 'bhub' (U(1), n
+    bosons per cell, d levels per site), 'qim' (Z(2)) or 'potts' (Z(q)), all with N = 2 sites per
+    unit cell."""
     if name == "xxz":
         return 2, xxz_i2k(2, (0,)), xxz_h(params.get("J", 1.0), params.get("Delta", -1.0), params.get("hz", 0.0))
     if name == "fhub":
         return 4, fhub_i2k(2, (2, 0)), fhub_h(params.get("t", 1.0), params.get("U", 4.0), params.get("V", 0.0),
                                               params.get("mu", 0.0), params.get("hz", 0.0))
+    if name == "qim":
+        return 2, qim_i2k(), qim_h(params.get("J", 1.0), params.get("h", 1.0))
+    if name == "potts":
+        q = int(params.get("q", 3))
+        return q, potts_i2k(q), potts_h(q, params.get("h", 1.0))
     if name == "bhub":
         d = int(params.get("d", 4))
         return d, bhub_i2k(2, (int(params.get("n", 2)),), d), bhub_h(d, params.get("t", 1.0), params.get("U", 4.0),

@@ -399,7 +399,9 @@ class VumpsGPU:
         The reference's BlockMat holds one block per incoming charge and std::map::emplace_hint
         drops a later block with another outgoing charge, so at the other sectors every diagonal
         contribution is lost and the trace (BlockObj.hpp:1340-1350) sees none of them."""
+        from . import charges
         d = len(I2K)
+        per = charges.periods_of(I2K)
         out = set()
         for q in keys:
             first = None
@@ -407,7 +409,7 @@ class VumpsGPU:
                 for c in range(d):
                     if O[r, c] == 0.0 or LA.find(c, q) < 0:
                         continue
-                    qb = tuple(a + b - e for a, b, e in zip(q, I2K[c], I2K[r]))
+                    qb = charges.sub(charges.add(q, I2K[c], per), I2K[r], per)
                     if LA.find(r, qb) < 0:
                         continue
                     first = tuple(I2K[c]) == tuple(I2K[r])
@@ -432,7 +434,9 @@ class VumpsGPU:
         d = self.d
         if obs and isinstance(obs[0], str):
             obs = models.observables(self._model, obs, d=self.d)
+        from . import charges
         charge = lambda s: tuple(self.I2K[s])
+        per = charges.periods_of(self.I2K)
         out = {}
         for name, O in obs:
             O = np.asarray(O, dtype=np.float64)
@@ -444,7 +448,7 @@ class VumpsGPU:
                 O = np.kron(O, np.eye(d))
             elif O.shape != (d * d, d * d):
                 raise ValueError(f"operator {name}: shape {O.shape}, expected ({d}, {d}) or ({d * d}, {d * d})")
-            q2 = [tuple(a + b for a, b in zip(charge(s1), charge(s2))) for s1 in range(d) for s2 in range(d)]
+            q2 = [charges.add(charge(s1), charge(s2), per) for s1 in range(d) for s2 in range(d)]
             keep = np.array([[q2[r] == q2[c] for c in range(d * d)] for r in range(d * d)])
             if O1 is None and np.any(O[keep] != 0.0) and np.any(O[~keep] != 0.0):
                 raise NotImplementedError(f"two-site operator {name} mixes charge-conserving and charge-changing "

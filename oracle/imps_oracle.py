@@ -26,12 +26,40 @@ import numpy as np
 # ----------------------------------------------------------------------------------------------
 
 
+# The charge group of the model being checked (symobj.hpp:120-158): None for U(1)^k, else one
+# period per component (0 for U(1), N for Z(N), representatives in [0, N)).
+_PERIODS = None
+
+
+class charge_group:
+    """Context in which kadd / ksub reduce the components with a nonzero period modulo it."""
+
+    def __init__(self, periods):
+        self.periods = tuple(periods) if periods else None
+
+    def __enter__(self):
+        global _PERIODS
+        self.prev, _PERIODS = _PERIODS, self.periods
+        return self
+
+    def __exit__(self, *exc):
+        global _PERIODS
+        _PERIODS = self.prev
+        return False
+
+
+def _reduce(t):
+    if not _PERIODS:
+        return t
+    return tuple(x % p if p else x for x, p in zip(t, _PERIODS))
+
+
 def kadd(a, b):
-    return tuple(x + y for x, y in zip(a, b))
+    return _reduce(tuple(x + y for x, y in zip(a, b)))
 
 
 def ksub(a, b):
-    return tuple(x - y for x, y in zip(a, b))
+    return _reduce(tuple(x - y for x, y in zip(a, b)))
 
 
 def xxz_dQ(N, QN):
@@ -63,6 +91,41 @@ def fhub_i2k(N, QN):
     """FermiHubbardModel::GetI2K, (N,M) representation (Models.cpp:701-718)."""
     (a1, a0), (b1, b0) = fhub_dQ(N, QN)
     return [(a0, b0 + b1), (a0 + a1, b0), (a0 + a1, b0 + 2 * b1), (a0 + 2 * a1, b0 + b1)]
+
+
+def qim_i2k():
+    """QuantumIsingModel::GetI2K (Models.cpp:371-375), charges in Z(2)."""
+    return [(0,), (1,)]
+
+
+def qim_h(J=1.0, h=1.0):
+    """XYZAbstractModel(QIM, J, 0, 0, h, 2) (Models.cpp:91): element by element, spin-1/2
+    basis |up>, |down>: -J/4 flips both spins, -h/4 (+-1 +-1) on the diagonal."""
+    H = np.zeros((4, 4))
+    for s0 in range(2):
+        for s1 in range(2):
+            r = 2 * s0 + s1
+            H[r, r] = -0.5 * h * ((0.5 if s0 == 0 else -0.5) + (0.5 if s1 == 0 else -0.5))
+            H[2 * (1 - s0) + (1 - s1), r] += -0.25 * J
+    return H
+
+
+def potts_i2k(q):
+    """QuantumPottsModel::GetI2K (Models.cpp:498-504), charges in Z(q)."""
+    return [(i,) for i in range(q)]
+
+
+def potts_h(q, h=1.0):
+    """QuantumPottsModel::MakeOps (Models.cpp:405-425) element by element: X^k lowers a level by
+    k (mod q), so X^k (x) X^(q-k) maps |i, j> to |i - k, j + k>; Z = q delta_{i0} - 1."""
+    H = np.zeros((q * q, q * q))
+    for i in range(q):
+        for j in range(q):
+            r = i * q + j
+            H[r, r] = -0.5 * h * ((q if i == 0 else 0) - 1 + (q if j == 0 else 0) - 1)
+            for k in range(1, q):
+                H[((i - k) % q) * q + (j + k) % q, r] -= 1.0
+    return H
 
 
 def bhub_dQ(N, QN):

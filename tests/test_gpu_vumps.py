@@ -100,3 +100,37 @@ def test_vumps_ground_state_energy_matches_oracle(cuda_ctx, oracle_ground_state,
     assert abs(Eg.mean() - Eo.mean()) <= bound, (precision, Eg, Eo, fmin)
     if precision == "fp64":
         assert fmin < 1e-11
+
+
+@pytest.mark.parametrize("model,params,dims,periods", [
+    ("qim", {"J": 1.0, "h": 0.7}, {(0,): 6, (1,): 6}, (2,)),
+    ("potts", {"q": 3, "h": 0.8}, {(0,): 4, (1,): 3, (2,): 3}, (3,)),
+])
+def test_zn_vumps_sweeps_match_oracle(cuda_ctx, model, params, dims, periods):
+    """Z(N) charges (quantum Ising Z(2), Potts Z(3)): the GPU driver against the oracle run with
+    the same modular charge arithmetic, from the same initial state."""
+    dimvec = models.make_dims(dims, 2, models.build_model(model, **params)[1])
+    with O.charge_group(periods):
+        ora, gpu = _pair(cuda_ctx, model, dimvec, seed=7, **params)
+        for sweep in range(3):
+            Eo, Fo, po = ora.sweep()
+            Eg, Fg, pg = gpu.sweep()
+            # sweep 0 from the random start: 3e-9 measured for Z(2) (nearly degenerate parity
+            # sectors amplify the 1e-12 solver differences); a wrong sector would show at 1e-2
+            assert np.abs(Eg - Eo).max() < (1e-8 if sweep == 0 else 1e-5), (sweep, Eg, Eo)
+
+
+def test_quantum_ising_exact_energy(cuda_ctx):
+    """The transverse-field Ising energy (exact) through the GPU path with Z(2) sectors."""
+    from scipy.integrate import quad
+    J, h = 1.0, 0.7
+    Jp, hp = J / 4, h / 2
+    e0 = -quad(lambda k: math.sqrt(Jp ** 2 + hp ** 2 - 2 * Jp * hp * math.cos(k)), -math.pi, math.pi,
+               epsabs=1e-14)[0] / (2 * math.pi)
+    b = {(0,): 8, (1,): 8}
+    gpu = VumpsGPU(cuda_ctx, "qim", dimvec=[b, b], seed=2, J=J, h=h)
+    for _ in range(60):
+        E, F, _ = gpu.sweep()
+        if F.max() < 1e-11:
+            break
+    assert F.max() < 1e-10 and np.abs(E - e0).max() < 1e-10, (E, e0)

@@ -197,3 +197,46 @@ def test_bose_hubbard_model():
         rem.append(E.mean() + 4 * t * t)
     assert 0 < rem[0] < 5e-5
     assert 14.0 < rem[1] / rem[0] < 18.0
+
+
+def test_zn_models():
+    """Quantum Ising (Z(2)) and quantum Potts (Z(q)) (Models.cpp:323-504): the package's h and
+    I2K against the oracle's element-wise restatement, charge conservation modulo N, and the
+    oracle's VUMPS with the Z(N) charge arithmetic (symobj.hpp:120-158):
+    * quantum Ising -J sx sx - h/2 (sz 1 + 1 sz) at the exact transverse-field Ising energy
+      e0 = -(1/2pi) int sqrt(J'^2 + h'^2 - 2 J' h' cos k) dk, J' = J/4, h' = h/2;
+    * Potts q = 3 deep in the field-polarised phase on strong-field perturbation theory,
+      e0 = -h(q-1) - (q-1)/(2hq) - 1/(18 h^2) + O(h^-3) (the h^-2 term: three shifts by the
+      same bond term return to |0 0>, X^3 = 1)."""
+    from scipy.integrate import quad
+    from imps_cpp_tools_gb300 import charges
+    assert np.array_equal(models.qim_h(0.7, 1.3), O.qim_h(0.7, 1.3))
+    assert list(models.qim_i2k()) == O.qim_i2k() and models.qim_i2k().periods == (2,)
+    for q in (2, 3, 4, 5):
+        assert np.array_equal(models.potts_h(q, 0.6), O.potts_h(q, 0.6))
+        assert list(models.potts_i2k(q)) == O.potts_i2k(q)
+    for name, kw in (("qim", {}), ("potts", {"q": 3}), ("potts", {"q": 4})):
+        d, I2K, h = models.build_model(name, **kw)
+        per = charges.periods_of(I2K)
+        qq = [charges.add(I2K[a], I2K[b], per) for a in range(d) for b in range(d)]
+        assert all(qq[r] == qq[c] for r in range(d * d) for c in range(d * d) if h[r, c] != 0.0)
+    J, hf = 1.0, 0.7
+    Jp, hp = J / 4, hf / 2
+    e0 = -quad(lambda k: math.sqrt(Jp ** 2 + hp ** 2 - 2 * Jp * hp * math.cos(k)), -math.pi, math.pi,
+               epsabs=1e-14)[0] / (2 * math.pi)
+    with O.charge_group((2,)):
+        v = O.VUMPS(O.qim_h(J, hf), 2, O.qim_i2k(), {(0,): 8, (1,): 8}, seed=2)
+        for _ in range(60):
+            E, F, _ = v.sweep()
+            if F.max() < 1e-11:
+                break
+    assert F.max() < 1e-10 and np.abs(E - e0).max() < 1e-11
+    for hq, tol in ((10.0, 5e-5), (20.0, 1e-5)):
+        with O.charge_group((3,)):
+            v = O.VUMPS(O.potts_h(3, hq), 3, O.potts_i2k(3), {(0,): 4, (1,): 2, (2,): 2}, seed=2)
+            for _ in range(60):
+                E, F, _ = v.sweep()
+                if F.max() < 1e-11:
+                    break
+        pt = -2 * hq - 2 / (6 * hq) - 1 / (18 * hq * hq)
+        assert F.max() < 1e-10 and abs(E.mean() - pt) < tol, (hq, E, pt)
