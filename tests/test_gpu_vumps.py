@@ -115,9 +115,12 @@ def test_zn_vumps_sweeps_match_oracle(cuda_ctx, model, params, dims, periods):
         for sweep in range(3):
             Eo, Fo, po = ora.sweep()
             Eg, Fg, pg = gpu.sweep()
-            # sweep 0 from the random start: 3e-9 measured for Z(2) (nearly degenerate parity
-            # sectors amplify the 1e-12 solver differences); a wrong sector would show at 1e-2
-            assert np.abs(Eg - Eo).max() < (1e-8 if sweep == 0 else 1e-5), (sweep, Eg, Eo)
+            # from the random start the Z(2) effective Hamiltonians are nearly degenerate: the
+            # first sweeps agree to 3e-9 .. 8e-7 depending on the oracle's ARPACK start vectors
+            # (scipy keeps ARPACK's random state across calls); a wrong sector shows at 1e-2.
+            # The converged energy is pinned to the exact solution by
+            # test_quantum_ising_exact_energy (GPU) and tests/test_oracle.py (oracle)
+            assert np.abs(Eg - Eo).max() < 1e-5, (sweep, Eg, Eo)
 
 
 def test_quantum_ising_exact_energy(cuda_ctx):
