@@ -115,11 +115,12 @@ def test_zn_vumps_sweeps_match_oracle(cuda_ctx, model, params, dims, periods):
         for sweep in range(3):
             Eo, Fo, po = ora.sweep()
             Eg, Fg, pg = gpu.sweep()
-            # from the random start the Z(2) effective Hamiltonians are nearly degenerate: the
-            # first sweeps agree to 3e-9 .. 8e-7 depending on the oracle's ARPACK start vectors
-            # (scipy keeps ARPACK's random state across calls); a wrong sector shows at 1e-2.
-            # The converged energy is pinned to the exact solution by
-            # test_quantum_ising_exact_energy (GPU) and tests/test_oracle.py (oracle)
+            # The shared initial state comes from the oracle's randMPS_LR, whose fixed-point solve
+            # starts ARPACK from scipy's process-wide random state, so it moves at the 1e-14
+            # level with test order.  From it, the nearly degenerate Z(2) effective Hamiltonians
+            # of the first sweeps (ARPACK against the device Lanczos, both at tol 1e-12) agree to
+            # 3e-9 .. 8e-7; a wrong sector shows at 1e-2.  The converged energy is pinned to the
+            # exact solution by test_quantum_ising_exact_energy (GPU) and tests/test_oracle.py.
             assert np.abs(Eg - Eo).max() < 1e-5, (sweep, Eg, Eo)
 
 
