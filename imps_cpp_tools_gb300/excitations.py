@@ -25,7 +25,7 @@ import numpy as np
 
 from . import _native as N
 from . import blocks as B
-from . import charges, ops
+from . import charges, models, ops
 
 OPS, XS, OUT, SCR, ES, RHS = range(6)
 
@@ -538,6 +538,54 @@ class ExcitationsGPU:
         return out[:nev], conv and len(out) >= nev
 
 
+def measure_excitations(v, K, obs, kfac, seed=1, tol=1e-13):
+    """MeasureExcitations (Excitations_helpers.hpp:754-808) on the device.  For each one-site
+    observable O: its ground-state mean <O> is subtracted, and the excitation-space operator
+    of sum_n (O_n - <O>) is applied to a random normalised X (complex, XDims order, seeded)
+    at kfac = e^{ip}; the values tr(X[n]^+ Xout[n]) per site are returned ({name: array}).
+
+    The reference builds OPeffConstants / ApplyOPeff for O; on an infinite chain sum_n O_n is the
+    same operator as sum_bonds (O x 1 + 1 x O) / 2, so here H_eff's device programs run with
+    that bond operator (minus <O>), whose environments come from excitation_inputs(op=...).
+    The two agree in the oracle to rounding (ApplyOPeff against ApplyHeff).  The mean is taken
+    from the right-canonical form; the reference averages it with the left-canonical one,
+    which agrees to the state's gauge error.  The environment solves are projected at K = 0,
+    p = 0 as in Excitations_main.cpp:205-215.  Charge-changing observables give zero (their
+    Xout has no block in X's sectors)."""
+    d = v.d
+    if obs and isinstance(obs[0], str):
+        obs = models.observables(v._model, obs, d=d)
+    rng = np.random.default_rng(seed)
+    p = float(np.angle(kfac))
+    out = {}
+    xs = None
+    for name, O in obs:
+        O = np.asarray(O, dtype=np.float64)
+        cons = np.array([[tuple(v.I2K[r]) == tuple(v.I2K[c]) for c in range(d)] for r in range(d)])
+        if not np.any(O[cons] != 0.0):
+            out[name] = np.zeros(2, dtype=complex)
+            continue
+        if np.any(O[~cons] != 0.0):
+            raise NotImplementedError(f"observable {name} mixes charge-conserving and charge-changing entries")
+        eobs = float(np.mean(v.measure([(name, O)])[name]))
+        hO = 0.5 * (np.kron(O, np.eye(d)) + np.kron(np.eye(d), O)) - eobs * np.eye(d * d)
+        inp = excitation_inputs(v, K, tol=tol, op=hO)
+        if xs is None:
+            sizes = [sum(ml * mr for (_, _, ml, mr) in dd) for dd in inp["xdims"]]
+            x = rng.standard_normal(sum(sizes)) + 1j * rng.standard_normal(sum(sizes))
+            x /= np.linalg.norm(x)
+            xs = np.split(x, np.cumsum(sizes)[:-1])
+        proj = all(k == 0 for k in K) and abs(p) < 10 * tol
+        H = HeffGPU(v.ctx, inp["AL"], inp["AR"], inp["NL"], inp["HLtot"], inp["HRtot"], inp["h"], d, inp["xdims"],
+                    kfac, tol=tol, LM=inp["LM"] if proj else None, RM=inp["RM"] if proj else None)
+        H.x_to_planes(xs)
+        if not H.apply():
+            raise RuntimeError("environment solve did not converge")
+        ys = H.y_from_planes()
+        out[name] = np.array([np.vdot(xs[n], ys[n]) for n in range(2)])
+    return out
+
+
 # ------------------------------------------------------------------------------------------------
 # dominant eigenmatrices of the mixed transfer matrix (EigsBlockFunctions.hpp:282-391,
 # Excitations_helpers.hpp:915-946)
@@ -672,24 +720,40 @@ def xdims_from_layouts(ns_layout, ar_layout, K, periods=None):
     return dims
 
 
-def excitation_inputs(v, K, tol=1e-13):
+def excitation_inputs(v, K, tol=1e-13, op=None):
     """AL, AR, N_L, HLtot, HRtot (HeffConstants, Excitations_helpers.hpp:258-331), h - E0 and
     XDims for charge K, from a converged VumpsGPU state (sites n: bond n -> n + 1; C[b] on bond
-    b), every contraction and solve on the device; host copies as map-of-blocks structures."""
+    b), every contraction and solve on the device; host copies as map-of-blocks structures.
+    op: another two-site operator (d^2 x d^2, its mean already subtracted) in place of h - E0."""
     from . import ops as _ops
+    from . import models as _models
     ctx, d, torch = v.ctx, v.d, v.torch
     AL, AR = v.AL, v.AR
-    E0 = float(np.mean(v.energy()))
     eye0 = v._eye(0)
+    if op is None:
+        E0 = float(np.mean(v.energy()))
+        optl, optr, onnz = v.optm_l, v.optm_r, v.hnnz
+    else:
+        E0 = 0.0
+        onnz = _models.h_nonzeros(np.asarray(op, dtype=np.float64))
+        optl = [B.plan_optm(ctx, v.LA[a], v.LA[1 - a], d, onnz, 0, v.LB[a]) for a in range(2)]
+        optr = [B.plan_optm(ctx, v.LA[a], v.LA[1 - a], d, onnz, 1, v.LB[a]) for a in range(2)]
+
+    def optm(plans, a, A, b):
+        p = plans[a]
+        out = v._z(v.LB[b])
+        p.bind(0, A[a]); p.bind(1, A[1 - a]); p.bind(2, out); p.run()
+        return out
+
     # left: HL[0] = OpTM(AL1 AL0) on bond 1, HL[1] = OpTM(AL0 AL1) + T_L(AL1, HL[0]) on bond 0
-    HL0 = v._optm(True, 1, AL, v._z(v.LB[1]))
-    HL1 = v._get_hl(0)
+    HL0 = optm(optl, 1, AL, 1)
+    HL1 = _ops.axpby(ctx, 1.0, optm(optl, 0, AL, 0), 1.0, v._tm(("L1", 1), AL, HL0, v._z(v.LB[0])))
     R0 = v._tm_dominant(("R", 0), AL, v._cct(0, right=True), 1e-15)
     EHL1 = v._invert_e(("L", 0), AL, HL1, eye0, R0, "l", None, tol)
     EHL0 = v._tm(("L1", 0), AL, EHL1, v._z(v.LB[1]))
     # right: HR[1] = OpTM(AR1 AR0) on bond 1, HR[0] = OpTM(AR0 AR1) + T_R(AR0, HR[1]) on bond 0
-    HR1 = v._optm(False, 1, AR, v._z(v.LB[1]))
-    HR0 = v._get_hr(0)
+    HR1 = optm(optr, 1, AR, 1)
+    HR0 = _ops.axpby(ctx, 1.0, optm(optr, 0, AR, 0), 1.0, v._tm(("R1", 0), AR, HR1, v._z(v.LB[0])))
     L0 = v._tm_dominant(("L", 0), AR, v._cct(0, right=False), 1e-15)
     EHR0 = v._invert_e(("R", 0), AR, HR0, L0, eye0, "r", None, tol)
     EHR1 = v._tm(("R1", 1), AR, EHR0, v._z(v.LB[1]))
@@ -705,10 +769,13 @@ def excitation_inputs(v, K, tol=1e-13):
         _ops.Nullspace(plan, AL[n], out)
         NL.append(mps_to_host(out, plan.nslayout, d))
         nsl.append(plan.nslayout)
-    hs = [(r, c, val - (E0 if r == c else 0.0)) for (r, c, val) in v.hnnz]
-    diag = {r for (r, c, _) in v.hnnz if r == c}
-    hs += [(i, i, -E0) for i in range(d * d) if i not in diag]
-    hs.sort(key=lambda t: (t[1], t[0]))
+    if op is None:
+        hs = [(r, c, val - (E0 if r == c else 0.0)) for (r, c, val) in v.hnnz]
+        diag = {r for (r, c, _) in v.hnnz if r == c}
+        hs += [(i, i, -E0) for i in range(d * d) if i not in diag]
+        hs.sort(key=lambda t: (t[1], t[0]))
+    else:
+        hs = list(onnz)
     per = charges.periods_of(v.I2K)
     xd = [xdims_from_layouts(nsl[n], v.LA[(n + 1) % 2], tuple(K), per) for n in range(2)]
     ALh = [mps_to_host(AL[n], v.LA[n], d) for n in range(2)]

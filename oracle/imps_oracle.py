@@ -860,6 +860,87 @@ def ApplyHeff(Xin, kfac, AL, AR, NL, hnnz, d, HLtot, HRtot, LM=None, RM=None, to
     return [ApplyTMmixedLeft(Bout[n], NL[n]) for n in range(N)]
 
 
+def OPeffConstants(AL, AR, L, R, onnz, tol=1e-14, rng=None):
+    """Excitations_helpers.hpp:548-606 for a one-site operator (its mean already subtracted):
+    OPLtot[n] (left environment up to and including site n) and OPRtot[n] (right environment
+    from site n on), the infinite parts closed by InvertE_proj."""
+    N = len(AL)
+    P = lambda x: (x + N) % N
+    OPL = [ApplyOpTMLeftDiag(onnz, AL[0])]
+    for n in range(1, N):
+        OPL.append(bd_add(ApplyOpTMLeftDiag(onnz, AL[n]), ApplyTMLeft(AL[n], OPL[-1])))
+    OPR = [None] * N
+    OPR[N - 1] = ApplyOpTMRightDiag(onnz, AR[N - 1])
+    for n in range(N - 2, -1, -1):
+        OPR[n] = bd_add(ApplyOpTMRightDiag(onnz, AR[n]), ApplyTMRight(AR[n], OPR[n + 1]))
+    OPLtot, OPRtot = [None] * N, [None] * N
+    EOPL = [None] * N
+    EOPL[N - 1], _ = InvertE_proj(AL, OPL[N - 1], bd_eye({q: M.shape[1] for q, M in R.items()}), R, "l", tol,
+                                  rng=rng)
+    OPLtot[N - 1] = EOPL[N - 1]
+    for n in range(N - 1):
+        EOPL[n] = ApplyTMLeft(AL[n], EOPL[P(n - 1)])
+        OPLtot[n] = bd_add(OPL[n], EOPL[n])
+    EOPR = [None] * N
+    EOPR[0], _ = InvertE_proj(AR, OPR[0], L, bd_eye({q: M.shape[1] for q, M in L.items()}), "r", tol, rng=rng)
+    OPRtot[0] = EOPR[0]
+    for n in range(N - 1, 0, -1):
+        EOPR[n] = ApplyTMRight(AR[n], EOPR[P(n + 1)])
+        OPRtot[n] = bd_add(EOPR[n], OPR[n])
+    return OPLtot, OPRtot
+
+
+def ApplyOPeff(Xin, kfac, AL, AR, NL, onnz, OPLtot, OPRtot, LM=None, RM=None, tol=1e-14, rng=None):
+    """Excitations_helpers.hpp:350-545: the one-site operator sum_n O_n of the excitation ansatz
+    applied to X, as the reference writes it (B on, left of and right of the output site, the
+    infinite sums closed by InvertE_fac / InvertE_proj_fac; the left solve skipped when its
+    source is below 10 tol, :478)."""
+    N = len(Xin)
+    ck = np.conj(kfac)
+    P = lambda x: (x + N) % N
+    proj = LM is not None and RM is not None
+    Bin = [mps_mul_bm(NL[n], Xin[n]) for n in range(N)]
+    ABR = [None] * N
+    ABR[N - 1] = ApplyTMmixedRight(Bin[N - 1], AR[N - 1])
+    for n in range(N - 1, 0, -1):
+        ABR[n - 1] = ApplyTMmixedRight(mps_add(Bin[n - 1], mps_mul_bm(AL[n - 1], ABR[n])), AR[n - 1])
+    if proj:
+        E, _ = InvertE_proj_fac(AL, AR, ABR[0], LM, RM, "r", kfac, tol, rng=rng)
+    else:
+        E, _ = InvertE_fac(AL, AR, ABR[0], "r", kfac, tol, rng=rng)
+    ABRtot = [None] * N
+    ABRtot[0] = bm_scale(E, kfac)
+    for n in range(N - 1, 0, -1):
+        E = ApplyTMmixedRightX(AL[n], AR[n], E)
+        ABRtot[n] = bm_add(ABR[n], bm_scale(E, kfac))
+    OPBL = [bm_add(ApplyTMmixedLeft(bd_mul_mps(OPLtot[N - 1], Bin[0]), AL[0]), ApplyOpTMLeftGen(onnz, Bin[0], AL[0]))]
+    for n in range(1, N):
+        OPBL.append(bm_add(ApplyTMmixedLeft(mps_add(bm_mul_mps(OPBL[-1], AR[n]), bd_mul_mps(OPLtot[n - 1], Bin[n])),
+                                            AL[n]),
+                           ApplyOpTMLeftGen(onnz, Bin[n], AL[n])))
+    norm_inf = max((float(np.abs(M).max()) for (_, M) in OPBL[-1].values() if M.size), default=0.0)
+    have = norm_inf > 10 * tol
+    if have:
+        if proj:
+            EOP, _ = InvertE_proj_fac(AR, AL, OPBL[-1], bm_t(LM), bm_t(RM), "l", ck, tol, rng=rng)
+        else:
+            EOP, _ = InvertE_fac(AR, AL, OPBL[-1], "l", ck, tol, rng=rng)
+    Bout = [mps_add(mps_add(bd_mul_mps(OPLtot[P(n - 1)], Bin[n]), mps_mul_bd(Bin[n], OPRtot[P(n + 1)])),
+                    ApplyOperator(Bin[n], onnz)) for n in range(N)]
+    if have:
+        Bout[0] = mps_add(Bout[0], bm_mul_mps(bm_scale(EOP, ck), AR[0]))
+    for n in range(1, N):
+        tmp = OPBL[n - 1]
+        if have:
+            EOP = ApplyTMmixedLeftX(AR[n - 1], AL[n - 1], EOP)
+            tmp = bm_add(tmp, bm_scale(EOP, ck))
+        Bout[n] = mps_add(Bout[n], bm_mul_mps(tmp, AR[n]))
+    for n in range(N):
+        Bout[n] = mps_add(Bout[n], mps_add(mps_mul_bm(bd_mul_mps(OPLtot[P(n - 1)], AL[n]), ABRtot[P(n + 1)]),
+                                          mps_mul_bm(ApplyOperator(AL[n], onnz), ABRtot[P(n + 1)])))
+    return [ApplyTMmixedLeft(Bout[n], NL[n]) for n in range(N)]
+
+
 def ApplyOperator(A, hnnz):
     """MPSBlockUtilities.hpp:17-34: out[ii] += h * in[jj]."""
     out = [dict() for _ in A]

@@ -399,3 +399,25 @@ def test_projected_energies_match_oracle(cuda_ctx):
     ref = np.sort(eigsh(LinearOperator((mtot, mtot), matvec=hop, dtype=np.complex128), k=3, which="SA",
                         tol=1e-11, return_eigenvectors=False))
     assert np.abs(np.sort(ev) - ref).max() < 1e-8 * max(1.0, np.abs(ref).max()), (ev, ref)
+
+
+def test_measure_excitations_total_sz(cuda_ctx):
+    """MeasureExcitations (Excitations_helpers.hpp:754-808) on the device, end to end.  The
+    excitation-space operator of the total Sz minus its mean is the sector's Sz shift times the
+    identity (the oracle's ApplyOPeff shows it exactly), so on the normalised random X the
+    per-site values sum to -K/2 in label units.  A charge-changing observable gives zero."""
+    from imps_cpp_tools_gb300 import models
+    from imps_cpp_tools_gb300.excitations import measure_excitations
+    from imps_cpp_tools_gb300.vumps import VumpsGPU
+    b0 = {(-2,): 3, (0,): 5, (2,): 3}
+    dimvec = models.make_dims(b0, 2, models.build_model("xxz", J=1.0, Delta=-1.0)[1])
+    v = VumpsGPU(cuda_ctx, "xxz", dimvec=dimvec, seed=5, InvETol=1e-13, J=1.0, Delta=-1.0)
+    for _ in range(200):
+        E, F, _ = v.sweep()
+        if F.max() < 1e-11:
+            break
+    assert F.max() < 1e-10
+    for K, p in (((2,), 0.7), ((-2,), 2.1)):
+        vals = measure_excitations(v, K, ["sz", "sx"], np.exp(1j * p))
+        assert abs(vals["sz"].sum() - (-K[0] / 2)) < 1e-8, (K, vals["sz"])
+        assert np.all(vals["sx"] == 0)

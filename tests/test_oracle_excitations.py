@@ -209,3 +209,42 @@ def test_projected_heff_is_hermitian():
     HY = O.ApplyHeff(Y, *args, LM=LM, RM=RM, tol=1e-13)
     a, b = x_inner(Y, HX, e["xdims"]), x_inner(HY, X, e["xdims"])
     assert abs(a - b) < 1e-10 * abs(a), (a, b)
+
+
+def _opeff_setup(K):
+    """The excitation setup with the one-site sz, its mean subtracted, in both forms: the
+    reference's OPeffConstants (Excitations_helpers.hpp:548-606) and the bond operator
+    (sz x 1 + 1 x sz) / 2 with HeffConstants."""
+    e = excitation_setup(K)
+    st = T.random_state("xxz", B0, seed=3, J=1.0, Delta=-1.0)
+    C = st["C"]
+    R, L = O.bd_mul(C[-1], O.bd_t(C[-1])), O.bd_mul(O.bd_t(C[-1]), C[-1])
+    Lb = [O.bd_mul(O.bd_t(C[0]), C[0]), L]  # left of site 1, left of site 0
+    sz = np.diag([0.5, -0.5])
+    eobs = float(np.mean(O.MeasureObservables([("sz", sz)], e["AR"], Lb)["sz"]))
+    onnz = O.sparse_nnz(sz - eobs * np.eye(2))
+    OPL, OPR = O.OPeffConstants(e["AL"], e["AR"], L, R, onnz, tol=1e-13)
+    hn = O.sparse_nnz(0.5 * (np.kron(sz, np.eye(2)) + np.kron(np.eye(2), sz)) - eobs * np.eye(4))
+    HL, HR = O.HeffConstants(e["AL"], e["AR"], L, R, hn, tol=1e-13)
+    return e, onnz, OPL, OPR, hn, HL, HR
+
+
+@pytest.mark.parametrize("K,p,proj", [((2,), 0.6, False), ((-2,), 2.4, False), ((0,), 0.0, True)])
+def test_opeff_is_the_bond_form_of_heff(K, p, proj):
+    """ApplyOPeff (Excitations_helpers.hpp:350-545) with a one-site O equals ApplyHeff with the
+    two-site (O x 1 + 1 x O) / 2 (the same operator on the infinite chain), which is how the
+    device evaluates MeasureExcitations; and for O = sz the excitation-space operator is the
+    sector's Sz shift times the identity (K = +-2 in label units: -+1), exactly."""
+    e, onnz, OPL, OPR, hn, HL, HR = _opeff_setup(K)
+    LM = RM = None
+    if proj:
+        LM, RM, _, _, _ = O.LRoverlaps(e["AL"], e["AR"], K, 2)
+    X = rand_x(e["xdims"], np.random.default_rng(7))
+    kfac = np.exp(1j * p)
+    XO = O.ApplyOPeff(X, kfac, e["AL"], e["AR"], e["NL"], onnz, OPL, OPR, LM=LM, RM=RM, tol=1e-13)
+    XH = O.ApplyHeff(X, kfac, e["AL"], e["AR"], e["NL"], hn, 2, HL, HR, LM=LM, RM=RM, tol=1e-13)
+    c = -K[0] / 2
+    for n, dims in enumerate(e["xdims"]):
+        for (q, _, _, _) in dims:
+            assert np.abs(XO[n][q][1] - XH[n][q][1]).max() < 1e-11
+            assert np.abs(XO[n][q][1] - c * X[n][q][1]).max() < 1e-11
