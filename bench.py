@@ -533,7 +533,7 @@ def run_excitations(args):
     ex = ExcitationsGPU(ctx, inp["AL"], inp["AR"], inp["NL"], inp["HLtot"], inp["HRtot"], inp["h"], inp["d"],
                         inp["xdims"], tol=1e-12)
     ps = np.linspace(0.0, np.pi, max(args.steps, 1) + 2)[1:-1]
-    rows, t_tot, applies0 = [], 0.0, 0
+    rows, t_tot = [], 0.0
     for p in ps:
         # compile + solve; the compile (host sector matching) is reported separately
         tc = time.perf_counter()

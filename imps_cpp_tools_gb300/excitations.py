@@ -128,7 +128,6 @@ class Program:
                                 terms.setdefault((1, key), []).append(term + (c.imag,))
         cplx = force_complex or any(p == 1 for (p, _) in terms) or target is not None
         if target is None:
-            blocks = {}
             off = 0
             keys = sorted(shape)
             nel = sum(shape[k][1] * shape[k][2] for k in keys)

@@ -114,7 +114,6 @@ def expand_from_h(ctx, I2K, hnnz, LA, AL, LR, AR, LC, Cc, dmmax):
     Returns a dict with ``dm`` ({charge: states added} for every charge considered), ``dims``
     (the grown centre bond), the new layouts ``LA``, ``LR``, ``LC`` and the new tensors ``AL``,
     ``AR``, ``C`` (device, in those layouts), and ``converged`` (the sector SVD's flag)."""
-    torch = __import__("torch")
     d = len(I2K)
     dl, dc, dR = LA.dims(0), LC.dims(0), LR.dims(1)
     # AL C, and the null spaces of AL (dir l) and of AR (as the dir-l complement of AR^T)
@@ -226,13 +225,13 @@ def expand_from_h(ctx, I2K, hnnz, LA, AL, LR, AR, LC, Cc, dmmax):
         # T = NL^T Phi  (nul_l x n)
         tl = []
         for (sl, ql, ra, mr) in e["rows"]:
-            o, nc = nl_off[(sl, ql)]
+            o, _ = nl_off[(sl, ql)]
             tl.append((SNL, o, mr, 1, SPHI, phi_off[c] + ra, e["m"], 0, mr, 1.0))
         s_t.append((ST, t_off[c], nul_l, nul_l, e["n"], tl))
         # M = T NR^T (nul_l x nul_r), or M^T = NR T^T when nul_l < nul_r
         tl = []
         for (sr, qr, ca, mc) in e["cols"]:
-            o, nc = nr_off[(sr, qr)]
+            o, _ = nr_off[(sr, qr)]
             if not e["tr"]:
                 tl.append((ST, t_off[c] + ca * nul_l, nul_l, 0, SNR, o, mc, 0, mc, 1.0))
             else:
@@ -304,11 +303,11 @@ def expand_from_h(ctx, I2K, hnnz, LA, AL, LR, AR, LC, Cc, dmmax):
         if not e["new"]:
             nul_l, nul_r = e["nul"]
             for (sl, ql, ra, mr) in e["rows"]:
-                o, nc = nl_off[(sl, ql)]
+                o, _ = nl_off[(sl, ql)]
                 ob, rr, cc = ial[(sl, ql)]
                 st.append((SAL, ob + m0 * rr, rr, rr, k, [(SNL, o, mr, 0) + opnd(um, 0, False) + (nul_l, 1.0)]))
             for (sr, qr, ca, mc) in e["cols"]:
-                o, nc = nr_off[(sr, qr)]
+                o, _ = nr_off[(sr, qr)]
                 ob, rr, cc = iar[(sr, c)]
                 st.append((SARn, ob + m0, rr, k, cc, [opnd(vm, 0, True) + (SNR, o, mc, 1, nul_r, 1.0)]))
         else:

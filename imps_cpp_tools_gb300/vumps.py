@@ -226,10 +226,9 @@ class VumpsGPU:
         """VUMPS_main.cpp:103-136: reduced operators, EHL/EHR, EHL1/EHR1."""
         torch = self.torch
         self._redops()
-        # R at bond 0 (right end of [AL(0), AL(1)]): C[0] C[0]^T ; L at bond 0 for [AR(0), AR(1)]:
-        # C[0]^T C[0] (the reference's initial shift puts these at the unit-cell boundary)
+        # R at bond 0 (right end of [AL(0), AL(1)]): C[0] C[0]^T (the reference's initial shift
+        # puts it at the unit-cell boundary); the right environment's L is C[1]^T C[1]
         R = self._cct(0, right=True)
-        L = self._cct(0, right=False)
         self.EHL = self._invert_e(("L", 0), self.AL, self._get_hl(0), self._eye(0), R, "l", None, self.InvETol)
         self.EHR = self._invert_e(("R", 1), self.AR, self._get_hr(1), self._cct(1, right=False),
                                   self._eye(1), "r", None, self.InvETol)
