@@ -537,6 +537,23 @@ class ExcitationsGPU:
         return out[:nev], conv and len(out) >= nev
 
 
+def save_alrn(v, inp, name, ending="bin", folder="."):
+    """saveALRN as the excitation driver writes it (Excitations_main.cpp:232-237): the ground
+    state the excitations of ``inp`` (excitation_inputs) are built from, with C[n] the centre
+    matrix right of site n, L[n] = C[n]^T C[n] and R[n] = C[n] C[n]^T (formed on the device),
+    AL, AR (after the sign fix of AR[0]) and the null spaces NL.  Returns the path written."""
+    from . import imps_io
+    Cv, Lv, Rv = [], [], []
+    for n in range(2):
+        b = (n + 1) % 2  # the C right of site n lives on bond n + 1
+        Cv.append(bd_to_host(v.C[b], v.LB[b]))
+        Lv.append(bd_to_host(v._cct(b, right=False), v.LB[b]))
+        Rv.append(bd_to_host(v._cct(b, right=True), v.LB[b]))
+    mps = lambda A: imps_io.MPSTensor(v.d, 1, A)
+    return imps_io.saveALRN(Cv, Lv, Rv, [mps(a) for a in inp["AL"]], [mps(a) for a in inp["AR"]],
+                            [mps(a) for a in inp["NL"]], name, ending, folder)
+
+
 def measure_excitations(v, K, obs, kfac, seed=1, tol=1e-13):
     """MeasureExcitations (Excitations_helpers.hpp:754-808) on the device.  For each one-site
     observable O: its ground-state mean <O> is subtracted, and the excitation-space operator

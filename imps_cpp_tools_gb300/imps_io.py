@@ -328,6 +328,58 @@ def loadIMPS(filename):
 
 
 # ------------------------------------------------------------------------------------------------
+# the excitation driver's file: ground state with environments and null spaces
+# ------------------------------------------------------------------------------------------------
+
+@dataclass
+class ALRNState:
+    """The six arrays of saveALRN, indexed by site n: C[n] (right of site n), L[n] = C[n]^T C[n],
+    R[n] = C[n] C[n]^T (Excitations_main.cpp:134-138), AL, AR (AR as the excitation driver
+    uses it, after its shifts and the sign fix of AR[0]) and the left null spaces NL."""
+    C: list
+    L: list
+    R: list
+    AL: list
+    AR: list
+    NL: list
+
+
+def save_alrn_stream(f, Cvec, Lvec, Rvec, ALvec, ARvec, NLvec):
+    """saveALRN(Cvec, Lvec, Rvec, ALvec, ARvec, NLvec, file) (Excitations_helpers.hpp:949-989)."""
+    for arr in (Cvec, Lvec, Rvec):
+        _write_array(f, HDR_BDMATARRAY, arr, write_blockdiag)
+    for arr in (ALvec, ARvec, NLvec):
+        _write_array(f, HDR_MPSARRAY, arr, write_mps)
+
+
+def saveALRN(Cvec, Lvec, Rvec, ALvec, ARvec, NLvec, name, ending="bin", folder="."):
+    """saveALRN(..., name, ending) (Excitations_helpers.hpp:992-1013, called at
+    Excitations_main.cpp:234-236): a new file named by ``unique_file_name``; returns its path."""
+    path = unique_file_name(name, ending, folder)
+    buf = io.BytesIO()
+    save_alrn_stream(buf, Cvec, Lvec, Rvec, ALvec, ARvec, NLvec)
+    with open(path, "wb") as f:
+        f.write(buf.getvalue())
+    return path
+
+
+def load_alrn_bytes(data):
+    """loadALRN(..., GroupObj, file) (Excitations_helpers.hpp:1017-1058)."""
+    r = _Reader(data)
+    C, L, R = (_read_array(r, HDR_BDMATARRAY, read_blockdiag) for _ in range(3))
+    AL, AR, NL = (_read_array(r, HDR_MPSARRAY, read_mps) for _ in range(3))
+    return ALRNState(C, L, R, AL, AR, NL)
+
+
+def loadALRN(filename):
+    """loadALRN(..., filename) (Excitations_helpers.hpp:1062-1085)."""
+    if not os.path.isfile(filename):
+        raise FileNotFoundError(f"file {filename} not found")
+    with open(filename, "rb") as f:
+        return load_alrn_bytes(f.read())
+
+
+# ------------------------------------------------------------------------------------------------
 # conversion to and from the flat Vectorize buffers of blocks.Layout
 # ------------------------------------------------------------------------------------------------
 

@@ -1,4 +1,5 @@
-// State files of the reference (saveIMPS / loadIMPS, MPSBlockUtilities.hpp:1215-1327) for C++
+// State files of the reference (saveIMPS / loadIMPS, MPSBlockUtilities.hpp:1215-1327, and the
+// excitation driver's saveALRN / loadALRN, Excitations_helpers.hpp:949-1085) for C++
 // host programs: header-only C++17, independent of the GPU library, so that a host can read a
 // state the reference wrote, hand its sector tables to imps_layout_create and its flat
 // Vectorize buffers to the plans, and write results back in the same format.
@@ -292,6 +293,33 @@ inline imps_state load_imps(const std::string& filename) {
   std::ifstream f(filename, std::ios::binary);
   if (!f) throw format_error("file " + filename + " not found");
   return load(f);
+}
+
+// ---- the excitation driver's file (saveALRN / loadALRN, Excitations_helpers.hpp:949-1085) -----
+struct alrn_state {  // indexed by site n: c[n] right of site n, l[n] = c^T c, r[n] = c c^T
+  std::vector<block_diag> c, l, r;
+  std::vector<mps_tensor> al, ar, nl;
+};
+
+inline void save(std::ostream& os, const alrn_state& st) {
+  save_array(os, kDiagArray, st.c);
+  save_array(os, kDiagArray, st.l);
+  save_array(os, kDiagArray, st.r);
+  save_array(os, kMpsArray, st.al);
+  save_array(os, kMpsArray, st.ar);
+  save_array(os, kMpsArray, st.nl);
+  if (!os) throw format_error("write failed");
+}
+
+inline alrn_state load_alrn(std::istream& is) {
+  alrn_state st;
+  st.c = load_array(is, kDiagArray, load_diag);
+  st.l = load_array(is, kDiagArray, load_diag);
+  st.r = load_array(is, kDiagArray, load_diag);
+  st.al = load_array(is, kMpsArray, load_mps);
+  st.ar = load_array(is, kMpsArray, load_mps);
+  st.nl = load_array(is, kMpsArray, load_mps);
+  return st;
 }
 
 // ---- to and from the sector tables and flat buffers of the C ABI ------------------------------

@@ -4,6 +4,7 @@
 //                               tensors back, print a one-line JSON summary (sectors, elements
 //                               and an order-sensitive checksum of every flat buffer), save OUT
 //   imps_io_check make OUT      write a fixed two-site state whose values are i/64 (exact)
+//   imps_io_check alrn IN OUT   load a saveALRN file, print the null spaces' summary, save OUT
 //
 // Exit status 0 on success; a format error prints it and exits 1.
 #include <cstdio>
@@ -116,13 +117,21 @@ imps_io::imps_state make_state() {
 int main(int argc, char** argv) {
   try {
     std::string mode = argc > 1 ? argv[1] : "";
+    if (mode == "alrn" && argc == 4) {  // loadALRN and saveALRN of the excitation driver's file
+      std::ifstream in(argv[2], std::ios::binary);
+      imps_io::alrn_state st = imps_io::load_alrn(in);
+      std::printf("{\"sites\": %zu, \"nl\": %s}\n", st.al.size(), summary_mps(st.nl).c_str());
+      std::ofstream f(argv[3], std::ios::binary);
+      imps_io::save(f, st);
+      return f.good() ? 0 : 1;
+    }
     if (mode == "make" && argc == 3) {
       std::ofstream f(argv[2], std::ios::binary);
       imps_io::save(f, make_state());
       return f.good() ? 0 : 1;
     }
     if (mode != "copy" || argc != 4) {
-      std::fprintf(stderr, "usage: %s copy IN OUT | make OUT\n", argv[0]);
+      std::fprintf(stderr, "usage: %s copy IN OUT | make OUT | alrn IN OUT\n", argv[0]);
       return 2;
     }
     imps_io::imps_state st = imps_io::load_imps(argv[2]);

@@ -234,3 +234,41 @@ def test_driver_rejects_an_incompatible_state(oracle_state, tmp_path):
     three = F.IMPSState(st.Lam * 2, st.C * 2, st.AL * 2, st.AR * 2)
     with pytest.raises(F.IMPSFormatError, match="two-site cells"):
         VumpsGPU.from_imps(None, "xxz", three)
+
+
+def _alrn_state(oracle_state):
+    d, I2K, st = oracle_state
+    L = [{q: m.T @ m for q, m in C.items()} for C in st.C]
+    R = [{q: m @ m.T for q, m in C.items()} for C in st.C]
+    NL = [F.MPSTensor(d, 1, O.Nullspace(A.blocks, "l")) for A in st.AL]
+    return st.C, L, R, st.AL, st.AR, NL
+
+
+def test_alrn_round_trip(oracle_state, tmp_path):
+    """saveALRN / loadALRN (Excitations_helpers.hpp:949-1085): C, L, R as RBLOCKDIAGMATARRAY,
+    then AL, AR, NL as RBLOCKMPSARRAY, in that order."""
+    arrs = _alrn_state(oracle_state)
+    path = F.saveALRN(*arrs, "x_ALRN", folder=str(tmp_path))
+    data = Path(path).read_bytes()
+    assert data.startswith(b"RBLOCKDIAGMATARRAY\n" + _u32(2) + b"RBLOCKDIAGMAT\n")
+    assert data.count(b"RBLOCKDIAGMATARRAY\n") == 3 and data.count(b"RBLOCKMPSARRAY\n") == 3
+    back = F.loadALRN(path)
+    for got, ref in zip((back.C, back.L, back.R), arrs[:3]):
+        for n in range(2):
+            assert got[n].keys() == ref[n].keys() and all(np.array_equal(got[n][q], ref[n][q]) for q in ref[n])
+    for got, ref in zip((back.AL, back.AR, back.NL), arrs[3:]):
+        for n in range(2):
+            assert all(got[n].blocks[s].keys() == ref[n].blocks[s].keys() for s in range(ref[n].d))
+    f = io.BytesIO()
+    F.save_alrn_stream(f, back.C, back.L, back.R, back.AL, back.AR, back.NL)
+    assert f.getvalue() == data
+    with pytest.raises(F.IMPSFormatError, match="should be RBLOCKDIAGMATARRAY"):
+        F.load_alrn_bytes(data[data.index(b"RBLOCKMPSARRAY"):])
+
+
+def test_cpp_alrn_round_trip(io_check, oracle_state, tmp_path):
+    src = F.saveALRN(*_alrn_state(oracle_state), "py_ALRN", folder=str(tmp_path))
+    dst = tmp_path / "cpp_ALRN.bin"
+    out = subprocess.run([str(io_check), "alrn", src, str(dst)], check=True, capture_output=True, text=True)
+    assert dst.read_bytes() == Path(src).read_bytes()
+    assert json.loads(out.stdout)["sites"] == 2
