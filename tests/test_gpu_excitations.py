@@ -400,51 +400,3 @@ def test_projected_energies_match_oracle(cuda_ctx):
                         tol=1e-11, return_eigenvectors=False))
     assert np.abs(np.sort(ev) - ref).max() < 1e-8 * max(1.0, np.abs(ref).max()), (ev, ref)
 
-
-def test_measure_excitations_total_sz(cuda_ctx):
-    """MeasureExcitations (Excitations_helpers.hpp:754-808) on the device, end to end.  The
-    excitation-space operator of the total Sz minus its mean is the sector's Sz shift times the
-    identity (the oracle's ApplyOPeff shows it exactly), so on the normalised random X the
-    per-site values sum to -K/2 in label units.  A charge-changing observable gives zero."""
-    from imps_cpp_tools_gb300 import models
-    from imps_cpp_tools_gb300.excitations import measure_excitations
-    from imps_cpp_tools_gb300.vumps import VumpsGPU
-    b0 = {(-2,): 3, (0,): 5, (2,): 3}
-    dimvec = models.make_dims(b0, 2, models.build_model("xxz", J=1.0, Delta=-1.0)[1])
-    v = VumpsGPU(cuda_ctx, "xxz", dimvec=dimvec, seed=5, InvETol=1e-13, J=1.0, Delta=-1.0)
-    for _ in range(200):
-        E, F, _ = v.sweep()
-        if F.max() < 1e-11:
-            break
-    assert F.max() < 1e-10
-    for K, p in (((2,), 0.7), ((-2,), 2.1)):
-        vals = measure_excitations(v, K, ["sz", "sx"], np.exp(1j * p))
-        assert abs(vals["sz"].sum() - (-K[0] / 2)) < 1e-8, (K, vals["sz"])
-        assert np.all(vals["sx"] == 0)
-
-
-def test_ising_dispersion_on_gpu(cuda_ctx):
-    """The device excitation pipeline with Z(2) charges (quantum Ising, odd sector K = 1): the
-    two lowest energies at cell momentum P are the exact quasiparticle energies at k = P/2 and
-    P/2 + pi, eps(k) = 2 sqrt(J'^2 + h'^2 - 2 J' h' cos k), J' = J/4, h' = h/2."""
-    import math
-    from imps_cpp_tools_gb300.excitations import ExcitationsGPU, excitation_inputs
-    from imps_cpp_tools_gb300.vumps import VumpsGPU
-    J, h = 1.0, 1.0
-    Jp, hp = J / 4, h / 2
-    eps = lambda k: 2 * math.sqrt(Jp ** 2 + hp ** 2 - 2 * Jp * hp * math.cos(k))
-    b = {(0,): 8, (1,): 8}
-    v = VumpsGPU(cuda_ctx, "qim", dimvec=[b, b], seed=2, InvETol=1e-13, J=J, h=h)
-    for _ in range(80):
-        E, F, _ = v.sweep()
-        if F.max() < 1e-12:
-            break
-    assert F.max() < 1e-10
-    inp = excitation_inputs(v, (1,), tol=1e-13)
-    ex = ExcitationsGPU(cuda_ctx, inp["AL"], inp["AR"], inp["NL"], inp["HLtot"], inp["HRtot"], inp["h"], inp["d"],
-                        inp["xdims"], tol=1e-13, LM=inp["LM"], RM=inp["RM"])
-    for P in (0.3, 2.0):
-        ev, conv = ex.energies(np.exp(1j * P), nev=2, eig_tol=1e-11)
-        assert conv
-        exact = sorted([eps(P / 2), eps(P / 2 + math.pi)])
-        assert np.abs(np.array(ev) - exact).max() < 1e-8, (P, ev, exact)

@@ -87,22 +87,3 @@ def test_excitations_from_the_file(cuda_ctx, saved):
         for q in a["HLtot"][n]:
             assert np.abs(a["HLtot"][n][q] - b["HLtot"][n][q]).max() < 1e-9
     assert np.abs(ea - eb).max() < 1e-8, (ea, eb)
-
-
-def test_alrn_file_of_the_excitation_inputs(cuda_ctx, saved, tmp_path):
-    """saveALRN as the excitation driver writes it (Excitations_main.cpp:232-237): C right of
-    each site, L = C^T C and R = C C^T formed on the device, AL as the state file has it."""
-    from imps_cpp_tools_gb300.excitations import excitation_inputs, save_alrn
-    v, path = saved
-    inp = excitation_inputs(v, (2,), tol=1e-13)
-    st = F.loadALRN(save_alrn(v, inp, "x_ALRN", folder=str(tmp_path)))
-    ref = F.loadIMPS(path)
-    for n in range(2):
-        assert st.C[n].keys() == ref.C[n].keys()
-        for q, C in st.C[n].items():
-            assert np.array_equal(C, ref.C[n][q])
-            assert np.allclose(st.L[n][q], C.T @ C, atol=1e-13) and np.allclose(st.R[n][q], C @ C.T, atol=1e-13)
-        for s in range(v.d):
-            for q, (qo, M) in st.AL[n].blocks[s].items():
-                assert np.array_equal(M, ref.AL[n].blocks[s][q][1])
-        assert sum(len(b) for b in st.NL[n].blocks) > 0
