@@ -134,12 +134,18 @@ def run_tables(stages, bufs):
 
 
 @pytest.mark.parametrize("K,p", [((2,), 0.6), ((-2,), 2.4)])
-def test_heff_program_tables_match_oracle(K, p):
+@pytest.mark.parametrize("which", ["h", "sz"])
+def test_heff_program_tables_match_oracle(K, p, which):
     """The host compilation of ApplyHeff (imps_cpp_tools_gb300.excitations.HeffProgram), executed
     table by table with numpy and the oracle's InvertE_fac for the two solves, reproduces the
-    oracle's ApplyHeff: a check of the sector matching and term expansion without a GPU."""
+    oracle's ApplyHeff: a check of the sector matching and term expansion without a GPU.  With
+    which = "sz" the two-site operator is the bond form of the one-site sz (mean subtracted),
+    as measure_excitations compiles it; its result is also -K/2 times X exactly."""
     from imps_cpp_tools_gb300 import excitations as EX
     e = excitation_setup(K)
+    if which == "sz":
+        _, _, _, _, hn, HLs, HRs = _opeff_setup(K)
+        e = dict(e, h=hn, HLtot=HLs, HRtot=HRs)
     kfac = np.exp(1j * p)
     pr = EX.HeffProgram(e["AL"], e["AR"], e["NL"], e["HLtot"], e["HRtot"], e["h"], e["d"], e["xdims"], kfac)
     bufs = {k: np.zeros(max(int(pr.sizes.get(k, 0)), 1)) for k in range(6)}
@@ -167,6 +173,9 @@ def test_heff_program_tables_match_oracle(K, p):
         got = bufs[EX.OUT][xo:xo + nn] + 1j * bufs[EX.OUT][xo + nn:xo + 2 * nn]
         refv = np.concatenate([ref[n][qi][1].reshape(-1, order="F") for (qi, _, _, _) in dims])
         assert np.linalg.norm(got - refv) / np.linalg.norm(refv) < 1e-9, n
+        if which == "sz":
+            xv = np.concatenate([X[n][qi][1].reshape(-1, order="F") for (qi, _, _, _) in dims])
+            assert np.linalg.norm(got - (-K[0] / 2) * xv) < 1e-9 * np.linalg.norm(xv), n
 
 
 def test_lroverlaps_dominant_eigenmatrices(state):
