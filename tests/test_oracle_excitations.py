@@ -259,6 +259,68 @@ def test_opeff_is_the_bond_form_of_heff(K, p, proj):
             assert np.abs(XO[n][q][1] - c * X[n][q][1]).max() < 1e-11
 
 
+def _ising_setup(J=1.0, h=1.0):
+    """A converged transverse-field Ising ground state (Z(2) charges, D = 8 + 8) and its
+    excitation inputs for the odd sector K = 1; call inside O.charge_group((2,))."""
+    H = O.qim_h(J, h)
+    v = O.VUMPS(H, 2, O.qim_i2k(), {(0,): 8, (1,): 8}, seed=2)
+    for _ in range(80):
+        E, F, _ = v.sweep()
+        if F.max() < 1e-12:
+            break
+    AL, AR, C0 = v.AL, O.shift(v.AR, 1), v.C[-1]
+    R, L = O.bd_mul(C0, O.bd_t(C0)), O.bd_mul(O.bd_t(C0), C0)
+    hs = O.sparse_nnz(H - float(E.mean()) * np.eye(4))
+    K = (1,)
+    _, _, OL, _, _ = O.LRoverlaps(AL, AR, K, 2)
+    if OL < 0:  # Excitations_main.cpp:177-178
+        AR = [[{q: (qo, -M) for q, (qo, M) in bm.items()} for bm in AR[0]], AR[1]]
+    HL, HR = O.HeffConstants(AL, AR, L, R, hs, tol=1e-13)
+    NL = [O.Nullspace(AL[n], "l") for n in range(2)]
+    return dict(AL=AL, AR=AR, NL=NL, h=hs, HLtot=HL, HRtot=HR, xdims=O.XDims(NL, AR, K), d=2, K=K)
+
+
+def test_ising_tables_and_xdims():
+    """The device path's host side with Z(2) charges: XDims from the layouts with the group's
+    modular arithmetic (excitations.xdims_from_layouts) equals the oracle's, and the H_eff
+    program tables, run with numpy, reproduce the oracle's ApplyHeff."""
+    from imps_cpp_tools_gb300 import blocks as B
+    from imps_cpp_tools_gb300 import excitations as EX
+    with O.charge_group((2,)):
+        e = _ising_setup()
+        lay = lambda A: B.Layout([(s, qi, bm[qi][0], bm[qi][1].shape[0], bm[qi][1].shape[1])
+                                  for s, bm in enumerate(A) for qi in sorted(bm)], 1)
+        for n in range(2):
+            got = EX.xdims_from_layouts(lay(e["NL"][n]), lay(e["AR"][(n + 1) % 2]), e["K"], (2,))
+            assert got == e["xdims"][n]
+        kfac = np.exp(0.9j)
+        pr = EX.HeffProgram(e["AL"], e["AR"], e["NL"], e["HLtot"], e["HRtot"], e["h"], 2, e["xdims"], kfac)
+        bufs = {k: np.zeros(max(int(pr.sizes.get(k, 0)), 1)) for k in range(6)}
+        bufs[EX.OPS][:pr.ops_vec.size] = pr.ops_vec
+        X = rand_x(e["xdims"], np.random.default_rng(4))
+        for (xo, nn), x in zip(pr.xoff, X):
+            vv = O.bm_vec(x)
+            bufs[EX.XS][xo:xo + nn], bufs[EX.XS][xo + nn:xo + 2 * nn] = vv.real, vv.imag
+        run_tables(pr.prog_a.stages, bufs)
+
+        def to_bm(t_re, t_im, slot):
+            return {k[1]: (qo, (bufs[slot][o1:o1 + r * c] + 1j * bufs[slot][t_im.blocks[k][3]:t_im.blocks[k][3] + r * c])
+                           .reshape(c, r).T) for k, (qo, r, c, o1) in t_re.blocks.items()}
+
+        yr, _ = O.InvertE_fac(e["AL"], e["AR"], to_bm(*pr.rhs_r, EX.RHS), "r", kfac, tol=1e-13)
+        yl, _ = O.InvertE_fac(e["AR"], e["AL"], to_bm(*pr.rhs_l, EX.RHS), "l", np.conj(kfac), tol=1e-13)
+        vr, vl = O.bm_vec(yr), O.bm_vec(yl)
+        nr, nl = pr.nr, pr.nl
+        bufs[EX.ES][:nr], bufs[EX.ES][nr:2 * nr] = vr.real, vr.imag
+        bufs[EX.ES][2 * nr:2 * nr + nl], bufs[EX.ES][2 * nr + nl:2 * nr + 2 * nl] = vl.real, vl.imag
+        run_tables(pr.prog_b.stages, bufs)
+        ref = O.ApplyHeff(X, kfac, e["AL"], e["AR"], e["NL"], e["h"], 2, e["HLtot"], e["HRtot"], tol=1e-13)
+    for n, ((xo, nn), dims) in enumerate(zip(pr.xoff, e["xdims"])):
+        got = bufs[EX.OUT][xo:xo + nn] + 1j * bufs[EX.OUT][xo + nn:xo + 2 * nn]
+        refv = np.concatenate([ref[n][qi][1].reshape(-1, order="F") for (qi, _, _, _) in dims])
+        assert np.linalg.norm(got - refv) / np.linalg.norm(refv) < 1e-9, n
+
+
 def test_ising_dispersion_is_exact():
     """The excitation ansatz on the transverse-field Ising chain with Z(2) charges (the odd
     sector K = 1) against its exact quasiparticle dispersion eps(k) = 2 sqrt(J'^2 + h'^2 -
@@ -270,22 +332,8 @@ def test_ising_dispersion_is_exact():
     Jp, hp = J / 4, h / 2
     eps = lambda k: 2 * math.sqrt(Jp ** 2 + hp ** 2 - 2 * Jp * hp * math.cos(k))
     with O.charge_group((2,)):
-        H = O.qim_h(J, h)
-        v = O.VUMPS(H, 2, O.qim_i2k(), {(0,): 8, (1,): 8}, seed=2)
-        for _ in range(80):
-            E, F, _ = v.sweep()
-            if F.max() < 1e-12:
-                break
-        AL, AR, C0 = v.AL, O.shift(v.AR, 1), v.C[-1]
-        R, L = O.bd_mul(C0, O.bd_t(C0)), O.bd_mul(O.bd_t(C0), C0)
-        hs = O.sparse_nnz(H - float(E.mean()) * np.eye(4))
-        K = (1,)
-        _, _, OL, _, _ = O.LRoverlaps(AL, AR, K, 2)
-        if OL < 0:  # Excitations_main.cpp:177-178
-            AR = [[{q: (qo, -M) for q, (qo, M) in bm.items()} for bm in AR[0]], AR[1]]
-        HL, HR = O.HeffConstants(AL, AR, L, R, hs, tol=1e-13)
-        NL = [O.Nullspace(AL[n], "l") for n in range(2)]
-        xd = O.XDims(NL, AR, K)
+        e = _ising_setup(J, h)
+        AL, AR, NL, hs, HL, HR, xd = e["AL"], e["AR"], e["NL"], e["h"], e["HLtot"], e["HRtot"], e["xdims"]
         n = sum(ml * mr for dd in xd for (_, _, ml, mr) in dd)
 
         def tox(vec):
