@@ -109,10 +109,48 @@ class plan {
     check(imps_plan_decomp(ctx.get(), A.get(), dir, &p), "imps_plan_decomp");
     return plan(p);
   }
+  // a grouped-GEMM program (see struct program below); bind every slot, then run()
+  static plan program(const context& ctx, const struct program& prog);
+  void run() { check(imps_plan_run(p_), "imps_plan_run"); }
 
  private:
   imps_plan* p_ = nullptr;
 };
+
+// Tables of imps_plan_program: stages of output blocks C (+)= sum alpha op(A) op(B), the form
+// into which the Python host code compiles the excitation ansatz, the energy gradient and the
+// bond expansion.  Blocks are column-major regions (slot, offset, leading dimension, M, N).
+struct program {
+  struct term { int a_slot; int64_t a_off; int a_ld; bool a_trans; int b_slot; int64_t b_off; int b_ld;
+                bool b_trans; int k; double alpha; };
+  struct out { int slot; int64_t off; int ld, M, N; bool accumulate; std::vector<term> terms; };
+  std::vector<int64_t> slot_nelem;
+  std::vector<std::vector<out>> stages;
+  std::vector<out>& stage() { stages.emplace_back(); return stages.back(); }
+};
+
+inline plan plan::program(const context& ctx, const struct program& prog) {
+  std::vector<int32_t> nouts;
+  std::vector<int64_t> outs, terms;
+  std::vector<double> alphas;
+  for (const auto& st : prog.stages) {
+    nouts.push_back((int32_t)st.size());
+    for (const auto& o : st) {
+      outs.insert(outs.end(), {(int64_t)o.slot, o.off, (int64_t)o.ld, (int64_t)o.M, (int64_t)o.N,
+                               (int64_t)o.accumulate, (int64_t)o.terms.size()});
+      for (const auto& t : o.terms) {
+        terms.insert(terms.end(), {(int64_t)t.a_slot, t.a_off, (int64_t)t.a_ld, (int64_t)t.a_trans, (int64_t)t.b_slot,
+                                   t.b_off, (int64_t)t.b_ld, (int64_t)t.b_trans, (int64_t)t.k});
+        alphas.push_back(t.alpha);
+      }
+    }
+  }
+  imps_plan* p = nullptr;
+  check(imps_plan_program(ctx.get(), (int)prog.slot_nelem.size(), prog.slot_nelem.data(), (int)nouts.size(),
+                          nouts.data(), outs.data(), terms.data(), alphas.data(), &p),
+        "imps_plan_program");
+  return plan(p);
+}
 
 // MultOPx of eigs_rs / eigs_n (eigs.h:43-58): out = Op(in), both of the operator's length
 using multop = std::function<void(double*, double*)>;

@@ -176,8 +176,8 @@ def test_nullspace_layout_matches_oracle_structure():
         assert got == ref
 
 
-def _build_cpp_host(tmp_path):
-    """Compile and link the C++ host program over the C ABI (include/imps_gb300.hpp)."""
+def _build_cpp_host(tmp_path, name="cpp_host_check"):
+    """Compile and link a C++ host program of tests/native over the C ABI (include/imps_gb300.hpp)."""
     import shutil
     import subprocess
     from pathlib import Path
@@ -188,9 +188,9 @@ def _build_cpp_host(tmp_path):
     N.load()
     lib = Path(N.lib_path()).parent
     root = Path(__file__).resolve().parent.parent
-    exe = tmp_path / "cpp_host_check"
+    exe = tmp_path / name
     cmd = [gxx, "-std=c++17", "-O2", "-I", str(root / "include"), "-I", str(cuda / "include"),
-           str(root / "tests" / "native" / "cpp_host_check.cpp"), "-L", str(lib), "-limps_gb300",
+           str(root / "tests" / "native" / f"{name}.cpp"), "-L", str(lib), "-limps_gb300",
            "-L", str(cuda / "lib64"), "-lcudart", f"-Wl,-rpath,{lib}", f"-Wl,-rpath,{cuda / 'lib64'}", "-o", str(exe)]
     subprocess.run(cmd, check=True)
     return exe
@@ -201,3 +201,9 @@ def test_cpp_host_program_builds(tmp_path):
     links against the in-tree library; tests/test_gpu_cpp_host.py runs it."""
     assert _build_cpp_host(tmp_path).exists()
 
+
+
+def test_cpp_program_check_builds(tmp_path):
+    """The C++ grouped-GEMM program builder (imps_cpp::program) compiles and links;
+    tests/test_zzz_gpu_cpp_program.py runs it."""
+    assert _build_cpp_host(tmp_path, "cpp_program_check").exists()
