@@ -1713,9 +1713,16 @@ class VUMPS:
     """Restatement of one VUMPS_main run with ExpandFromH disabled (mmax = D)."""
 
     def __init__(self, h, d, I2K, dmap0, N=2, seed=1, InvETol=5e-15, InvEfac=2.0, fixed_tol=None,
-                 tolmin=5e-16, tolmax=1e-6, trueLR=True, svdthresh=5e-7, dimvec=None, init=None, gmres_maxit=0):
+                 tolmin=5e-16, tolmax=1e-6, trueLR=True, svdthresh=5e-7, dimvec=None, init=None, gmres_maxit=0,
+                 mmax=None, dmmax=20, expand_pause=5, expand_thresh=1e-5, lamthresh=1e-12):
         self.hnnz = sparse_nnz(h)
         self.gmres_maxit = gmres_maxit  # 0: the reference's maxit = problem size
+        # bond expansion (VUMPS_main.cpp:31-35, 149, 168, 270-308), off unless mmax is given
+        self.mmax = None if mmax is None else ([int(mmax)] * N if np.isscalar(mmax) else [int(x) for x in mmax])
+        self.dmmax, self.expand_pause, self.expand_thresh, self.lamthresh = dmmax, expand_pause, expand_thresh, lamthresh
+        self.expand_ct = [0] * N
+        self.exp_prec = 1.0
+        self.expansions = 0
         self.d, self.N, self.I2K = d, N, I2K
         self.InvETol, self.InvEfac, self.fixed_tol, self.trueLR = InvETol, InvEfac, fixed_tol, trueLR
         self.tolmin, self.tolmax = tolmin, tolmax  # VUMPS_main.cpp:37-38
@@ -1809,13 +1816,53 @@ class VUMPS:
         HAR = GetHR(AR, hn)
         EHR0_next = self.EHR0[(nn + 1) % N]
         EHR, _ = InvertE_proj(AR, HAR, Lm, bd_eye({q: m.shape[0] for q, m in C[0].items()}), "r", gtol, self.gmres_maxit, EHR0_next)
-        EHL = EHLtmp
+        if self.mmax is not None and self._expand_now(nn, C[-1]):
+            # VUMPS_main.cpp:280-301: grow the bond between AL.back() and AR.back(), pad AR[N-2]
+            # with zeros to AL.back()'s sectors, and EHL on the grown bond
+            self.expand_ct[nn] = 0
+            mr_tot = sum(m.shape[1] for m in C[-1].values())
+            AL[-1], AR[-1], C[-1], _ = ExpandFromH(hn, self.I2K, AL[-1], AR[-1], C[-1],
+                                                   min(self.dmmax, self.mmax[nn] - mr_tot))
+            for s_ in range(d):
+                for ql, (c, Mal) in AL[-1][s_].items():
+                    if ql in AR[N - 2][s_]:
+                        qo, Mar = AR[N - 2][s_][ql]
+                        AR[N - 2][s_][ql] = (qo, np.hstack([Mar, np.zeros((Mar.shape[0], Mal.shape[1] - Mar.shape[1]))]))
+                    else:
+                        AR[N - 2][s_][ql] = (c, np.zeros(Mal.shape))
+            EHL = bd_add(ApplyOpTMLeftDiag(hn, mps_mul_mps(AL[N - 2], AL[-1])), ApplyTMLeft(AL[-1], EHL))
+            self.expansions += 1
+        else:
+            EHL = EHLtmp
         self.EHR1 = bd_add(ApplyTMRight(AR[-1], EHR), ApplyOpTMRightDiag(hn, mps_mul_mps(AR[-1], AR[0])))
         self.HL = ReducedOp(hn, AL[-1], d, "l")
         self.HR = ReducedOp(hn, AR[0], d, "r")
         self.EHL, self.EHR = EHL, EHR
 
+    def _expand_now(self, nn, Cr):
+        """VUMPS_main.cpp:272-277 and the else branch at :303-306."""
+        mr_tot = sum(m.shape[1] for m in Cr.values())
+        now = self.expand_ct[nn] >= self.expand_pause and self.exp_prec < self.expand_thresh and mr_tot < self.mmax[nn]
+        if now:
+            minlam = max(float(np.linalg.svd(M, compute_uv=False).min()) for M in Cr.values() if M.size)
+            now = minlam > self.lamthresh
+        if not now:
+            self.expand_ct[nn] += 1
+        return now
+
+    def keep_running(self, thresh=1e-14):
+        """run_IDMRG (VUMPS_main.cpp:331-340)."""
+        if float(np.max(self.F)) > thresh:
+            return True
+        if self.mmax is None:
+            return False
+        too_large = [any(float(np.linalg.svd(M, compute_uv=False).min()) > self.lamthresh for M in Cn.values() if M.size)
+                     for Cn in self.C]
+        too_small = [sum(M.shape[1] for M in self.C[n].values()) < self.mmax[n] for n in range(self.N)]
+        return any(too_large) and any(too_small)
+
     def sweep(self):
+        self.exp_prec = float(np.max(self.prec))  # VUMPS_main.cpp:168
         for nn in range(self.N):
             self.site_update(nn)
         for n in range(self.N):

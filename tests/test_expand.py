@@ -228,3 +228,35 @@ def test_relayout_pads_with_zeros(host_only):
             assert np.array_equal(M[:, :c0], AL[g][qi][1]) and not np.any(M[:, c0:])
         else:
             assert not np.any(M)
+
+
+def test_oracle_vumps_with_bond_expansion():
+    """The oracle's VUMPS loop with the reference's expansion branch (VUMPS_main.cpp:270-308):
+    from D = 7 per bond, mmax 24, dmmax 8, expansion after every second site update once the
+    previous sweep's error is below 1e-5.  The bonds grow to mmax, the state stays a consistent
+    mixed-canonical cell, and the energy approaches the Bethe-ansatz value far closer than at
+    the starting dimension."""
+    import math
+    d, I2K, h = models.build_model("xxz", J=1.0, Delta=-1.0)
+    dimvec = models.make_dims({(-2,): 2, (0,): 3, (2,): 2}, 2, I2K)
+    v = O.VUMPS(O.xxz_h(1.0, -1.0), 2, O.xxz_i2k(2, [0]), dimvec[0], dimvec=dimvec, seed=4, mmax=24, dmmax=8,
+                expand_pause=2)
+    e7 = None
+    for k in range(80):
+        E, F, prec = v.sweep()
+        if k == 24:
+            e7 = float(E.mean())  # converged at D = 7, before the first expansion
+            assert v.expansions == 0 and F.max() < 1e-4
+        if not v.keep_running(1e-9):
+            break
+    dims = [sum(M.shape[1] for M in C.values()) for C in v.C]
+    e0 = 0.25 - math.log(2)
+    assert v.expansions >= 3 and dims == [24, 24]
+    assert float(E.mean()) < e7 - 5e-4 and abs(float(E.mean()) - e0) < 5e-5
+    # AL(n) C(n) = C(n-1) AR(n) in the reference's arrangement (AR shifted back by one)
+    AR = O.shift(v.AR, 1)
+    for n in range(2):
+        Cr, Cl = v.C[n], v.C[(n - 1) % 2]
+        for s in range(d):
+            for q, (qo, al) in v.AL[n][s].items():
+                assert np.abs(al @ Cr[qo] - Cl[q] @ AR[n][s][q][1]).max() < 1e-5
