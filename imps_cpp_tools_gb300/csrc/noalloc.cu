@@ -16,9 +16,13 @@
 // but calls whose work overlaps on the GPU race on the scratch: issue them on one stream or
 // otherwise serialise them.  The host-side staging of the task tables is also shared, so
 // calls must not run concurrently from several host threads.
+// Task tables: built on the host for every call and copied to the device (a copy from
+// pageable host memory) only when they differ from the last ones copied to this device, so
+// a loop over one set of layouts copies them once.
 #include <cuda_runtime.h>
 
 #include <cstdio>
+#include <cstring>
 
 #include "../../include/imps_gb300.h"
 #include "imps_handles.h"
@@ -50,6 +54,38 @@ struct StageOut {
   int ntiles = 0, nterms = 0;
   bool overflow = false;
 };
+
+// the tables last copied to a device (one record: the device and the stage contents)
+static TableImage h_last;
+static int last_dev = -1;
+static StageOut last_stage[2];
+
+bool same_as_last(int dev, const StageOut* so) {
+  if (dev != last_dev) return false;
+  for (int s = 0; s < 2; ++s) {
+    if (so[s].ntiles != last_stage[s].ntiles || so[s].nterms != last_stage[s].nterms) return false;
+    if (memcmp(h_img.tiles[s], h_last.tiles[s], so[s].ntiles * sizeof(imps::Tile)) ||
+        memcmp(h_img.terms[s], h_last.terms[s], so[s].nterms * sizeof(imps::Term)))
+      return false;
+  }
+  return true;
+}
+
+void remember(int dev, const StageOut* so) {
+  for (int s = 0; s < 2; ++s) {
+    memcpy(h_last.tiles[s], h_img.tiles[s], so[s].ntiles * sizeof(imps::Tile));
+    memcpy(h_last.terms[s], h_img.terms[s], so[s].nterms * sizeof(imps::Term));
+    last_stage[s] = so[s];
+  }
+  last_dev = dev;
+}
+
+// every block of a BlockDiagMat layout must be square (the products below assume it)
+bool square_blocks(const imps::Layout& L) {
+  for (const imps::Block& b : L.blocks)
+    if (b.rows != b.cols) return false;
+  return true;
+}
 
 // emit an output block's tiles (all sharing the block's term range [t0, t1))
 void emit_tiles(StageOut& so, imps::Tile* tiles, int c_slot, int64_t c_off, int ld, int M, int N, int t0, int t1) {
@@ -89,6 +125,10 @@ extern "C" int imps_tm_apply_noalloc(const imps_layout* A, const imps_layout* in
   const imps::Layout& LA = A->L;
   const imps::Layout& LI = in->L;
   const imps::Layout& LO = out->L;
+  if (!square_blocks(LI) || !square_blocks(LO)) {
+    fprintf(stderr, "imps_tm_apply_noalloc: in and out must be BlockDiagMat layouts (square blocks)\n");
+    return IMPS_ERR_BAD_TABLE;
+  }
   if (LA.nelem > kNoAllocMaxScratch) {
     fprintf(stderr, "imps_tm_apply_noalloc: MPS tensor has %lld elements, the static scratch holds %lld\n",
             (long long)LA.nelem, (long long)kNoAllocMaxScratch);
@@ -154,15 +194,20 @@ extern "C" int imps_tm_apply_noalloc(const imps_layout* A, const imps_layout* in
   }
   cudaStream_t st = (cudaStream_t)stream;
   TableImage* dimg = (TableImage*)d_tables[dev];
-  // pageable-host copies return once the staging buffer has been consumed
-  for (int s = 0; s < 2; ++s) {
-    const StageOut& so = s == 0 ? s1 : s2;
-    if (so.ntiles && cudaMemcpyAsync(dimg->tiles[s], h_img.tiles[s], so.ntiles * sizeof(imps::Tile),
-                                     cudaMemcpyHostToDevice, st) != cudaSuccess)
-      return IMPS_ERR_CUDA;
-    if (so.nterms && cudaMemcpyAsync(dimg->terms[s], h_img.terms[s], so.nterms * sizeof(imps::Term),
-                                     cudaMemcpyHostToDevice, st) != cudaSuccess)
-      return IMPS_ERR_CUDA;
+  const StageOut stages[2] = {s1, s2};
+  if (!same_as_last(dev, stages)) {
+    last_dev = -1;  // a failed copy leaves the device tables unknown
+    // pageable-host copies return once the staging buffer has been consumed
+    for (int s = 0; s < 2; ++s) {
+      const StageOut& so = stages[s];
+      if (so.ntiles && cudaMemcpyAsync(dimg->tiles[s], h_img.tiles[s], so.ntiles * sizeof(imps::Tile),
+                                       cudaMemcpyHostToDevice, st) != cudaSuccess)
+        return IMPS_ERR_CUDA;
+      if (so.nterms && cudaMemcpyAsync(dimg->terms[s], h_img.terms[s], so.nterms * sizeof(imps::Term),
+                                       cudaMemcpyHostToDevice, st) != cudaSuccess)
+        return IMPS_ERR_CUDA;
+    }
+    remember(dev, stages);
   }
   imps_dslots sl{};
   sl.p[SX] = const_cast<double*>(dX);

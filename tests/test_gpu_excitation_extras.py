@@ -1,7 +1,6 @@
 """GPU tests of the excitation-side additions: MeasureExcitations (Excitations_helpers.hpp:754-808),
 the excitation ansatz with Z(2) charges (the exact transverse-field Ising dispersion) and the
-excitation driver's saveALRN file (Excitations_main.cpp:232-237).  Kept in a file that runs
-last, so that the established GPU suite runs in full before them."""
+excitation driver's saveALRN file (Excitations_main.cpp:232-237)."""
 import numpy as np
 import pytest
 

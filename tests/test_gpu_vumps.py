@@ -17,10 +17,26 @@ B0 = {(-4,): 3, (-2,): 8, (0,): 10, (2,): 8, (4,): 3}
 B1 = {(-5,): 1, (-3,): 5, (-1,): 10, (1,): 10, (3,): 5, (5,): 1}
 
 
-def _pair(cuda_ctx, model, dimvec, seed, fixed_tol=1e-12, **params):
+def warm_state(model, dimvec, seed, sweeps, fixed_tol=1e-12, **params):
+    """The oracle's state after `sweeps` sweeps from randMPS_LR(seed), in randMPS_LR's
+    arrangement (ALvec, ARvec, Cvec).  The first sweeps from a random state are chaotic: a
+    1e-13 change of the start moves the energies of sweep 1 by up to 1e-3 in the oracle alone
+    (tests/test_oracle.py::test_vumps_transient_is_chaotic); from a state a few sweeps on, the
+    same change stays at the rounding level, so parity is checked from there."""
+    import copy
     d, I2K, h = models.build_model(model, **params)
-    rng = np.random.default_rng(seed)
-    AL, AR, C = O.randMPS_LR(2, I2K, dimvec, rng)
+    AL, AR, C = O.randMPS_LR(2, I2K, dimvec, np.random.default_rng(seed))
+    if sweeps == 0:
+        return AL, AR, C
+    ora = O.VUMPS(h, d, I2K, dimvec[0], dimvec=dimvec, init=(AL, AR, C), fixed_tol=fixed_tol, seed=seed)
+    for _ in range(sweeps):
+        ora.sweep()
+    return copy.deepcopy(ora.AL), O.shift(copy.deepcopy(ora.AR), 1), copy.deepcopy(ora.C)
+
+
+def _pair(cuda_ctx, model, dimvec, seed, fixed_tol=1e-12, warm=0, **params):
+    d, I2K, h = models.build_model(model, **params)
+    AL, AR, C = warm_state(model, dimvec, seed, warm, fixed_tol, **params)
     ora = O.VUMPS(h, d, I2K, dimvec[0], dimvec=dimvec, init=(AL, AR, C), fixed_tol=fixed_tol, seed=seed)
     init = {"AL": [dev(O.mps_vec(a)) for a in AL], "AR": [dev(O.mps_vec(a)) for a in AR],
             "C": [dev(O.bd_vec(C[1])), dev(O.bd_vec(C[0]))]}  # C[b] = C on bond b
@@ -31,28 +47,31 @@ def _pair(cuda_ctx, model, dimvec, seed, fixed_tol=1e-12, **params):
 BH = {(-2,): 1, (-1,): 3, (0,): 4, (1,): 3, (2,): 1}
 
 
+@pytest.mark.parametrize("warm", [0, 5])
 @pytest.mark.parametrize("model,dimvec,params", [
     ("xxz", [B0, B1], {"J": 1.0, "Delta": -1.0}),
     ("fhub", None, {"t": 1.0, "U": 4.0}),
     ("bhub", [BH, BH], {"d": 4, "t": 0.3, "U": 2.0, "n": 2}),
 ])
-def test_vumps_sweeps_match_oracle(cuda_ctx, model, dimvec, params):
+def test_vumps_sweeps_match_oracle(cuda_ctx, model, dimvec, params, warm):
+    """The GPU driver against the oracle from the same state.  From the seeded random start
+    (warm = 0) sweep 0 agrees to 1e-9; the sweeps after it run the SVD polar step on a state far
+    from convergence, where the iteration itself amplifies rounding-level differences (in the
+    oracle alone a 1e-13 change of the start moves sweep 2 by up to 5e-6, see warm_state), so
+    they are held to 1e-5.  From the oracle's state after 5 sweeps (warm = 5) every sweep
+    agrees to 1e-9."""
     if dimvec is None:
         dims0 = {(0, 0): 4, (1, 1): 2, (-1, -1): 2, (1, -1): 2, (-1, 1): 2, (2, 0): 1, (0, 2): 1, (-2, 0): 1,
                  (0, -2): 1}
         dimvec = models.make_dims(dims0, 2, models.fhub_i2k())
-    ora, gpu = _pair(cuda_ctx, model, dimvec, seed=7, **params)
-    # Sweep 0 must agree to 1e-9.  Later sweeps of this far-from-converged start run the SVD
-    # polar step (prec > 5e-7, VUMPS_main.cpp:211-220), whose polar factor amplifies the
-    # 1e-12-level differences between ARPACK and the device Lanczos (different Krylov
-    # sequences, same tolerance); there the trajectories agree to ~1e-7.
+    ora, gpu = _pair(cuda_ctx, model, dimvec, seed=7, warm=warm, **params)
     for sweep in range(3):
         Eo, Fo, po = ora.sweep()
         Eg, Fg, pg = gpu.sweep()
-        tol = 1e-9 if sweep == 0 else 1e-5
+        tol = 1e-9 if (sweep == 0 or warm) else 1e-5
         assert np.abs(Eg - Eo).max() < tol, (sweep, Eg, Eo)
-        assert np.allclose(Fg, Fo, rtol=1e-3 if sweep else 1e-5, atol=1e-12), (sweep, Fg, Fo)
-        assert np.allclose(pg, po, rtol=1e-3 if sweep else 1e-4, atol=1e-12), (sweep, pg, po)
+        assert np.allclose(Fg, Fo, rtol=1e-3 if (sweep or warm) else 1e-5, atol=1e-12), (sweep, Fg, Fo)
+        assert np.allclose(pg, po, rtol=1e-3 if (sweep or warm) else 1e-4, atol=1e-12), (sweep, pg, po)
 
 
 def test_vumps_gpu_bethe_ansatz(cuda_ctx):
@@ -108,20 +127,17 @@ def test_vumps_ground_state_energy_matches_oracle(cuda_ctx, oracle_ground_state,
 ])
 def test_zn_vumps_sweeps_match_oracle(cuda_ctx, model, params, dims, periods):
     """Z(N) charges (quantum Ising Z(2), Potts Z(3)): the GPU driver against the oracle run with
-    the same modular charge arithmetic, from the same initial state."""
+    the same modular charge arithmetic, from the same state: the oracle's after 5 sweeps from
+    the seeded random start (the sweeps before are chaotic, see warm_state).  Every sweep
+    agrees to 1e-9 in the energies."""
     dimvec = models.make_dims(dims, 2, models.build_model(model, **params)[1])
     with O.charge_group(periods):
-        ora, gpu = _pair(cuda_ctx, model, dimvec, seed=7, **params)
+        ora, gpu = _pair(cuda_ctx, model, dimvec, seed=7, warm=5, **params)
         for sweep in range(3):
             Eo, Fo, po = ora.sweep()
             Eg, Fg, pg = gpu.sweep()
-            # The shared initial state comes from the oracle's randMPS_LR, whose fixed-point solve
-            # starts ARPACK from scipy's process-wide random state, so it moves at the 1e-14
-            # level with test order.  From it, the nearly degenerate Z(2) effective Hamiltonians
-            # of the first sweeps (ARPACK against the device Lanczos, both at tol 1e-12) agree to
-            # 3e-9 .. 8e-7; a wrong sector shows at 1e-2.  The converged energy is pinned to the
-            # exact solution by test_quantum_ising_exact_energy (GPU) and tests/test_oracle.py.
-            assert np.abs(Eg - Eo).max() < 1e-5, (sweep, Eg, Eo)
+            assert np.abs(Eg - Eo).max() < 1e-9, (sweep, Eg, Eo)
+            assert np.allclose(Fg, Fo, rtol=1e-3, atol=1e-10), (sweep, Fg, Fo)
 
 
 def test_quantum_ising_exact_energy(cuda_ctx):

@@ -205,5 +205,28 @@ def test_cpp_host_program_builds(tmp_path):
 
 def test_cpp_program_check_builds(tmp_path):
     """The C++ grouped-GEMM program builder (imps_cpp::program) compiles and links;
-    tests/test_zzz_gpu_cpp_program.py runs it."""
+    tests/test_gpu_cpp_program.py runs it."""
     assert _build_cpp_host(tmp_path, "cpp_program_check").exists()
+
+
+def test_noalloc_rejects_bad_layouts_before_device_access():
+    """imps_tm_apply_noalloc validates its layouts before it touches a device: an `out` (or
+    `in`) layout with a non-square block is IMPS_ERR_BAD_TABLE, an MPS tensor beyond the static
+    scratch is IMPS_ERR_TOO_LARGE.  The data pointers are dummies that are never read (no GPU
+    here)."""
+    import ctypes as C
+    from imps_cpp_tools_gb300 import _native as N
+    I2K = [(1,), (-1,)]
+    b0 = {(-1,): 2, (1,): 2}
+    b1 = {(0,): 3, (2,): 1, (-2,): 1}
+    la = B.Layout.mps(I2K, b0, b1)
+    lin = B.Layout.blockdiag(b0)
+    bad_out = B.Layout([(0, (-2,), (-2,), 1, 1), (0, (0,), (0,), 3, 2), (0, (2,), (2,), 1, 1)], 1)
+    dummy = C.c_void_p(16)
+    lib = N.load()
+    assert lib.imps_tm_apply_noalloc(la.handle, lin.handle, bad_out.handle, 0, dummy, dummy, dummy, None) == -2
+    assert lib.imps_tm_apply_noalloc(la.handle, bad_out.handle, lin.handle, 1, dummy, dummy, dummy, None) == -2
+    big = {(q,): 400 for q in range(-3, 4)}  # 2 * 7 * 400^2 > 1,048,576 elements
+    lbig = B.Layout.mps(I2K, big, {(q + 1,): m for (q,), m in big.items()})
+    lb_in, lb_out = B.Layout.blockdiag(big), B.Layout.blockdiag({(q + 1,): m for (q,), m in big.items()})
+    assert lib.imps_tm_apply_noalloc(lbig.handle, lb_in.handle, lb_out.handle, 0, dummy, dummy, dummy, None) == -9

@@ -240,3 +240,35 @@ def test_zn_models():
                     break
         pt = -2 * hq - 2 / (6 * hq) - 1 / (18 * hq * hq)
         assert F.max() < 1e-10 and abs(E.mean() - pt) < tol, (hq, E, pt)
+
+
+def _zn_run(model, params, dims, periods, warm, pert, sweeps):
+    """The oracle's VUMPS from randMPS_LR(7) after `warm` sweeps, C of bond 1 scaled by
+    (1 + pert), then `sweeps` sweeps; returns the energies."""
+    import copy
+    d, I2K, h = models.build_model(model, **params)
+    with O.charge_group(periods):
+        dimvec = models.make_dims(dims, 2, I2K)
+        AL, AR, C = O.randMPS_LR(2, I2K, dimvec, np.random.default_rng(7))
+        if warm:
+            o = O.VUMPS(h, d, I2K, dimvec[0], dimvec=dimvec, init=(AL, AR, C), fixed_tol=1e-12, seed=7)
+            for _ in range(warm):
+                o.sweep()
+            AL, AR, C = copy.deepcopy(o.AL), O.shift(copy.deepcopy(o.AR), 1), copy.deepcopy(o.C)
+        C[0] = {q: M * (1.0 + pert) for q, M in C[0].items()}
+        o = O.VUMPS(h, d, I2K, dimvec[0], dimvec=dimvec, init=(AL, AR, C), fixed_tol=1e-12, seed=7)
+        return np.array([o.sweep()[0] for _ in range(sweeps)])
+
+
+def test_vumps_transient_is_chaotic():
+    """Why the sweep-parity tests start from a few sweeps on: in the oracle alone, a relative
+    change of 1e-13 of the random start state (transverse-field Ising, Z(2) sectors 6 + 6,
+    J = 1, h = 0.7) moves the energies of sweep 1 by more than 1e-5 (measured 3e-4); from the
+    state after 5 sweeps the same change stays below 1e-11 (measured 4e-13).  So two correct
+    eigensolvers at tol 1e-12 (ARPACK, the device Lanczos) cannot agree on the first sweeps
+    from a random state, and agree to the rounding level once the iteration contracts."""
+    args = ("qim", {"J": 1.0, "h": 0.7}, {(0,): 6, (1,): 6}, (2,))
+    a, b = _zn_run(*args, 0, 0.0, 2), _zn_run(*args, 0, 1e-13, 2)
+    assert np.abs(a[1] - b[1]).max() > 1e-5
+    a, b = _zn_run(*args, 5, 0.0, 3), _zn_run(*args, 5, 1e-13, 3)
+    assert np.abs(a - b).max() < 1e-11

@@ -3,8 +3,9 @@
 It exists for callers that cannot call cudaMalloc when they apply the transfer matrix (GPU
 memory reserved up front by another allocator, or a latency-critical loop that must not pay
 cudaMalloc's implicit synchronisation).  Its result must equal the regular plan-based entry
-point (imps_plan_tm + imps_tm_apply) to the FP64 tolerance of the other parity tests, on two
-calls in a row (the second call reuses the static scratch left behind by the first).
+point (imps_plan_tm + imps_tm_apply) and the oracle's ApplyTMLeft / ApplyTMRight to the FP64
+tolerance of the other parity tests, on two calls in a row (the second call reuses the static
+scratch and the task tables left behind by the first).
 This file is collected last on purpose."""
 import ctypes as C
 
@@ -24,6 +25,10 @@ RTOL = 1e-12
 def _dev(x):
     import torch
     return torch.tensor(np.ascontiguousarray(x), dtype=torch.float64, device="cuda")
+
+
+def _bd_dims(lay):
+    return {qi: np.zeros((r, c)) for (_, qi, _, r, c) in lay.blocks}
 
 
 def _relerr(a, b):
@@ -63,6 +68,10 @@ def test_noalloc_matches_plan_path(cuda_ctx, model, dims0, direction):
         y, r = Y.cpu().numpy(), ref.cpu().numpy()
         assert np.isfinite(y).all()
         assert _relerr(y, r) < RTOL, (call, _relerr(y, r))
+        # and the oracle's ApplyTMLeft / ApplyTMRight (TMBlockFunctions.hpp:33-84, 155-205)
+        xin = O.bd_from_vec(X.cpu().numpy(), O.bd_sizes(_bd_dims(lin)))
+        want = O.bd_vec((O.ApplyTMLeft if direction == 0 else O.ApplyTMRight)(A, xin))
+        assert _relerr(y, want) < RTOL, (call, _relerr(y, want))
 
 
 def test_noalloc_rejects_oversized(cuda_ctx):
