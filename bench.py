@@ -2,15 +2,18 @@
 
 Workload (default): XXZ spin-1/2 chain, J=1, Delta=1 (antiferromagnet; --Delta=-1 in the
 reference's sign convention), two-site unit cell, U(1) Sz sectors q=-10..10 with dims
-~exp(-q^2/18) summing to D=512, seeded random initial state, the reference's eigensolver
-tolerance schedule tol = min(max(prec/100, tolmin), tolmax) (VUMPS_main.cpp:37-38, 177) with
-tolmin = GMRES tolerance = 1e-12, bond expansion off.  A step is one VUMPS sweep (both site
-updates of VUMPS_main.cpp:165-354); the default 3 warm-up + 47 timed steps are the 50 sweeps
-of the workload.  The headline value is the FP64 path (--precision fp64, the default); the
-split-BF16 (tcgen05) path runs the same sweeps from the same initial state and is reported
-beside it, with the energy difference of the two after the last sweep.  Under torchrun every
-rank runs its own replica of the sweeps (the path does not shard); the step time is the maximum
-over ranks and the value N / that time.
+~exp(-q^2/18) summing to D=512, bond expansion off.  The timed sweeps start from a warmed
+state (the committed tests/golden/warm_<workload>.npz: 20 sweeps of the reference's tolerance
+schedule from seed 1; workloads without one warm up on the device the same way) and run at the
+fixed eigensolver tolerance 1e-12 of the configuration and GMRES tolerance 1e-8 (TIMED_TOLS).
+A step is one VUMPS sweep (both site updates of VUMPS_main.cpp:165-354); W warm-up sweeps are
+run before the K timed ones.  The headline value is the FP64 path (--precision fp64, the
+default); the split-BF16 (tcgen05) path runs the same sweeps from the same state and is reported
+beside it, with the energy difference of the two after the last sweep.  Rank 0 also runs one
+sweep of the CPU restatement from the same start state (cpu_baseline) and reports its energies
+beside the GPU's first sweep (parity_vs_oracle).  Under torchrun every rank runs its own replica
+of the sweeps (the path does not shard); the step time is the maximum over ranks and the value
+N / that time.
 
 --mode hac times H_AC applies only (ApplyHAvec; a step = 20 applies).
 --mode excitations converges the XXZ D=256 ground state and times the 4 lowest excitation
@@ -21,8 +24,9 @@ D=1024 starts against the oracle on the same state.
 cycles; FP64 at an unreachable tolerance, split-BF16 at its 2e-7 floor) on the synthetic H_AC,
 next to the same number of bare applies: the difference is the per-iteration
 orthogonalisation, convergence-check and launch cost.
-The reference arm (--impl reference) times the CPU restatement of the same sweeps (the
-reference itself cannot be built: armadillo/ARPACK are not available).
+The reference arm (--impl reference) times site updates of the CPU restatement of the same
+sweeps from the same start state (the reference itself cannot be built: armadillo/ARPACK are not
+available).
 """
 from __future__ import annotations
 
@@ -42,17 +46,23 @@ sys.path.insert(0, ROOT)
 METRIC = "VUMPS sweeps/s + H_AC TFLOP/s, mixed vs FP64 on one GB300 at |dE|<=1e-9"
 APPLIES_PER_STEP = 20
 L2_FLUSH_BYTES = 512 << 20
-TOLMIN = 1e-12  # floor of the eigensolver tolerance schedule and the GMRES tolerance
 # DRAM bytes (read + write) of one H_AC apply from one ncu capture of `bench.py --mode hac`
 # (profiles/tc_gemm_hac_xxz_d512.md: tc_gemm 5.26 MB + pack 0.40 MB;
 # profiles/grouped_gemm_f64_hac_xxz_d512.md: 2.38 MB), cold caches
 NCU_TRAFFIC_BYTES = {"bf16x6": 5.66e6, "fp64": 2.38e6}
-_SCHEDULE = ("2-site VUMPS sweep, tolerance schedule min(max(prec/100, 1e-12), 1e-6) (VUMPS_main.cpp:177), "
-             "GMRES tol 1e-12, expansion off")
+# tolerances of the timed sweeps: the eigensolver tolerance of the configuration (1e-12); GMRES
+# 1e-8, because the environment systems of these states do not reach 1e-12 in floating point:
+# measured at XXZ D=512 from the warmed state, the relative residual of the left-environment
+# solves floors at 2e-11 (site 0) and 1e-9 (site 1, warm start of norm 3e5) after ~200
+# iterations, where the reference's unrestarted GMRES then runs on towards maxit = 24,368
+TIMED_TOLS = {"eig": 1e-12, "gmres": 1e-8}
+_TIMED = ("2-site VUMPS sweep from a warmed state (20/30 sweeps of the tolerance schedule "
+          "min(max(prec/100, 1e-12), 1e-6), VUMPS_main.cpp:177, from seed 1), then fixed eigensolver tol 1e-12 and "
+          "GMRES tol 1e-8, expansion off")
 WORKLOAD_DESCS = {
-    "xxz_d512": "XXZ D=512 (21 U(1) sectors, dims ~exp(-q^2/18)), " + _SCHEDULE,
+    "xxz_d512": "XXZ D=512 (21 U(1) sectors, dims ~exp(-q^2/18)), " + _TIMED,
     "hubbard_d1024": "Fermi-Hubbard t=1, U=4, half filling, D=1024 (60 U(1)xU(1) (N, Sz) sectors, dims "
-                     "~exp(-(dN^2+4Sz^2)/8)), " + _SCHEDULE,
+                     "~exp(-(dN^2+4Sz^2)/8)), " + _TIMED,
 }
 _WORKLOAD = ["xxz_d512"]  # the VUMPS workload of this run (--workload)
 
@@ -146,106 +156,100 @@ def _fp64_peak_tflops(torch):
     return 2 * n ** 3 / best / 1e12
 
 
-def _xxz_params():
-    """(model, bond dims, couplings) of the VUMPS workload of this run (default XXZ D=512)."""
-    from imps_cpp_tools_gb300 import configs
-    model, fn, params = configs.WORKLOADS[_WORKLOAD[0]]
-    return model, fn(), params
-
-
 def _workload_desc():
-    return WORKLOAD_DESCS.get(_WORKLOAD[0], _WORKLOAD[0] + ", " + _SCHEDULE)
+    return WORKLOAD_DESCS.get(_WORKLOAD[0], _WORKLOAD[0] + ", " + _TIMED)
 
 
 # ------------------------------------------------------------------------------------------------
 # CPU restatement (oracle port): the reference arm and the cpu_baseline leg
 # ------------------------------------------------------------------------------------------------
 
-# Per-sweep operator applications of the FP64 GPU path on this workload (mean over the 47 timed
-# sweeps of the default run, seed 1): H_AC applies (Lanczos + gradient), H_C applies (two
-# Lanczos solves per site update), unit-cell transfer-matrix applies (GMRES iterations of the
-# environment and fixed-point solves).  The reference arm weights its CPU operator times with
-# these; the GPU arm uses the counts of its own timed sweeps.
-REF_COUNTS_BY_WORKLOAD = {"xxz_d512": {"hac": 281.6, "hc": 448.4, "tm": 293.0},
-                          # --workload hubbard_d1024 --steps 37 --warmup 3
-                          "hubbard_d1024": {"hac": 570.5, "hc": 1029.8, "tm": 296.3}}
-
-
-def cpu_op_times(budget_per_op=2.0, seed=1):
-    """CPU time of one H_AC apply (ApplyHAvec), one H_C apply (ApplyHCvec) and one unit-cell
-    transfer-matrix apply (ApplyTMLeftUC) of the numpy restatement on operands of the VUMPS
-    workload's sector structure (values seeded random: the cost does not depend on them), all
-    host threads.  Each is repeated until budget_per_op seconds (at least twice)."""
-    from imps_cpp_tools_gb300 import models
+def _oracle_state(name, state):
+    """(ALvec, ARvec, Cvec) in the arrangement of the oracle's randMPS_LR (Cvec[n] = the C right
+    of site n) from a flat host state (workload.load_warm_state / VumpsGPU.host_state)."""
+    from imps_cpp_tools_gb300 import blocks as B
+    from imps_cpp_tools_gb300.workload import bond_layouts
     from oracle import imps_oracle as O
-    model, dims0, params = _xxz_params()
-    d, I2K, h = models.build_model(model, **params)
-    hnnz = O.sparse_nnz(h)
-    b0, b1 = models.make_dims(dims0, 2, I2K)
-    rng = np.random.default_rng(seed)
-    D = sum(b0.values())
+    model, d, I2K, h, dimvec = bond_layouts(name)
 
-    def mps(dl, dr):
-        A = O.mps_rand(I2K, dl, dr, rng)
-        return [{q: (qo, M / np.sqrt(D)) for q, (qo, M) in bm.items()} for bm in A]
-
-    def sym(dims):
-        X = {}
-        for q in sorted(dims):
-            M = rng.standard_normal((dims[q], dims[q]))
-            X[q] = 0.5 * (M + M.T)
-        return X
-
-    AL1, AR1 = mps(b1, b0), mps(b1, b0)  # sites mapping bond 1 -> bond 0
-    AL0, AR0 = mps(b0, b1), mps(b0, b1)  # sites mapping bond 0 -> bond 1
-    HL, HR = O.ReducedOp(hnnz, AL1, d, "l"), O.ReducedOp(hnnz, AR1, d, "r")
-    ac = O.mps_vec(AR0)
-    ac_sizes = O.mps_sizes(AR0)
-    EHL0, EHR1, EHR0 = sym(b0), sym(b1), sym(b0)
-    c = O.bd_vec(sym(b0))
-    c_sizes = O.bd_sizes(sym(b0))
-    X = sym(b0)
-    ops = {"hac": lambda: O.ApplyHAvec(ac, ac_sizes, EHL0, EHR1, HL, HR),
-           "hc": lambda: O.ApplyHCvec(c, c_sizes, EHL0, EHR0, hnnz, d, AL1, AR0),
-           "tm": lambda: O.ApplyTMLeftUC([AL0, AL1], X)}
-    out, reps = {}, {}
-    for k, f in ops.items():
-        f()  # warm-up
-        n, t0 = 0, time.perf_counter()
-        while n < 2 or time.perf_counter() - t0 < budget_per_op:
-            f()
-            n += 1
-        out[k] = (time.perf_counter() - t0) / n
-        reps[k] = n
-    return out, reps
+    def sizes(n):
+        lay = B.Layout.mps(I2K, dimvec[n], dimvec[1 - n])
+        return [[(qi, qo, r, c) for (g, qi, qo, r, c) in lay.blocks if g == s] for s in range(d)]
+    AL = [O.mps_from_vec(state["AL"][n], sizes(n)) for n in range(2)]
+    AR = [O.mps_from_vec(state["AR"][n], sizes(n)) for n in range(2)]
+    C = [O.bd_from_vec(state["C"][1], sorted(dimvec[1].items())),
+         O.bd_from_vec(state["C"][0], sorted(dimvec[0].items()))]
+    return AL, AR, C
 
 
-def cpu_sweep_model(counts, times):
-    """CPU seconds per sweep for the given per-sweep operator counts: operator applies only
-    (Krylov orthogonalisation, decompositions and small solves are left out, so this is a
-    lower bound on the CPU sweep time)."""
-    return sum(counts[k] * times[k] for k in ("hac", "hc", "tm"))
+def _oracle_vumps(name, state):
+    """The oracle's VUMPS (VUMPS_main.cpp restated: ARPACK eigs_rs at ncv 20, the reference's
+    unrestarted MGS GMRES, per-sector LAPACK decompositions on the host) at the timed
+    tolerances, started from `state`; its constructor solves the initial environments."""
+    from imps_cpp_tools_gb300 import models
+    from imps_cpp_tools_gb300.workload import bond_layouts
+    from oracle import imps_oracle as O
+    model, d, I2K, h, dimvec = bond_layouts(name)
+    return O.VUMPS(h, d, I2K, dimvec[0], dimvec=dimvec, init=_oracle_state(name, state),
+                   fixed_tol=TIMED_TOLS["eig"], InvETol=TIMED_TOLS["gmres"])
+
+
+def cpu_site_updates(name, state, warmup, steps):
+    """Time `steps` site updates (VUMPS_main.cpp:171-313, one half of a sweep each) of the
+    oracle's VUMPS after `warmup` untimed ones, from `state`, on the host's cores (numpy's
+    BLAS threads).  Returns (seconds per site update, the energies after the first full sweep
+    or None, threads)."""
+    ora = _oracle_vumps(name, state)
+    times, E = [], None
+    for i in range(warmup + steps):
+        t0 = time.perf_counter()
+        ora.site_update(i % 2)
+        dt = time.perf_counter() - t0
+        if i >= warmup:
+            times.append(dt)
+        if i == 1:
+            E = _oracle_sweep_energy(ora)
+    return times, E, os.cpu_count()
+
+
+def _oracle_sweep_energy(ora):
+    """The energies the oracle's sweep() reports after its two site updates."""
+    from oracle import imps_oracle as O
+    if not hasattr(ora, "C"):
+        return None
+    for n in range(ora.N):
+        ora.L[(n - 1) % ora.N] = O.bd_mul(O.bd_t(ora.C[n]), ora.C[n])
+    return O.energy_right(ora.hnnz, ora.AR, ora.L)
 
 
 def run_reference(args):
+    """--impl reference: the CPU restatement of the reference's VUMPS (the reference itself cannot
+    be built: armadillo and ARPACK are absent) timed on the host's cores.  A step is one site
+    update (half a sweep) from the committed warmed state, at the same fixed tolerances as the
+    GPU arm; sweeps/s = 1 / (2 x mean site-update time)."""
     ws, rank, _ = _dist()
     if rank != 0:
         return
-    per = []
-    for i in range(args.warmup + args.steps):
-        times, reps = cpu_op_times(budget_per_op=0.5)
-        if i >= args.warmup:
-            per.append(cpu_sweep_model(REF_COUNTS_BY_WORKLOAD[_WORKLOAD[0]], times))
-    value = 1.0 / float(np.mean(per))
-    cores = os.cpu_count()
-    sample = ("per step: H_AC, H_C and unit-cell TM applies of the numpy restatement of the reference's "
-              f"operators on {_WORKLOAD[0]} operands (>= 2 applies each, 0.5 s per operator), weighted by the "
-              f"per-sweep operator counts of the FP64 path {REF_COUNTS_BY_WORKLOAD[_WORKLOAD[0]]}; orthogonalisation and "
-              "decompositions excluded (lower bound on the CPU sweep time); all host threads")
+    from imps_cpp_tools_gb300 import workload as W
+    state = W.load_warm_state(_WORKLOAD[0])
+    if state is None:
+        print(json.dumps({"impl": "reference", "unavailable": f"no committed warmed start state for {_WORKLOAD[0]} "
+                          "(tests/golden/warm_<workload>.npz); the CPU restatement from a random start does not "
+                          "finish its first sweeps in minutes"}), flush=True)
+        return
+    t0 = time.perf_counter()
+    times, _, cores = cpu_site_updates(_WORKLOAD[0], state, args.warmup, args.steps)
+    t_site = float(np.mean(times))
+    value = 1.0 / (2.0 * t_site)
+    sample = (f"{len(times)} timed site updates (after {args.warmup} untimed) of the numpy/ARPACK restatement of "
+              f"VUMPS_main.cpp on {_WORKLOAD[0]} from the committed warmed state, {cores} host threads; "
+              f"sweeps/s = 1 / (2 x mean site update); wall {time.perf_counter() - t0:.1f} s incl. setup")
     line = {"impl": "reference", "metric": METRIC, "value": value, "unit": "sweeps/s", "n_gpus": ws,
-            "steps": len(per), "warmup": args.warmup, "ms_per_step": 1e3 * float(np.mean(per)),
+            "steps": len(times), "warmup": args.warmup, "ms_per_step": 1e3 * t_site,
             "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic",
-            "config": {"workload": _workload_desc(), "implementation": "numpy restatement of the reference's operators"},
+            "config": {"workload": _workload_desc(), "implementation": "CPU restatement of the reference (oracle)",
+                       "step": "one site update (half a sweep)",
+                       "ms_per_site_update_median": 1e3 * float(np.median(times))},
             "cpu_baseline": {"value": value, "unit": "sweeps/s", "cores": cores, "kind": "port", "sample": sample},
             "e2e": {"value": value, "unit": "sweeps/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
     print(json.dumps(line), flush=True)
@@ -280,24 +284,44 @@ def _time_hac_applies(torch, plan, n, stream, reps=APPLIES_PER_STEP):
     return float(np.median(times))
 
 
-def _new_vumps(precision):
-    from imps_cpp_tools_gb300.vumps import VumpsGPU
-    model, dims0, params = _xxz_params()
-    return VumpsGPU(_CTX[0], model, dims0=dims0, seed=1, tolmin=TOLMIN, InvETol=TOLMIN, precision=precision,
-                    verbose=True, **params)
-
-
 _CTX = [None]
 
 
-def _run_vumps(torch, precision, steps, warmup, stream, clocks=None, e2e=False):
-    """W warm-up sweeps, then K device-timed sweeps (CUDA events on the launching stream).
-    With e2e, every timed step also uploads the MPS state from pinned host memory before the
-    sweep and reads the state and the energies back after it (wall clock around all three)."""
+def _start_state():
+    """The start state of the timed sweeps: the committed warmed state of the workload if there
+    is one, else the same warm-up computed on the device (seed 1, WARM_SWEEPS sweeps of the
+    tolerance schedule).  Returns (host state, description)."""
+    from imps_cpp_tools_gb300 import workload as W
+    st = W.load_warm_state(_WORKLOAD[0])
+    if st is not None:
+        return st, f"tests/golden/warm_{_WORKLOAD[0]}.npz ({W.WARM_SWEEPS[_WORKLOAD[0]]} schedule sweeps from seed 1)"
+    st, _, _ = W.warm_on_device(_CTX[0], _WORKLOAD[0])
+    return st, f"{W.WARM_SWEEPS[_WORKLOAD[0]]} schedule sweeps from seed 1 on the device"
+
+
+def _new_vumps(precision, state):
+    import torch
+    from imps_cpp_tools_gb300 import configs
+    from imps_cpp_tools_gb300.vumps import VumpsGPU
+    model, fn, params = configs.WORKLOADS[_WORKLOAD[0]]
+    init = {k: [torch.from_numpy(np.ascontiguousarray(a)).to("cuda") for a in state[k]] for k in ("AL", "AR", "C")}
+    # eig_margin 1: the device Lanczos stops at the configured tolerance itself, as ARPACK does
+    return VumpsGPU(_CTX[0], model, dims0=fn(), init_state=init, fixed_tol=TIMED_TOLS["eig"],
+                    InvETol=TIMED_TOLS["gmres"], eig_margin=1.0, precision=precision, verbose=True, **params)
+
+
+def _run_vumps(torch, precision, state, steps, warmup, stream, clocks=None, e2e=False):
+    """W warm-up sweeps, then K device-timed sweeps (CUDA events on the launching stream), from
+    `state`.  With e2e, every timed step also uploads the MPS state from pinned host memory
+    before the sweep and reads the state and the energies back after it (wall clock around all
+    three)."""
     from imps_cpp_tools_gb300 import _native as N
-    v = _new_vumps(precision)
-    for _ in range(warmup):
-        v.sweep()
+    v = _new_vumps(precision, state)
+    E_first = None
+    for i in range(warmup):
+        E, _, _ = v.sweep()
+        if i == 0:
+            E_first = E.copy()
     torch.cuda.synchronize()
     lib = N.load()
     host = {k: [t.detach().cpu().pin_memory() for t in getattr(v, k)] for k in ("AL", "AR", "C")} if e2e else None
@@ -331,7 +355,7 @@ def _run_vumps(torch, precision, steps, warmup, stream, clocks=None, e2e=False):
     launches = lib.imps_launch_count() - l0
     counts = {k: v.stats[k] - s0.get(k, 0) for k in v.stats}
     return {"v": v, "times": times, "walls": walls, "E": E, "F": F, "prec": prec, "launches": launches,
-            "counts": counts, "clocks": clk, "h2d": h2d}
+            "counts": counts, "clocks": clk, "h2d": h2d, "E_first": E_first}
 
 
 def run_vumps(args):
@@ -347,14 +371,15 @@ def run_vumps(args):
     _CTX[0] = ctx
     stream = torch.cuda.current_stream()
     ctx.set_stream(stream)
+    state, state_src = _start_state()
 
     # the headline precision (timed with clocks and end to end) and the other one for comparison,
-    # from the same seeded initial state
+    # from the same start state
     other = "bf16x6" if args.precision == "fp64" else "fp64"
-    roth = _run_vumps(torch, other, args.steps, args.warmup, stream)
+    roth = _run_vumps(torch, other, state, args.steps, args.warmup, stream)
     if ws > 1:
         dist.barrier()
-    rmx = _run_vumps(torch, args.precision, args.steps, args.warmup, stream, ClockSampler(local), e2e=True)
+    rmx = _run_vumps(torch, args.precision, state, args.steps, args.warmup, stream, ClockSampler(local), e2e=True)
     r64, rsp = (rmx, roth) if args.precision == "fp64" else (roth, rmx)
     t_step = float(np.mean(rmx["times"]))
     t_wall = float(np.mean(rmx["walls"]))
@@ -375,6 +400,8 @@ def run_vumps(args):
     fp64_peak = _fp64_peak_tflops(torch)
     h_ac = {"fp64_tflops": flops / t_hac64 / 1e12, "mixed_tflops": flops / t_hacmx / 1e12,
             "flops_per_apply": flops, "fp64_us": t_hac64 * 1e6, "mixed_us": t_hacmx * 1e6}
+    fp64_src = ("dense FP64 matmul (torch, cuBLAS DGEMM 4096^3) measured in this run: GB300 has no FP64 tensor "
+                "rate, the FP64 pipe bounds this kernel (not in MEASURED_PEAKS.json)")
     if args.precision == "bf16x6":
         achieved = 6 * flops / t_hacmx / 1e12
         roof = {"bound": "tensor", "achieved": achieved, "peak": bf16_peak, "unit": "TFLOP/s",
@@ -383,17 +410,11 @@ def run_vumps(args):
                 "kernel": "tc_gemm_kernel + pack_kernel (H_AC apply, 6 split-BF16 products per FP64 flop)",
                 "achieved_fp64_equivalent_tflops": flops / t_hacmx / 1e12,
                 "fp64_engine": {"achieved": flops / t_hac64 / 1e12, "peak": fp64_peak,
-                                "frac": flops / t_hac64 / 1e12 / fp64_peak,
-                                "peak_source": "dense FP64 matmul measured in this run"}}
+                                "frac": flops / t_hac64 / 1e12 / fp64_peak, "peak_source": fp64_src}}
     else:
-        # the FP64 grouped GEMM dominates the timed sweeps (every solve below the split-BF16
-        # floor runs on it); GB300 has no FP64 tensor rate, so its roof is the FP64 pipe, taken
-        # as the dense FP64 matmul rate measured in this run
         achieved = flops / t_hac64 / 1e12
-        roof = {"bound": "tensor", "achieved": achieved, "peak": fp64_peak, "unit": "TFLOP/s",
-                "frac": achieved / fp64_peak, "traffic": NCU_TRAFFIC_BYTES["fp64"],
-                "peak_source": "dense FP64 matmul (torch, cuBLAS DGEMM 4096^3) measured in this run; the FP64 "
-                               "pipe, not a tensor pipe, bounds this kernel on GB300",
+        roof = {"bound": "fp64_pipe", "achieved": achieved, "peak": fp64_peak, "unit": "TFLOP/s",
+                "frac": achieved / fp64_peak, "traffic": NCU_TRAFFIC_BYTES["fp64"], "peak_source": fp64_src,
                 "kernel": "grouped_gemm_f64 (H_AC apply; the dominant kernel of the timed sweeps)",
                 "split_bf16_engine": {"achieved_fp64_equivalent_tflops": flops / t_hacmx / 1e12,
                                       "tensor_tflops": 6 * flops / t_hacmx / 1e12, "tensor_peak": bf16_peak,
@@ -404,35 +425,32 @@ def run_vumps(args):
            "path": "VumpsGPU.sweep (public driver) with the MPS state uploaded from pinned host memory before "
                    "and read back after every timed sweep"}
 
-    cpu = None
+    cpu, parity = None, None
     if rank == 0 and not args.no_cpu:
-        K = max(args.steps, 1)
-        counts = {"hac": rmx["counts"]["hac_applies"] / K, "hc": rmx["counts"]["hc_applies"] / K,
-                  "tm": rmx["counts"]["gmres_iters"] / K}
-        times, reps = cpu_op_times()
-        t_cpu = cpu_sweep_model(counts, times)
-        cpu = {"value": 1.0 / t_cpu, "unit": "sweeps/s", "cores": os.cpu_count(), "kind": "port",
-               "sample": f"H_AC, H_C and unit-cell TM applies of the numpy restatement on {_WORKLOAD[0]} operands "
-                         f"({reps} applies), weighted by the per-sweep operator counts of the timed GPU sweeps "
-                         f"{ {k: round(v, 1) for k, v in counts.items()} }; orthogonalisation and decompositions "
-                         "excluded (lower bound on the CPU sweep time); all host threads",
-               "ms_per_apply": {k: 1e3 * v for k, v in times.items()}}
+        # bounded CPU sample: one sweep (two site updates) of the oracle from the same start state
+        times, E_cpu, cores = cpu_site_updates(_WORKLOAD[0], state, 0, 2)
+        t_cpu = float(np.sum(times))
+        cpu = {"value": 1.0 / t_cpu, "unit": "sweeps/s", "cores": cores, "kind": "port",
+               "sample": f"one sweep (2 site updates, {t_cpu:.1f} s) of the numpy/ARPACK restatement of VUMPS_main.cpp "
+                         f"from the start state of the timed sweeps, same tolerances, {cores} host threads"}
+        if E_cpu is not None and r64["E_first"] is not None:
+            parity = {"what": "energies after the first sweep from the same start state: GPU FP64 vs the oracle",
+                      "gpu": [float(x) for x in r64["E_first"]], "oracle": [float(x) for x in E_cpu],
+                      "max_abs_diff": float(np.abs(np.asarray(r64["E_first"]) - np.asarray(E_cpu)).max())}
     line = {"metric": METRIC, "value": value, "unit": "sweeps/s", "n_gpus": ws, "steps": args.steps,
             "warmup": args.warmup, "ms_per_step": t_step * 1e3, "higher_is_better": True, "scaling": "weak",
             "vs_baseline": None, "dtype": "bf16x6->f32 applies, f64 Krylov/decompositions" if args.precision == "bf16x6"
             else "f64", "data": "synthetic",
-            "config": {"workload": _workload_desc(), "precision": args.precision, "seed": 1,
+            "config": {"workload": _workload_desc(), "precision": args.precision, "start_state": state_src,
                        "l2": "working set (~40 MB) is L2-resident by design; H_AC timing flushes L2 (512 MB write)",
                        "parallelism": f"replicas x{ws}"},
             "fp64": {"sweeps_per_s": 1.0 / float(np.mean(r64["times"])), "ms_per_step": 1e3 * float(np.mean(r64["times"])),
                      "energy": float(E64.mean()), "grad_norm": float(r64["F"].max()), "counts": r64["counts"]},
-            "mixed": {"sweeps_per_s": 1.0 / float(np.mean(rsp["times"])), "energy": float(Emx.mean()),
-                      "grad_norm": float(rsp["F"].max()), "counts": rsp["counts"],
-                      "note": "split-BF16 applies serve only solves with tol >= 2e-7 (their linearity floor); "
-                              "below it the precision ladder runs FP64, which at this tolerance schedule is every "
-                              "solve, so the two arms take the same path"},
+            "mixed": {"sweeps_per_s": 1.0 / float(np.mean(rsp["times"])), "ms_per_step": 1e3 * float(np.mean(rsp["times"])),
+                      "energy": float(Emx.mean()), "grad_norm": float(rsp["F"].max()), "counts": rsp["counts"]},
             "dE_mixed_vs_fp64": dE,
             "speedup_mixed_vs_fp64": float(np.mean(r64["times"])) / float(np.mean(rsp["times"])),
+            "parity_vs_oracle": parity,
             "h_ac": h_ac, "roofline": roof, "cpu_baseline": cpu, "e2e": e2e, "gpu_launches": rmx["launches"],
             "clocks": rmx["clocks"]}
     if rank == 0:

@@ -68,3 +68,44 @@ class HacWorkload:
     def host_copies(self):
         """numpy copies of every operand (for the CPU baseline restatement)."""
         return {k: getattr(self, k).cpu().numpy() for k in ("EHL", "EHR", "HL", "HR")}
+
+
+# ------------------------------------------------------------------------------------------------
+# VUMPS start states of the sweep benchmark
+# ------------------------------------------------------------------------------------------------
+
+# sweeps of the reference's tolerance schedule (VUMPS_main.cpp:177) from randMPS_LR(seed 1)
+# before a state counts as warmed: past the chaotic first sweeps of a random start
+WARM_SWEEPS = {"xxz_d512": 20, "hubbard_d1024": 30}
+WARM_SEED = 1
+
+
+def warm_state_path(name):
+    import os
+    return os.path.join(os.path.dirname(os.path.dirname(os.path.abspath(__file__))), "tests", "golden",
+                        f"warm_{name}.npz")
+
+
+def warm_on_device(ctx, name, verbose=False):
+    """The warmed state of workload `name` computed on the device: VumpsGPU (FP64) from
+    randMPS_LR(seed 1) for WARM_SWEEPS[name] sweeps of the tolerance schedule with tolmin =
+    GMRES tolerance = 1e-12.  Returns (host state {"AL", "AR", "C"}, energy, gradient norm)."""
+    from .vumps import VumpsGPU
+    model, fn, params = configs.WORKLOADS[name]
+    v = VumpsGPU(ctx, model, dims0=fn(), seed=WARM_SEED, tolmin=1e-12, InvETol=1e-12, verbose=verbose, **params)
+    for _ in range(WARM_SWEEPS[name]):
+        E, F, _ = v.sweep()
+    return v.host_state(), E, F
+
+
+def load_warm_state(name):
+    """The committed warmed state of workload `name` (tests/golden/warm_<name>.npz, written by
+    warm_on_device), or None: {"AL": [AL(0), AL(1)], "AR": [...], "C": [C on bond 0, bond 1]} as
+    flat float64 arrays in the reference's Vectorize order."""
+    import os
+    path = warm_state_path(name)
+    if not os.path.exists(path):
+        return None
+    f = np.load(path)
+    return {k: [np.array(f[f"{k}{n}"]) for n in range(2)] for k in ("AL", "AR", "C")}
+

@@ -23,32 +23,23 @@ HERE = os.path.dirname(os.path.abspath(__file__))
 ROOT = os.path.dirname(os.path.dirname(HERE))
 sys.path.insert(0, ROOT)
 
-# workload -> sweeps of the tolerance schedule before the state is saved
-WARM_SWEEPS = {"xxz_d512": 20, "hubbard_d1024": 30}
-
-
 def main():
     import torch
     from imps_cpp_tools_gb300 import blocks as B
-    from imps_cpp_tools_gb300 import configs
-    from imps_cpp_tools_gb300.vumps import VumpsGPU
+    from imps_cpp_tools_gb300 import workload as W
     ap = argparse.ArgumentParser()
     ap.add_argument("--out", default=HERE)
-    ap.add_argument("--workload", nargs="*", default=sorted(WARM_SWEEPS))
+    ap.add_argument("--workload", nargs="*", default=sorted(W.WARM_SWEEPS))
     args = ap.parse_args()
     ctx = B.Context(0)
     ctx.set_stream(torch.cuda.current_stream())
     for name in args.workload:
-        model, fn, params = configs.WORKLOADS[name]
-        v = VumpsGPU(ctx, model, dims0=fn(), seed=1, tolmin=1e-12, InvETol=1e-12, verbose=True, **params)
-        for _ in range(WARM_SWEEPS[name]):
-            E, F, prec = v.sweep()
-        h = v.host_state()
+        h, E, F = W.warm_on_device(ctx, name, verbose=True)
         out = {f"{k}{n}": h[k][n] for k in ("AL", "AR", "C") for n in range(2)}
-        out.update(sweeps=WARM_SWEEPS[name], energy=E, grad_norm=F, prec=prec, seed=1)
+        out.update(sweeps=W.WARM_SWEEPS[name], energy=E, grad_norm=F, seed=W.WARM_SEED)
         path = os.path.join(args.out, f"warm_{name}.npz")
         np.savez_compressed(path, **out)
-        print(f"{name}: {WARM_SWEEPS[name]} sweeps, E={E.mean():.12f} |grad|={F.max():.2e} -> {path}", flush=True)
+        print(f"{name}: {W.WARM_SWEEPS[name]} sweeps, E={E.mean():.12f} |grad|={F.max():.2e} -> {path}", flush=True)
 
 
 if __name__ == "__main__":

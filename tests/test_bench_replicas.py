@@ -67,11 +67,23 @@ def test_reference_arm_prints_on_rank0_only(monkeypatch):
     def fail(*a, **k):
         raise AssertionError("a non-zero rank must not time the CPU arm")
 
-    monkeypatch.setattr(bench, "cpu_op_times", fail)
+    monkeypatch.setattr(bench, "_oracle_vumps", fail)
     out = io.StringIO()
     with redirect_stdout(out):
         bench.run_reference(type("A", (), {"steps": 1, "warmup": 3})())
     assert out.getvalue() == ""
+
+
+class _FakeOracle:
+    """Stands in for the oracle's VUMPS: each site update takes a fixed, known time."""
+
+    def __init__(self, dt):
+        self.dt, self.calls = dt, []
+
+    def site_update(self, nn):
+        import time
+        self.calls.append(nn)
+        time.sleep(self.dt)
 
 
 def test_reference_arm_line_on_rank0(monkeypatch):
@@ -79,15 +91,16 @@ def test_reference_arm_line_on_rank0(monkeypatch):
     monkeypatch.setenv("WORLD_SIZE", "2")
     monkeypatch.setenv("RANK", "0")
     monkeypatch.setenv("LOCAL_RANK", "0")
-    # a fixed operator timing table keeps the test short; the line's arithmetic is what is checked
-    monkeypatch.setattr(bench, "cpu_op_times", lambda budget_per_op=0.5: ({"hac": 1e-3, "hc": 1e-4, "tm": 2e-4}, 2))
+    fake = _FakeOracle(0.02)
+    monkeypatch.setattr(bench, "_oracle_vumps", lambda name, state: fake)
     out = io.StringIO()
     with redirect_stdout(out):
         bench.run_reference(type("A", (), {"steps": 2, "warmup": 3})())
     line = json.loads(out.getvalue())
-    counts = bench.REF_COUNTS_BY_WORKLOAD[bench._WORKLOAD[0]]
-    t = bench.cpu_sweep_model(counts, {"hac": 1e-3, "hc": 1e-4, "tm": 2e-4})
+    assert fake.calls == [0, 1, 0, 1, 0]  # 3 untimed + 2 timed site updates, alternating sites
     assert line["impl"] == "reference" and line["n_gpus"] == 2 and line["steps"] == 2
-    assert line["value"] == pytest.approx(1.0 / t)
+    # a step is one site update: sweeps/s = 1 / (2 x site-update time)
+    assert line["value"] == pytest.approx(1.0 / (2 * 0.02), rel=0.3)
+    assert line["ms_per_step"] == pytest.approx(20.0, rel=0.3)
     assert line["e2e"]["value"] == line["value"] and line["cpu_baseline"]["value"] == line["value"]
     assert line["e2e"]["h2d_bytes_per_step"] == 0 and line["e2e"]["d2h_bytes_per_step"] == 0
