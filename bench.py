@@ -20,6 +20,8 @@ N / that time.
 energies in the Sz = +1 sector at --steps momenta (H_eff compiled into grouped-GEMM programs).
 --mode expand times one bond expansion (ExpandFromH, dmmax 20) at the XXZ D=512 and Hubbard
 D=1024 starts against the oracle on the same state.
+--mode trace runs the timed FP64 sweeps under torch.profiler: summed kernel time against wall time,
+kernels by share.
 --mode krylov times one bounded thick-restart Lanczos solve (eigs_rs, ncv 64, at most 8 restart
 cycles; FP64 at an unreachable tolerance, split-BF16 at its 2e-7 floor) on the synthetic H_AC,
 next to the same number of bare applies: the difference is the per-iteration
@@ -299,6 +301,10 @@ def _start_state():
     return st, f"{W.WARM_SWEEPS[_WORKLOAD[0]]} schedule sweeps from seed 1 on the device"
 
 
+_MIXED_TM = [False]
+_NCV = [126]
+
+
 def _new_vumps(precision, state):
     import torch
     from imps_cpp_tools_gb300 import configs
@@ -307,7 +313,8 @@ def _new_vumps(precision, state):
     init = {k: [torch.from_numpy(np.ascontiguousarray(a)).to("cuda") for a in state[k]] for k in ("AL", "AR", "C")}
     # eig_margin 1: the device Lanczos stops at the configured tolerance itself, as ARPACK does
     return VumpsGPU(_CTX[0], model, dims0=fn(), init_state=init, fixed_tol=TIMED_TOLS["eig"],
-                    InvETol=TIMED_TOLS["gmres"], eig_margin=1.0, precision=precision, verbose=True, **params)
+                    InvETol=TIMED_TOLS["gmres"], eig_margin=1.0, precision=precision,
+                    mixed_tm=_MIXED_TM[0] and precision != "fp64", lanczos_ncv=_NCV[0], verbose=True, **params)
 
 
 def _run_vumps(torch, precision, state, steps, warmup, stream, clocks=None, e2e=False):
@@ -376,10 +383,15 @@ def run_vumps(args):
     # the headline precision (timed with clocks and end to end) and the other one for comparison,
     # from the same start state
     other = "bf16x6" if args.precision == "fp64" else "fp64"
-    roth = _run_vumps(torch, other, state, args.steps, args.warmup, stream)
+    _MIXED_TM[0] = bool(getattr(args, "mixed_tm", False))
+    _NCV[0] = int(getattr(args, "ncv", 126))
+    roth = None if getattr(args, "headline_only", False) else _run_vumps(torch, other, state, args.steps, args.warmup,
+                                                                            stream)
     if ws > 1:
         dist.barrier()
     rmx = _run_vumps(torch, args.precision, state, args.steps, args.warmup, stream, ClockSampler(local), e2e=True)
+    if roth is None:
+        roth = rmx
     r64, rsp = (rmx, roth) if args.precision == "fp64" else (roth, rmx)
     t_step = float(np.mean(rmx["times"]))
     t_wall = float(np.mean(rmx["walls"]))
@@ -447,7 +459,11 @@ def run_vumps(args):
             "fp64": {"sweeps_per_s": 1.0 / float(np.mean(r64["times"])), "ms_per_step": 1e3 * float(np.mean(r64["times"])),
                      "energy": float(E64.mean()), "grad_norm": float(r64["F"].max()), "counts": r64["counts"]},
             "mixed": {"sweeps_per_s": 1.0 / float(np.mean(rsp["times"])), "ms_per_step": 1e3 * float(np.mean(rsp["times"])),
-                      "energy": float(Emx.mean()), "grad_norm": float(rsp["F"].max()), "counts": rsp["counts"]},
+                      "energy": float(Emx.mean()), "grad_norm": float(rsp["F"].max()), "counts": rsp["counts"],
+                      "policy": "H_AC/H_C Lanczos on split-BF16 (tcgen05) applies while the tolerance is above "
+                                "their 2e-7 floor, FP64 applies below it; GMRES "
+                                + ("split-BF16 TM with FP64-residual refinement" if _MIXED_TM[0] else "FP64 TM")
+                                + "; Krylov vectors, reorthogonalisation, decompositions, gradient and energy FP64"},
             "dE_mixed_vs_fp64": dE,
             "speedup_mixed_vs_fp64": float(np.mean(r64["times"])) / float(np.mean(rsp["times"])),
             "parity_vs_oracle": parity,
@@ -458,6 +474,48 @@ def run_vumps(args):
     if ws > 1:
         dist.barrier()
         dist.destroy_process_group()
+
+
+def run_trace(args):
+    """--mode trace: the timed FP64 sweeps under torch.profiler (CUPTI kernel records): the
+    summed duration of every kernel the sweeps launch against the wall time of the sweeps, and
+    the kernels by total time.  The difference is what launch gaps, host round trips and the
+    Python driver cost; the profiler's own per-launch overhead is part of it."""
+    import torch
+    from torch.profiler import ProfilerActivity, profile
+    from imps_cpp_tools_gb300 import blocks as B
+    ctx = B.Context(0)
+    _CTX[0] = ctx
+    stream = torch.cuda.current_stream()
+    ctx.set_stream(stream)
+    _NCV[0] = int(args.ncv)
+    state, src = _start_state()
+    v = _new_vumps(args.precision, state)
+    for _ in range(args.warmup):
+        v.sweep()
+    torch.cuda.synchronize()
+    with profile(activities=[ProfilerActivity.CUDA]) as prof:
+        t0 = time.perf_counter()
+        for _ in range(args.steps):
+            v.sweep()
+        torch.cuda.synchronize()
+        wall = time.perf_counter() - t0
+    per = {}
+    for e in prof.key_averages():
+        dt = getattr(e, "device_time_total", None)
+        if dt is None:
+            dt = getattr(e, "cuda_time_total", 0.0)
+        if dt and e.count:
+            per[e.key] = (per.get(e.key, (0.0, 0))[0] + dt * 1e-6, e.count)
+    # kernels only (memcpy/memset records carry "Memcpy"/"Memset" keys)
+    kern = {k: t for k, t in per.items() if not k.startswith(("Memcpy", "Memset", "cudaLaunch"))}
+    total = sum(t for t, _ in kern.values())
+    top = sorted(kern.items(), key=lambda kv: -kv[1][0])[:12]
+    print(json.dumps({"mode": "trace", "workload": _WORKLOAD[0], "precision": args.precision, "sweeps": args.steps,
+                      "start_state": src, "wall_s_per_sweep": wall / args.steps,
+                      "kernel_s_per_sweep": total / args.steps, "wall_over_kernel": wall / max(total, 1e-12),
+                      "kernels": [{"name": k[:100], "s_per_sweep": t / args.steps, "launches": c,
+                                   "share": t / max(total, 1e-12)} for k, (t, c) in top]}), flush=True)
 
 
 def run_hac(args):
@@ -680,13 +738,17 @@ def main():
     ap.add_argument("--steps", type=int, default=47)
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
-    ap.add_argument("--mode", default="vumps", choices=["vumps", "hac", "krylov", "excitations", "adjoint", "expand"])
+    ap.add_argument("--mode", default="vumps", choices=["vumps", "hac", "krylov", "excitations", "adjoint", "expand", "trace"])
     ap.add_argument("--workload", default="xxz_d512")
     ap.add_argument("--precision", default="fp64", choices=["fp64", "bf16x6"])
     ap.add_argument("--no-cpu", action="store_true")
+    ap.add_argument("--mixed-tm", action="store_true",
+                    help="split-BF16 transfer matrices in the mixed arm's GMRES solves (FP64-residual refinement)")
+    ap.add_argument("--headline-only", action="store_true", help="skip the other precision's arm (profiling)")
+    ap.add_argument("--ncv", type=int, default=126, help="Krylov dimension of the H_AC / H_C Lanczos solves")
     args = ap.parse_args()
     args.warmup = max(args.warmup, 3)
-    if args.mode in ("vumps",) or args.impl == "reference":
+    if args.mode in ("vumps", "trace") or args.impl == "reference":
         if args.workload not in WORKLOAD_DESCS:
             raise SystemExit(f"--workload for the VUMPS bench: one of {sorted(WORKLOAD_DESCS)}")
         _WORKLOAD[0] = args.workload
@@ -702,6 +764,8 @@ def main():
         run_expand(args)
     elif args.mode == "excitations":
         run_excitations(args)
+    elif args.mode == "trace":
+        run_trace(args)
     else:
         run_vumps(args)
 

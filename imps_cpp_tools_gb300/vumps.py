@@ -20,7 +20,7 @@ from . import models, ops
 class VumpsGPU:
     def __init__(self, ctx, model, dims0=None, dimvec=None, seed=1, InvETol=5e-15, InvEfac=2.0,
                  fixed_tol=None, tolmin=5e-16, tolmax=1e-6, trueLR=True, svdthresh=5e-7, precision="fp64",
-                 init_state=None, lanczos_maxit=300, gmres_maxit=4000, lanczos_ncv=96, eig_margin=0.1,
+                 init_state=None, lanczos_maxit=300, gmres_maxit=4000, lanczos_ncv=126, eig_margin=0.1,
                  mixed_tm=False, verbose=False, mmax=None, dmmax=20, expand_pause=5, expand_thresh=1e-5,
                  lamthresh=1e-12, **params):
         import torch
@@ -41,7 +41,9 @@ class VumpsGPU:
         # Hamiltonians of a poorly converged state have spectra spanning ~1e6 |E0|, where a
         # larger thick-restart basis needs far fewer applies.  Measured on XXZ D=512 over 50
         # sweeps (same final energy and gradient from 64 up): ncv 32: 0.36 sweeps/s (not
-        # converged), 48: 2.3, 64: 5.1, 80: 6.1, 96: 6.2, 112: 5.8, 126: 6.5.
+        # converged), 48: 2.3, 64: 5.1, 80: 6.1, 96: 6.2, 112: 5.8, 126: 6.5.  At the fixed
+        # tolerance 1e-12 from a warmed XXZ D=512 state (4 sweeps): 32: 0.28, 48: 1.8, 64: 4.2,
+        # 96: 4.4, 126: 4.65 (the largest basis one projection kernel takes).
         self.lanczos_ncv = lanczos_ncv
         self.eig_margin = eig_margin
         self.mixed_tm = mixed_tm
