@@ -175,3 +175,83 @@ def test_mps_bd_products(cuda_ctx):
     p2.run()
     ref = O.mps_vec(O.mps_mul_bd(AR[0], O.bd_t(C[0])))
     assert relerr(host(o2), -2.0 * ref) < RTOL
+
+
+FULL = ["xxz_d512", "hubbard_d1024"]
+
+
+def _full_state(name, seed):
+    model, dims0, params = T.workload_dims(name)
+    return T.random_state(model, dims0, seed=seed, **params)
+
+
+@pytest.mark.parametrize("name", FULL)
+def test_hc_apply_full_size(cuda_ctx, name):
+    """ApplyHCvec (VUMPS_helpers.hpp:114-133) at the benchmark sizes against the oracle's
+    literal chained form, 1e-12."""
+    st = _full_state(name, 31)
+    d, AL, AR, C, rng = st["d"], st["AL"], st["AR"], st["C"], st["rng"]
+    ns = len(st["I2K"][0])
+    Cd = {q: m.shape[0] for q, m in C[1].items()}
+    EHL, EHR = T.rand_bd(Cd, rng), T.rand_bd(Cd, rng)
+    lc = B.Layout(T.bd_blocks(C[1]), ns)
+    plan = B.plan_hc(cuda_ctx, lc, lc, lc, B.Layout(T.mps_blocks(AL[1]), ns), B.Layout(T.mps_blocks(AR[0]), ns),
+                     d, st["hnnz"])
+    for slot, v in ((2, O.bd_vec(EHL)), (3, O.bd_vec(EHR)), (4, O.mps_vec(AL[1])), (5, O.mps_vec(AR[0]))):
+        plan.bind(slot, dev(v))
+    plan.prepare()
+    x = rng.standard_normal(lc.nelem)
+    ref = O.ApplyHCvec(x, O.bd_sizes(C[1]), EHL, EHR, st["hnnz"], d, AL[1], AR[0])
+    out = dev(np.full(lc.nelem, np.nan))
+    ops.ApplyHCvec(plan, dev(x), out)
+    assert relerr(host(out), ref) < RTOL
+
+
+@pytest.mark.parametrize("name", FULL)
+@pytest.mark.parametrize("direction", [0, 1])
+def test_tm_chain_and_proj_full_size(cuda_ctx, name, direction):
+    """The unit-cell TM chain (TMBlockFunctions.hpp:542-625) and InvEfun_proj
+    (InvEBlockFunctions.hpp:12-47) at the benchmark sizes against the oracle, 1e-12."""
+    st = _full_state(name, 37)
+    AL, dv, rng = st["AL"], st["dimvec"], st["rng"]
+    ns = len(st["I2K"][0])
+    l0, l1 = B.Layout(T.mps_blocks(AL[0]), ns), B.Layout(T.mps_blocks(AL[1]), ns)
+    bond = B.Layout.blockdiag(dv[0])
+    plan = B.plan_tm(cuda_ctx, [l0, l1], direction, bond, bond)
+    plan.bind(2, dev(O.mps_vec(AL[0])))
+    plan.bind(3, dev(O.mps_vec(AL[1])))
+    X = T.rand_bd(dv[0], rng, sym=False)
+    fun = (lambda Y: O.ApplyTMLeftUC(AL, Y)) if direction == 0 else (lambda Y: O.ApplyTMRightUC(AL, Y))
+    out = dev(np.full(bond.nelem, np.nan))
+    ops.ApplyTM(plan, dev(O.bd_vec(X)), out)
+    assert relerr(host(out), O.bd_vec(fun(X))) < RTOL
+    rin, rout = T.rand_bd(dv[0], rng), T.rand_bd(dv[0], rng)
+    ref = O.InvEfun_proj(O.bd_vec(X), fun, rin, rout, O.bd_sizes(X))
+    out2 = dev(np.zeros(bond.nelem))
+    ops.InvEfun_proj(plan, dev(O.bd_vec(X)), dev(O.bd_vec(rin)), dev(O.bd_vec(rout)), out2)
+    assert relerr(host(out2), ref) < RTOL
+
+
+@pytest.mark.parametrize("name", FULL)
+def test_inverte_proj_full_size(cuda_ctx, name):
+    """InvertE_proj (InvEBlockFunctions.hpp:201-266) for the left environment of a canonical
+    unit cell at the benchmark sizes: the device's restarted GMRES against the reference's
+    GMRES restated in the oracle, both to 1e-12; solutions agree to 1e-8 relative."""
+    st = _full_state(name, 41)
+    AL, C, dv, hnnz = st["AL"], st["C"], st["dimvec"], st["hnnz"]
+    ns = len(st["I2K"][0])
+    l0, l1 = B.Layout(T.mps_blocks(AL[0]), ns), B.Layout(T.mps_blocks(AL[1]), ns)
+    bond = B.Layout.blockdiag(dv[0])
+    R = O.bd_mul(C[1], O.bd_t(C[1]))
+    _, R = O.TMDominantEig(AL, dv[0], "r", 1e-14, R)
+    x = O.GetHL(AL, hnnz)
+    eye = O.bd_eye(dv[0])
+    yref, flag = O.InvertE_proj(AL, x, eye, R, "l", 1e-12)
+    assert flag > 0
+    plan = B.plan_tm(cuda_ctx, [l0, l1], 0, bond, bond)
+    plan.bind(2, dev(O.mps_vec(AL[0])))
+    plan.bind(3, dev(O.mps_vec(AL[1])))
+    y = dev(np.zeros(bond.nelem))
+    it, rr, conv = ops.InvertE_proj(plan, dev(O.bd_vec(x)), dev(O.bd_vec(eye)), dev(O.bd_vec(R)), "l", y, 1e-12)
+    assert conv, (it, rr)
+    assert relerr(host(y), O.bd_vec(yref)) < 1e-8

@@ -154,3 +154,23 @@ def test_quantum_ising_exact_energy(cuda_ctx):
         if F.max() < 1e-11:
             break
     assert F.max() < 1e-10 and np.abs(E - e0).max() < 1e-10, (E, e0)
+
+
+def test_sweep_from_warm_state_matches_oracle_full_size(cuda_ctx):
+    """The benchmark's configuration at full size: XXZ D=512 (21 sectors), one sweep from the
+    committed warmed state at eigensolver tol 1e-12 and GMRES tol 1e-8, on the GPU and in the
+    oracle (ARPACK, the reference's GMRES): the energies agree to 1e-9 (measured 1.8e-10)."""
+    import torch
+    import bench
+    from imps_cpp_tools_gb300 import configs
+    from imps_cpp_tools_gb300 import workload as W
+    name = "xxz_d512"
+    state = W.load_warm_state(name)
+    assert state is not None
+    model, fn, params = configs.WORKLOADS[name]
+    init = {k: [torch.from_numpy(a).to("cuda") for a in state[k]] for k in ("AL", "AR", "C")}
+    gpu = VumpsGPU(cuda_ctx, model, dims0=fn(), init_state=init, fixed_tol=bench.TIMED_TOLS["eig"],
+                   InvETol=bench.TIMED_TOLS["gmres"], eig_margin=1.0, **params)
+    Eg, Fg, _ = gpu.sweep()
+    times, Eo, _ = bench.cpu_site_updates(name, state, 0, 2)
+    assert np.abs(Eg - np.asarray(Eo)).max() < 1e-9, (Eg, Eo)
