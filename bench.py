@@ -303,6 +303,7 @@ def _start_state():
 
 _MIXED_TM = [False]
 _NCV = [126]
+_AUTOTUNE = [True]
 
 
 def _new_vumps(precision, state):
@@ -314,7 +315,8 @@ def _new_vumps(precision, state):
     # eig_margin 1: the device Lanczos stops at the configured tolerance itself, as ARPACK does
     return VumpsGPU(_CTX[0], model, dims0=fn(), init_state=init, fixed_tol=TIMED_TOLS["eig"],
                     InvETol=TIMED_TOLS["gmres"], eig_margin=1.0, precision=precision,
-                    mixed_tm=_MIXED_TM[0] and precision != "fp64", lanczos_ncv=_NCV[0], verbose=True, **params)
+                    mixed_tm=_MIXED_TM[0] and precision != "fp64", lanczos_ncv=_NCV[0], autotune=_AUTOTUNE[0],
+                    verbose=True, **params)
 
 
 def _run_vumps(torch, precision, state, steps, warmup, stream, clocks=None, e2e=False):
@@ -385,6 +387,7 @@ def run_vumps(args):
     other = "bf16x6" if args.precision == "fp64" else "fp64"
     _MIXED_TM[0] = bool(getattr(args, "mixed_tm", False))
     _NCV[0] = int(getattr(args, "ncv", 126))
+    _AUTOTUNE[0] = not getattr(args, "no_autotune", False)
     roth = None if getattr(args, "headline_only", False) else _run_vumps(torch, other, state, args.steps, args.warmup,
                                                                             stream)
     if ws > 1:
@@ -410,8 +413,11 @@ def run_vumps(args):
     peaks = _peaks()
     bf16_peak = peaks.get("bf16_tflops", 1893.6)
     fp64_peak = _fp64_peak_tflops(torch)
+    tile, splits, _ = v64.p_hac[0].stage_shape(0)
     h_ac = {"fp64_tflops": flops / t_hac64 / 1e12, "mixed_tflops": flops / t_hacmx / 1e12,
-            "flops_per_apply": flops, "fp64_us": t_hac64 * 1e6, "mixed_us": t_hacmx * 1e6}
+            "flops_per_apply": flops, "fp64_us": t_hac64 * 1e6, "mixed_us": t_hacmx * 1e6,
+            "fp64_launch_shape": {"tile": tile, "splits": splits,
+                                  "source": "autotuner" if _AUTOTUNE[0] else "makespan estimate"}}
     fp64_src = ("dense FP64 matmul (torch, cuBLAS DGEMM 4096^3) measured in this run: GB300 has no FP64 tensor "
                 "rate, the FP64 pipe bounds this kernel (not in MEASURED_PEAKS.json)")
     if args.precision == "bf16x6":
@@ -454,6 +460,7 @@ def run_vumps(args):
             "vs_baseline": None, "dtype": "bf16x6->f32 applies, f64 Krylov/decompositions" if args.precision == "bf16x6"
             else "f64", "data": "synthetic",
             "config": {"workload": _workload_desc(), "precision": args.precision, "start_state": state_src,
+                       "lanczos_ncv": _NCV[0], "autotune": _AUTOTUNE[0],
                        "l2": "working set (~40 MB) is L2-resident by design; H_AC timing flushes L2 (512 MB write)",
                        "parallelism": f"replicas x{ws}"},
             "fp64": {"sweeps_per_s": 1.0 / float(np.mean(r64["times"])), "ms_per_step": 1e3 * float(np.mean(r64["times"])),
@@ -489,6 +496,7 @@ def run_trace(args):
     stream = torch.cuda.current_stream()
     ctx.set_stream(stream)
     _NCV[0] = int(args.ncv)
+    _AUTOTUNE[0] = not args.no_autotune
     state, src = _start_state()
     v = _new_vumps(args.precision, state)
     for _ in range(args.warmup):
@@ -745,6 +753,7 @@ def main():
     ap.add_argument("--mixed-tm", action="store_true",
                     help="split-BF16 transfer matrices in the mixed arm's GMRES solves (FP64-residual refinement)")
     ap.add_argument("--headline-only", action="store_true", help="skip the other precision's arm (profiling)")
+    ap.add_argument("--no-autotune", action="store_true", help="launch shapes from the makespan estimate only")
     ap.add_argument("--ncv", type=int, default=126, help="Krylov dimension of the H_AC / H_C Lanczos solves")
     args = ap.parse_args()
     args.warmup = max(args.warmup, 3)

@@ -71,6 +71,9 @@ _PROTOS = {
     "imps_plan_table": (c_int, [c_vp, c_int, c_int, P_i64, P_i64, P_i32, P_i32, P_i32, P_i32, P_i64,
                                 P_i32, P_i64, P_i32, P_dbl]),
     "imps_plan_set_precision": (c_int, [c_vp, c_int]),
+    "imps_plan_autotune": (c_int, [c_vp, c_int, C.POINTER(c_int)]),
+    "imps_plan_stage_shape": (c_int, [c_vp, c_int, C.POINTER(c_int), C.POINTER(c_int), C.POINTER(C.c_uint64)]),
+    "imps_autotune_clear": (c_int, []),
     "imps_hac_apply": (c_int, [c_vp, c_vp, c_vp, c_int]),
     "imps_hc_apply": (c_int, [c_vp, c_vp, c_vp, c_int]),
     "imps_tm_apply": (c_int, [c_vp, c_vp, c_vp, c_int]),

@@ -214,6 +214,20 @@ class Plan:
     def set_precision(self, prec):
         N.call("imps_plan_set_precision", self._h, int(prec))
 
+    def autotune(self, reps=5):
+        """Time the FP64 launch shapes of every apply stage not yet tuned in this process and
+        install the fastest (imps_plan_autotune; on stand-in buffers, nothing needs to be
+        bound).  Returns the number of stages timed."""
+        n = C.c_int()
+        N.call("imps_plan_autotune", self._h, int(reps), C.byref(n))
+        return n.value
+
+    def stage_shape(self, stage=0):
+        """(tile, splits, histogram key) of an apply stage."""
+        t, sp, k = C.c_int(), C.c_int(), C.c_uint64()
+        N.call("imps_plan_stage_shape", self._h, int(stage), C.byref(t), C.byref(sp), C.byref(k))
+        return t.value, sp.value, k.value
+
     def table(self, stage=0, prep=False):
         """Sector-matching table of one stage: list over output blocks of
         (tag, [(a_slot, a_off, b_slot, b_off, k, alpha), ...])."""
@@ -315,3 +329,8 @@ def plan_decomp(ctx, A, direction):
     if direction in ("l", 0):
         p.nslayout = p.derived(2)  # left null space (Nullspace(A, l))
     return p
+
+
+def autotune_clear():
+    """Forget every launch shape the autotuner cached in this process."""
+    N.call("imps_autotune_clear")

@@ -2,6 +2,10 @@
 // reference-facing functors and the device Krylov solvers.
 #include <cuda_runtime.h>
 
+#include <array>
+#include <mutex>
+#include <unordered_map>
+
 #include <algorithm>
 #include <cmath>
 #include <cstdio>
@@ -77,6 +81,7 @@ std::atomic<long long>& imps::launch_counter() {
 
 constexpr int PLAN_DECOMP = 12;
 constexpr double kMixedEigTol = 2e-7;    // Ritz-residual floor of split-BF16 applies
+constexpr double kAttainableRes = 64.0;  // FP64 Lanczos residual floor, in units of eps |T|
 constexpr double kMixedInnerTol = 1e-6;  // residual reduction per mixed GMRES cycle
 constexpr double kDominantTolFloor = 1e-14;  // attainable residual of the fixed-point solve
 
@@ -101,6 +106,66 @@ std::vector<HNnz> make_h(int nnz, const int32_t* r, const int32_t* c, const doub
   std::vector<HNnz> h;
   for (int i = 0; i < nnz; ++i) h.push_back({r[i], c[i], v[i]});
   return h;
+}
+
+// ---- FP64 grouped-GEMM launch shape per stage: tile size and split-K ----
+// A stage's work is set by the histogram of its output blocks (rows, cols, summed K, terms).
+// The autotuner (imps_plan_autotune) times every candidate shape of a stage once and caches the
+// fastest under the hash of that histogram; stages of later plans with the same histogram take
+// the cached shape, others the makespan estimate below.
+struct TuneChoice {
+  int T = 16, splits = 1;
+  float us = 0.f;
+};
+static std::mutex g_tune_mu;
+static std::unordered_map<uint64_t, TuneChoice> g_tune;
+
+static uint64_t stage_key(const Stage& S) {
+  std::vector<std::array<int64_t, 4>> h;
+  h.reserve(S.outs.size());
+  for (const OutBlock& o : S.outs) {
+    int64_t k = 0;
+    for (int t = o.t0; t < o.t1; ++t) k += S.terms[t].k;
+    h.push_back({(int64_t)o.M, (int64_t)o.N, k, (int64_t)(o.t1 - o.t0)});
+  }
+  std::sort(h.begin(), h.end());
+  uint64_t x = 1469598103934665603ull;  // FNV-1a over the sorted histogram
+  auto mix = [&](uint64_t v) {
+    for (int b = 0; b < 8; ++b) { x ^= (v >> (8 * b)) & 0xFF; x *= 1099511628211ull; }
+  };
+  mix(h.size());
+  for (const auto& e : h)
+    for (int64_t v : e) mix((uint64_t)v);
+  return x;
+}
+
+// largest useful split for tile size T: at least one K chunk per K group of the kernel
+static int max_splits(const Stage& S, int T) {
+  int max_chunks = 0;
+  for (const OutBlock& o : S.outs) {
+    int ch = 0;
+    for (int t = o.t0; t < o.t1; ++t) ch += (S.terms[t].k + 15) / 16;
+    max_chunks = std::max(max_chunks, ch);
+  }
+  return std::max(1, std::min(8, max_chunks / (T == 16 ? 4 : 2)));
+}
+
+// (re)build the stage's tiles for shape (T, splits) and upload them
+static int install_stage(Stage& S, int T, int splits) {
+  cudaFree(S.d_tiles); cudaFree(S.d_ws); cudaFree(S.d_cnt);
+  S.d_tiles = nullptr; S.d_ws = nullptr; S.d_cnt = nullptr;
+  finalize_tiles(S, T, T);
+  S.splits = splits;
+  if (!S.tiles.empty()) {
+    CK(cudaMalloc(&S.d_tiles, S.tiles.size() * sizeof(Tile)));
+    CK(cudaMemcpy(S.d_tiles, S.tiles.data(), S.tiles.size() * sizeof(Tile), cudaMemcpyHostToDevice));
+    if (S.splits > 1) {
+      CK(cudaMalloc(&S.d_ws, S.tiles.size() * S.splits * (size_t)T * T * sizeof(double)));
+      CK(cudaMalloc(&S.d_cnt, S.tiles.size() * sizeof(int)));
+      CK(cudaMemset(S.d_cnt, 0, S.tiles.size() * sizeof(int)));
+    }
+  }
+  return IMPS_OK;
 }
 
 int upload_stage(Stage& S) {
@@ -130,18 +195,14 @@ int upload_stage(Stage& S) {
   };
   int s16 = 1, s32 = 1;
   const int64_t m16 = plan_for(16, &s16), m32 = plan_for(32, &s32);
-  const int T = m16 <= m32 ? 16 : 32;
-  finalize_tiles(S, T, T);
-  S.splits = T == 16 ? s16 : s32;
-  if (!S.tiles.empty()) {
-    CK(cudaMalloc(&S.d_tiles, S.tiles.size() * sizeof(Tile)));
-    CK(cudaMemcpy(S.d_tiles, S.tiles.data(), S.tiles.size() * sizeof(Tile), cudaMemcpyHostToDevice));
-    if (S.splits > 1) {
-      CK(cudaMalloc(&S.d_ws, S.tiles.size() * S.splits * (size_t)T * T * sizeof(double)));
-      CK(cudaMalloc(&S.d_cnt, S.tiles.size() * sizeof(int)));
-      CK(cudaMemset(S.d_cnt, 0, S.tiles.size() * sizeof(int)));
-    }
+  int T = m16 <= m32 ? 16 : 32;
+  int sp = T == 16 ? s16 : s32;
+  {
+    std::lock_guard<std::mutex> lk(g_tune_mu);
+    auto it = g_tune.find(stage_key(S));
+    if (it != g_tune.end()) { T = it->second.T; sp = it->second.splits; }
   }
+  RC(install_stage(S, T, sp));
   if (!S.terms.empty()) {
     CK(cudaMalloc(&S.d_terms, S.terms.size() * sizeof(Term)));
     CK(cudaMemcpy(S.d_terms, S.terms.data(), S.terms.size() * sizeof(Term), cudaMemcpyHostToDevice));
@@ -703,6 +764,107 @@ int imps_plan_table(const imps_plan* p, int prep, int stage, int64_t* n_outs, in
   return IMPS_OK;
 }
 
+int imps_plan_autotune(imps_plan* p, int reps, int* n_tuned) {
+  if (!p) return IMPS_ERR_BAD_ARG;
+  if (p->ctx->device < 0) return IMPS_ERR_NO_DEVICE;
+  if (reps < 1) reps = 5;
+  cudaStream_t st = p->ctx->stream;
+  // the candidates run on zero-filled stand-ins of the caller's slots (the plan's own scratch
+  // slots are used as they are), so no bound buffer is read or written
+  imps_dslots sl{};
+  std::vector<double*> temps;
+  auto free_temps = [&]() { for (double* t : temps) cudaFree(t); };
+  for (size_t i = 0; i < p->P.slots.size() && i < (size_t)kMaxSlots; ++i) {
+    const Slot& sd = p->P.slots[i];
+    if (sd.kind == SLOT_INTERNAL) { sl.p[i] = sd.dptr; continue; }
+    if (sd.nelem <= 0) continue;
+    double* t = nullptr;
+    if (cudaMalloc(&t, sd.nelem * sizeof(double)) != cudaSuccess) { free_temps(); return IMPS_ERR_OOM; }
+    temps.push_back(t);
+    if (cudaMemsetAsync(t, 0, sd.nelem * sizeof(double), st) != cudaSuccess) { free_temps(); return IMPS_ERR_CUDA; }
+    sl.p[i] = t;
+  }
+  for (const Stage& S : p->P.stages) {
+    for (const Term& t : S.terms)
+      if (!sl.p[t.a_slot] || !sl.p[t.b_slot]) { free_temps(); return IMPS_ERR_BAD_TABLE; }
+    for (const OutBlock& o : S.outs)
+      if (!sl.p[o.c_slot]) { free_temps(); return IMPS_ERR_BAD_TABLE; }
+  }
+  cudaEvent_t e0, e1;
+  if (cudaEventCreate(&e0) != cudaSuccess) { free_temps(); return IMPS_ERR_CUDA; }
+  if (cudaEventCreate(&e1) != cudaSuccess) { cudaEventDestroy(e0); free_temps(); return IMPS_ERR_CUDA; }
+  int tuned = 0, rc = IMPS_OK;
+  for (Stage& S : p->P.stages) {
+    if (S.outs.empty() || S.terms.empty()) continue;
+    const uint64_t key = stage_key(S);
+    TuneChoice best;
+    bool have = false;
+    {
+      std::lock_guard<std::mutex> lk(g_tune_mu);
+      auto it = g_tune.find(key);
+      if (it != g_tune.end()) { best = it->second; have = true; }
+    }
+    if (!have) {
+      best.us = std::numeric_limits<float>::infinity();
+      for (int T : {16, 32}) {
+        const int smax = max_splits(S, T);
+        for (int sp = 1; sp <= smax && !rc; sp *= 2) {
+          if ((rc = install_stage(S, T, sp))) break;
+          auto launch = [&]() {
+            return imps_launch_grouped_f64(S.d_tiles, (int)S.tiles.size(), S.d_terms, sl, S.tile_m, S.splits,
+                                           S.d_ws, S.d_cnt, st);
+          };
+          if ((rc = launch())) break;  // warm-up
+          std::vector<float> ts;
+          for (int r = 0; r < reps && !rc; ++r) {
+            if (cudaEventRecord(e0, st) != cudaSuccess) { rc = IMPS_ERR_CUDA; break; }
+            rc = launch();
+            if (rc || cudaEventRecord(e1, st) != cudaSuccess || cudaEventSynchronize(e1) != cudaSuccess) {
+              if (!rc) rc = IMPS_ERR_CUDA;
+              break;
+            }
+            float ms = 0.f;
+            cudaEventElapsedTime(&ms, e0, e1);
+            ts.push_back(ms * 1e3f);
+          }
+          if (rc) break;
+          std::sort(ts.begin(), ts.end());
+          const float us = ts[ts.size() / 2];
+          if (us < best.us) { best.T = T; best.splits = sp; best.us = us; }
+        }
+        if (rc) break;
+      }
+      if (rc) break;
+      std::lock_guard<std::mutex> lk(g_tune_mu);
+      g_tune[key] = best;
+      ++tuned;
+    }
+    if (S.tile_m != best.T || S.splits != best.splits)
+      if ((rc = install_stage(S, best.T, best.splits))) break;
+  }
+  if (cudaStreamSynchronize(st) != cudaSuccess && !rc) rc = IMPS_ERR_CUDA;
+  cudaEventDestroy(e0);
+  cudaEventDestroy(e1);
+  free_temps();
+  if (n_tuned) *n_tuned = tuned;
+  return rc;
+}
+
+int imps_plan_stage_shape(const imps_plan* p, int stage, int* tile, int* splits, uint64_t* key) {
+  if (!p || stage < 0 || stage >= (int)p->P.stages.size()) return IMPS_ERR_BAD_ARG;
+  const Stage& S = p->P.stages[stage];
+  if (tile) *tile = S.tile_m;
+  if (splits) *splits = S.splits;
+  if (key) *key = stage_key(S);
+  return IMPS_OK;
+}
+
+int imps_autotune_clear(void) {
+  std::lock_guard<std::mutex> lk(g_tune_mu);
+  g_tune.clear();
+  return IMPS_OK;
+}
+
 int imps_plan_set_precision(imps_plan* p, int prec) {
   if (!p) return IMPS_ERR_BAD_ARG;
   if (prec == IMPS_PREC_FP64) { p->prec = prec; return IMPS_OK; }
@@ -898,8 +1060,18 @@ static int eigs_impl(imps_ctx* c, imps_plan* p, int64_t n, const DevApply& op, d
       if (res < 0.5 * best) {
         best = res;
         best_at = used;
-      } else if (stall_exit && used - best_at > stall_window) {
-        return 1;
+      } else if (used - best_at > stall_window) {
+        if (stall_exit) return 1;
+        // A tolerance below what FP64 resolves for this operator: the Ritz residual cannot fall
+        // below ~eps |H| (|H| bounded by the Gershgorin radius of T), where it only fluctuates.
+        // Once it has stopped halving there, the solve ends converged to that accuracy.
+        double normT = 0.0;
+        for (int q = 0; q < k; ++q)
+          normT = std::max(normT, std::fabs(ta[q]) + std::fabs(tb[q]) + (q ? std::fabs(tb[q - 1]) : 0.0));
+        if (res <= kAttainableRes * kEps * normT) {
+          status = IMPS_OK;
+          return 1;
+        }
       }
       return 0;
     };

@@ -22,7 +22,7 @@ class VumpsGPU:
                  fixed_tol=None, tolmin=5e-16, tolmax=1e-6, trueLR=True, svdthresh=5e-7, precision="fp64",
                  init_state=None, lanczos_maxit=300, gmres_maxit=4000, lanczos_ncv=126, eig_margin=0.1,
                  mixed_tm=False, verbose=False, mmax=None, dmmax=20, expand_pause=5, expand_thresh=1e-5,
-                 lamthresh=1e-12, **params):
+                 lamthresh=1e-12, autotune=False, **params):
         import torch
         self.torch = torch
         self.verbose = verbose
@@ -48,6 +48,8 @@ class VumpsGPU:
         self.eig_margin = eig_margin
         self.mixed_tm = mixed_tm
         self.precision = precision
+        # time the FP64 launch shapes of every plan's stages once per process (imps_plan_autotune)
+        self.autotune = autotune
         self.rng = np.random.default_rng(seed)
         self.stats = {"lanczos_applies": 0, "gmres_iters": 0, "hac_applies": 0, "hc_applies": 0, "expansions": 0}
         # bond expansion (ExpandFromH at VUMPS_main.cpp:270-308), off unless mmax (the largest total
@@ -114,6 +116,11 @@ class VumpsGPU:
         self.optm_l = [B.plan_optm(ctx, LA[a], LA[1 - a], d, hnnz, 0, LB[a]) for a in range(2)]
         self.optm_r = [B.plan_optm(ctx, LA[a], LA[1 - a], d, hnnz, 1, LB[a]) for a in range(2)]
         self.flops_hac = [p.info()["flops_apply"] for p in self.p_hac]
+        if self.autotune:
+            plans = (self.redop_l + self.redop_r + self.p_ac + self.p_hac + self.p_grad + self.p_hcl + self.p_hcr
+                     + self.p_mul_r_t + self.p_mul_l_t + self.p_mul_r + self.p_mul_l + self.optm_l + self.optm_r
+                     + list(self.tm.values()))
+            self.tuned_stages = sum(p.autotune() for p in plans)
         if self.precision == "bf16x6":
             # tensor-core applies inside the Krylov solvers; Krylov vectors, residuals,
             # decompositions and the energy stay FP64

@@ -147,6 +147,20 @@ int imps_plan_table(const imps_plan* P, int prep, int stage, int64_t* n_outs, in
                     int32_t* out_tag, int32_t* out_t0, int32_t* out_t1, int32_t* term_aslot,
                     int64_t* term_aoff, int32_t* term_bslot, int64_t* term_boff,
                     int32_t* term_k, double* term_alpha);
+/* Tile-shape autotuner of the FP64 grouped GEMM (no counterpart in the reference, whose
+ * products are per-block dgemm calls).  A stage's launch shape (tile 16 or 32, split-K 1..8)
+ * is keyed on the histogram of its output blocks (rows, cols, summed K, terms).  For every
+ * apply stage of `plan` whose key has no cached shape, each candidate is timed (median of
+ * `reps` launches with CUDA events on the context's stream, on zero-filled stand-ins of the
+ * caller's slots: no bound buffer is touched, nothing needs to be bound) and the fastest is
+ * cached for the process; cached shapes are installed.  Plans
+ * created later pick cached shapes up; stages without one use a makespan estimate.
+ * Synchronises the stream.  n_tuned (optional): stages timed by this call. */
+int imps_plan_autotune(imps_plan* plan, int reps, int* n_tuned);
+/* the launch shape of an apply stage and its histogram key */
+int imps_plan_stage_shape(const imps_plan* plan, int stage, int* tile, int* splits, uint64_t* key);
+/* forget every cached shape */
+int imps_autotune_clear(void);
 /* select the GEMM engine of a plan: IMPS_PREC_FP64 (DFMA) or IMPS_PREC_BF16X6 (tcgen05) */
 int imps_plan_set_precision(imps_plan* P, int prec);
 

@@ -230,3 +230,20 @@ def test_noalloc_rejects_bad_layouts_before_device_access():
     lbig = B.Layout.mps(I2K, big, {(q + 1,): m for (q,), m in big.items()})
     lb_in, lb_out = B.Layout.blockdiag(big), B.Layout.blockdiag({(q + 1,): m for (q,), m in big.items()})
     assert lib.imps_tm_apply_noalloc(lbig.handle, lb_in.handle, lb_out.handle, 0, dummy, dummy, dummy, None) == -9
+
+
+def test_autotune_needs_a_device():
+    """The autotuner times launches: a host-only context refuses it (IMPS_ERR_NO_DEVICE) and
+    still reports the stage's histogram key and the estimated shape."""
+    import ctypes as C
+    from imps_cpp_tools_gb300 import _native as N
+    ctx = B.Context(-1)
+    I2K = [(1,), (-1,)]
+    b0 = {(-1,): 2, (1,): 2}
+    b1 = {(0,): 3, (2,): 1, (-2,): 1}
+    la = B.Layout.mps(I2K, b0, b1)
+    plan = B.plan_tm(ctx, [la], 0, B.Layout.blockdiag(b0), B.Layout.blockdiag(b1))
+    n = C.c_int(-1)
+    assert N.load().imps_plan_autotune(plan.handle, 3, C.byref(n)) == -6
+    tile, splits, key = plan.stage_shape(0)
+    assert tile in (16, 32) and splits >= 1 and key != 0
