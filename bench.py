@@ -58,6 +58,10 @@ NCU_TRAFFIC_BYTES = {"bf16x6": 5.66e6, "fp64": 2.38e6}
 # solves floors at 2e-11 (site 0) and 1e-9 (site 1, warm start of norm 3e5) after ~200
 # iterations, where the reference's unrestarted GMRES then runs on towards maxit = 24,368
 TIMED_TOLS = {"eig": 1e-12, "gmres": 1e-8}
+# wall-clock bounds of the CPU restatement: the reference arm (warm-up and timed site updates
+# together) and the cpu_baseline sample of the GPU arm (one sweep)
+REF_BUDGET_S = 300.0
+CPU_SAMPLE_BUDGET_S = 90.0
 _TIMED = ("2-site VUMPS sweep from a warmed state (20/30 sweeps of the tolerance schedule "
           "min(max(prec/100, 1e-12), 1e-6), VUMPS_main.cpp:177, from seed 1), then fixed eigensolver tol 1e-12 and "
           "GMRES tol 1e-8, expansion off")
@@ -196,22 +200,58 @@ def _oracle_vumps(name, state):
                    fixed_tol=TIMED_TOLS["eig"], InvETol=TIMED_TOLS["gmres"])
 
 
-def cpu_site_updates(name, state, warmup, steps):
+class _Deadline(Exception):
+    """The CPU restatement ran past its time budget (raised from inside an operator apply)."""
+
+
+_DEADLINE = [None]
+_PATCHED = [False]
+
+
+def _install_deadline():
+    """Every operator apply of the oracle checks the wall-clock budget first, so a solve that
+    would run for hours (ARPACK's maxit is the problem size, eigs.cpp:386; the reference's GMRES
+    runs to maxit = dimension on a system whose residual floors above the tolerance) ends the
+    CPU measurement instead."""
+    if _PATCHED[0]:
+        return
+    from oracle import imps_oracle as O
+    for name in ("ApplyHAvec", "ApplyHCvec", "ApplyTMLeftUC", "ApplyTMRightUC"):
+        f = getattr(O, name)
+
+        def w(*a, _f=f, **k):
+            if _DEADLINE[0] is not None and time.perf_counter() > _DEADLINE[0]:
+                raise _Deadline()
+            return _f(*a, **k)
+        setattr(O, name, w)
+    _PATCHED[0] = True
+
+
+def cpu_site_updates(name, state, warmup, steps, budget_s=None):
     """Time `steps` site updates (VUMPS_main.cpp:171-313, one half of a sweep each) of the
     oracle's VUMPS after `warmup` untimed ones, from `state`, on the host's cores (numpy's
-    BLAS threads).  Returns (seconds per site update, the energies after the first full sweep
-    or None, threads)."""
+    BLAS threads), within `budget_s` seconds of wall time for the whole call (None: no bound).
+    Returns (seconds per completed timed site update, the energies after the first full sweep or
+    None, threads, whether the budget cut the run short)."""
     ora = _oracle_vumps(name, state)
-    times, E = [], None
-    for i in range(warmup + steps):
-        t0 = time.perf_counter()
-        ora.site_update(i % 2)
-        dt = time.perf_counter() - t0
-        if i >= warmup:
-            times.append(dt)
-        if i == 1:
-            E = _oracle_sweep_energy(ora)
-    return times, E, os.cpu_count()
+    times, E, cut = [], None, False
+    if budget_s is not None:
+        _install_deadline()
+        _DEADLINE[0] = time.perf_counter() + budget_s
+    try:
+        for i in range(warmup + steps):
+            t0 = time.perf_counter()
+            ora.site_update(i % 2)
+            dt = time.perf_counter() - t0
+            if i >= warmup:
+                times.append(dt)
+            if i == 1:
+                E = _oracle_sweep_energy(ora)
+    except _Deadline:
+        cut = True
+    finally:
+        _DEADLINE[0] = None
+    return times, E, os.cpu_count(), cut
 
 
 def _oracle_sweep_energy(ora):
@@ -240,17 +280,24 @@ def run_reference(args):
                           "finish its first sweeps in minutes"}), flush=True)
         return
     t0 = time.perf_counter()
-    times, _, cores = cpu_site_updates(_WORKLOAD[0], state, args.warmup, args.steps)
+    times, _, cores, cut = cpu_site_updates(_WORKLOAD[0], state, args.warmup, args.steps, REF_BUDGET_S)
+    if not times:
+        print(json.dumps({"impl": "reference", "unavailable": f"no site update of the CPU restatement finished "
+                          f"within {REF_BUDGET_S:.0f} s"}), flush=True)
+        return
     t_site = float(np.mean(times))
     value = 1.0 / (2.0 * t_site)
     sample = (f"{len(times)} timed site updates (after {args.warmup} untimed) of the numpy/ARPACK restatement of "
               f"VUMPS_main.cpp on {_WORKLOAD[0]} from the committed warmed state, {cores} host threads; "
-              f"sweeps/s = 1 / (2 x mean site update); wall {time.perf_counter() - t0:.1f} s incl. setup")
+              f"sweeps/s = 1 / (2 x mean site update); wall {time.perf_counter() - t0:.1f} s incl. setup"
+              + (f"; the {REF_BUDGET_S:.0f} s budget ended the run after {len(times)} of {args.steps} timed steps "
+                 "(the site update in progress is not counted)" if cut else ""))
     line = {"impl": "reference", "metric": METRIC, "value": value, "unit": "sweeps/s", "n_gpus": ws,
             "steps": len(times), "warmup": args.warmup, "ms_per_step": 1e3 * t_site,
             "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic",
             "config": {"workload": _workload_desc(), "implementation": "CPU restatement of the reference (oracle)",
-                       "step": "one site update (half a sweep)",
+                       "step": "one site update (half a sweep)", "budget_s": REF_BUDGET_S,
+                       "truncated_by_budget": cut,
                        "ms_per_site_update_median": 1e3 * float(np.median(times))},
             "cpu_baseline": {"value": value, "unit": "sweeps/s", "cores": cores, "kind": "port", "sample": sample},
             "e2e": {"value": value, "unit": "sweeps/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
@@ -446,7 +493,8 @@ def run_vumps(args):
     cpu, parity = None, None
     if rank == 0 and not args.no_cpu:
         # bounded CPU sample: one sweep (two site updates) of the oracle from the same start state
-        times, E_cpu, cores = cpu_site_updates(_WORKLOAD[0], state, 0, 2)
+        times, E_cpu, cores, cut = cpu_site_updates(_WORKLOAD[0], state, 0, 2, CPU_SAMPLE_BUDGET_S)
+    if rank == 0 and not args.no_cpu and len(times) == 2:
         t_cpu = float(np.sum(times))
         cpu = {"value": 1.0 / t_cpu, "unit": "sweeps/s", "cores": cores, "kind": "port",
                "sample": f"one sweep (2 site updates, {t_cpu:.1f} s) of the numpy/ARPACK restatement of VUMPS_main.cpp "

@@ -172,5 +172,6 @@ def test_sweep_from_warm_state_matches_oracle_full_size(cuda_ctx):
     gpu = VumpsGPU(cuda_ctx, model, dims0=fn(), init_state=init, fixed_tol=bench.TIMED_TOLS["eig"],
                    InvETol=bench.TIMED_TOLS["gmres"], eig_margin=1.0, **params)
     Eg, Fg, _ = gpu.sweep()
-    times, Eo, _ = bench.cpu_site_updates(name, state, 0, 2)
+    times, Eo, _, cut = bench.cpu_site_updates(name, state, 0, 2, 600.0)
+    assert not cut
     assert np.abs(Eg - np.asarray(Eo)).max() < 1e-9, (Eg, Eo)
