@@ -1081,7 +1081,10 @@ static int eigs_impl(imps_ctx* c, imps_plan* p, int64_t n, const DevApply& op, d
         pre_applied = false;
         ++applies;
         ++used;
-        RC(kr_cgs2_step(c->ws, V, n, j + 1, w, n, Hd + (size_t)j * ld, tmp, V + (size_t)(j + 1) * n, bflag, st));
+        // the kept block is rotated at every restart so that the projected matrix stays
+        // tridiagonal: w couples to v_j and v_{j-1} only, the first CGS pass takes those two
+        RC(kr_cgs2_step(c->ws, V, n, j + 1, w, n, Hd + (size_t)j * ld, tmp, V + (size_t)(j + 1) * n, bflag, st,
+                        2));
         if (pending >= 0) {  // the check of an earlier step, evaluated while step j runs
           const int r = evaluate(pending);
           pending = -1;

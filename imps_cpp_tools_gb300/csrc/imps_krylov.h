@@ -29,9 +29,13 @@ int kr_gemv(const double* V, int64_t ldv, int ncols, const double* h, double* y,
 // One CGS2 Lanczos/Arnoldi step on w = A v_{nc-1} against V[:, 0..nc-1]: h[0..nc-1] = total
 // projection coefficients, h[nc] = |w| after projection, vnext = w / h[nc] (flag set when
 // |w| underflows); h2 (nc doubles) is scratch.  One cooperative launch when n <= 152 * 2048
-// (else, or when the cooperative launch is refused, four launches).
+// (else, or when the cooperative launch is refused, four launches).  nloc > 0 (Lanczos, whose
+// projected matrix is tridiagonal): the first pass projects out only the last nloc columns,
+// the second pass all of them — half the FP64 work of two full passes, the same orthogonality
+// (the first pass removes the large components, the second the rounding-level ones).  The
+// four-launch path always runs two full passes.
 int kr_cgs2_step(const KrylovWs& ws, const double* V, int64_t ldv, int nc, double* w, int64_t n,
-                 double* h, double* h2, double* vnext, int* flag, cudaStream_t st);
+                 double* h, double* h2, double* vnext, int* flag, cudaStream_t st, int nloc = 0);
 int kr_basis_rotate(const double* V, int64_t ldv, int m, const double* W, int kk, double* out,
                     int64_t ldo, int64_t n, cudaStream_t st);
 int kr_scale_inv(const double* x, const double* nrm, double* y, int64_t n, int* flag, cudaStream_t st);

@@ -299,11 +299,13 @@ __device__ void update_rows(const double* __restrict__ Vb, int64_t ldv, int nc, 
   }
 }
 
+// c_loc: the first pass projects out columns c_loc..nc-1 only (Lanczos: the two columns the
+// three-term recurrence couples w to; 0 = all columns); the second pass is always full.
 __global__ void __launch_bounds__(CT) cgs2_coop_kernel(const double* __restrict__ V, int64_t ldv, int nc,
                                                       double* __restrict__ w, int64_t n, int sub, double* h,
                                                       double* __restrict__ vnext, int* flag,
                                                       double* __restrict__ partials, unsigned int* sync,
-                                                      int* err) {
+                                                      int* err, int c_loc) {
   __shared__ double wsm[COOP_SUB];
   __shared__ double h1[imps::kMaxCols];
   __shared__ double h2[imps::kMaxCols + 1];
@@ -318,15 +320,18 @@ __global__ void __launch_bounds__(CT) cgs2_coop_kernel(const double* __restrict_
   double* P2 = P1 + (int64_t)G * imps::kMaxCols;
   bool ok = true;
   for (int t = threadIdx.x; t < len; t += blockDim.x) wsm[t] = w[base + t];
+  for (int c = threadIdx.x; c < c_loc; c += blockDim.x) h1[c] = 0.0;
   __syncthreads();
-  // pass 1: h1 = V^T w
-  block_dots(Vb, ldv, nc, wsm, len, P0, G);
+  // pass 1: h1 = V^T w over columns c_loc..nc-1
+  const int nloc = nc - c_loc;
+  const double* Vloc = Vb + (int64_t)c_loc * ldv;
+  block_dots(Vloc, ldv, nloc, wsm, len, P0, G);
   ok = grid_barrier(sync, (unsigned)G, err, ok);
-  if (ok) reduce_partials(P0, G, nc, h1);
+  if (ok) reduce_partials(P0, G, nloc, h1 + c_loc);
   __syncthreads();
   // pass 2: w -= V h1; h2 = V^T w
   if (ok) {
-    update_rows(Vb, ldv, nc, h1, wsm, len);
+    update_rows(Vloc, ldv, nloc, h1 + c_loc, wsm, len);
     __syncthreads();
     block_dots(Vb, ldv, nc, wsm, len, P1, G);
   }
@@ -679,8 +684,9 @@ int kr_basis_rotate(const double* V, int64_t ldv, int m, const double* W, int kk
 }
 
 int kr_cgs2_step(const KrylovWs& ws, const double* V, int64_t ldv, int nc, double* w, int64_t n,
-                 double* h, double* h2, double* vnext, int* flag, cudaStream_t st) {
+                 double* h, double* h2, double* vnext, int* flag, cudaStream_t st, int nloc) {
   if (nc < 1 || nc > kMaxCols) return IMPS_ERR_BAD_ARG;
+  int c_loc = (nloc > 0 && nloc < nc) ? nc - nloc : 0;
   // (column nc of the second partials region carries |w|^2, hence nc < kMaxCols)
   if (ws.sync && ws.err && n <= (int64_t)CGRID * COOP_SUB && nc < kMaxCols) {
     // one cooperative launch: w stays in shared memory, one grid barrier per reduction
@@ -694,7 +700,7 @@ int kr_cgs2_step(const KrylovWs& ws, const double* V, int64_t ldv, int nc, doubl
     unsigned int* sync = ws.sync;
     int* err = ws.err;
     void* args[] = {(void*)&V, (void*)&ldv, (void*)&nc, (void*)&w, (void*)&n, (void*)&subi, (void*)&h,
-                    (void*)&vnext, (void*)&flag, (void*)&partials, (void*)&sync, (void*)&err};
+                    (void*)&vnext, (void*)&flag, (void*)&partials, (void*)&sync, (void*)&err, (void*)&c_loc};
     if (cudaLaunchCooperativeKernel((const void*)cgs2_coop_kernel, dim3(gridc), dim3(CT), args, 0, st) ==
         cudaSuccess) {
       imps::count_launch();
