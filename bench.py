@@ -583,12 +583,15 @@ def run_hac(args):
     stream = torch.cuda.current_stream()
     ctx.set_stream(stream)
     w = HacWorkload(ctx, args.workload)
+    if not args.no_autotune:
+        w.plan.autotune()
     if args.precision == "bf16x6":
         w.plan.set_precision(N.PREC_BF16X6)
     t = _time_hac_applies(torch, w.plan, w.n, stream)
     print(json.dumps({"mode": "hac", "workload": args.workload, "precision": args.precision, "us_per_apply": t * 1e6,
                       "tflops": w.flops / t / 1e12, "flops_per_apply": w.flops,
-                      "bytes_per_apply": w.bytes_per_apply()}), flush=True)
+                      "bytes_per_apply": w.bytes_per_apply(), "launch_shape": w.plan.stage_shape(0)[:2]}),
+          flush=True)
 
 
 def run_krylov(args):
