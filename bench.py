@@ -50,8 +50,8 @@ APPLIES_PER_STEP = 20
 L2_FLUSH_BYTES = 512 << 20
 # DRAM bytes (read + write) of one H_AC apply from one ncu capture of `bench.py --mode hac`
 # (profiles/tc_gemm_hac_xxz_d512.md: tc_gemm 5.26 MB + pack 0.40 MB;
-# profiles/grouped_gemm_f64_hac_xxz_d512.md: 2.38 MB), cold caches
-NCU_TRAFFIC_BYTES = {"bf16x6": 5.66e6, "fp64": 2.38e6}
+# profiles/grouped_gemm_f64_hac_xxz_d512.md, autotuned shape 16x16 split 2: 2.38 + 0.03 MB)
+NCU_TRAFFIC_BYTES = {"bf16x6": 5.66e6, "fp64": 2.41e6}
 # tolerances of the timed sweeps: the eigensolver tolerance of the configuration (1e-12); GMRES
 # 1e-8, because the environment systems of these states do not reach 1e-12 in floating point:
 # measured at XXZ D=512 from the warmed state, the relative residual of the left-environment
