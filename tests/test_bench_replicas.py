@@ -92,12 +92,18 @@ def test_reference_arm_line_on_rank0(monkeypatch):
     monkeypatch.setenv("RANK", "0")
     monkeypatch.setenv("LOCAL_RANK", "0")
     fake = _FakeOracle(0.02)
-    monkeypatch.setattr(bench, "_oracle_vumps", lambda name, state: fake)
+    made = []
+
+    def make(name, state):
+        made.append(state)
+        return fake
+    monkeypatch.setattr(bench, "_oracle_vumps", make)
     out = io.StringIO()
     with redirect_stdout(out):
         bench.run_reference(type("A", (), {"steps": 2, "warmup": 3})())
     line = json.loads(out.getvalue())
     assert fake.calls == [0, 1, 0, 1, 0]  # 3 untimed + 2 timed site updates, alternating sites
+    assert len(made) == 3  # every cycle of two site updates starts from the start state
     assert line["impl"] == "reference" and line["n_gpus"] == 2 and line["steps"] == 2
     # a step is one site update: sweeps/s = 1 / (2 x site-update time)
     assert line["value"] == pytest.approx(1.0 / (2 * 0.02), rel=0.3)
