@@ -74,6 +74,12 @@ _PROTOS = {
     "imps_plan_autotune": (c_int, [c_vp, c_int, C.POINTER(c_int)]),
     "imps_plan_stage_shape": (c_int, [c_vp, c_int, C.POINTER(c_int), C.POINTER(c_int), C.POINTER(C.c_uint64)]),
     "imps_autotune_clear": (c_int, []),
+    "imps_plan_replicate": (c_int, [c_vp, c_int, C.POINTER(c_vp)]),
+    "imps_invert_e_fac_batch": (c_int, [c_vp, c_int, C.POINTER(c_vp), C.POINTER(c_vp), C.POINTER(c_dbl),
+                                        C.POINTER(c_dbl), C.POINTER(c_vp), C.POINTER(c_vp), c_dbl, c_int, c_int,
+                                        C.POINTER(c_int), C.POINTER(c_dbl)]),
+    "imps_eigs_rs_batch_op": (c_int, [c_vp, c_int, c_i64, APPLY_FN, c_vp, c_vp, c_int, c_dbl, c_int, c_int,
+                                      C.POINTER(c_dbl), C.POINTER(c_int), C.POINTER(c_int)]),
     "imps_hac_apply": (c_int, [c_vp, c_vp, c_vp, c_int]),
     "imps_hc_apply": (c_int, [c_vp, c_vp, c_vp, c_int]),
     "imps_tm_apply": (c_int, [c_vp, c_vp, c_vp, c_int]),

@@ -527,6 +527,48 @@ int imps_plan_tm_mixed(imps_ctx* ctx, int nsites, const imps_layout* const* A, c
 // contractions whose sector matching is compiled by a caller (the excitation effective
 // Hamiltonian).  Every term's operands and every output region are bounds-checked against
 // the slot sizes here, so a table can never make a kernel access memory outside its slots.
+int imps_plan_replicate(const imps_plan* src, int copies, imps_plan** out) {
+  if (!src || copies < 1 || !out) return IMPS_ERR_BAD_ARG;
+  const Plan& S = src->P;
+  if (!S.prep.empty()) return IMPS_ERR_UNSUPPORTED;  // operator-derived stages would need sharing rules
+  Plan Q;
+  Q.kind = PLAN_PROGRAM;
+  // per copy: the input, the output and the plan's own scratch; shared: the operator slots
+  std::vector<char> per(S.slots.size(), 0);
+  for (size_t i = 0; i < S.slots.size(); ++i) {
+    per[i] = S.slots[i].kind == SLOT_INTERNAL || (int)i == S.n_in || (int)i == S.n_out;
+    Slot sl = S.slots[i];
+    if (per[i]) sl.nelem *= copies;
+    if (sl.kind == SLOT_INTERNAL || per[i]) sl.dptr = nullptr;  // operators keep their bindings
+    Q.slots.push_back(sl);
+  }
+  Q.n_in = S.n_in;
+  Q.n_out = S.n_out;
+  for (const Stage& st : S.stages) {
+    Stage R;
+    for (int c = 0; c < copies; ++c) {
+      for (const OutBlock& o : st.outs) {
+        OutBlock ob = o;
+        if (per[o.c_slot]) ob.c_off += (int64_t)c * S.slots[o.c_slot].nelem;
+        ob.t0 = (int32_t)R.terms.size();
+        for (int t = o.t0; t < o.t1; ++t) {
+          Term tm = st.terms[t];
+          if (per[tm.a_slot]) tm.a_off += (int64_t)c * S.slots[tm.a_slot].nelem;
+          if (per[tm.b_slot]) tm.b_off += (int64_t)c * S.slots[tm.b_slot].nelem;
+          R.terms.push_back(tm);
+        }
+        ob.t1 = (int32_t)R.terms.size();
+        R.outs.push_back(ob);
+      }
+    }
+    R.flops = st.flops * copies;
+    Q.stages.push_back(std::move(R));
+  }
+  Q.flops_apply = S.flops_apply * copies;
+  Q.dropped = S.dropped * copies;
+  return finish_plan(src->ctx, Q, out);
+}
+
 int imps_plan_program(imps_ctx* ctx, int nslots, const int64_t* slot_nelem, int nstages,
                       const int32_t* stage_nouts, const int64_t* outs, const int64_t* terms,
                       const double* alphas, imps_plan** out) {
@@ -1206,6 +1248,181 @@ int imps_eigs_rs_op(imps_ctx* c, int64_t n, imps_apply_fn fn, void* user, double
   return eigs_impl(c, nullptr, n, op, x, mem, nev, tol, ncv, maxit, evals, evecs, n_applies);
 }
 
+// ---- Lanczos over P independent symmetric systems in lockstep ----
+// Every step applies the operator of all P systems at once (one callback on P x n vectors,
+// system-major), then runs each system's CGS step on its own basis.  Per system: thick restart
+// (Wu & Simon) with the kept block rotated to keep the projected matrix tridiagonal, ARPACK's
+// Ritz test on the nev lowest pairs, and the attainable-accuracy exit of eigs_impl.  The systems
+// restart together (they advance in lockstep); a converged system stops taking CGS steps (its
+// slot of the batched apply is then unused).  Convergence is checked every 4 steps, synchronously.
+int imps_eigs_rs_batch_op(imps_ctx* c, int P, int64_t n, imps_apply_fn fn, void* user, double* X, int nev,
+                          double tol, int ncv, int maxit, double* evals, int* n_applies, int* converged) {
+  if (!c || P < 1 || !fn || !X || !evals || n < 2 || nev < 1 || nev > 16 || nev >= n) return IMPS_ERR_BAD_ARG;
+  if (c->device < 0) return IMPS_ERR_NO_DEVICE;
+  cudaStream_t st = c->stream;
+  int m = ncv > 0 ? ncv : std::max(20, 2 * nev);
+  if (m > n) m = (int)n;
+  if (m > kMaxCols - 2) m = kMaxCols - 2;
+  if (m < nev + 3) m = (int)std::min<int64_t>(nev + 3, n);
+  if (maxit <= 0) maxit = (int)std::min<int64_t>(n, 100000);
+  const int64_t max_applies = (int64_t)maxit * m;
+  const int ld = m + 1;
+  const int kk = std::max(nev, std::max(1, std::min(m / 2, m - 3)));
+  if (kk >= m) return IMPS_ERR_BAD_ARG;
+  // the callback's own solves use the context's main arena: the bases live in the callback arena
+  RC(arena_reserve(c, round256((size_t)P * n * 8) * (m + 1) + round256(n * 8) * (kk + 1) +
+                          round256((size_t)P * n * 8) * 2 + round256((size_t)P * ld * ld * 8) +
+                          round256((size_t)m * kk * 8) + round256(ld * 8) + round256((size_t)P * 4) + 4096,
+                      true));
+  Bump bp{c->arena_cb};
+  double* V = bp.take((size_t)P * n * (m + 1));  // system s: V + s * n * (m + 1), column j at + j * n
+  double* Wk = bp.take((size_t)n * kk);
+  double* IN = bp.take((size_t)P * n);
+  double* OUT = bp.take((size_t)P * n);
+  double* Hd = bp.take((size_t)P * ld * ld);
+  double* Wrot = bp.take((size_t)m * kk);
+  double* tmp = bp.take(ld);
+  int* bflag = (int*)bp.take((P + 1) / 2 + 1);
+  double* nrm = c->dscal + 8;
+  auto Vs = [&](int sy) { return V + (size_t)sy * n * (m + 1); };
+  CK(cudaMemsetAsync(Hd, 0, (size_t)P * ld * ld * 8, st));
+  CK(cudaMemsetAsync(bflag, 0, P * sizeof(int), st));
+  for (int sy = 0; sy < P; ++sy) {
+    RC(kr_multidot(c->ws, X + (size_t)sy * n, n, 1, X + (size_t)sy * n, n, tmp, 0, nrm, st));
+    RC(kr_scale_inv(X + (size_t)sy * n, nrm, Vs(sy), n, bflag + sy, st));
+  }
+  struct Sys {
+    std::vector<double> ta, tb, z, thv, Zv;
+    bool active = true, ok = false;
+    int kfinal = 0, jpulled = 0;
+    double best = std::numeric_limits<double>::infinity(), res = 0.0;
+    int64_t best_at = 0;
+  };
+  std::vector<Sys> sys(P);
+  for (Sys& q : sys) {
+    q.ta.assign(m + 1, 0.0); q.tb.assign(m + 1, 0.0); q.z.assign(m, 0.0);
+    q.thv.assign(nev, 0.0); q.Zv.assign((size_t)m * nev, 0.0);
+  }
+  std::vector<double> th(kk), Z((size_t)m * kk), sv(kk), Q((size_t)kk * kk), qa(kk), qb(kk), Wr((size_t)m * kk);
+  std::vector<int> hflags(P);
+  const double eps23 = std::cbrt(kEps * kEps);
+  const int64_t stall_window = 3 * (int64_t)(m - kk) + m;
+  int64_t applies = 0;
+  int jstart = 0;
+  const int chk = 4;
+  auto n_active = [&]() { int a = 0; for (const Sys& q : sys) a += q.active; return a; };
+  // convergence test of every active system at step j (columns jpulled..j come to the host)
+  auto evaluate = [&](int j) -> int {
+    CK(cudaMemcpyAsync(hflags.data(), bflag, P * sizeof(int), cudaMemcpyDeviceToHost, st));
+    CK(cudaStreamSynchronize(st));
+    for (int sy = 0; sy < P; ++sy) {
+      Sys& q = sys[sy];
+      if (!q.active) continue;
+      const int cols = j + 1 - q.jpulled;
+      CK(cudaMemcpy(c->hpin, Hd + (size_t)sy * ld * ld + (size_t)q.jpulled * ld, (size_t)cols * ld * 8,
+                    cudaMemcpyDeviceToHost));
+      for (int r = q.jpulled; r <= j; ++r) {
+        q.ta[r] = c->hpin[(size_t)(r - q.jpulled) * ld + r];
+        q.tb[r] = c->hpin[(size_t)(r - q.jpulled) * ld + r + 1];
+      }
+      q.jpulled = j + 1;
+      const int k = j + 1, nw = std::min(nev, k);
+      tri_lowest_pairs(k, q.ta.data(), q.tb.data(), nw, q.thv.data(), q.Zv.data());
+      if (!std::isfinite(q.thv[0])) return IMPS_ERR_NAN;
+      std::copy(q.Zv.begin(), q.Zv.begin() + k, q.z.begin());
+      q.kfinal = k;
+      bool all = nw == nev;
+      double res = 0.0;
+      for (int i = 0; i < nw; ++i) {
+        const double ri = std::fabs(q.tb[k - 1] * q.Zv[(size_t)(k - 1) + (size_t)i * k]);
+        res = std::max(res, ri);
+        all = all && ri <= tol * std::max(std::fabs(q.thv[i]), eps23);
+      }
+      q.res = res;
+      if (all || hflags[sy]) { q.ok = true; q.active = false; continue; }
+      if (res < 0.5 * q.best) {
+        q.best = res;
+        q.best_at = applies;
+      } else if (applies - q.best_at > stall_window) {
+        double normT = 0.0;
+        for (int r = 0; r < k; ++r)
+          normT = std::max(normT, std::fabs(q.ta[r]) + std::fabs(q.tb[r]) + (r ? std::fabs(q.tb[r - 1]) : 0.0));
+        if (res <= kAttainableRes * kEps * normT) { q.ok = true; q.active = false; }
+      }
+    }
+    return IMPS_OK;
+  };
+  bool done = false;
+  while (!done) {
+    for (int j = jstart; j < m; ++j) {
+      for (int sy = 0; sy < P; ++sy)
+        if (sys[sy].active)
+          CK(cudaMemcpyAsync(IN + (size_t)sy * n, Vs(sy) + (size_t)j * n, n * 8, cudaMemcpyDeviceToDevice, st));
+      const int frc = fn(user, IN, OUT);
+      if (frc < 0) return frc;
+      ++applies;
+      for (int sy = 0; sy < P; ++sy)
+        if (sys[sy].active)
+          RC(kr_cgs2_step(c->ws, Vs(sy), n, j + 1, OUT + (size_t)sy * n, n, Hd + (size_t)sy * ld * ld + (size_t)j * ld,
+                          tmp, Vs(sy) + (size_t)(j + 1) * n, bflag + sy, st, 2));
+      const bool last = j == m - 1 || applies >= max_applies;
+      if (((j + 1 - jstart) % chk == 0) || last) {
+        RC(evaluate(j));
+        if (n_active() == 0 || applies >= max_applies) { done = true; break; }
+      }
+    }
+    if (done) break;
+    // thick restart of every active system
+    for (int sy = 0; sy < P; ++sy) {
+      Sys& q = sys[sy];
+      if (!q.active) continue;
+      tri_lowest_pairs(m, q.ta.data(), q.tb.data(), kk, th.data(), Z.data());
+      for (int i = 0; i < kk; ++i) sv[i] = q.tb[m - 1] * Z[(size_t)(m - 1) + (size_t)i * m];
+      arrow_tridiag(kk, th.data(), sv.data(), Q.data(), qa.data(), qb.data());
+      double sn = 0.0;
+      for (int i = 0; i < kk; ++i) sn += sv[i] * sv[i];
+      sn = std::sqrt(sn);
+      for (int pc = 0; pc < kk; ++pc) {
+        const double* qq = Q.data() + (size_t)(kk - 1 - pc) * kk;
+        for (int r = 0; r < m; ++r) {
+          double acc = 0.0;
+          for (int i = 0; i < kk; ++i) acc += Z[(size_t)r + (size_t)i * m] * qq[i];
+          Wr[(size_t)r + (size_t)pc * m] = acc;
+        }
+      }
+      CK(cudaMemcpy(Wrot, Wr.data(), (size_t)m * kk * 8, cudaMemcpyHostToDevice));
+      RC(kr_basis_rotate(Vs(sy), n, m, Wrot, kk, Wk, n, n, st));
+      CK(cudaMemcpyAsync(Vs(sy), Wk, (size_t)kk * n * 8, cudaMemcpyDeviceToDevice, st));
+      CK(cudaMemcpyAsync(Vs(sy) + (size_t)kk * n, Vs(sy) + (size_t)m * n, n * 8, cudaMemcpyDeviceToDevice, st));
+      CK(cudaStreamSynchronize(st));  // Wrot and Wk are reused by the next system
+      for (int pc = 0; pc < kk; ++pc) q.ta[pc] = qa[kk - 1 - pc];
+      for (int pc = 0; pc + 1 < kk; ++pc) q.tb[pc] = qb[kk - 2 - pc];
+      q.tb[kk - 1] = sn;
+      q.jpulled = kk;
+    }
+    jstart = kk;
+  }
+  // lowest Ritz vector of every system into X, normalised; the nev Ritz values into evals
+  for (int sy = 0; sy < P; ++sy) {
+    Sys& q = sys[sy];
+    if (q.kfinal < 1) continue;
+    CK(cudaMemcpy(tmp, q.z.data(), q.kfinal * 8, cudaMemcpyHostToDevice));
+    RC(kr_gemv(Vs(sy), n, q.kfinal, tmp, X + (size_t)sy * n, n, st));
+    RC(kr_multidot(c->ws, X + (size_t)sy * n, n, 1, X + (size_t)sy * n, n, tmp, 0, nrm, st));
+    RC(kr_scale_inv(X + (size_t)sy * n, nrm, X + (size_t)sy * n, n, nullptr, st));
+    CK(cudaStreamSynchronize(st));
+    for (int i = 0; i < nev; ++i) evals[(size_t)sy * nev + i] = i < q.kfinal ? q.thv[i] : 0.0;
+    if (converged) converged[sy] = q.ok ? 1 : 0;
+  }
+  if (n_applies) *n_applies = (int)applies;
+  if (debug_on())
+    fprintf(stderr, "[imps eigs_rs_batch] P=%d n=%lld applies=%lld converged=%d\n", P, (long long)n,
+            (long long)applies, P - n_active());
+  int allok = 1;
+  for (const Sys& q : sys) allok &= q.ok;
+  return allok ? IMPS_OK : IMPS_WARN_NOT_CONVERGED;
+}
+
 // ---- Arnoldi: eigs_n for the nev wanted eigenpairs of a real nonsymmetric operator ----
 // Restart of Krylov-Schur type (Stewart, SIAM J. Matrix Anal. Appl. 23 (2001) 601): at the end
 // of a cycle the kept Ritz vectors of the projected matrix G = V^T A V span an invariant
@@ -1749,6 +1966,52 @@ int imps_invert_e_proj_fac(imps_plan* p, const double* x_re, const double* x_im,
     return IMPS_ERR_BAD_ARG;  // the plan's direction and the projector's roles must agree
   return invert_fac_impl(p, x_re, x_im, L, R, dir, true, fac_re, fac_im, y_re, y_im, mem, tol, maxit, krylov,
                          iters, relres);
+}
+
+int imps_invert_e_fac_batch(imps_plan* rep, int P, const double* const* x_re, const double* const* x_im,
+                            const double* fac_re, const double* fac_im, double* const* y_re, double* const* y_im,
+                            double tol, int maxit, int krylov, int* iters, double* relres) {
+  if (!rep || P < 1 || !x_re || !x_im || !fac_re || !fac_im || !y_re || !y_im) return IMPS_ERR_BAD_ARG;
+  imps_ctx* c = rep->ctx;
+  if (c->device < 0) return IMPS_ERR_NO_DEVICE;
+  const int64_t ntot = rep->P.slots[rep->P.n_in].nelem;
+  if (ntot % (2 * (int64_t)P) || rep->P.slots[rep->P.n_out].nelem != ntot) return IMPS_ERR_BAD_ARG;
+  const int64_t n = ntot / (2 * (int64_t)P);
+  cudaStream_t st = c->stream;
+  int m = krylov > 0 ? std::min(krylov, kMaxCols - 2) : kGmresKrylov;
+  if (maxit <= 0) maxit = (int)std::min<int64_t>(ntot, 100000);
+  RC(arena_reserve(c, round256(ntot * 8) * (m + 12) + round256((size_t)(m + 1) * (m + 1) * 8) +
+                          2 * round256((size_t)P * 8) + 16 * 4096));
+  Bump bp{c->arena};
+  double* b = bp.take(ntot);
+  double* y = bp.take(ntot);
+  double* t = bp.take(ntot);
+  double* dfr = bp.take(P);
+  double* dfi = bp.take(P);
+  CK(cudaMemcpyAsync(dfr, fac_re, P * 8, cudaMemcpyHostToDevice, st));
+  CK(cudaMemcpyAsync(dfi, fac_im, P * 8, cudaMemcpyHostToDevice, st));
+  for (int j = 0; j < P; ++j) {  // stack [re_j | im_j]
+    CK(cudaMemcpyAsync(b + 2 * j * n, x_re[j], n * 8, cudaMemcpyDeviceToDevice, st));
+    CK(cudaMemcpyAsync(b + (2 * j + 1) * n, x_im[j], n * 8, cudaMemcpyDeviceToDevice, st));
+    CK(cudaMemcpyAsync(y + 2 * j * n, y_re[j], n * 8, cudaMemcpyDeviceToDevice, st));
+    CK(cudaMemcpyAsync(y + (2 * j + 1) * n, y_im[j], n * 8, cudaMemcpyDeviceToDevice, st));
+  }
+  // one apply of the replicated transfer matrix takes every plane of every system
+  DevOp A = [&](const double* u, double* out, bool) -> int {
+    RC(apply_dev(rep, u, t));
+    return kr_fac_epilogue_batch(u, t, dfr, dfi, out, n, P, st);
+  };
+  const int prec_saved = rep->prec;
+  rep->prec = IMPS_PREC_FP64;
+  const int rc = gmres_dev(c, ntot, A, false, b, y, tol, maxit, m, iters, relres, bp);
+  rep->prec = prec_saved;
+  if (rc < 0) return rc;
+  for (int j = 0; j < P; ++j) {
+    CK(cudaMemcpyAsync(y_re[j], y + 2 * j * n, n * 8, cudaMemcpyDeviceToDevice, st));
+    CK(cudaMemcpyAsync(y_im[j], y + (2 * j + 1) * n, n * 8, cudaMemcpyDeviceToDevice, st));
+  }
+  CK(cudaStreamSynchronize(st));
+  return rc;
 }
 
 int imps_tm_dominant(imps_plan* p, const double* x0, double* V, int mem, double tol, int maxit,

@@ -48,6 +48,8 @@ int kr_trace_prod(const KrylovWs& ws, const double* X, const double* R, const in
 int kr_fac_epilogue(const double* ure, const double* uim, const double* tre, const double* tim, double c,
                     double s, const double* tau, const double* rho, double* ore, double* oim, int64_t n,
                     cudaStream_t st);
+int kr_fac_epilogue_batch(const double* u, const double* t, const double* fre, const double* fim, double* out,
+                          int64_t n, int P, cudaStream_t st);
 int kr_segsq(const KrylovWs& ws, const double* X, const int64_t* soff, const int64_t* slen, int ns,
              double* out, cudaStream_t st);
 int kr_absmax(const KrylovWs& ws, const double* x, int64_t n, double* out, cudaStream_t st);

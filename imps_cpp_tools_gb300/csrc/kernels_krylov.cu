@@ -781,6 +781,28 @@ int kr_fac_epilogue(const double* ure, const double* uim, const double* tre, con
   return IMPS_OK;
 }
 
+// Batched form over P systems stacked as [re_0 | im_0 | re_1 | im_1 | ...] (planes of n):
+// out_j = u_j - f_j T u_j with the complex factor f_j = fre[j] + i fim[j] (device arrays).
+__global__ void fac_epilogue_batch_kernel(const double* __restrict__ u, const double* __restrict__ t,
+                                          const double* __restrict__ fre, const double* __restrict__ fim,
+                                          double* __restrict__ out, int64_t n, int P) {
+  const int64_t total = (int64_t)P * n;
+  for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < total; i += (int64_t)gridDim.x * blockDim.x) {
+    const int64_t j = i / n, r = i - j * n;
+    const int64_t re = 2 * j * n + r, im = re + n;
+    const double c = fre[j], sn = fim[j], a = t[re], b = t[im];
+    out[re] = u[re] - (c * a - sn * b);
+    out[im] = u[im] - (sn * a + c * b);
+  }
+}
+
+int kr_fac_epilogue_batch(const double* u, const double* t, const double* fre, const double* fim, double* out,
+                          int64_t n, int P, cudaStream_t st) {
+  imps::count_launch();
+  fac_epilogue_batch_kernel<<<grid_for((int64_t)P * n), 256, 0, st>>>(u, t, fre, fim, out, n, P);
+  return IMPS_OK;
+}
+
 int kr_segsq(const KrylovWs& ws, const double* X, const int64_t* soff, const int64_t* slen, int ns,
              double* out, cudaStream_t st) {
   imps::count_launch();

@@ -537,6 +537,139 @@ class ExcitationsGPU:
         return out[:nev], conv and len(out) >= nev
 
 
+class ExcitationsBatchGPU:
+    """Excitation energies at P momenta together (the momentum loop of Excitations_main.cpp:255-297,
+    unprojected solves: K != 0 or p != 0).  The H_eff programs of the momenta have the same tables
+    and differ only in their alphas, so P copies of each (every slot but the shared operands offset
+    per copy) run as one grouped-GEMM launch per stage; the two environment solves of all momenta
+    are one GMRES each on the stacked systems with the mixed transfer matrix replicated 2P times
+    (one launch per stage for every plane of every momentum); the eigensolves are P Lanczos runs
+    in lockstep (imps_eigs_rs_batch_op), one batched H_eff apply per step."""
+
+    def __init__(self, ctx, AL, AR, NL, HLtot, HRtot, hnnz, d, xdims, kfacs, tol=1e-14, maxit=0):
+        import torch
+        self.torch, self.ctx = torch, ctx
+        self.kfacs = [complex(k) for k in kfacs]
+        P = self.P = len(self.kfacs)
+        self.tol, self.maxit = tol, maxit
+        # momentum 0's HeffGPU holds the operands (OPS), the single-plane mixed TM plans and their
+        # operand bindings; every momentum's program is compiled for its alphas
+        self.H0 = HeffGPU(ctx, AL, AR, NL, HLtot, HRtot, hnnz, d, xdims, self.kfacs[0], tol=tol, maxit=maxit)
+        prs = [self.H0.pr] + [HeffProgram(AL, AR, NL, HLtot, HRtot, hnnz, d, xdims, k) for k in self.kfacs[1:]]
+        self.pr = pr0 = prs[0]
+        self.sizes = S = {k: max(int(pr0.sizes.get(k, 0)), 1) for k in range(6)}
+        for pr in prs[1:]:
+            if {k: max(int(pr.sizes.get(k, 0)), 1) for k in range(6)} != S:
+                raise ValueError("the momenta's H_eff programs differ in their slot sizes")
+        self.mtot, self.nr, self.nl = pr0.mtot, pr0.nr, pr0.nl
+        if S[XS] != 2 * self.mtot or S[OUT] != 2 * self.mtot:
+            raise ValueError("unexpected X layout")
+        dev = lambda n: torch.zeros(max(int(n), 1), dtype=torch.float64, device="cuda")
+        self.buf = {k: (self.H0.buf[OPS] if k == OPS else dev(P * S[k])) for k in range(6)}
+        self.plan_a = self._batched_plan([pr.prog_a for pr in prs])
+        self.plan_b = self._batched_plan([pr.prog_b for pr in prs])
+        self.rep_r = ops.plan_replicate(self.H0.plan_r, 2 * P)
+        self.rep_l = ops.plan_replicate(self.H0.plan_l, 2 * P)
+        self.stats = {"gmres_iters": 0, "applies": 0}
+
+    def _batched_plan(self, progs):
+        """One imps_plan_program holding P copies of a program (structure of the first, alphas of
+        each), copy j's slots offset by j times their length (OPS shared)."""
+        P, S = self.P, self.sizes
+        tabs = [pg.tables() for pg in progs]
+        nouts0, outs0, terms0, _ = tabs[0]
+        for (no, ou, te, _) in tabs[1:]:
+            if not (np.array_equal(no, nouts0) and np.array_equal(ou, outs0) and np.array_equal(te, terms0)):
+                raise ValueError("the momenta's H_eff programs differ in structure (a special momentum?)")
+        shift = np.array([0 if k == OPS else S[k] for k in range(6)], np.int64)
+        nouts, outs, terms, alphas = [], [], [], []
+        o0 = t0 = 0
+        for st_n in nouts0:
+            so = outs0[o0:o0 + st_n]
+            nt = int(so[:, 6].sum())
+            stt = terms0[t0:t0 + nt]
+            for j in range(P):
+                oj = so.copy()
+                oj[:, 1] += j * shift[oj[:, 0]]
+                tj = stt.copy()
+                tj[:, 1] += j * shift[tj[:, 0]]
+                tj[:, 5] += j * shift[tj[:, 4]]
+                outs.append(oj)
+                terms.append(tj)
+                alphas.append(tabs[j][3][t0:t0 + nt])
+            nouts.append(P * int(st_n))
+            o0 += int(st_n)
+            t0 += nt
+        nouts = np.array(nouts, np.int32)
+        outs = np.ascontiguousarray(np.concatenate(outs) if outs else np.zeros((0, 7), np.int64))
+        terms = np.ascontiguousarray(np.concatenate(terms) if terms else np.zeros((0, 9), np.int64))
+        alphas = np.ascontiguousarray(np.concatenate(alphas) if alphas else np.zeros(0))
+        sizes = np.array([S[k] if k == OPS else P * S[k] for k in range(6)], np.int64)
+        h = C.c_void_p()
+        N.call("imps_plan_program", self.ctx.handle, 6, sizes.ctypes.data_as(N.P_i64), len(nouts),
+               nouts.ctypes.data_as(N.P_i32), outs.ctypes.data_as(N.P_i64), terms.ctypes.data_as(N.P_i64),
+               alphas.ctypes.data_as(N.P_dbl), C.byref(h))
+        plan = B.Plan(self.ctx, h, "program")
+        for k in range(6):
+            plan.bind(k, self.buf[k])
+        return plan
+
+    def apply(self):
+        """Y_j = H_eff(p_j) X_j for every momentum (XS -> OUT, copy j at j times the slot length)."""
+        P, S = self.P, self.sizes
+        self.plan_a.run()
+        (off_r, off_ri, nr), (off_l, off_li, nl) = self.pr.rhs_planes()
+        rhs, es = self.buf[RHS], self.buf[ES]
+        xr_re = [rhs[j * S[RHS] + off_r: j * S[RHS] + off_r + nr] for j in range(P)]
+        xr_im = [rhs[j * S[RHS] + off_ri: j * S[RHS] + off_ri + nr] for j in range(P)]
+        xl_re = [rhs[j * S[RHS] + off_l: j * S[RHS] + off_l + nl] for j in range(P)]
+        xl_im = [rhs[j * S[RHS] + off_li: j * S[RHS] + off_li + nl] for j in range(P)]
+        b = lambda j: j * S[ES]
+        yr_re = [es[b(j):b(j) + nr] for j in range(P)]
+        yr_im = [es[b(j) + nr:b(j) + 2 * nr] for j in range(P)]
+        yl_re = [es[b(j) + 2 * nr:b(j) + 2 * nr + nl] for j in range(P)]
+        yl_im = [es[b(j) + 2 * nr + nl:b(j) + 2 * nr + 2 * nl] for j in range(P)]
+        # the stacked residual bounds every system's: tol / sqrt(P) keeps each within tol
+        tol = self.tol / np.sqrt(P)
+        it, _, cr = ops.InvertE_fac_batch(self.rep_r, xr_re, xr_im, self.kfacs, yr_re, yr_im, tol, self.maxit)
+        self.stats["gmres_iters"] += it
+        it, _, cl = ops.InvertE_fac_batch(self.rep_l, xl_re, xl_im, [k.conjugate() for k in self.kfacs], yl_re,
+                                          yl_im, tol, self.maxit)
+        self.stats["gmres_iters"] += it
+        self.plan_b.run()
+        self.stats["applies"] += 1
+        return cr and cl
+
+    def energies(self, nev=4, eig_tol=1e-10, ncv=64, seed=1):
+        """The nev lowest energies at every momentum (list of lists) and per-momentum convergence,
+        from the real form of each Hermitian H_eff (eigenvalues doubled; 2 nev Ritz pairs kept, the
+        nev lowest distinct values returned), every momentum started from the same seeded vector
+        as ExcitationsGPU.energies."""
+        import torch
+        P, n = self.P, 2 * self.mtot
+        xs, out = self.buf[XS], self.buf[OUT]
+
+        def apply(pin, pout):
+            N.call("imps_axpby", self.ctx.handle, 1.0, C.c_void_p(pin), 0.0, C.c_void_p(xs.data_ptr()), P * n)
+            if not self.apply():
+                raise RuntimeError("environment solve did not converge")
+            N.call("imps_axpby", self.ctx.handle, 1.0, C.c_void_p(out.data_ptr()), 0.0, C.c_void_p(pout), P * n)
+
+        g = torch.Generator(device="cpu").manual_seed(seed)
+        x0 = torch.randn(n, generator=g, dtype=torch.float64)
+        X = x0.repeat(P).to("cuda")
+        want = min(2 * nev, n - 1)
+        ev, na, conv = ops.eigs_rs_batch_op(self.ctx, P, n, apply, X, nev=want, tol=eig_tol, ncv=ncv)
+        res = []
+        for j in range(P):
+            vals = []
+            for v in sorted(ev[j]):
+                if not vals or abs(v - vals[-1]) > 10 * eig_tol * max(abs(v), 1.0):
+                    vals.append(v)
+            res.append(vals[:nev])
+        return res, [c and len(r) >= nev for c, r in zip(conv, res)], na
+
+
 def save_alrn(v, inp, name, ending="bin", folder="."):
     """saveALRN as the excitation driver writes it (Excitations_main.cpp:232-237): the ground
     state the excitations of ``inp`` (excitation_inputs) are built from, with C[n] the centre

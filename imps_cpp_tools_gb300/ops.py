@@ -232,3 +232,49 @@ def GradNormRight(plan):
     F = C.c_double()
     N.call("imps_grad_norm_right", plan.handle, C.byref(F))
     return F.value
+
+
+def plan_replicate(plan, copies):
+    """imps_plan_replicate: a plan that applies `plan` to `copies` inputs in one launch per stage
+    (inputs, outputs and scratch `copies` times as long, operators shared)."""
+    from . import blocks as B
+    h = C.c_void_p()
+    N.call("imps_plan_replicate", plan.handle, int(copies), C.byref(h))
+    return B.Plan(plan.ctx, h, "replicated")
+
+
+def InvertE_fac_batch(rep, xs_re, xs_im, facs, ys_re, ys_im, tol, maxit=0, krylov=0):
+    """InvertE_fac (InvEBlockFunctions.hpp:346-476) for P momenta at once on a replicated mixed-TM
+    plan (plan_replicate(tm, 2P)): (1 - f_j T) y_j = x_j.  xs_*, ys_*: lists of P device tensors
+    (ys_*: initial guesses, overwritten with the solutions).  Returns (iterations, relative
+    residual of the stacked system, converged)."""
+    P = len(facs)
+    ptrs = lambda lst: (C.c_void_p * P)(*[t.data_ptr() for t in lst])
+    fre = (C.c_double * P)(*[complex(f).real for f in facs])
+    fim = (C.c_double * P)(*[complex(f).imag for f in facs])
+    it, rr = C.c_int(), C.c_double()
+    st = N.call("imps_invert_e_fac_batch", rep.handle, P, ptrs(xs_re), ptrs(xs_im), fre, fim, ptrs(ys_re),
+                ptrs(ys_im), float(tol), int(maxit), int(krylov), C.byref(it), C.byref(rr))
+    return it.value, rr.value, st == 0
+
+
+def eigs_rs_batch_op(ctx, P, n, apply, X, nev=1, tol=1e-12, ncv=0, maxit=0):
+    """The nev lowest eigenpairs of P symmetric operators at once (imps_eigs_rs_batch_op): apply(in_ptr,
+    out_ptr) applies all P operators to P consecutive device vectors of length n.  X: device (P, n)
+    start vectors, on return each system's lowest Ritz vector.  Returns (eigenvalues as a (P, nev)
+    array, batched applies, per-system convergence flags)."""
+    ev = (C.c_double * (P * nev))()
+    na = C.c_int()
+    conv = (C.c_int * P)()
+
+    def cb(user, pin, pout):
+        try:
+            apply(pin, pout)
+            return 0
+        except Exception:  # a failing apply aborts the solve with an error status
+            return -3
+
+    fn = N.APPLY_FN(cb)
+    N.call("imps_eigs_rs_batch_op", ctx.handle, int(P), int(n), fn, None, _dptr(X), int(nev), float(tol), int(ncv),
+           int(maxit), ev, C.byref(na), conv)
+    return np.array(list(ev)).reshape(P, nev), na.value, [bool(conv[i]) for i in range(P)]

@@ -137,6 +137,11 @@ int imps_plan_derived_layout(const imps_plan* P, int which, imps_layout** out);
 int imps_plan_info(const imps_plan* P, int64_t* flops_apply, int64_t* flops_prep,
                    int64_t* dropped, int* nslots, int* nstages);
 int imps_plan_slot_info(const imps_plan* P, int slot, int* kind, int64_t* nelem);
+/* A plan applying `src` to `copies` inputs at once (no counterpart in the reference): every stage
+ * of src repeated per copy in one launch, the input, output and scratch slots `copies` times as
+ * long (copy c at offset c x src's length), the operator slots shared (bindings copied).  src
+ * must have no prepare stages (TM and mixed-TM plans).  Destroy with imps_plan_destroy. */
+int imps_plan_replicate(const imps_plan* src, int copies, imps_plan** out);
 /* bind a device pointer to an external slot (kept until rebound or the plan is destroyed) */
 int imps_plan_bind(imps_plan* P, int slot, double* device_ptr);
 int imps_plan_prepare(imps_plan* P);
@@ -191,6 +196,14 @@ typedef int (*imps_apply_fn)(void* user, const double* in, double* out);
  * [re; im] (every eigenvalue twice; a Lanczos run from one start vector finds each once). */
 int imps_eigs_rs_op(imps_ctx* ctx, int64_t n, imps_apply_fn fn, void* user, double* x, int mem, int nev,
                     double tol, int ncv, int maxit, double* evals, double* evecs, int* n_applies);
+/* The lowest nev eigenpairs of P independent symmetric operators at once (Excitations_main.cpp:
+ * 255-297 solves one eigs_n per momentum; here all momenta advance together): P thick-restart
+ * Lanczos runs in lockstep, every step one callback fn(user, in, out) applying all P operators to
+ * P vectors of length n stored one after the other (device).  X (device, P x n): start vectors
+ * on entry, the normalised lowest Ritz vector of each system on exit; evals (host, P x nev);
+ * converged (host, P, optional).  Returns IMPS_OK when every system converged. */
+int imps_eigs_rs_batch_op(imps_ctx* ctx, int P, int64_t n, imps_apply_fn fn, void* user, double* X, int nev,
+                          double tol, int ncv, int maxit, double* evals, int* n_applies, int* converged);
 /* eigs_n(fun, N, vals, vecs, nev, whch, tol, x0) (eigs.cpp:193-342, real nonsymmetric
  * operator, ARPACK dnaupd/dneupd) on the device: Arnoldi with CGS2 orthogonalisation and a
  * Krylov-Schur restart, convergence as dnaupd (Ritz estimate <= tol max(eps^(2/3), |theta|)),
@@ -230,6 +243,16 @@ int imps_invert_e_fac(imps_plan* tmx, const double* x_re, const double* x_im, do
 int imps_invert_e_proj_fac(imps_plan* tmx, const double* x_re, const double* x_im, const double* L,
                            const double* R, int dir, double fac_re, double fac_im, double* y_re, double* y_im,
                            int mem, double tol, int maxit, int krylov, int* iters, double* relres);
+/* InvertE_fac (InvEBlockFunctions.hpp:346-476) for P systems (1 - f_j T) y_j = x_j at once, one
+ * per momentum of the excitation ansatz (Excitations_main.cpp:255-297 runs them one momentum at a
+ * time): one restarted GMRES on the stacked [re_j; im_j] planes, whose every iteration applies T
+ * to all 2P planes in one launch per stage of `rep`, a plan made by imps_plan_replicate(tm, 2P)
+ * from the mixed TM plan.  x_*, y_* (device, P pointers each, n elements): right-hand sides;
+ * initial guesses on entry, solutions on exit.  fac_re / fac_im (host, P).  The stopping test is
+ * on the stacked residual: |r| <= tol |b|. */
+int imps_invert_e_fac_batch(imps_plan* rep, int P, const double* const* x_re, const double* const* x_im,
+                            const double* fac_re, const double* fac_im, double* const* y_re, double* const* y_im,
+                            double tol, int maxit, int krylov, int* iters, double* relres);
 /* TMDominantEig (EigsBlockFunctions.hpp:91-172) for a left/right-isometric unit cell: the
  * dominant eigenvalue is 1 and the fixed point solves (1 - T + |x0)(1|) v = x0; v is
  * normalised to unit trace as in the reference.  x0 may be NULL (identity). */

@@ -247,3 +247,32 @@ def test_autotune_needs_a_device():
     assert N.load().imps_plan_autotune(plan.handle, 3, C.byref(n)) == -6
     tile, splits, key = plan.stage_shape(0)
     assert tile in (16, 32) and splits >= 1 and key != 0
+
+
+def test_plan_replicate_tables():
+    """imps_plan_replicate (host-only context: tables only): every stage repeated per copy, the
+    input / output / scratch offsets shifted by the copy index times the slot's length, the
+    operator slots shared."""
+    from imps_cpp_tools_gb300 import ops
+    ctx = B.Context(-1)
+    I2K = [(1,), (-1,)]
+    b0 = {(-1,): 2, (1,): 3}
+    b1 = {(0,): 4, (2,): 1, (-2,): 2}
+    la = B.Layout.mps(I2K, b0, b1)
+    lb = B.Layout.mps(I2K, b1, b0)
+    src = B.plan_tm(ctx, [la, lb], 0, B.Layout.blockdiag(b0), B.Layout.blockdiag(b0))
+    rep = ops.plan_replicate(src, 3)
+    nst = src.info()["nstages"]
+    assert rep.info()["nstages"] == nst
+    per = {0, 1} | {s for s in range(src.info()["nslots"]) if s > 3}  # in, out, and the plan's scratch
+    for st in range(nst):
+        a, b = src.table(st), rep.table(st)
+        assert len(b) == 3 * len(a)
+        for c in range(3):
+            for (tag, terms), (tag2, terms2) in zip(a, b[c * len(a):(c + 1) * len(a)]):
+                assert tag == tag2 and len(terms) == len(terms2)
+                for (sa, oa, sb, ob, k, al), (sa2, oa2, sb2, ob2, k2, al2) in zip(terms, terms2):
+                    assert (sa, sb, k, al) == (sa2, sb2, k2, al2)
+                    assert oa2 == oa + (c * src.slot_nelem(sa) if sa in per else 0)
+                    assert ob2 == ob + (c * src.slot_nelem(sb) if sb in per else 0)
+    assert rep.info()["flops_apply"] == 3 * src.info()["flops_apply"]
