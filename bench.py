@@ -16,8 +16,9 @@ of the sweeps (the path does not shard); the step time is the maximum over ranks
 N / that time.
 
 --mode hac times H_AC applies only (ApplyHAvec; a step = 20 applies).
---mode excitations converges the XXZ D=256 ground state and times the 4 lowest excitation
-energies in the Sz = +1 sector at --steps momenta (H_eff compiled into grouped-GEMM programs).
+--mode excitations grows the XXZ D=256 ground state by bond expansion and times the 4 lowest Sz = +1
+excitation energies at 32 momenta in one batched run, beside the per-momentum path on --steps
+of them.
 --mode expand times one bond expansion (ExpandFromH, dmmax 20) at the XXZ D=512 and Hubbard
 D=1024 starts against the oracle on the same state.
 --mode trace runs the timed FP64 sweeps under torch.profiler: summed kernel time against wall time,
@@ -672,55 +673,80 @@ def run_krylov(args):
 
 
 def run_excitations(args):
-    """Excitation energies on a converged ground state (Excitations_main.cpp:255-297): XXZ D=256
-    (17 U(1) sectors, dims ~exp(-q^2/10)) converged by VumpsGPU to |grad| < 1e-10 (at most 120
-    sweeps), then for a sample of momenta p in [0, pi] the 4 lowest energies of H_eff in the
-    Sz = +1 sector (charge label K = 2) by the device Lanczos on H_eff's real form."""
+    """Excitation energies (Excitations_main.cpp:255-297), configs' excitation workload: the XXZ
+    ground state at D=256 grown by bond expansion (ExpandFromH, VUMPS_main.cpp:270-308) from D=32
+    and converged to |grad| < 1e-10; then the 4 lowest Sz = +1 energies (charge label K = 2) at 32
+    momenta p = pi (k + 1/2) / 32, k = 0..31, all momenta in one batched run (ExcitationsBatchGPU:
+    one launch per H_eff program stage and per transfer-matrix stage for every momentum, the
+    Lanczos runs in lockstep).  Beside it: the per-momentum path (ExcitationsGPU) on --steps of
+    the momenta (time per momentum, energy agreement) and one H_eff apply of the oracle on the
+    host (the CPU cost per apply)."""
     import torch
     from imps_cpp_tools_gb300 import blocks as B
     from imps_cpp_tools_gb300 import configs
-    from imps_cpp_tools_gb300.excitations import ExcitationsGPU, HeffGPU, excitation_inputs
+    from imps_cpp_tools_gb300.excitations import ExcitationsBatchGPU, ExcitationsGPU, excitation_inputs
     from imps_cpp_tools_gb300.vumps import VumpsGPU
     ctx = B.Context(0)
     ctx.set_stream(torch.cuda.current_stream())
-    model, fn, params = configs.WORKLOADS["xxz_d256"]
     t0 = time.perf_counter()
-    v = VumpsGPU(ctx, model, dims0=fn(), seed=1, tolmin=1e-12, InvETol=1e-12, **params)
-    nsw = 0
-    for nsw in range(1, 121):
+    v = VumpsGPU(ctx, "xxz", dims0=configs.xxz_bond_dims(32, 4, 4.0), seed=1, tolmin=1e-12, InvETol=1e-12, mmax=256,
+                 dmmax=32, expand_pause=3, J=1.0, Delta=-1.0)
+    nsw, F = 0, None
+    for nsw in range(1, 301):
         E, F, _ = v.sweep()
-        if F.max() < 1e-10:
+        D = sum(v.LB[0].dims().values())
+        if D >= 256 and F.max() < 1e-10:
             break
     torch.cuda.synchronize()
     t_gs = time.perf_counter() - t0
-    t0 = time.perf_counter()
     inp = excitation_inputs(v, (2,), tol=1e-12)
+    args_ = (inp["AL"], inp["AR"], inp["NL"], inp["HLtot"], inp["HRtot"], inp["h"], inp["d"], inp["xdims"])
+    P = 32
+    ps = [np.pi * (k + 0.5) / P for k in range(P)]
+    kfs = [np.exp(1j * p) for p in ps]
+    tb = time.perf_counter()
+    ex = ExcitationsBatchGPU(ctx, *args_, kfs, tol=1e-12)
+    t_build = time.perf_counter() - tb
+    tb = time.perf_counter()
+    ev_b, conv_b, na_b = ex.energies(nev=4, eig_tol=1e-10)
     torch.cuda.synchronize()
-    t_inp = time.perf_counter() - t0
-    ex = ExcitationsGPU(ctx, inp["AL"], inp["AR"], inp["NL"], inp["HLtot"], inp["HRtot"], inp["h"], inp["d"],
-                        inp["xdims"], tol=1e-12)
-    ps = np.linspace(0.0, np.pi, max(args.steps, 1) + 2)[1:-1]
-    rows, t_tot = [], 0.0
-    for p in ps:
-        # compile + solve; the compile (host sector matching) is reported separately
-        tc = time.perf_counter()
-        HeffGPU(ctx, *ex.args, np.exp(1j * p), tol=1e-12)
-        t_compile = time.perf_counter() - tc
-        a0 = ex.applies
-        tq = time.perf_counter()
-        ev, conv = ex.energies(np.exp(1j * p), nev=4, eig_tol=1e-10)
+    t_batch = time.perf_counter() - tb
+    # the per-momentum path on a sample of the momenta
+    single = ExcitationsGPU(ctx, *args_, tol=1e-12)
+    sample = [int(round(x)) for x in np.linspace(0, P - 1, max(1, min(args.steps, P)))]
+    rows, t_single = [], 0.0
+    for k in sample:
+        ts = time.perf_counter()
+        ev, conv = single.energies(kfs[k], nev=4, eig_tol=1e-10)
         torch.cuda.synchronize()
-        dt = time.perf_counter() - tq
-        t_tot += dt
-        rows.append({"p": float(p), "energies": [float(x) for x in ev], "converged": bool(conv), "s": dt,
-                     "compile_s": t_compile, "heff_applies": ex.applies - a0})
-    napp = sum(r["heff_applies"] for r in rows)
+        dt = time.perf_counter() - ts
+        t_single += dt
+        rows.append({"p": ps[k], "s": dt, "max_abs_diff_vs_batched": float(np.abs(np.array(ev) - np.array(ev_b[k])).max()),
+                     "converged": bool(conv)})
+    # CPU: one H_eff apply of the oracle on the same inputs (host copies)
+    cpu = None
+    if not args.no_cpu:
+        from oracle import imps_oracle as O
+        rng = np.random.default_rng(1)
+        X = [{qi: (qo, rng.standard_normal((ml, mr)) + 1j * rng.standard_normal((ml, mr))) for (qi, qo, ml, mr) in dd}
+             for dd in inp["xdims"]]
+        tc = time.perf_counter()
+        O.ApplyHeff(X, kfs[0], inp["AL"], inp["AR"], inp["NL"], inp["h"], inp["d"], inp["HLtot"], inp["HRtot"], tol=1e-12)
+        cpu = {"s_per_heff_apply": time.perf_counter() - tc, "cores": os.cpu_count(), "kind": "port"}
     mtot = sum(r * c for dd in inp["xdims"] for (_, _, r, c) in dd)
-    print(json.dumps({"mode": "excitations", "workload": "XXZ D=256 ground state (VumpsGPU, %d sweeps, |grad| "
-                      "%.1e), K = Sz +1, 4 lowest states" % (nsw, float(F.max())), "mtot": mtot,
-                      "ground_state_s": t_gs, "inputs_s": t_inp, "momenta": rows,
-                      "s_per_momentum": t_tot / max(len(rows), 1), "ms_per_heff_apply": 1e3 * t_tot / max(napp, 1),
-                      "E0": inp["E0"]}), flush=True)
+    t_per_single = t_single / max(len(rows), 1)
+    print(json.dumps({"mode": "excitations", "metric": "excitation energies, 32 momenta x 4 bands (s per run)",
+                      "workload": "XXZ D=%d ground state (VumpsGPU with ExpandFromH from D=32, %d sweeps, |grad| "
+                      "%.1e, E=%.10f), K = Sz +1, 4 lowest states, p = pi (k + 1/2)/32"
+                      % (sum(v.LB[0].dims().values()), nsw, float(F.max()), float(E.mean())),
+                      "mtot": mtot, "ground_state_s": t_gs, "batched": {
+                          "momenta": P, "s": t_batch, "build_s": t_build, "batched_applies": na_b,
+                          "gmres_iters": ex.stats["gmres_iters"], "converged": all(conv_b),
+                          "energies": [[float(x) for x in e] for e in ev_b], "p": ps},
+                      "per_momentum": {"sampled": rows, "s_per_momentum": t_per_single,
+                                       "s_for_32_extrapolated": t_per_single * P},
+                      "speedup_batched_vs_per_momentum": t_per_single * P / t_batch,
+                      "cpu_baseline": cpu, "E0": inp["E0"]}), flush=True)
 
 
 def run_adjoint(args):
