@@ -1968,6 +1968,174 @@ int imps_invert_e_proj_fac(imps_plan* p, const double* x_re, const double* x_im,
                          iters, relres);
 }
 
+// Restarted GMRES on P independent systems in lockstep.  Every iteration applies the operators
+// of all systems at once (Ab: stacked input -> stacked output, system s at s * n), then runs each
+// system's CGS step on its own Krylov basis; the Givens rotations of every system run on the
+// host at the checks (every 4 iterations), as in gmres_dev.  A system whose cycle met its
+// tolerance stops extending its basis while the others go on; every system restarts from its
+// recomputed residual.  Returns the largest iteration count and relative residual.
+using BatchOp = std::function<int(const double* in, double* out)>;
+static int gmres_batch(imps_ctx* c, int P, int64_t n, const BatchOp& Ab, const double* b, double* y, double tol,
+                       int maxit, int krylov, int* iters, double* relres, Bump& bp) {
+  cudaStream_t st = c->stream;
+  int m = krylov > 0 ? krylov : kGmresKrylov;
+  if (m > kMaxCols - 2) m = kMaxCols - 2;
+  if (m > n) m = (int)n;
+  const int ld = m + 1;
+  const int64_t ntot = (int64_t)P * n;
+  double* V = bp.take((size_t)ntot * (m + 1));  // system s: V + s * n * (m + 1)
+  double* U = bp.take(ntot);
+  double* W = bp.take(ntot);
+  double* Tm = bp.take(n);
+  double* Hd = bp.take((size_t)P * ld * m);
+  double* tmp = bp.take(ld);
+  double* ys = bp.take(ld);
+  double* nrm = bp.take(P);
+  auto Vs = [&](int sy) { return V + (size_t)sy * n * (m + 1); };
+  struct Sys {
+    std::vector<double> Rh, gh, yh, csh, snh;
+    double bnorm = 0.0, rn = 0.0, rn_prev = 0.0;
+    int stall = 0, kdim = 0, jpulled = 0, it = 0;
+    bool done = false, in_cycle = false, inner_hit = false;
+  };
+  std::vector<Sys> sys(P);
+  std::vector<double> hnorm(P), col(ld + 1);
+  for (Sys& q : sys) {
+    q.Rh.assign((size_t)ld * ld, 0.0); q.gh.assign(ld, 0.0); q.yh.assign(ld, 0.0);
+    q.csh.assign(ld, 0.0); q.snh.assign(ld, 0.0);
+  }
+  auto norms = [&](const double* X, std::vector<double>& out) -> int {
+    for (int sy = 0; sy < P; ++sy) RC(kr_multidot(c->ws, X + (size_t)sy * n, n, 1, X + (size_t)sy * n, n, tmp, 0,
+                                                  nrm + sy, st));
+    CK(cudaMemcpyAsync(out.data(), nrm, P * 8, cudaMemcpyDeviceToHost, st));
+    CK(cudaStreamSynchronize(st));
+    return IMPS_OK;
+  };
+  RC(norms(b, hnorm));
+  for (int sy = 0; sy < P; ++sy) {
+    sys[sy].bnorm = hnorm[sy];
+    if (!std::isfinite(hnorm[sy])) return IMPS_ERR_NAN;
+    if (hnorm[sy] == 0.0) {
+      CK(cudaMemsetAsync(y + (size_t)sy * n, 0, n * 8, st));
+      sys[sy].done = true;
+    }
+  }
+  int it = 0;
+  auto any_open = [&]() { for (const Sys& q : sys) if (!q.done) return true; return false; };
+  for (int outer = 0; any_open() && it < maxit; ++outer) {
+    // r = b - A(y) for every system
+    RC(Ab(y, W));
+    RC(kr_axpby(1.0, b, -1.0, W, ntot, st));
+    RC(norms(W, hnorm));
+    for (int sy = 0; sy < P; ++sy) {
+      Sys& q = sys[sy];
+      q.in_cycle = false;
+      if (q.done) continue;
+      q.rn = hnorm[sy];
+      if (!std::isfinite(q.rn)) return IMPS_ERR_NAN;
+      if (q.rn < tol * q.bnorm) { q.done = true; continue; }
+      // the stagnation rule of gmres_dev, per system
+      q.stall = outer > 0 && q.inner_hit && q.rn > 0.9 * q.rn_prev ? q.stall + 1 : 0;
+      q.rn_prev = q.rn;
+      if (q.stall >= 3) { q.done = true; continue; }
+      q.inner_hit = false;
+      q.in_cycle = true;
+      q.kdim = 0;
+      q.jpulled = 0;
+      std::fill(q.gh.begin(), q.gh.end(), 0.0);
+      q.gh[0] = q.rn;
+      RC(kr_scale_inv(W + (size_t)sy * n, nrm + sy, Vs(sy), n, nullptr, st));
+    }
+    for (int j = 0; j < m && it < maxit; ++j) {
+      bool any = false;
+      for (int sy = 0; sy < P; ++sy)
+        if (sys[sy].in_cycle) {
+          any = true;
+          CK(cudaMemcpyAsync(U + (size_t)sy * n, Vs(sy) + (size_t)j * n, n * 8, cudaMemcpyDeviceToDevice, st));
+        }
+      if (!any) break;
+      RC(Ab(U, W));
+      ++it;
+      for (int sy = 0; sy < P; ++sy) {
+        Sys& q = sys[sy];
+        if (!q.in_cycle) continue;
+        RC(kr_cgs2_step(c->ws, Vs(sy), n, j + 1, W + (size_t)sy * n, n, Hd + (size_t)sy * ld * m + (size_t)j * ld,
+                        tmp, Vs(sy) + (size_t)(j + 1) * n, nullptr, st));
+        q.kdim = j + 1;
+        ++q.it;
+      }
+      if (!((j + 1) % 4 == 0 || j == m - 1 || it >= maxit)) continue;
+      CK(cudaStreamSynchronize(st));
+      for (int sy = 0; sy < P; ++sy) {
+        Sys& q = sys[sy];
+        if (!q.in_cycle) continue;
+        CK(cudaMemcpy(c->hpin_g, Hd + (size_t)sy * ld * m + (size_t)q.jpulled * ld,
+                      (size_t)(j + 1 - q.jpulled) * ld * 8, cudaMemcpyDeviceToHost));
+        double res = 0.0;
+        bool brk = false;
+        for (int qq = q.jpulled; qq <= j; ++qq) {
+          const double* hc = c->hpin_g + (size_t)(qq - q.jpulled) * ld;
+          for (int i = 0; i <= qq + 1; ++i) col[i] = hc[i];
+          for (int i = 0; i < qq; ++i) {
+            const double h1 = col[i], h2 = col[i + 1];
+            col[i] = q.csh[i] * h1 + q.snh[i] * h2;
+            col[i + 1] = -q.snh[i] * h1 + q.csh[i] * h2;
+          }
+          const double hqq = col[qq], hq1 = col[qq + 1];
+          const double beta = std::sqrt(hqq * hqq + hq1 * hq1);
+          if (!std::isfinite(beta)) return IMPS_ERR_NAN;
+          if (!(beta >= 2e-16)) { brk = true; q.kdim = qq; break; }
+          const double habs = std::fabs(hqq);
+          const double phase = habs > 0.0 ? hqq / habs : 1.0;
+          q.snh[qq] = phase * hq1 / beta;
+          q.csh[qq] = habs / beta;
+          col[qq] = phase * beta;
+          q.gh[qq + 1] = -q.snh[qq] * q.gh[qq];
+          q.gh[qq] *= q.csh[qq];
+          for (int i = 0; i <= qq; ++i) q.Rh[i + (size_t)qq * ld] = col[i];
+          res = std::fabs(q.gh[qq + 1]);
+        }
+        q.jpulled = j + 1;
+        if (brk) { q.in_cycle = false; continue; }
+        if (res < tol * q.bnorm) { q.inner_hit = true; q.in_cycle = false; }
+      }
+    }
+    // y_s += V_s[:, :kdim] R^{-1} gamma for every system that extended its basis this cycle
+    for (int sy = 0; sy < P; ++sy) {
+      Sys& q = sys[sy];
+      if (q.done || q.kdim <= 0) continue;
+      for (int i = q.kdim - 1; i >= 0; --i) {
+        double sacc = q.gh[i];
+        for (int qq = i + 1; qq < q.kdim; ++qq) sacc -= q.Rh[i + (size_t)qq * ld] * q.yh[qq];
+        q.yh[i] = sacc / q.Rh[i + (size_t)i * ld];
+      }
+      CK(cudaMemcpy(ys, q.yh.data(), q.kdim * 8, cudaMemcpyHostToDevice));
+      RC(kr_gemv(Vs(sy), n, q.kdim, ys, Tm, n, st));
+      RC(kr_axpby(1.0, Tm, 1.0, y + (size_t)sy * n, n, st));
+      CK(cudaStreamSynchronize(st));  // ys and Tm are reused by the next system
+      q.kdim = 0;
+    }
+  }
+  // final residuals
+  RC(Ab(y, W));
+  RC(kr_axpby(1.0, b, -1.0, W, ntot, st));
+  RC(norms(W, hnorm));
+  double worst = 0.0;
+  bool ok = true;
+  for (int sy = 0; sy < P; ++sy) {
+    const Sys& q = sys[sy];
+    const double r = q.bnorm > 0.0 ? hnorm[sy] / q.bnorm : 0.0;
+    worst = std::max(worst, r);
+    ok = ok && r < tol;
+  }
+  if (iters) *iters = it;
+  if (relres) *relres = worst;
+  if (debug_on())
+    fprintf(stderr, "[imps gmres_batch] P=%d n=%lld iters=%d worst relres=%.3e tol=%.1e\n", P, (long long)n, it,
+            worst, tol);
+  return ok ? IMPS_OK : IMPS_WARN_NOT_CONVERGED;
+}
+
 int imps_invert_e_fac_batch(imps_plan* rep, int P, const double* const* x_re, const double* const* x_im,
                             const double* fac_re, const double* fac_im, double* const* y_re, double* const* y_im,
                             double tol, int maxit, int krylov, int* iters, double* relres) {
@@ -1976,12 +2144,12 @@ int imps_invert_e_fac_batch(imps_plan* rep, int P, const double* const* x_re, co
   if (c->device < 0) return IMPS_ERR_NO_DEVICE;
   const int64_t ntot = rep->P.slots[rep->P.n_in].nelem;
   if (ntot % (2 * (int64_t)P) || rep->P.slots[rep->P.n_out].nelem != ntot) return IMPS_ERR_BAD_ARG;
-  const int64_t n = ntot / (2 * (int64_t)P);
+  const int64_t n = ntot / (2 * (int64_t)P);  // one plane; a system is [re | im], 2n
   cudaStream_t st = c->stream;
   int m = krylov > 0 ? std::min(krylov, kMaxCols - 2) : kGmresKrylov;
-  if (maxit <= 0) maxit = (int)std::min<int64_t>(ntot, 100000);
-  RC(arena_reserve(c, round256(ntot * 8) * (m + 12) + round256((size_t)(m + 1) * (m + 1) * 8) +
-                          2 * round256((size_t)P * 8) + 16 * 4096));
+  if (maxit <= 0) maxit = (int)std::min<int64_t>(2 * n, 100000);
+  RC(arena_reserve(c, round256(ntot * 8) * (m + 6) + round256(2 * n * 8) + round256((size_t)P * (m + 1) * (m + 1) * 8) +
+                          4 * round256((size_t)P * 8) + 16 * 4096));
   Bump bp{c->arena};
   double* b = bp.take(ntot);
   double* y = bp.take(ntot);
@@ -1997,13 +2165,13 @@ int imps_invert_e_fac_batch(imps_plan* rep, int P, const double* const* x_re, co
     CK(cudaMemcpyAsync(y + (2 * j + 1) * n, y_im[j], n * 8, cudaMemcpyDeviceToDevice, st));
   }
   // one apply of the replicated transfer matrix takes every plane of every system
-  DevOp A = [&](const double* u, double* out, bool) -> int {
+  BatchOp A = [&](const double* u, double* out) -> int {
     RC(apply_dev(rep, u, t));
     return kr_fac_epilogue_batch(u, t, dfr, dfi, out, n, P, st);
   };
   const int prec_saved = rep->prec;
   rep->prec = IMPS_PREC_FP64;
-  const int rc = gmres_dev(c, ntot, A, false, b, y, tol, maxit, m, iters, relres, bp);
+  const int rc = gmres_batch(c, P, 2 * n, A, b, y, tol, maxit, m, iters, relres, bp);
   rep->prec = prec_saved;
   if (rc < 0) return rc;
   for (int j = 0; j < P; ++j) {

@@ -542,12 +542,13 @@ class ExcitationsBatchGPU:
     unprojected solves: K != 0 or p != 0).  The H_eff programs of the momenta have the same tables
     and differ only in their alphas, so P copies of each (every slot but the shared operands offset
     per copy) run as one grouped-GEMM launch per stage; the two environment solves of all momenta
-    are one GMRES each on the stacked systems with the mixed transfer matrix replicated 2P times
-    (one launch per stage for every plane of every momentum); the eigensolves are P Lanczos runs
-    in lockstep (imps_eigs_rs_batch_op), one batched H_eff apply per step."""
+    are P GMRES runs in lockstep with the mixed transfer matrix replicated 2P times (one launch per
+    stage for every plane of every momentum, imps_invert_e_fac_batch); the eigensolves are P
+    Lanczos runs in lockstep (imps_eigs_rs_batch_op), one batched H_eff apply per step."""
 
-    def __init__(self, ctx, AL, AR, NL, HLtot, HRtot, hnnz, d, xdims, kfacs, tol=1e-14, maxit=0):
+    def __init__(self, ctx, AL, AR, NL, HLtot, HRtot, hnnz, d, xdims, kfacs, tol=1e-14, maxit=0, verbose=False):
         import torch
+        self.verbose = verbose
         self.torch, self.ctx = torch, ctx
         self.kfacs = [complex(k) for k in kfacs]
         P = self.P = len(self.kfacs)
@@ -629,8 +630,7 @@ class ExcitationsBatchGPU:
         yr_im = [es[b(j) + nr:b(j) + 2 * nr] for j in range(P)]
         yl_re = [es[b(j) + 2 * nr:b(j) + 2 * nr + nl] for j in range(P)]
         yl_im = [es[b(j) + 2 * nr + nl:b(j) + 2 * nr + 2 * nl] for j in range(P)]
-        # the stacked residual bounds every system's: tol / sqrt(P) keeps each within tol
-        tol = self.tol / np.sqrt(P)
+        tol = self.tol
         it, _, cr = ops.InvertE_fac_batch(self.rep_r, xr_re, xr_im, self.kfacs, yr_re, yr_im, tol, self.maxit)
         self.stats["gmres_iters"] += it
         it, _, cl = ops.InvertE_fac_batch(self.rep_l, xl_re, xl_im, [k.conjugate() for k in self.kfacs], yl_re,
@@ -638,6 +638,10 @@ class ExcitationsBatchGPU:
         self.stats["gmres_iters"] += it
         self.plan_b.run()
         self.stats["applies"] += 1
+        if self.verbose and self.stats["applies"] % 20 == 0:
+            import sys
+            print(f"[excitations batch] {self.stats['applies']} applies, {self.stats['gmres_iters']} GMRES iterations",
+                  file=sys.stderr, flush=True)
         return cr and cl
 
     def energies(self, nev=4, eig_tol=1e-10, ncv=64, seed=1):

@@ -246,8 +246,8 @@ def plan_replicate(plan, copies):
 def InvertE_fac_batch(rep, xs_re, xs_im, facs, ys_re, ys_im, tol, maxit=0, krylov=0):
     """InvertE_fac (InvEBlockFunctions.hpp:346-476) for P momenta at once on a replicated mixed-TM
     plan (plan_replicate(tm, 2P)): (1 - f_j T) y_j = x_j.  xs_*, ys_*: lists of P device tensors
-    (ys_*: initial guesses, overwritten with the solutions).  Returns (iterations, relative
-    residual of the stacked system, converged)."""
+    (ys_*: initial guesses, overwritten with the solutions).  P GMRES runs in lockstep.  Returns
+    (lockstep iterations, the largest relative residual, every system converged)."""
     P = len(facs)
     ptrs = lambda lst: (C.c_void_p * P)(*[t.data_ptr() for t in lst])
     fre = (C.c_double * P)(*[complex(f).real for f in facs])

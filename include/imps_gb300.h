@@ -245,11 +245,12 @@ int imps_invert_e_proj_fac(imps_plan* tmx, const double* x_re, const double* x_i
                            int mem, double tol, int maxit, int krylov, int* iters, double* relres);
 /* InvertE_fac (InvEBlockFunctions.hpp:346-476) for P systems (1 - f_j T) y_j = x_j at once, one
  * per momentum of the excitation ansatz (Excitations_main.cpp:255-297 runs them one momentum at a
- * time): one restarted GMRES on the stacked [re_j; im_j] planes, whose every iteration applies T
- * to all 2P planes in one launch per stage of `rep`, a plan made by imps_plan_replicate(tm, 2P)
- * from the mixed TM plan.  x_*, y_* (device, P pointers each, n elements): right-hand sides;
- * initial guesses on entry, solutions on exit.  fac_re / fac_im (host, P).  The stopping test is
- * on the stacked residual: |r| <= tol |b|. */
+ * time): P restarted GMRES runs in lockstep, each on its own Krylov basis of [re_j; im_j], every
+ * iteration applying T to all 2P planes in one launch per stage of `rep`, a plan made by
+ * imps_plan_replicate(tm, 2P) from the mixed TM plan.  x_*, y_* (device, P pointers each, n
+ * elements): right-hand sides; initial guesses on entry, solutions on exit.  fac_re / fac_im
+ * (host, P).  Each system stops at |r_j| <= tol |x_j| (or stagnation, as imps_invert_e_fac);
+ * iters: lockstep iterations; relres: the largest relative residual. */
 int imps_invert_e_fac_batch(imps_plan* rep, int P, const double* const* x_re, const double* const* x_im,
                             const double* fac_re, const double* fac_im, double* const* y_re, double* const* y_im,
                             double tol, int maxit, int krylov, int* iters, double* relres);
