@@ -82,6 +82,7 @@ std::atomic<long long>& imps::launch_counter() {
 constexpr int PLAN_DECOMP = 12;
 constexpr double kMixedEigTol = 2e-7;    // Ritz-residual floor of split-BF16 applies
 constexpr double kAttainableRes = 64.0;  // FP64 Lanczos residual floor, in units of eps |T|
+constexpr int CGS_BATCH_GRID = 152;      // row blocks per system of kr_cgs2_step_batch (its CGRID)
 constexpr double kMixedInnerTol = 1e-6;  // residual reduction per mixed GMRES cycle
 constexpr double kDominantTolFloor = 1e-14;  // attainable residual of the fixed-point solve
 
@@ -1272,8 +1273,9 @@ int imps_eigs_rs_batch_op(imps_ctx* c, int P, int64_t n, imps_apply_fn fn, void*
   // the callback's own solves use the context's main arena: the bases live in the callback arena
   RC(arena_reserve(c, round256((size_t)P * n * 8) * (m + 1) + round256(n * 8) * (kk + 1) +
                           round256((size_t)P * n * 8) * 2 + round256((size_t)P * ld * ld * 8) +
-                          round256((size_t)m * kk * 8) + round256(ld * 8) + round256((size_t)P * 4) + 4096,
-                      true));
+                          round256((size_t)m * kk * 8) + round256(ld * 8) + 2 * round256((size_t)P * 8) +
+                          round256((size_t)P * kMaxCols * 8) + round256((size_t)P * CGS_BATCH_GRID * kMaxCols * 8) +
+                          4096, true));
   Bump bp{c->arena_cb};
   double* V = bp.take((size_t)P * n * (m + 1));  // system s: V + s * n * (m + 1), column j at + j * n
   double* Wk = bp.take((size_t)n * kk);
@@ -1283,17 +1285,22 @@ int imps_eigs_rs_batch_op(imps_ctx* c, int P, int64_t n, imps_apply_fn fn, void*
   double* Wrot = bp.take((size_t)m * kk);
   double* tmp = bp.take(ld);
   int* bflag = (int*)bp.take((P + 1) / 2 + 1);
+  double* h2 = bp.take((size_t)P * kMaxCols);
+  double* parts = bp.take((size_t)P * CGS_BATCH_GRID * kMaxCols);
+  unsigned int* counters = (unsigned int*)bp.take((P + 1) / 2 + 1);
   double* nrm = c->dscal + 8;
   auto Vs = [&](int sy) { return V + (size_t)sy * n * (m + 1); };
   CK(cudaMemsetAsync(Hd, 0, (size_t)P * ld * ld * 8, st));
   CK(cudaMemsetAsync(bflag, 0, P * sizeof(int), st));
+  CK(cudaMemsetAsync(counters, 0, P * sizeof(unsigned int), st));
+  CK(cudaMemsetAsync(IN, 0, (size_t)P * n * 8, st));
   for (int sy = 0; sy < P; ++sy) {
     RC(kr_multidot(c->ws, X + (size_t)sy * n, n, 1, X + (size_t)sy * n, n, tmp, 0, nrm, st));
     RC(kr_scale_inv(X + (size_t)sy * n, nrm, Vs(sy), n, bflag + sy, st));
   }
   struct Sys {
     std::vector<double> ta, tb, z, thv, Zv;
-    bool active = true, ok = false;
+    bool active = true, ok = false, final = false;
     int kfinal = 0, jpulled = 0;
     double best = std::numeric_limits<double>::infinity(), res = 0.0;
     int64_t best_at = 0;
@@ -1352,6 +1359,23 @@ int imps_eigs_rs_batch_op(imps_ctx* c, int P, int64_t n, imps_apply_fn fn, void*
     }
     return IMPS_OK;
   };
+  // the lowest Ritz vector of system sy into X (normalised) and its Ritz values into evals; done
+  // as soon as a system stops, because the batched CGS steps go on writing its unused columns
+  auto finalize = [&](int sy) -> int {
+    Sys& q = sys[sy];
+    if (q.final) return IMPS_OK;
+    q.final = true;
+    for (int i = 0; i < nev; ++i) evals[(size_t)sy * nev + i] = i < q.kfinal ? q.thv[i] : 0.0;
+    if (converged) converged[sy] = q.ok ? 1 : 0;
+    if (q.kfinal < 1) return IMPS_OK;
+    CK(cudaStreamSynchronize(st));
+    CK(cudaMemcpy(tmp, q.z.data(), q.kfinal * 8, cudaMemcpyHostToDevice));
+    RC(kr_gemv(Vs(sy), n, q.kfinal, tmp, X + (size_t)sy * n, n, st));
+    RC(kr_multidot(c->ws, X + (size_t)sy * n, n, 1, X + (size_t)sy * n, n, tmp, 0, nrm, st));
+    RC(kr_scale_inv(X + (size_t)sy * n, nrm, X + (size_t)sy * n, n, nullptr, st));
+    CK(cudaStreamSynchronize(st));
+    return IMPS_OK;
+  };
   bool done = false;
   while (!done) {
     for (int j = jstart; j < m; ++j) {
@@ -1361,13 +1385,15 @@ int imps_eigs_rs_batch_op(imps_ctx* c, int P, int64_t n, imps_apply_fn fn, void*
       const int frc = fn(user, IN, OUT);
       if (frc < 0) return frc;
       ++applies;
-      for (int sy = 0; sy < P; ++sy)
-        if (sys[sy].active)
-          RC(kr_cgs2_step(c->ws, Vs(sy), n, j + 1, OUT + (size_t)sy * n, n, Hd + (size_t)sy * ld * ld + (size_t)j * ld,
-                          tmp, Vs(sy) + (size_t)(j + 1) * n, bflag + sy, st, 2));
+      // every system's CGS step in one set of launches (converged systems work on their own
+      // columns, which are no longer read)
+      RC(kr_cgs2_step_batch(parts, counters, P, V, n * (m + 1), n, j + 1, OUT, n, n, Hd + (size_t)j * ld,
+                            (int64_t)ld * ld, h2, V + (size_t)(j + 1) * n, bflag, st));
       const bool last = j == m - 1 || applies >= max_applies;
       if (((j + 1 - jstart) % chk == 0) || last) {
         RC(evaluate(j));
+        for (int sy = 0; sy < P; ++sy)
+          if (!sys[sy].active) RC(finalize(sy));
         if (n_active() == 0 || applies >= max_applies) { done = true; break; }
       }
     }
@@ -1402,18 +1428,8 @@ int imps_eigs_rs_batch_op(imps_ctx* c, int P, int64_t n, imps_apply_fn fn, void*
     }
     jstart = kk;
   }
-  // lowest Ritz vector of every system into X, normalised; the nev Ritz values into evals
-  for (int sy = 0; sy < P; ++sy) {
-    Sys& q = sys[sy];
-    if (q.kfinal < 1) continue;
-    CK(cudaMemcpy(tmp, q.z.data(), q.kfinal * 8, cudaMemcpyHostToDevice));
-    RC(kr_gemv(Vs(sy), n, q.kfinal, tmp, X + (size_t)sy * n, n, st));
-    RC(kr_multidot(c->ws, X + (size_t)sy * n, n, 1, X + (size_t)sy * n, n, tmp, 0, nrm, st));
-    RC(kr_scale_inv(X + (size_t)sy * n, nrm, X + (size_t)sy * n, n, nullptr, st));
-    CK(cudaStreamSynchronize(st));
-    for (int i = 0; i < nev; ++i) evals[(size_t)sy * nev + i] = i < q.kfinal ? q.thv[i] : 0.0;
-    if (converged) converged[sy] = q.ok ? 1 : 0;
-  }
+  // systems still running at the apply limit: their current lowest Ritz vectors
+  for (int sy = 0; sy < P; ++sy) RC(finalize(sy));
   if (n_applies) *n_applies = (int)applies;
   if (debug_on())
     fprintf(stderr, "[imps eigs_rs_batch] P=%d n=%lld applies=%lld converged=%d\n", P, (long long)n,
@@ -1991,6 +2007,11 @@ static int gmres_batch(imps_ctx* c, int P, int64_t n, const BatchOp& Ab, const d
   double* tmp = bp.take(ld);
   double* ys = bp.take(ld);
   double* nrm = bp.take(P);
+  double* h2 = bp.take((size_t)P * kMaxCols);
+  double* parts = bp.take((size_t)P * CGS_BATCH_GRID * kMaxCols);
+  unsigned int* counters = (unsigned int*)bp.take((P + 1) / 2 + 1);
+  CK(cudaMemsetAsync(counters, 0, P * sizeof(unsigned int), st));
+  CK(cudaMemsetAsync(U, 0, ntot * 8, st));
   auto Vs = [&](int sy) { return V + (size_t)sy * n * (m + 1); };
   struct Sys {
     std::vector<double> Rh, gh, yh, csh, snh;
@@ -2056,11 +2077,13 @@ static int gmres_batch(imps_ctx* c, int P, int64_t n, const BatchOp& Ab, const d
       if (!any) break;
       RC(Ab(U, W));
       ++it;
+      // every system's CGS step in one set of launches (systems outside their cycle work on
+      // their own unused columns)
+      RC(kr_cgs2_step_batch(parts, counters, P, V, n * (m + 1), n, j + 1, W, n, n, Hd + (size_t)j * ld,
+                            (int64_t)ld * m, h2, V + (size_t)(j + 1) * n, nullptr, st));
       for (int sy = 0; sy < P; ++sy) {
         Sys& q = sys[sy];
         if (!q.in_cycle) continue;
-        RC(kr_cgs2_step(c->ws, Vs(sy), n, j + 1, W + (size_t)sy * n, n, Hd + (size_t)sy * ld * m + (size_t)j * ld,
-                        tmp, Vs(sy) + (size_t)(j + 1) * n, nullptr, st));
         q.kdim = j + 1;
         ++q.it;
       }
@@ -2149,7 +2172,8 @@ int imps_invert_e_fac_batch(imps_plan* rep, int P, const double* const* x_re, co
   int m = krylov > 0 ? std::min(krylov, kMaxCols - 2) : kGmresKrylov;
   if (maxit <= 0) maxit = (int)std::min<int64_t>(2 * n, 100000);
   RC(arena_reserve(c, round256(ntot * 8) * (m + 6) + round256(2 * n * 8) + round256((size_t)P * (m + 1) * (m + 1) * 8) +
-                          4 * round256((size_t)P * 8) + 16 * 4096));
+                          4 * round256((size_t)P * 8) + round256((size_t)P * kMaxCols * 8) +
+                          round256((size_t)P * CGS_BATCH_GRID * kMaxCols * 8) + 16 * 4096));
   Bump bp{c->arena};
   double* b = bp.take(ntot);
   double* y = bp.take(ntot);

@@ -36,6 +36,14 @@ int kr_gemv(const double* V, int64_t ldv, int ncols, const double* h, double* y,
 // four-launch path always runs two full passes.
 int kr_cgs2_step(const KrylovWs& ws, const double* V, int64_t ldv, int nc, double* w, int64_t n,
                  double* h, double* h2, double* vnext, int* flag, cudaStream_t st, int nloc = 0);
+// One CGS2 step (two full passes) of P systems in four launches (blockIdx.y = system): system q
+// has its basis at V + q sV (columns ldv apart), w at w + q sw, its coefficient column at
+// h + q sh (h[nc] = |w| after projection), its new basis vector at vnext + q sV and its breakdown
+// flag at flags[q] (flags may be NULL).  h2: P x kMaxCols scratch; partials: P x CGRID x
+// kMaxCols doubles; counters: P zeroed counters (each reset by its last block).
+int kr_cgs2_step_batch(double* partials, unsigned int* counters, int P, const double* V, int64_t sV, int64_t ldv,
+                       int nc, double* w, int64_t sw, int64_t n, double* h, int64_t sh, double* h2, double* vnext,
+                       int* flags, cudaStream_t st);
 int kr_basis_rotate(const double* V, int64_t ldv, int m, const double* W, int kk, double* out,
                     int64_t ldo, int64_t n, cudaStream_t st);
 int kr_scale_inv(const double* x, const double* nrm, double* y, int64_t n, int* flag, cudaStream_t st);

@@ -86,12 +86,27 @@ __global__ void __launch_bounds__(RB) multidot_kernel(const double* __restrict__
 // block to finish reduces them in a fixed order (bitwise reproducible), with L2 loads unrolled
 // four deep so that the tail is one round of latency per column group, and resets the counter.
 constexpr int CT = 512;
+// Batched over systems (blockIdx.y = system): every pointer advances by its stride per system
+// (sV for V, sw for w, s_in / s_out / s_acc for hin / hout / hacc, sp for partials, one counter
+// each); the single-system launches pass zero strides and one grid row.
 template <int MODE>
 __global__ void __launch_bounds__(CT) cgs_pass_kernel(const double* __restrict__ V, int64_t ldv, int nc,
                                                      double* __restrict__ w, int64_t n, int sub,
                                                      const double* hin, double* hout, double* hacc,
                                                      double* __restrict__ partials,
-                                                     unsigned int* __restrict__ counter) {
+                                                     unsigned int* __restrict__ counter, int64_t sV = 0,
+                                                     int64_t sw = 0, int64_t s_in = 0, int64_t s_out = 0,
+                                                     int64_t s_acc = 0, int64_t sp = 0) {
+  {
+    const int64_t sy = blockIdx.y;
+    V += sy * sV;
+    w += sy * sw;
+    if (hin) hin += sy * s_in;
+    hout += sy * s_out;
+    if (hacc) hacc += sy * s_acc;
+    partials += sy * sp;
+    counter += sy;
+  }
   __shared__ double wsm[CSUB];
   __shared__ double hs[imps::kMaxCols];
   __shared__ double sacc[imps::kMaxCols];
@@ -472,7 +487,15 @@ __global__ void __launch_bounds__(256) basis_rotate_kernel(const double* __restr
 }
 
 __global__ void scale_inv_kernel(const double* __restrict__ x, const double* __restrict__ nrm,
-                                 double* __restrict__ y, int64_t n, int* __restrict__ flag) {
+                                 double* __restrict__ y, int64_t n, int* __restrict__ flag, int64_t sx = 0,
+                                 int64_t sn = 0, int64_t sy = 0) {
+  {  // batched: blockIdx.y = system (x, nrm, y, flag advance by their strides)
+    const int64_t q = blockIdx.y;
+    x += q * sx;
+    nrm += q * sn;
+    y += q * sy;
+    if (flag) flag += q;
+  }
   const double s = *nrm;
   const bool bad = !(fabs(s) > 1e-300) || !isfinite(s);
   if (bad && flag && blockIdx.x == 0 && threadIdx.x == 0) *flag = 1;
@@ -723,6 +746,31 @@ int kr_cgs2_step(const KrylovWs& ws, const double* V, int64_t ldv, int nc, doubl
                                           ws.counter);
   scale_inv_kernel<<<grid_for(n), 256, 0, st>>>(w, h + nc, vnext, n, flag);
   return IMPS_OK;
+}
+
+int kr_cgs2_step_batch(double* partials, unsigned int* counters, int P, const double* V, int64_t sV, int64_t ldv,
+                       int nc, double* w, int64_t sw, int64_t n, double* h, int64_t sh, double* h2, double* vnext,
+                       int* flags, cudaStream_t st) {
+  if (nc < 1 || nc >= kMaxCols || P < 1) return IMPS_ERR_BAD_ARG;
+  int64_t g = (n + 255) / 256;
+  if (g > CGRID) g = CGRID;
+  if (g < 1) g = 1;
+  int64_t sub = (n + g - 1) / g;
+  sub = ((sub + 31) / 32) * 32;
+  if (sub > CSUB) sub = CSUB;
+  const dim3 grid((unsigned)g, (unsigned)P);
+  const int64_t sp = (int64_t)g * kMaxCols;  // partials per system (column c at c * g)
+  const int64_t sh2 = kMaxCols;              // h2: one kMaxCols block per system
+  imps::count_launch(4);
+  // h = V^T w; then w -= V h, h2 = V^T w, h += h2; then w -= V h2, |w| -> h[nc]
+  cgs_pass_kernel<0><<<grid, CT, 0, st>>>(V, ldv, nc, w, n, (int)sub, nullptr, h, nullptr, partials, counters, sV,
+                                          sw, 0, sh, 0, sp);
+  cgs_pass_kernel<1><<<grid, CT, 0, st>>>(V, ldv, nc, w, n, (int)sub, h, h2, h, partials, counters, sV, sw, sh, sh2,
+                                          sh, sp);
+  cgs_pass_kernel<2><<<grid, CT, 0, st>>>(V, ldv, nc, w, n, (int)sub, h2, h + nc, nullptr, partials, counters, sV,
+                                          sw, sh2, sh, 0, sp);
+  scale_inv_kernel<<<dim3((unsigned)grid_for(n), (unsigned)P), 256, 0, st>>>(w, h + nc, vnext, n, flags, sw, sh, sV);
+  return cudaGetLastError() == cudaSuccess ? IMPS_OK : IMPS_ERR_CUDA;
 }
 
 int kr_scale_inv(const double* x, const double* nrm, double* y, int64_t n, int* flag, cudaStream_t st) {
