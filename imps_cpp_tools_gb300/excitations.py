@@ -537,6 +537,47 @@ class ExcitationsGPU:
         return out[:nev], conv and len(out) >= nev
 
 
+def batched_program_tables(progs, sizes):
+    """The tables of P copies of one H_eff program (the programs of P momenta, which must share
+    their structure and differ only in their alphas) as one program: every stage holds the P
+    copies' output blocks in turn, copy j's regions in every slot but the shared operands (OPS)
+    offset by j times the slot's length, its terms carrying momentum j's alphas.  sizes: the
+    single program's slot lengths.  Returns (stage_nouts, outs, terms, alphas, slot lengths) for
+    imps_plan_program."""
+    P = len(progs)
+    S = {k: max(int(sizes.get(k, 0)), 1) for k in range(6)}
+    tabs = [pg.tables() for pg in progs]
+    nouts0, outs0, terms0, _ = tabs[0]
+    for (no, ou, te, _) in tabs[1:]:
+        if not (np.array_equal(no, nouts0) and np.array_equal(ou, outs0) and np.array_equal(te, terms0)):
+            raise ValueError("the momenta's H_eff programs differ in structure (a special momentum?)")
+    shift = np.array([0 if k == OPS else S[k] for k in range(6)], np.int64)
+    nouts, outs, terms, alphas = [], [], [], []
+    o0 = t0 = 0
+    for st_n in nouts0:
+        so = outs0[o0:o0 + st_n]
+        nt = int(so[:, 6].sum())
+        stt = terms0[t0:t0 + nt]
+        for j in range(P):
+            oj = so.copy()
+            oj[:, 1] += j * shift[oj[:, 0]]
+            tj = stt.copy()
+            tj[:, 1] += j * shift[tj[:, 0]]
+            tj[:, 5] += j * shift[tj[:, 4]]
+            outs.append(oj)
+            terms.append(tj)
+            alphas.append(tabs[j][3][t0:t0 + nt])
+        nouts.append(P * int(st_n))
+        o0 += int(st_n)
+        t0 += nt
+    nouts = np.array(nouts, np.int32)
+    outs = np.ascontiguousarray(np.concatenate(outs) if outs else np.zeros((0, 7), np.int64))
+    terms = np.ascontiguousarray(np.concatenate(terms) if terms else np.zeros((0, 9), np.int64))
+    alphas = np.ascontiguousarray(np.concatenate(alphas) if alphas else np.zeros(0))
+    sizes_b = np.array([S[k] if k == OPS else P * S[k] for k in range(6)], np.int64)
+    return nouts, outs, terms, alphas, sizes_b
+
+
 class ExcitationsBatchGPU:
     """Excitation energies at P momenta together (the momentum loop of Excitations_main.cpp:255-297,
     unprojected solves: K != 0 or p != 0).  The H_eff programs of the momenta have the same tables
@@ -574,38 +615,8 @@ class ExcitationsBatchGPU:
         self.stats = {"gmres_iters": 0, "applies": 0}
 
     def _batched_plan(self, progs):
-        """One imps_plan_program holding P copies of a program (structure of the first, alphas of
-        each), copy j's slots offset by j times their length (OPS shared)."""
-        P, S = self.P, self.sizes
-        tabs = [pg.tables() for pg in progs]
-        nouts0, outs0, terms0, _ = tabs[0]
-        for (no, ou, te, _) in tabs[1:]:
-            if not (np.array_equal(no, nouts0) and np.array_equal(ou, outs0) and np.array_equal(te, terms0)):
-                raise ValueError("the momenta's H_eff programs differ in structure (a special momentum?)")
-        shift = np.array([0 if k == OPS else S[k] for k in range(6)], np.int64)
-        nouts, outs, terms, alphas = [], [], [], []
-        o0 = t0 = 0
-        for st_n in nouts0:
-            so = outs0[o0:o0 + st_n]
-            nt = int(so[:, 6].sum())
-            stt = terms0[t0:t0 + nt]
-            for j in range(P):
-                oj = so.copy()
-                oj[:, 1] += j * shift[oj[:, 0]]
-                tj = stt.copy()
-                tj[:, 1] += j * shift[tj[:, 0]]
-                tj[:, 5] += j * shift[tj[:, 4]]
-                outs.append(oj)
-                terms.append(tj)
-                alphas.append(tabs[j][3][t0:t0 + nt])
-            nouts.append(P * int(st_n))
-            o0 += int(st_n)
-            t0 += nt
-        nouts = np.array(nouts, np.int32)
-        outs = np.ascontiguousarray(np.concatenate(outs) if outs else np.zeros((0, 7), np.int64))
-        terms = np.ascontiguousarray(np.concatenate(terms) if terms else np.zeros((0, 9), np.int64))
-        alphas = np.ascontiguousarray(np.concatenate(alphas) if alphas else np.zeros(0))
-        sizes = np.array([S[k] if k == OPS else P * S[k] for k in range(6)], np.int64)
+        """One imps_plan_program holding P copies of a program (batched_program_tables)."""
+        nouts, outs, terms, alphas, sizes = batched_program_tables(progs, self.sizes)
         h = C.c_void_p()
         N.call("imps_plan_program", self.ctx.handle, 6, sizes.ctypes.data_as(N.P_i64), len(nouts),
                nouts.ctypes.data_as(N.P_i32), outs.ctypes.data_as(N.P_i64), terms.ctypes.data_as(N.P_i64),

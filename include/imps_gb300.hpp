@@ -112,6 +112,20 @@ class plan {
   // a grouped-GEMM program (see struct program below); bind every slot, then run()
   static plan program(const context& ctx, const struct program& prog);
   void run() { check(imps_plan_run(p_), "imps_plan_run"); }
+  // the plan applied to `copies` inputs at once (imps_plan_replicate), e.g. a mixed TM on the
+  // 2P planes of P momenta
+  static plan replicate(const plan& src, int copies) {
+    imps_plan* p = nullptr;
+    check(imps_plan_replicate(src.get(), copies, &p), "imps_plan_replicate");
+    return plan(p);
+  }
+  // time every FP64 launch shape of the stages not tuned yet in this process, install the
+  // fastest (imps_plan_autotune); returns the number of stages timed
+  int autotune(int reps = 5) {
+    int n = 0;
+    check(imps_plan_autotune(p_, reps, &n), "imps_plan_autotune");
+    return n;
+  }
 
  private:
   imps_plan* p_ = nullptr;
@@ -221,6 +235,47 @@ inline int InvertE_proj(plan& tm, const double* x, const double* L, const double
                        "InvertE_proj");
   if (iters) *iters = it;
   return st;
+}
+
+// InvertE_fac (InvEBlockFunctions.hpp:346-476) for P momenta at once on rep = plan::replicate(
+// tmx, 2P): (1 - f_j T) y_j = x_j, device vectors; returns the status (1: some system not
+// converged)
+inline int InvertE_fac_batch(plan& rep, const std::vector<const double*>& x_re, const std::vector<const double*>& x_im,
+                             const std::vector<double>& f_re, const std::vector<double>& f_im,
+                             const std::vector<double*>& y_re, const std::vector<double*>& y_im, double tol,
+                             int* iters = nullptr) {
+  int it = 0;
+  double rr = 0.0;
+  const int st = check(imps_invert_e_fac_batch(rep.get(), (int)x_re.size(), x_re.data(), x_im.data(), f_re.data(),
+                                               f_im.data(), y_re.data(), y_im.data(), tol, 0, 0, &it, &rr),
+                       "InvertE_fac_batch");
+  if (iters) *iters = it;
+  return st;
+}
+
+// The nev lowest eigenvalues of P symmetric operators at once (imps_eigs_rs_batch_op): op
+// applies all P operators to P consecutive device vectors of length n; X (device, P x n) holds
+// the start vectors and receives each system's lowest Ritz vector.  Returns P x nev values.
+using batch_op = std::function<void(const double* in, double* out)>;
+inline std::vector<double> eigs_rs_batch(context& ctx, int P, int64_t n, const batch_op& op, double* X, int nev,
+                                         double tol, int ncv = 0, int* applies = nullptr) {
+  struct tramp {
+    static int call(void* user, const double* in, double* out) {
+      try {
+        (*static_cast<const batch_op*>(user))(in, out);
+        return IMPS_OK;
+      } catch (...) {
+        return IMPS_ERR_CUDA;  // a failing apply ends the solve with an error status
+      }
+    }
+  };
+  std::vector<double> ev((size_t)P * nev);
+  int na = 0;
+  check(imps_eigs_rs_batch_op(ctx.get(), P, n, &tramp::call, const_cast<batch_op*>(&op), X, nev, tol, ncv, 0,
+                              ev.data(), &na, nullptr),
+        "eigs_rs_batch");
+  if (applies) *applies = na;
+  return ev;
 }
 
 // qr(R, MPS, dir) (MPSBlockUtilities.hpp:181-244) on device buffers: Q in A's layout, R in

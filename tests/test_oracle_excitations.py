@@ -356,3 +356,47 @@ def test_ising_dispersion_is_exact():
             w = np.sort(eigsh(op, k=2, which="SA", tol=1e-10)[0])
             exact = sorted([eps(P / 2), eps(P / 2 + math.pi)])
             assert np.abs(w - exact).max() < 1e-10, (P, w, exact)
+
+
+def run_flat_tables(nouts, outs, terms, alphas, bufs):
+    """Execute flat imps_plan_program tables (stage_nouts, outs, terms, alphas) with numpy."""
+    stages, o, t = [], 0, 0
+    for n in nouts:
+        st = []
+        for _ in range(int(n)):
+            cs, coff, cld, M, Nn, acc, nt = (int(x) for x in outs[o])
+            tl = [tuple(int(x) for x in terms[t + q]) + (float(alphas[t + q]),) for q in range(nt)]
+            st.append((cs, coff, cld, M, Nn, acc, tl))
+            o += 1
+            t += nt
+        stages.append(st)
+    run_tables(stages, bufs)
+
+
+def test_batched_heff_tables_equal_per_momentum():
+    """The batched H_eff program tables (excitations.batched_program_tables: P momenta, copy j in
+    slot region j) executed with numpy give, in every copy, exactly what the single momentum's
+    program gives: a CPU check of the offsets and per-copy alphas of ExcitationsBatchGPU."""
+    from imps_cpp_tools_gb300 import excitations as EX
+    e = excitation_setup((2,))
+    kfs = [np.exp(1j * p) for p in (0.4, 1.3, 2.7)]
+    prs = [EX.HeffProgram(e["AL"], e["AR"], e["NL"], e["HLtot"], e["HRtot"], e["h"], e["d"], e["xdims"], k)
+           for k in kfs]
+    S = {k: max(int(prs[0].sizes.get(k, 0)), 1) for k in range(6)}
+    for which in ("prog_a", "prog_b"):
+        nouts, outs, terms, alphas, sizes = EX.batched_program_tables([getattr(p, which) for p in prs], prs[0].sizes)
+        assert list(sizes) == [S[k] if k == EX.OPS else 3 * S[k] for k in range(6)]
+        rng = np.random.default_rng(5)
+        big = {k: rng.standard_normal(int(sizes[k])) for k in range(6)}
+        big[EX.OPS][:prs[0].ops_vec.size] = prs[0].ops_vec
+        ref = []
+        for j, pr in enumerate(prs):
+            small = {k: (big[k].copy() if k == EX.OPS else big[k][j * S[k]:(j + 1) * S[k]].copy()) for k in range(6)}
+            run_tables(getattr(pr, which).stages, small)
+            ref.append(small)
+        run_flat_tables(nouts, outs, terms, alphas, big)
+        for j in range(3):
+            for k in range(6):
+                if k == EX.OPS:
+                    continue
+                assert np.array_equal(big[k][j * S[k]:(j + 1) * S[k]], ref[j][k]), (which, j, k)
