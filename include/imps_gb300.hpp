@@ -90,6 +90,13 @@ class plan {
   plan(const plan&) = delete;
   plan& operator=(const plan&) = delete;
   plan(plan&& o) noexcept : p_(std::exchange(o.p_, nullptr)) {}
+  plan& operator=(plan&& o) noexcept {
+    if (this != &o) {
+      if (p_) imps_plan_destroy(p_);
+      p_ = std::exchange(o.p_, nullptr);
+    }
+    return *this;
+  }
   imps_plan* get() const { return p_; }
   void bind(int slot, double* device_ptr) { check(imps_plan_bind(p_, slot, device_ptr), "imps_plan_bind"); }
   void prepare() { check(imps_plan_prepare(p_), "imps_plan_prepare"); }

@@ -276,3 +276,9 @@ def test_plan_replicate_tables():
                     assert oa2 == oa + (c * src.slot_nelem(sa) if sa in per else 0)
                     assert ob2 == ob + (c * src.slot_nelem(sb) if sb in per else 0)
     assert rep.info()["flops_apply"] == 3 * src.info()["flops_apply"]
+
+
+def test_cpp_vumps_check_builds(tmp_path):
+    """The C++ VUMPS driver (include/imps_vumps.hpp) compiles and links;
+    tests/test_gpu_cpp_vumps.py runs it against the Python driver."""
+    assert _build_cpp_host(tmp_path, "cpp_vumps_check").exists()
