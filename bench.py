@@ -21,6 +21,8 @@ excitation energies at 32 momenta in one batched run, beside the per-momentum pa
 of them.
 --mode expand times one bond expansion (ExpandFromH, dmmax 20) at the XXZ D=512 and Hubbard
 D=1024 starts against the oracle on the same state.
+--mode cpp runs the same timed sweeps through the C++ host driver (include/imps_vumps.hpp) beside
+the Python driver.
 --mode trace runs the timed FP64 sweeps under torch.profiler: summed kernel time against wall time,
 kernels by share.
 --mode krylov times one bounded thick-restart Lanczos solve (eigs_rs, ncv 64, at most 8 restart
@@ -607,6 +609,75 @@ def run_trace(args):
                                    "share": t / max(total, 1e-12)} for k, (t, c) in top]}), flush=True)
 
 
+def _build_cpp_vumps():
+    """Compile tests/native/cpp_vumps_check.cpp (the C++ VUMPS driver include/imps_vumps.hpp over
+    the C ABI) against the in-tree library."""
+    import shutil
+    from pathlib import Path
+    from imps_cpp_tools_gb300 import _native as N
+    gxx, nvcc = shutil.which("g++"), shutil.which("nvcc") or "/usr/local/cuda/bin/nvcc"
+    cuda = Path(nvcc).resolve().parent.parent
+    N.load()
+    lib = Path(N.lib_path()).parent
+    exe = Path(ROOT) / "imps_cpp_tools_gb300" / "_lib" / "cpp_vumps_check"
+    cmd = [gxx, "-std=c++17", "-O2", "-I", os.path.join(ROOT, "include"), "-I", str(cuda / "include"),
+           os.path.join(ROOT, "tests", "native", "cpp_vumps_check.cpp"), "-L", str(lib), "-limps_gb300",
+           "-L", str(cuda / "lib64"), "-lcudart", f"-Wl,-rpath,{lib}", f"-Wl,-rpath,{cuda / 'lib64'}", "-o", str(exe)]
+    subprocess.run(cmd, check=True)
+    return exe
+
+
+def run_cpp(args):
+    """--mode cpp: the timed sweeps of the default measurement run by the C++ host driver
+    (include/imps_vumps.hpp, no Python in the loop) from the same warmed state and at the same
+    tolerances, next to the Python driver: sweeps/s of both and the largest energy difference
+    of their sweeps."""
+    import torch
+    from imps_cpp_tools_gb300 import blocks as B
+    from imps_cpp_tools_gb300 import models
+    from imps_cpp_tools_gb300 import workload as W
+    ctx = B.Context(0)
+    _CTX[0] = ctx
+    stream = torch.cuda.current_stream()
+    ctx.set_stream(stream)
+    name = _WORKLOAD[0]
+    model, d, I2K, h, dimvec = W.bond_layouts(name)
+    hnnz = models.h_nonzeros(h)
+    state, src = _start_state()
+    nsw = args.warmup + args.steps
+    lines = [f"{d} {len(I2K[0])}", " ".join(str(x) for q in I2K for x in q)]
+    for b in range(2):
+        lines.append(str(len(dimvec[b])))
+        lines += [" ".join(str(x) for x in q) + f" {m}" for q, m in sorted(dimvec[b].items())]
+    lines.append(str(len(hnnz)))
+    lines += [f"{r} {c} {v!r}" for (r, c, v) in hnnz]
+    lines.append(f"{nsw} {TIMED_TOLS['eig']!r} {TIMED_TOLS['gmres']!r} 1.0 {0 if args.no_autotune else 1}")
+    for k in ("AL", "AR", "C"):
+        for n in range(2):
+            lines.append(" ".join(repr(float(x)) for x in state[k][n]))
+    inp = os.path.join(ROOT, "imps_cpp_tools_gb300", "_lib", f"cpp_vumps_{name}.txt")
+    with open(inp, "w") as f:
+        f.write("\n".join(lines) + "\n")
+    exe = _build_cpp_vumps()
+    r = subprocess.run([str(exe), inp], capture_output=True, text=True, timeout=1800)
+    if r.returncode != 0:
+        raise RuntimeError(r.stdout + r.stderr)
+    rows = [list(map(float, ln.split()[2:])) for ln in r.stdout.splitlines() if ln.startswith("sweep ")]
+    cpp_ms = [row[6] for row in rows[args.warmup:]]
+    _AUTOTUNE[0] = not args.no_autotune
+    py = _run_vumps(torch, "fp64", state, args.steps, args.warmup, stream)
+    E_py_last = py["E"]
+    dE = float(np.abs(np.array(rows[-1][0:2]) - np.asarray(E_py_last)).max())
+    print(json.dumps({"mode": "cpp", "workload": _workload_desc(), "start_state": src, "sweeps_timed": args.steps,
+                      "cpp": {"sweeps_per_s": 1e3 / float(np.mean(cpp_ms)), "ms_per_sweep": float(np.mean(cpp_ms)),
+                              "energy": float(np.mean(rows[-1][0:2])), "grad_norm": max(rows[-1][2:4]),
+                              "timing": "wall clock per sweep, device synchronised before and after"},
+                      "python": {"sweeps_per_s": 1.0 / float(np.mean(py["times"])),
+                                 "ms_per_sweep": 1e3 * float(np.mean(py["times"])), "energy": float(E_py_last.mean()),
+                                 "grad_norm": float(py["F"].max()), "timing": "CUDA events around each sweep"},
+                      "max_abs_dE_last_sweep": dE}), flush=True)
+
+
 def run_hac(args):
     import torch
     from imps_cpp_tools_gb300 import _native as N
@@ -861,7 +932,7 @@ def main():
     ap.add_argument("--steps", type=int, default=47)
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
-    ap.add_argument("--mode", default="vumps", choices=["vumps", "hac", "krylov", "excitations", "adjoint", "expand", "trace"])
+    ap.add_argument("--mode", default="vumps", choices=["vumps", "hac", "krylov", "excitations", "adjoint", "expand", "trace", "cpp"])
     ap.add_argument("--workload", default="xxz_d512")
     ap.add_argument("--precision", default="fp64", choices=["fp64", "bf16x6"])
     ap.add_argument("--no-cpu", action="store_true")
@@ -873,7 +944,7 @@ def main():
     ap.add_argument("--ncv", type=int, default=126, help="Krylov dimension of the H_AC / H_C Lanczos solves")
     args = ap.parse_args()
     args.warmup = max(args.warmup, 3)
-    if args.mode in ("vumps", "trace") or args.impl == "reference":
+    if args.mode in ("vumps", "trace", "cpp") or args.impl == "reference":
         if args.workload not in WORKLOAD_DESCS:
             raise SystemExit(f"--workload for the VUMPS bench: one of {sorted(WORKLOAD_DESCS)}")
         _WORKLOAD[0] = args.workload
@@ -891,6 +962,8 @@ def main():
         run_excitations(args)
     elif args.mode == "trace":
         run_trace(args)
+    elif args.mode == "cpp":
+        run_cpp(args)
     else:
         run_vumps(args)
 

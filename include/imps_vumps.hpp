@@ -50,6 +50,7 @@ struct vumps_options {
   double eig_margin = 0.1;  // the Lanczos tests every 4 steps, ARPACK once per cycle (vumps.py)
   int lanczos_ncv = 126, lanczos_maxit = 300, gmres_maxit = 4000;
   bool trueLR = true;
+  bool autotune = false;  // time every plan's FP64 launch shapes once (imps_plan_autotune)
 };
 
 // a device vector of doubles
@@ -264,6 +265,13 @@ class vumps {
                                           hv_.data(), 0, LB_[a].get(), &p), p, "imps_plan_optm"));
       optm_r_.push_back(mk(imps_plan_optm(c, LA_[a].get(), LA_[1 - a].get(), d, nnz, hr_.data(), hc_.data(),
                                           hv_.data(), 1, LB_[a].get(), &p), p, "imps_plan_optm"));
+    }
+    if (o_.autotune) {
+      for (auto* v : {&redop_l_, &redop_r_, &p_ac_, &p_hac_, &p_grad_, &p_hcl_, &p_hcr_, &p_mul_r_t_, &p_mul_l_t_,
+                      &p_mul_r_, &p_mul_l_, &optm_l_, &optm_r_})
+        for (plan& q : *v) q.autotune();
+      for (auto& kv : tm_) kv.second.autotune();
+      for (plan& q : cct_) q.autotune();
     }
   }
 

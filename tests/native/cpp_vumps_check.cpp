@@ -4,8 +4,10 @@
 //
 // Input (whitespace separated): d nsym; I2K (d x nsym ints); for bonds 0 and 1: nsectors, then per
 // sector nsym ints and the dimension; nnz, then per nonzero row col value; nsweeps fixed_tol
-// InvETol; then the flat AL(0), AL(1), AR(0), AR(1), C[0], C[1] (their lengths follow from the
-// layouts).
+// InvETol eig_margin autotune(0/1); then the flat AL(0), AL(1), AR(0), AR(1), C[0], C[1] (their
+// lengths follow from the layouts).  Per sweep it also prints the wall time of the sweep
+// (synchronised) in ms.
+#include <chrono>
 #include <cstdio>
 #include <fstream>
 #include <iostream>
@@ -41,7 +43,9 @@ int main(int argc, char** argv) {
   }
   int nsweeps = 0;
   imps_cpp::vumps_options o;
-  in >> nsweeps >> o.fixed_tol >> o.InvETol;
+  int tune = 0;
+  in >> nsweeps >> o.fixed_tol >> o.InvETol >> o.eig_margin >> tune;
+  o.autotune = tune != 0;
   std::array<std::vector<double>, 6> init;
   for (int n = 0; n < 2; ++n) {
     const int64_t na = imps_cpp::layout(nsym, imps_cpp::mps_blocks(m.I2K, dims[n], dims[1 - n])).nelem();
@@ -56,9 +60,13 @@ int main(int argc, char** argv) {
     imps_cpp::context ctx(0);
     imps_cpp::vumps v(ctx, m, dims, init, o);
     for (int s = 0; s < nsweeps; ++s) {
+      cudaDeviceSynchronize();
+      const auto t0 = std::chrono::steady_clock::now();
       const auto E = v.sweep();
-      std::printf("sweep %d %.17g %.17g %.17g %.17g %.17g %.17g\n", s, E[0], E[1], v.F[0], v.F[1], v.prec[0],
-                  v.prec[1]);
+      cudaDeviceSynchronize();
+      const double ms = std::chrono::duration<double, std::milli>(std::chrono::steady_clock::now() - t0).count();
+      std::printf("sweep %d %.17g %.17g %.17g %.17g %.17g %.17g %.3f\n", s, E[0], E[1], v.F[0], v.F[1], v.prec[0],
+                  v.prec[1], ms);
     }
     std::printf("cpp vumps check ok: %d Lanczos applies, %d GMRES iterations\n", v.lanczos_applies, v.gmres_iters);
   } catch (const std::exception& e) {

@@ -30,7 +30,7 @@ def test_cpp_vumps_matches_python_driver(cuda_ctx, tmp_path):
         lines += [" ".join(str(x) for x in q) + f" {m}" for q, m in sorted(dimvec[b].items())]
     lines.append(str(len(hnnz)))
     lines += [f"{r} {c} {v!r}" for (r, c, v) in hnnz]
-    lines.append(f"{nsweeps} {tol!r} {invetol!r}")
+    lines.append(f"{nsweeps} {tol!r} {invetol!r} 0.1 0")
     lines += [" ".join(repr(float(x)) for x in v) for v in flat]
     inp = tmp_path / "vumps_input.txt"
     inp.write_text("\n".join(lines) + "\n")
@@ -44,7 +44,7 @@ def test_cpp_vumps_matches_python_driver(cuda_ctx, tmp_path):
     assert len(got) == nsweeps
     for s in range(nsweeps):
         E, F, prec = gpu.sweep()
-        e_cpp, f_cpp, p_cpp = np.array(got[s][0:2]), np.array(got[s][2:4]), np.array(got[s][4:6])
+        e_cpp, f_cpp, p_cpp = np.array(got[s][0:2]), np.array(got[s][2:4]), np.array(got[s][4:6])  # then ms
         assert np.abs(e_cpp - E).max() < 1e-12, (s, e_cpp, E)
         assert np.allclose(f_cpp, F, rtol=1e-9, atol=1e-14), (s, f_cpp, F)
         assert np.allclose(p_cpp, prec, rtol=1e-9, atol=1e-14), (s, p_cpp, prec)
