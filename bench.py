@@ -401,7 +401,7 @@ def _new_vumps(precision, state):
                     verbose=True, **params)
 
 
-def _run_vumps(torch, precision, state, steps, warmup, stream, clocks=None, e2e=False):
+def _run_vumps(torch, precision, state, steps, warmup, stream, clocks=None, e2e=False, per_sweep=False):
     """W warm-up sweeps, then K device-timed sweeps (CUDA events on the launching stream), from
     `state`.  With e2e, every timed step also uploads the MPS state from pinned host memory
     before the sweep and reads the state and the energies back after it (wall clock around all
@@ -421,9 +421,10 @@ def _run_vumps(torch, precision, state, steps, warmup, stream, clocks=None, e2e=
     s0 = dict(v.stats)
     if clocks:
         clocks.start()
-    times, walls = [], []
+    times, walls, applies_each = [], [], []
     torch.cuda.nvtx.range_push(f"timed_sweeps_{precision}")  # ncu --nvtx-include selects these
     for _ in range(steps):
+        a0 = v.stats["lanczos_applies"]
         torch.cuda.synchronize()
         w0 = time.perf_counter()
         if e2e:
@@ -441,12 +442,13 @@ def _run_vumps(torch, precision, state, steps, warmup, stream, clocks=None, e2e=
         torch.cuda.synchronize()
         walls.append(time.perf_counter() - w0)
         times.append(e0.elapsed_time(e1) * 1e-3)
+        applies_each.append(v.stats["lanczos_applies"] - a0)
     torch.cuda.nvtx.range_pop()
     clk = clocks.stop() if clocks else None
     launches = lib.imps_launch_count() - l0
     counts = {k: v.stats[k] - s0.get(k, 0) for k in v.stats}
     return {"v": v, "times": times, "walls": walls, "E": E, "F": F, "prec": prec, "launches": launches,
-            "counts": counts, "clocks": clk, "h2d": h2d, "E_first": E_first}
+            "counts": counts, "clocks": clk, "h2d": h2d, "E_first": E_first, "applies_each": applies_each}
 
 
 def run_vumps(args):
@@ -664,16 +666,20 @@ def run_cpp(args):
         raise RuntimeError(r.stdout + r.stderr)
     rows = [list(map(float, ln.split()[2:])) for ln in r.stdout.splitlines() if ln.startswith("sweep ")]
     cpp_ms = [row[6] for row in rows[args.warmup:]]
+    cpp_applies = [int(rows[i][7] - (rows[i - 1][7] if i else 0)) for i in range(len(rows))][args.warmup:]
     _AUTOTUNE[0] = not args.no_autotune
-    py = _run_vumps(torch, "fp64", state, args.steps, args.warmup, stream)
+    py = _run_vumps(torch, "fp64", state, args.steps, args.warmup, stream, per_sweep=True)
     E_py_last = py["E"]
     dE = float(np.abs(np.array(rows[-1][0:2]) - np.asarray(E_py_last)).max())
     print(json.dumps({"mode": "cpp", "workload": _workload_desc(), "start_state": src, "sweeps_timed": args.steps,
                       "cpp": {"sweeps_per_s": 1e3 / float(np.mean(cpp_ms)), "ms_per_sweep": float(np.mean(cpp_ms)),
+                              "ms_each": [round(x, 1) for x in cpp_ms], "lanczos_applies_each": cpp_applies,
                               "energy": float(np.mean(rows[-1][0:2])), "grad_norm": max(rows[-1][2:4]),
                               "timing": "wall clock per sweep, device synchronised before and after"},
                       "python": {"sweeps_per_s": 1.0 / float(np.mean(py["times"])),
-                                 "ms_per_sweep": 1e3 * float(np.mean(py["times"])), "energy": float(E_py_last.mean()),
+                                 "ms_per_sweep": 1e3 * float(np.mean(py["times"])),
+                                 "ms_each": [round(1e3 * x, 1) for x in py["times"]],
+                                 "lanczos_applies_each": py["applies_each"], "energy": float(E_py_last.mean()),
                                  "grad_norm": float(py["F"].max()), "timing": "CUDA events around each sweep"},
                       "max_abs_dE_last_sweep": dE}), flush=True)
 

@@ -6,7 +6,7 @@
 // sector nsym ints and the dimension; nnz, then per nonzero row col value; nsweeps fixed_tol
 // InvETol eig_margin autotune(0/1); then the flat AL(0), AL(1), AR(0), AR(1), C[0], C[1] (their
 // lengths follow from the layouts).  Per sweep it also prints the wall time of the sweep
-// (synchronised) in ms.
+// (synchronised) in ms and the Lanczos applies so far.
 #include <chrono>
 #include <cstdio>
 #include <fstream>
@@ -65,8 +65,8 @@ int main(int argc, char** argv) {
       const auto E = v.sweep();
       cudaDeviceSynchronize();
       const double ms = std::chrono::duration<double, std::milli>(std::chrono::steady_clock::now() - t0).count();
-      std::printf("sweep %d %.17g %.17g %.17g %.17g %.17g %.17g %.3f\n", s, E[0], E[1], v.F[0], v.F[1], v.prec[0],
-                  v.prec[1], ms);
+      std::printf("sweep %d %.17g %.17g %.17g %.17g %.17g %.17g %.3f %d\n", s, E[0], E[1], v.F[0], v.F[1], v.prec[0],
+                  v.prec[1], ms, v.lanczos_applies);
     }
     std::printf("cpp vumps check ok: %d Lanczos applies, %d GMRES iterations\n", v.lanczos_applies, v.gmres_iters);
   } catch (const std::exception& e) {

@@ -44,7 +44,7 @@ def test_cpp_vumps_matches_python_driver(cuda_ctx, tmp_path):
     assert len(got) == nsweeps
     for s in range(nsweeps):
         E, F, prec = gpu.sweep()
-        e_cpp, f_cpp, p_cpp = np.array(got[s][0:2]), np.array(got[s][2:4]), np.array(got[s][4:6])  # then ms
+        e_cpp, f_cpp, p_cpp = np.array(got[s][0:2]), np.array(got[s][2:4]), np.array(got[s][4:6])  # then ms, applies
         assert np.abs(e_cpp - E).max() < 1e-12, (s, e_cpp, E)
         assert np.allclose(f_cpp, F, rtol=1e-9, atol=1e-14), (s, f_cpp, F)
         assert np.allclose(p_cpp, prec, rtol=1e-9, atol=1e-14), (s, p_cpp, prec)
