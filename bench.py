@@ -386,6 +386,7 @@ def _start_state():
 _MIXED_TM = [False]
 _NCV = [126]
 _AUTOTUNE = [True]
+_CONCURRENT = [True]
 
 
 def _new_vumps(precision, state):
@@ -398,7 +399,7 @@ def _new_vumps(precision, state):
     return VumpsGPU(_CTX[0], model, dims0=fn(), init_state=init, fixed_tol=TIMED_TOLS["eig"],
                     InvETol=TIMED_TOLS["gmres"], eig_margin=1.0, precision=precision,
                     mixed_tm=_MIXED_TM[0] and precision != "fp64", lanczos_ncv=_NCV[0], autotune=_AUTOTUNE[0],
-                    verbose=True, **params)
+                    concurrent=_CONCURRENT[0], verbose=True, **params)
 
 
 def _run_vumps(torch, precision, state, steps, warmup, stream, clocks=None, e2e=False, per_sweep=False):
@@ -545,7 +546,7 @@ def run_vumps(args):
             "vs_baseline": None, "dtype": "bf16x6->f32 applies, f64 Krylov/decompositions" if args.precision == "bf16x6"
             else "f64", "data": "synthetic",
             "config": {"workload": _workload_desc(), "precision": args.precision, "start_state": state_src,
-                       "lanczos_ncv": _NCV[0], "autotune": _AUTOTUNE[0],
+                       "lanczos_ncv": _NCV[0], "autotune": _AUTOTUNE[0], "concurrent_hc_solves": _CONCURRENT[0],
                        "l2": "working set (~40 MB) is L2-resident by design; H_AC timing flushes L2 (512 MB write)",
                        "parallelism": f"replicas x{ws}"},
             "fp64": {"sweeps_per_s": 1.0 / float(np.mean(r64["times"])), "ms_per_step": 1e3 * float(np.mean(r64["times"])),
@@ -653,7 +654,8 @@ def run_cpp(args):
         lines += [" ".join(str(x) for x in q) + f" {m}" for q, m in sorted(dimvec[b].items())]
     lines.append(str(len(hnnz)))
     lines += [f"{r} {c} {v!r}" for (r, c, v) in hnnz]
-    lines.append(f"{nsw} {TIMED_TOLS['eig']!r} {TIMED_TOLS['gmres']!r} 1.0 {0 if args.no_autotune else 1}")
+    lines.append(f"{nsw} {TIMED_TOLS['eig']!r} {TIMED_TOLS['gmres']!r} 1.0 {0 if args.no_autotune else 1} "
+                 f"{0 if args.serial_solves else 1}")
     for k in ("AL", "AR", "C"):
         for n in range(2):
             lines.append(" ".join(repr(float(x)) for x in state[k][n]))
@@ -947,9 +949,12 @@ def main():
     ap.add_argument("--headline-only", action="store_true", help="skip the other precision's arm (profiling)")
     ap.add_argument("--no-autotune", action="store_true", help="launch shapes from the makespan estimate only")
     ap.add_argument("--momenta", type=int, default=32, help="momenta of --mode excitations")
+    ap.add_argument("--serial-solves", action="store_true",
+                    help="run the H_C eigensolves after the H_AC eigensolve on one stream")
     ap.add_argument("--ncv", type=int, default=126, help="Krylov dimension of the H_AC / H_C Lanczos solves")
     args = ap.parse_args()
     args.warmup = max(args.warmup, 3)
+    _CONCURRENT[0] = not args.serial_solves
     if args.mode in ("vumps", "trace", "cpp") or args.impl == "reference":
         if args.workload not in WORKLOAD_DESCS:
             raise SystemExit(f"--workload for the VUMPS bench: one of {sorted(WORKLOAD_DESCS)}")

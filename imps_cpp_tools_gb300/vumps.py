@@ -22,7 +22,7 @@ class VumpsGPU:
                  fixed_tol=None, tolmin=5e-16, tolmax=1e-6, trueLR=True, svdthresh=5e-7, precision="fp64",
                  init_state=None, lanczos_maxit=300, gmres_maxit=4000, lanczos_ncv=126, eig_margin=0.1,
                  mixed_tm=False, verbose=False, mmax=None, dmmax=20, expand_pause=5, expand_thresh=1e-5,
-                 lamthresh=1e-12, autotune=False, **params):
+                 lamthresh=1e-12, autotune=False, concurrent=True, **params):
         import torch
         self.torch = torch
         self.verbose = verbose
@@ -50,6 +50,17 @@ class VumpsGPU:
         self.precision = precision
         # time the FP64 launch shapes of every plan's stages once per process (imps_plan_autotune)
         self.autotune = autotune
+        # The two H_C eigensolves of a site update (VUMPS_main.cpp:199-200) do not depend on its
+        # H_AC eigensolve (:186).  With concurrent=True each runs on a context of its own (own
+        # stream, Krylov workspace and pinned staging) from a host thread of its own, beside the
+        # H_AC eigensolve on this context: their small launches and host convergence checks fill
+        # each other's gaps.  The results are those of the serial order (no shared state).
+        self.concurrent = bool(concurrent)
+        if self.concurrent:
+            from concurrent.futures import ThreadPoolExecutor
+            self._side_streams = [torch.cuda.Stream() for _ in range(2)]
+            self._side_ctx = [B.Context(ctx.device, s) for s in self._side_streams]
+            self._pool = ThreadPoolExecutor(max_workers=2, thread_name_prefix="imps-hc")
         self.rng = np.random.default_rng(seed)
         self.stats = {"lanczos_applies": 0, "gmres_iters": 0, "hac_applies": 0, "hc_applies": 0, "expansions": 0}
         # bond expansion (ExpandFromH at VUMPS_main.cpp:270-308), off unless mmax (the largest total
@@ -89,14 +100,15 @@ class VumpsGPU:
         self.p_ac, self.p_hac, self.p_grad, self.p_hcl, self.p_hcr = [], [], [], [], []
         self.p_mul_r_t, self.p_mul_l_t, self.p_mul_r, self.p_mul_l = [], [], [], []
         self.dec_ac_l, self.dec_ac_r = [], []
+        hc_ctx = self._side_ctx if self.concurrent else [ctx, ctx]
         self.tm = {}
         for n in range(2):
             l, r, m = n, 1 - n, 1 - n
             self.p_ac.append(B.plan_mps_bd(ctx, LA[n], LB[l], 0))                       # C[n] * AR(n)
             self.p_hac.append(B.plan_hac(ctx, LA[n], LB[l], LB[r], self.lHL[m], self.lHR[m], d))
             self.p_grad.append(B.plan_grad_right(ctx, LA[n], LA[n]))
-            self.p_hcl.append(B.plan_hc(ctx, LB[l], LB[l], LB[l], LA[m], LA[n], d, hnnz))  # CL = C[n]
-            self.p_hcr.append(B.plan_hc(ctx, LB[r], LB[r], LB[r], LA[n], LA[m], d, hnnz))  # CR = C[n+1]
+            self.p_hcl.append(B.plan_hc(hc_ctx[0], LB[l], LB[l], LB[l], LA[m], LA[n], d, hnnz))  # CL = C[n]
+            self.p_hcr.append(B.plan_hc(hc_ctx[1], LB[r], LB[r], LB[r], LA[n], LA[m], d, hnnz))  # CR = C[n+1]
             self.p_mul_r_t.append(B.plan_mps_bd(ctx, LA[n], LB[r], 1, transpose_x=True))  # A * X^T
             self.p_mul_l_t.append(B.plan_mps_bd(ctx, LA[n], LB[l], 0, transpose_x=True))  # X^T * A
             self.p_mul_r.append(B.plan_mps_bd(ctx, LA[n], LB[r], 1))                      # A * X
@@ -132,6 +144,10 @@ class VumpsGPU:
                 mixed += [self.tm[(k, n)] for k in ("L", "R") for n in range(2)]
             for p in mixed:
                 p.set_precision(N.PREC_BF16X6)
+        if self.concurrent:
+            # plan tables are uploaded by synchronous copies on the legacy default stream, whose
+            # last DMA the non-blocking streams of the H_C contexts do not wait for
+            self.torch.cuda.synchronize()
 
     # ------------------------------------------------------------------ small helpers
     def _tm(self, key, A, vin, vout):
@@ -293,18 +309,30 @@ class VumpsGPU:
         # no longer contracts prec (eigenvector error ~ tol |theta| / gap ~ prec).  The margin
         # restores the reference's effective accuracy.
         tol_eig = tol * self.eig_margin
-        # H_AC eigensolve (eigs_rs "SA", x0 = AC)
-        ev, na, _ = ops.eigs_rs(hac, AC, tol_eig, ncv=self.lanczos_ncv, maxit=self.lanczos_maxit)
-        self.stats["lanczos_applies"] += na
-        self.stats["hac_applies"] += na + 1
         # H_C eigensolves for CL = C[n] (EHL, EHR1) and CR = C[n+1] (EHL1, EHR)
+        CL, CR = self.C[l].clone(), self.C[r].clone()
+        main = torch.cuda.current_stream()
+        if self.concurrent:
+            for s in self._side_streams:
+                s.wait_stream(main)  # the operands and start vectors are written on this stream
         pl = self.p_hcl[n]
         pl.bind(2, self.EHL); pl.bind(3, self.EHR1); pl.bind(4, self.AL[m]); pl.bind(5, self.AR[n]); pl.prepare()
         pr = self.p_hcr[n]
         pr.bind(2, self.EHL1); pr.bind(3, self.EHR); pr.bind(4, self.AL[n]); pr.bind(5, self.AR[m]); pr.prepare()
-        CL, CR = self.C[l].clone(), self.C[r].clone()
-        _, na1, _ = ops.eigs_rs(pl, CL, tol_eig, ncv=self.lanczos_ncv, maxit=self.lanczos_maxit)
-        _, na2, _ = ops.eigs_rs(pr, CR, tol_eig, ncv=self.lanczos_ncv, maxit=self.lanczos_maxit)
+        kw = dict(ncv=self.lanczos_ncv, maxit=self.lanczos_maxit)
+        if self.concurrent:
+            jobs = [self._pool.submit(ops.eigs_rs, p, x, tol_eig, **kw) for p, x in ((pl, CL), (pr, CR))]
+        # H_AC eigensolve (eigs_rs "SA", x0 = AC)
+        ev, na, _ = ops.eigs_rs(hac, AC, tol_eig, **kw)
+        self.stats["lanczos_applies"] += na
+        self.stats["hac_applies"] += na + 1
+        if self.concurrent:
+            (_, na1, _), (_, na2, _) = (j.result() for j in jobs)
+            for s in self._side_streams:
+                main.wait_stream(s)
+        else:
+            _, na1, _ = ops.eigs_rs(pl, CL, tol_eig, **kw)
+            _, na2, _ = ops.eigs_rs(pr, CR, tol_eig, **kw)
         self.stats["lanczos_applies"] += na1 + na2
         self.stats["hc_applies"] += na1 + na2
         ops.sign_normalize(ctx, CL)

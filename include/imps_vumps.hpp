@@ -20,7 +20,9 @@
 #include <array>
 #include <cmath>
 #include <map>
+#include <exception>
 #include <memory>
+#include <thread>
 #include <vector>
 
 #include "imps_gb300.hpp"
@@ -51,6 +53,10 @@ struct vumps_options {
   int lanczos_ncv = 126, lanczos_maxit = 300, gmres_maxit = 4000;
   bool trueLR = true;
   bool autotune = false;  // time every plan's FP64 launch shapes once (imps_plan_autotune)
+  // the two H_C eigensolves of a site update (VUMPS_main.cpp:199-200) on contexts of their own
+  // (non-blocking streams, own Krylov workspaces) from threads of their own, beside the H_AC
+  // eigensolve (:186); the results are those of the serial order
+  bool concurrent = true;
 };
 
 // a device vector of doubles
@@ -124,6 +130,12 @@ class vumps {
         const std::array<std::vector<double>, 6>& init, const vumps_options& o = vumps_options())
       : ctx_(ctx), m_(m), dims_(dimvec), o_(o) {
     check(imps_ctx_set_stream(ctx_.get(), nullptr), "imps_ctx_set_stream");
+    if (o_.concurrent) {
+      int dev = 0;
+      cuda_check(cudaGetDevice(&dev), "cudaGetDevice");
+      cuda_check(cudaEventCreateWithFlags(&ev_main_, cudaEventDisableTiming), "cudaEventCreate");
+      for (side_ctx& s : side_) s.open(dev);
+    }
     const int nsym = (int)m_.I2K.at(0).size();
     for (const auto& z : m_.h) { hr_.push_back(z.row); hc_.push_back(z.col); hv_.push_back(z.val); }
     for (int n = 0; n < 2; ++n) {
@@ -131,6 +143,9 @@ class vumps {
       LB_.emplace_back(nsym, bd_blocks(dims_[n]));
     }
     build_plans();
+    // plan tables are uploaded by synchronous copies on the legacy default stream, whose last DMA
+    // the non-blocking streams of the H_C contexts do not wait for
+    if (o_.concurrent) cuda_check(cudaDeviceSynchronize(), "cudaDeviceSynchronize");
     for (int n = 0; n < 2; ++n) {
       AL_[n] = dvec(LA_[n].nelem()); AL_[n].upload(init[n]);
       AR_[n] = dvec(LA_[n].nelem()); AR_[n].upload(init[2 + n]);
@@ -168,12 +183,48 @@ class vumps {
     return E;
   }
 
+  ~vumps() {
+    if (ev_main_) cudaEventDestroy(ev_main_);
+  }
+  vumps(const vumps&) = delete;
+  vumps& operator=(const vumps&) = delete;
+
   const dvec& AL(int n) const { return AL_[n]; }
   const dvec& AR(int n) const { return AR_[n]; }
   const dvec& C(int b) const { return C_[b]; }
 
  private:
+  static void cuda_check(cudaError_t e, const char* what) {
+    if (e != cudaSuccess) throw error(IMPS_ERR_CUDA, what);
+  }
+  // a context of its own for one H_C eigensolve: a non-blocking stream, ordered with the legacy
+  // default stream of the main context by events
+  struct side_ctx {
+    cudaStream_t stream = nullptr;
+    cudaEvent_t done = nullptr;
+    std::unique_ptr<context> ctx;
+    int device = 0;
+    side_ctx() = default;
+    side_ctx(const side_ctx&) = delete;
+    side_ctx& operator=(const side_ctx&) = delete;
+    void open(int dev) {
+      device = dev;
+      ctx = std::make_unique<context>(dev);
+      cuda_check(cudaStreamCreateWithFlags(&stream, cudaStreamNonBlocking), "cudaStreamCreate");
+      cuda_check(cudaEventCreateWithFlags(&done, cudaEventDisableTiming), "cudaEventCreate");
+      check(imps_ctx_set_stream(ctx->get(), stream), "imps_ctx_set_stream");
+    }
+    ~side_ctx() {
+      ctx.reset();  // synchronises its stream
+      if (stream) cudaStreamDestroy(stream);
+      if (done) cudaEventDestroy(done);
+    }
+  };
+
   context& ctx_;
+  // destroyed after the plans below (declared before them), which synchronise their context
+  std::array<side_ctx, 2> side_;
+  cudaEvent_t ev_main_ = nullptr;
   model m_;
   std::array<bond_dims, 2> dims_;
   vumps_options o_;
@@ -217,6 +268,7 @@ class vumps {
 
   void build_plans() {
     imps_ctx* c = ctx_.get();
+    imps_ctx* hc_ctx[2] = {o_.concurrent ? side_[0].ctx->get() : c, o_.concurrent ? side_[1].ctx->get() : c};
     const int d = m_.d, nnz = (int)hv_.size();
     imps_plan* p = nullptr;
     for (int mm = 0; mm < 2; ++mm) {
@@ -235,10 +287,12 @@ class vumps {
       p_hac_.push_back(mk(imps_plan_hac(c, LA_[n].get(), LB_[l].get(), LB_[r].get(), lHL_[mm].get(), lHR_[mm].get(),
                                         d, &p), p, "imps_plan_hac"));
       p_grad_.push_back(mk(imps_plan_grad_right(c, LA_[n].get(), LA_[n].get(), &p), p, "imps_plan_grad_right"));
-      p_hcl_.push_back(mk(imps_plan_hc(c, LB_[l].get(), LB_[l].get(), LB_[l].get(), LA_[mm].get(), LA_[n].get(), d,
-                                       nnz, hr_.data(), hc_.data(), hv_.data(), &p), p, "imps_plan_hc"));
-      p_hcr_.push_back(mk(imps_plan_hc(c, LB_[r].get(), LB_[r].get(), LB_[r].get(), LA_[n].get(), LA_[mm].get(), d,
-                                       nnz, hr_.data(), hc_.data(), hv_.data(), &p), p, "imps_plan_hc"));
+      p_hcl_.push_back(mk(imps_plan_hc(hc_ctx[0], LB_[l].get(), LB_[l].get(), LB_[l].get(), LA_[mm].get(),
+                                       LA_[n].get(), d, nnz, hr_.data(), hc_.data(), hv_.data(), &p), p,
+                          "imps_plan_hc"));
+      p_hcr_.push_back(mk(imps_plan_hc(hc_ctx[1], LB_[r].get(), LB_[r].get(), LB_[r].get(), LA_[n].get(),
+                                       LA_[mm].get(), d, nnz, hr_.data(), hc_.data(), hv_.data(), &p), p,
+                          "imps_plan_hc"));
       p_mul_r_t_.push_back(mk(imps_plan_mps_bd(c, LA_[n].get(), LB_[r].get(), 1 | 2, 1.0, &p), p, "mps_bd"));
       p_mul_l_t_.push_back(mk(imps_plan_mps_bd(c, LA_[n].get(), LB_[l].get(), 0 | 2, 1.0, &p), p, "mps_bd"));
       p_mul_r_.push_back(mk(imps_plan_mps_bd(c, LA_[n].get(), LB_[r].get(), 1, 1.0, &p), p, "mps_bd"));
@@ -357,13 +411,13 @@ class vumps {
     gmres_iters += it;
     return V;
   }
-  double eigs(plan& p, dvec& x, double tol) {
+  // eigs_rs "SA" with x0 = x; returns the number of applies
+  int eigs(plan& p, dvec& x, double tol) const {
     double e = 0.0;
     int na = 0;
     check(imps_eigs_rs(p.get(), x.get(), IMPS_MEM_DEVICE, tol, o_.lanczos_ncv, o_.lanczos_maxit, &e, &na),
           "eigs_rs");
-    lanczos_applies += na;
-    return e;
+    return na;
   }
   double absmax(const dvec& x) {
     double r = 0.0;
@@ -412,16 +466,58 @@ class vumps {
     check(imps_grad_norm_right(g.get(), &F[n]), "GradNormRight");
     const double tol = o_.fixed_tol > 0 ? o_.fixed_tol : std::min(std::max(prec[n] / 100.0, o_.tolmin), o_.tolmax);
     const double tol_eig = tol * o_.eig_margin;
-    eigs(hac, AC, tol_eig);
+    // H_C eigensolves for CL = C[n] (EHL, EHR1) and CR = C[n+1] (EHL1, EHR)
+    dvec CL = C_[l].clone(), CR = C_[r].clone();
+    if (o_.concurrent) {
+      // the operands and start vectors were written on the legacy default stream
+      cuda_check(cudaEventRecord(ev_main_, nullptr), "cudaEventRecord");
+      for (side_ctx& s : side_) cuda_check(cudaStreamWaitEvent(s.stream, ev_main_, 0), "cudaStreamWaitEvent");
+    }
     plan& pl = p_hcl_[n];
     pl.bind(2, EHL_.get()); pl.bind(3, EHR1_.get()); pl.bind(4, AL_[mm].get()); pl.bind(5, AR_[n].get());
     pl.prepare();
     plan& pr = p_hcr_[n];
     pr.bind(2, EHL1_.get()); pr.bind(3, EHR_.get()); pr.bind(4, AL_[n].get()); pr.bind(5, AR_[mm].get());
     pr.prepare();
-    dvec CL = C_[l].clone(), CR = C_[r].clone();
-    eigs(pl, CL, tol_eig);
-    eigs(pr, CR, tol_eig);
+    int na_c[2] = {0, 0};
+    std::exception_ptr err[2];
+    std::thread jobs[2];
+    if (o_.concurrent) {
+      plan* ps[2] = {&pl, &pr};
+      dvec* xs[2] = {&CL, &CR};
+      for (int k = 0; k < 2; ++k)
+        jobs[k] = std::thread([this, k, ps, xs, tol_eig, &na_c, &err] {
+          try {
+            cuda_check(cudaSetDevice(side_[k].device), "cudaSetDevice");
+            na_c[k] = eigs(*ps[k], *xs[k], tol_eig);
+          } catch (...) {
+            err[k] = std::current_exception();
+          }
+        });
+    }
+    // H_AC eigensolve (eigs_rs "SA", x0 = AC)
+    std::exception_ptr err_ac;
+    try {
+      lanczos_applies += eigs(hac, AC, tol_eig);
+    } catch (...) {
+      err_ac = std::current_exception();
+    }
+    if (o_.concurrent) {
+      for (std::thread& t : jobs) t.join();
+    }
+    if (err_ac) std::rethrow_exception(err_ac);
+    if (o_.concurrent) {
+      for (const std::exception_ptr& e : err)
+        if (e) std::rethrow_exception(e);
+      for (side_ctx& s : side_) {
+        cuda_check(cudaEventRecord(s.done, s.stream), "cudaEventRecord");
+        cuda_check(cudaStreamWaitEvent(nullptr, s.done, 0), "cudaStreamWaitEvent");
+      }
+    } else {
+      na_c[0] = eigs(pl, CL, tol_eig);
+      na_c[1] = eigs(pr, CR, tol_eig);
+    }
+    lanczos_applies += na_c[0] + na_c[1];
     check(imps_sign_normalize(c, CL.get(), CL.size()), "sign");
     check(imps_sign_normalize(c, CR.get(), CR.size()), "sign");
     if (dosvd_ && prec[n] < o_.svdthresh) dosvd_ = false;

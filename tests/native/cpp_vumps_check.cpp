@@ -4,7 +4,7 @@
 //
 // Input (whitespace separated): d nsym; I2K (d x nsym ints); for bonds 0 and 1: nsectors, then per
 // sector nsym ints and the dimension; nnz, then per nonzero row col value; nsweeps fixed_tol
-// InvETol eig_margin autotune(0/1); then the flat AL(0), AL(1), AR(0), AR(1), C[0], C[1] (their
+// InvETol eig_margin autotune(0/1) concurrent(0/1); then the flat AL(0), AL(1), AR(0), AR(1), C[0], C[1] (their
 // lengths follow from the layouts).  Per sweep it also prints the wall time of the sweep
 // (synchronised) in ms and the Lanczos applies so far.
 #include <chrono>
@@ -43,9 +43,10 @@ int main(int argc, char** argv) {
   }
   int nsweeps = 0;
   imps_cpp::vumps_options o;
-  int tune = 0;
-  in >> nsweeps >> o.fixed_tol >> o.InvETol >> o.eig_margin >> tune;
+  int tune = 0, conc = 1;
+  in >> nsweeps >> o.fixed_tol >> o.InvETol >> o.eig_margin >> tune >> conc;
   o.autotune = tune != 0;
+  o.concurrent = conc != 0;
   std::array<std::vector<double>, 6> init;
   for (int n = 0; n < 2; ++n) {
     const int64_t na = imps_cpp::layout(nsym, imps_cpp::mps_blocks(m.I2K, dims[n], dims[1 - n])).nelem();

@@ -17,7 +17,10 @@ from tests.test_native_host import _build_cpp_host
 pytestmark = pytest.mark.gpu
 
 
-def test_cpp_vumps_matches_python_driver(cuda_ctx, tmp_path):
+@pytest.mark.parametrize("concurrent", [1, 0])
+def test_cpp_vumps_matches_python_driver(cuda_ctx, tmp_path, concurrent):
+    """concurrent = 1: the C++ driver's H_C eigensolves run on their own contexts and threads
+    beside the H_AC eigensolve; 0: after it, on one stream."""
     d, I2K, h = models.build_model("xxz", J=1.0, Delta=-1.0)
     hnnz = models.h_nonzeros(h)
     dimvec = [B0, B1]
@@ -30,7 +33,7 @@ def test_cpp_vumps_matches_python_driver(cuda_ctx, tmp_path):
         lines += [" ".join(str(x) for x in q) + f" {m}" for q, m in sorted(dimvec[b].items())]
     lines.append(str(len(hnnz)))
     lines += [f"{r} {c} {v!r}" for (r, c, v) in hnnz]
-    lines.append(f"{nsweeps} {tol!r} {invetol!r} 0.1 0")
+    lines.append(f"{nsweeps} {tol!r} {invetol!r} 0.1 0 {concurrent}")
     lines += [" ".join(repr(float(x)) for x in v) for v in flat]
     inp = tmp_path / "vumps_input.txt"
     inp.write_text("\n".join(lines) + "\n")

@@ -175,3 +175,30 @@ def test_sweep_from_warm_state_matches_oracle_full_size(cuda_ctx):
     times, Eo, _, cut = bench.cpu_site_updates(name, state, 0, 2, 600.0)
     assert not cut
     assert np.abs(Eg - np.asarray(Eo)).max() < 1e-9, (Eg, Eo)
+
+
+def test_concurrent_hc_solves_equal_serial(cuda_ctx):
+    """The H_C eigensolves run on their own contexts and host threads beside the H_AC eigensolve
+    (concurrent=True, the default) or after it on one stream: the sweeps are bit-identical (no
+    state is shared between the solves), from the committed warmed XXZ D=512 state at the
+    benchmark's tolerances."""
+    import torch
+    import bench
+    from imps_cpp_tools_gb300 import configs
+    from imps_cpp_tools_gb300 import workload as W
+    name = "xxz_d512"
+    state = W.load_warm_state(name)
+    model, fn, params = configs.WORKLOADS[name]
+    runs = []
+    for concurrent in (False, True):
+        init = {k: [torch.from_numpy(a).to("cuda") for a in state[k]] for k in ("AL", "AR", "C")}
+        gpu = VumpsGPU(cuda_ctx, model, dims0=fn(), init_state=init, fixed_tol=bench.TIMED_TOLS["eig"],
+                       InvETol=bench.TIMED_TOLS["gmres"], eig_margin=1.0, concurrent=concurrent, **params)
+        runs.append([gpu.sweep() for _ in range(2)] + [dict(gpu.stats)] + [gpu.host_state()])
+    for a, b in zip(runs[0][:2], runs[1][:2]):
+        for x, y in zip(a, b):
+            assert np.array_equal(x, y), (x, y)
+    assert runs[0][2] == runs[1][2]
+    for k in ("AL", "AR", "C"):
+        for x, y in zip(runs[0][3][k], runs[1][3][k]):
+            assert np.array_equal(x, y)
