@@ -17,6 +17,16 @@ from . import blocks as B
 from . import models, ops
 
 
+class _PlanSet:
+    """Transfer-matrix plans of the right-environment chain of a site update on a context of its
+    own, so that the chain runs beside the left-environment chain (VumpsGPU(concurrent=True))."""
+
+    def __init__(self, ctx, stream):
+        self.ctx, self.stream = ctx, stream
+        self.tm, self.optm_r = {}, []
+        self.iters = 0  # GMRES / fixed-point iterations, added to the driver's count after the join
+
+
 class VumpsGPU:
     def __init__(self, ctx, model, dims0=None, dimvec=None, seed=1, InvETol=5e-15, InvEfac=2.0,
                  fixed_tol=None, tolmin=5e-16, tolmax=1e-6, trueLR=True, svdthresh=5e-7, precision="fp64",
@@ -51,10 +61,12 @@ class VumpsGPU:
         # time the FP64 launch shapes of every plan's stages once per process (imps_plan_autotune)
         self.autotune = autotune
         # The two H_C eigensolves of a site update (VUMPS_main.cpp:199-200) do not depend on its
-        # H_AC eigensolve (:186).  With concurrent=True each runs on a context of its own (own
-        # stream, Krylov workspace and pinned staging) from a host thread of its own, beside the
-        # H_AC eigensolve on this context: their small launches and host convergence checks fill
-        # each other's gaps.  The results are those of the serial order (no shared state).
+        # H_AC eigensolve (:186), nor the right environment (:241-247) on the left one
+        # (:236-240).  With concurrent=True each H_C eigensolve, and then the right-environment
+        # chain, runs on a context of its own (own stream, Krylov workspace and pinned staging)
+        # from a host thread of its own, beside the H_AC eigensolve / the left-environment chain
+        # on this context: their small launches and host convergence checks fill each other's
+        # gaps.  The results are those of the serial order (no shared state).
         self.concurrent = bool(concurrent)
         if self.concurrent:
             from concurrent.futures import ThreadPoolExecutor
@@ -128,10 +140,27 @@ class VumpsGPU:
         self.optm_l = [B.plan_optm(ctx, LA[a], LA[1 - a], d, hnnz, 0, LB[a]) for a in range(2)]
         self.optm_r = [B.plan_optm(ctx, LA[a], LA[1 - a], d, hnnz, 1, LB[a]) for a in range(2)]
         self.flops_hac = [p.info()["flops_apply"] for p in self.p_hac]
+        # identity BlockDiagMats of the two bonds (made here, on this stream, for both chains)
+        self.eyes = [self._make_eye(b) for b in range(2)]
+        self._env = None
+        if self.concurrent:
+            # the right-environment chain's own plans (the left chain binds the same unit-cell
+            # transfer matrices to AL at the same time), on the second H_C context
+            ps = _PlanSet(self._side_ctx[1], self._side_streams[1])
+            for n in range(2):
+                l, r, m = n, 1 - n, 1 - n
+                for kind, dirc in (("L", 0), ("R", 1)):
+                    ps.tm[(kind, n)] = B.plan_tm(ps.ctx, [LA[n], LA[m]], dirc, LB[l], LB[l])
+                ps.tm[("R1", n)] = B.plan_tm(ps.ctx, [LA[n]], 1, LB[r], LB[l])
+                ps.tm[("cct", n, False)] = B.plan_mps_bd(ps.ctx, LB[n], LB[n], 0, transpose_x=True)
+            ps.optm_r = [B.plan_optm(ps.ctx, LA[a], LA[1 - a], d, hnnz, 1, LB[a]) for a in range(2)]
+            self._env = ps
         if self.autotune:
             plans = (self.redop_l + self.redop_r + self.p_ac + self.p_hac + self.p_grad + self.p_hcl + self.p_hcr
                      + self.p_mul_r_t + self.p_mul_l_t + self.p_mul_r + self.p_mul_l + self.optm_l + self.optm_r
                      + list(self.tm.values()))
+            if self._env is not None:
+                plans += list(self._env.tm.values()) + self._env.optm_r
             self.tuned_stages = sum(p.autotune() for p in plans)
         if self.precision == "bf16x6":
             # tensor-core applies inside the Krylov solvers; Krylov vectors, residuals,
@@ -142,6 +171,8 @@ class VumpsGPU:
             # GMRES back to FP64 accuracy restarts the Krylov space and doubles the iterations
             if self.mixed_tm:
                 mixed += [self.tm[(k, n)] for k in ("L", "R") for n in range(2)]
+                if self._env is not None:
+                    mixed += [self._env.tm[(k, n)] for k in ("L", "R") for n in range(2)]
             for p in mixed:
                 p.set_precision(N.PREC_BF16X6)
         if self.concurrent:
@@ -150,8 +181,8 @@ class VumpsGPU:
             self.torch.cuda.synchronize()
 
     # ------------------------------------------------------------------ small helpers
-    def _tm(self, key, A, vin, vout):
-        p = self.tm[key]
+    def _tm(self, key, A, vin, vout, ps=None):
+        p = (self.tm if ps is None else ps.tm)[key]
         n = key[1]
         if key[0] in ("L", "R"):
             p.bind(2, A[n]); p.bind(3, A[1 - n])
@@ -161,8 +192,8 @@ class VumpsGPU:
         p.run()
         return vout
 
-    def _optm(self, left, a, A, out):
-        p = (self.optm_l if left else self.optm_r)[a]
+    def _optm(self, left, a, A, out, ps=None):
+        p = (self.optm_l if left else (self.optm_r if ps is None else ps.optm_r))[a]
         p.bind(0, A[a]); p.bind(1, A[1 - a]); p.bind(2, out)
         p.run()
         return out
@@ -172,11 +203,15 @@ class VumpsGPU:
         plan.run()
         return out
 
-    def _eye(self, b):
+    def _make_eye(self, b):
         v = np.zeros(self.LB[b].nelem)
         for (g, qi, qo, r, c), o in zip(self.LB[b].blocks, self.LB[b].offsets):
             v[o:o + r * c] = np.eye(r).reshape(-1)
         return self.torch.tensor(v, dtype=self.torch.float64, device="cuda")
+
+    def _eye(self, b):
+        """The identity BlockDiagMat of bond b (read only)."""
+        return self.eyes[b]
 
     def _redops(self, sites=(0, 1)):
         """ReducedOp (MPSBlockUtilities.hpp:37-74): HL from AL(m), HR from AR(m)."""
@@ -192,35 +227,42 @@ class VumpsGPU:
         t2 = self._optm(True, n, self.AL, self._z(self.LB[n]))       # OpTM(AL(n) AL(n+1)) on bond n
         return ops.axpby(self.ctx, 1.0, t2, 1.0, out)
 
-    def _get_hr(self, n):
+    def _get_hr(self, n, ps=None):
         """GetHR (VUMPS_helpers.hpp:20-36) of the unit cell [AR(n), AR(n+1)] -> bond n."""
         m = 1 - n
-        t = self._optm(False, m, self.AR, self._z(self.LB[m]))      # OpTM(AR(n+1) AR(n)) on bond n+1
-        out = self._tm(("R1", n), self.AR, t, self._z(self.LB[n]))   # through AR(n) -> bond n
-        t2 = self._optm(False, n, self.AR, self._z(self.LB[n]))      # OpTM(AR(n) AR(n+1)) on bond n
-        return ops.axpby(self.ctx, 1.0, t2, 1.0, out)
+        t = self._optm(False, m, self.AR, self._z(self.LB[m]), ps)      # OpTM(AR(n+1) AR(n)) on bond n+1
+        out = self._tm(("R1", n), self.AR, t, self._z(self.LB[n]), ps)   # through AR(n) -> bond n
+        t2 = self._optm(False, n, self.AR, self._z(self.LB[n]), ps)      # OpTM(AR(n) AR(n+1)) on bond n
+        return ops.axpby(self.ctx if ps is None else ps.ctx, 1.0, t2, 1.0, out)
 
-    def _bind_uc(self, key, A):
-        p = self.tm[key]
+    def _bind_uc(self, key, A, ps=None):
+        p = (self.tm if ps is None else ps.tm)[key]
         n = key[1]
         p.bind(2, A[n]); p.bind(3, A[1 - n])
         return p
 
-    def _invert_e(self, key, A, x, L, R, direction, y0, tol):
+    def _count_iters(self, it, ps):
+        if ps is None:
+            self.stats["gmres_iters"] += it
+        else:
+            ps.iters += it
+
+    def _invert_e(self, key, A, x, L, R, direction, y0, tol, ps=None):
         """InvertE_proj on the unit cell [A(n), A(n+1)], n = key[1]."""
         y = y0.clone() if y0 is not None else self._z_like(x)
-        it, rr, conv = ops.InvertE_proj(self._bind_uc(key, A), x, L, R, direction, y, tol, maxit=self.gmres_maxit)
-        self.stats["gmres_iters"] += it
+        it, rr, conv = ops.InvertE_proj(self._bind_uc(key, A, ps), x, L, R, direction, y, tol,
+                                        maxit=self.gmres_maxit)
+        self._count_iters(it, ps)
         return y
 
     def _z_like(self, x):
         return self.torch.zeros_like(x)
 
-    def _tm_dominant(self, key, A, x0, tol):
+    def _tm_dominant(self, key, A, x0, tol, ps=None):
         """TMDominantEig on the unit cell [A(n), A(n+1)], n = key[1]."""
         V = self._z_like(x0)
-        _, it, _ = ops.TMDominantEig(self._bind_uc(key, A), V, x0, tol, maxit=self.gmres_maxit)
-        self.stats["gmres_iters"] += it
+        _, it, _ = ops.TMDominantEig(self._bind_uc(key, A, ps), V, x0, tol, maxit=self.gmres_maxit)
+        self._count_iters(it, ps)
         return V
 
     # ------------------------------------------------------------------ initial state
@@ -268,15 +310,15 @@ class VumpsGPU:
         self.E = None
         torch.cuda.synchronize()
 
-    def _cct(self, b, right=True):
+    def _cct(self, b, right=True, ps=None):
         """C C^T (right=True) or C^T C on bond b."""
         out = self._z(self.LB[b])
-        ctx = self.ctx
+        ctx, tm = (self.ctx, self.tm) if ps is None else (ps.ctx, ps.tm)
         # BlockDiag products through the MPS x BlockDiag plans with d = 1 (layout of a BD)
         key = ("cct", b, right)
-        if key not in self.tm:
-            self.tm[key] = B.plan_mps_bd(ctx, self.LB[b], self.LB[b], 1 if right else 0, transpose_x=True)
-        p = self.tm[key]
+        if key not in tm:
+            tm[key] = B.plan_mps_bd(ctx, self.LB[b], self.LB[b], 1 if right else 0, transpose_x=True)
+        p = tm[key]
         # right: C * C^T ; left: C^T * C
         return self._mul(p, self.C[b], self.C[b], out)
 
@@ -371,6 +413,11 @@ class VumpsGPU:
         self.AL[n], self.AR[n], self.C[r], self.C[l] = ALnew, ARnew, CR, CL
         # left environment: R = CL CL^T, fixed point of [AL(n), AL(n+1)], EHL on bond n
         gtol = max(tol / self.InvEfac, self.InvETol)
+        if self.concurrent:
+            # the right-environment chain on its own context and thread (see __init__)
+            ps = self._env
+            ps.stream.wait_stream(main)  # AL, AR, C of this site update are written on this stream
+            job = self._pool.submit(self._right_env_job, n, gtol, ps)
         R = self._cct(l, right=True)
         if self.trueLR:
             R = self._tm_dominant(("R", n), self.AL, R, 1e-15)
@@ -381,13 +428,14 @@ class VumpsGPU:
                            self._tm(("L1", n), self.AL, self.EHL, self._z(self.LB[r])))
         self.EHL1 = ops.axpby(ctx, 1.0, self._optm(True, n, self.AL, self._z(self.LB[l])), 1.0,
                               self._tm(("L1", m), self.AL, EHLtmp, self._z(self.LB[l])))
-        # right environment for site n+1: L = C^T C on bond n (= bond n+2), [AR(n), AR(n+1)]
-        Lm = self._cct(l, right=False)
-        if self.trueLR:
-            Lm = self._tm_dominant(("L", n), self.AR, Lm, 1e-15)
-        HAR = self._get_hr(n)
-        y0 = self.EHR0[m]
-        self.EHR = self._invert_e(("R", n), self.AR, HAR, Lm, self._eye(l), "r", y0, gtol)
+        if self.concurrent:
+            self.EHR = job.result()
+            main.wait_stream(ps.stream)
+            self.EHR.record_stream(main)  # allocated on the chain's stream, used on this one
+            self.stats["gmres_iters"] += ps.iters
+            ps.iters = 0
+        else:
+            self.EHR = self._right_env(n, gtol)
         if self.mmax is not None and self._expand_now(n) and self._expand(n):
             # EHL on the grown bond (VUMPS_main.cpp:301); EHL1, EHR and the bond-n objects keep
             # their values (AL(n+1) only gained zero rows)
@@ -398,6 +446,21 @@ class VumpsGPU:
                               self._optm(False, m, self.AR, self._z(self.LB[r])))
         # HL = ReducedOp(H, AL(n), l), HR = ReducedOp(H, AR(n), r) (VUMPS_main.cpp:311-312)
         self._redops((n,))
+
+    def _right_env(self, n, gtol, ps=None):
+        """Right environment for site n+1 (VUMPS_main.cpp:241-247): L = C^T C on bond n (= bond
+        n+2), its fixed point of [AR(n), AR(n+1)], then EHR by InvertE_proj from the previous
+        EHR of this site; with the plans of `ps` (default: this context's)."""
+        l, m = n, 1 - n
+        Lm = self._cct(l, right=False, ps=ps)
+        if self.trueLR:
+            Lm = self._tm_dominant(("L", n), self.AR, Lm, 1e-15, ps)
+        HAR = self._get_hr(n, ps)
+        return self._invert_e(("R", n), self.AR, HAR, Lm, self._eye(l), "r", self.EHR0[m], gtol, ps)
+
+    def _right_env_job(self, n, gtol, ps):
+        with self.torch.cuda.stream(ps.stream):  # temporaries of the chain on its own stream
+            return self._right_env(n, gtol, ps)
 
     def sweep(self):
         """One iteration of the outer loop (VUMPS_main.cpp:165-354); returns (E, F, prec)."""
