@@ -233,7 +233,7 @@ class vumps {
   std::vector<layout> LA_, LB_;
   std::array<dvec, 2> AL_, AR_, C_, eye_, HLbuf_, HRbuf_, EHR0_;
   std::array<bool, 2> have_ehr0_{false, false};
-  dvec EHL_, EHR_, EHL1_, EHR1_;
+  dvec EHL_, EHR_, EHL1_, EHR1_, EHLtmp_;
   bool dosvd_ = true;
   // plans (vumps.py _build_plans)
   std::vector<plan> redop_l_, redop_r_, p_ac_, p_hac_, p_grad_, p_hcl_, p_hcr_, p_mul_r_t_, p_mul_l_t_, p_mul_r_,
@@ -241,6 +241,11 @@ class vumps {
   std::map<std::pair<int, int>, plan> tm_;  // (kind, n): kind 0 L, 1 R, 2 L1, 3 R1
   std::vector<layout> lHL_, lHR_, rl_ac_l_, rl_ac_r_;
   std::array<plan, 4> cct_;  // (bond, right) -> C C^T (right) or C^T C
+  // the right-environment chain's own plans on side_[1] (the left chain binds the same unit-cell
+  // transfer matrices to AL at the same time), with o_.concurrent
+  std::map<std::pair<int, int>, plan> env_tm_;
+  std::vector<plan> env_optm_r_;
+  std::array<plan, 4> env_cct_;
 
   dvec z(const layout& L) const { return dvec(L.nelem()); }
 
@@ -320,12 +325,29 @@ class vumps {
       optm_r_.push_back(mk(imps_plan_optm(c, LA_[a].get(), LA_[1 - a].get(), d, nnz, hr_.data(), hc_.data(),
                                           hv_.data(), 1, LB_[a].get(), &p), p, "imps_plan_optm"));
     }
+    if (o_.concurrent) {
+      imps_ctx* e = side_[1].ctx->get();
+      for (int n = 0; n < 2; ++n) {
+        const int l = n, r = 1 - n, mm = 1 - n;
+        const imps_layout* uc[2] = {LA_[n].get(), LA_[mm].get()};
+        env_tm_.emplace(std::make_pair(0, n), mk(imps_plan_tm(e, 2, uc, 0, LB_[l].get(), LB_[l].get(), &p), p, "tm"));
+        env_tm_.emplace(std::make_pair(1, n), mk(imps_plan_tm(e, 2, uc, 1, LB_[l].get(), LB_[l].get(), &p), p, "tm"));
+        const imps_layout* one[1] = {LA_[n].get()};
+        env_tm_.emplace(std::make_pair(3, n), mk(imps_plan_tm(e, 1, one, 1, LB_[r].get(), LB_[l].get(), &p), p, "tm"));
+        env_cct_[2 * n] = mk(imps_plan_mps_bd(e, LB_[n].get(), LB_[n].get(), 0 | 2, 1.0, &p), p, "mps_bd");
+        env_optm_r_.push_back(mk(imps_plan_optm(e, LA_[n].get(), LA_[1 - n].get(), d, nnz, hr_.data(), hc_.data(),
+                                                hv_.data(), 1, LB_[n].get(), &p), p, "imps_plan_optm"));
+      }
+    }
     if (o_.autotune) {
       for (auto* v : {&redop_l_, &redop_r_, &p_ac_, &p_hac_, &p_grad_, &p_hcl_, &p_hcr_, &p_mul_r_t_, &p_mul_l_t_,
-                      &p_mul_r_, &p_mul_l_, &optm_l_, &optm_r_})
+                      &p_mul_r_, &p_mul_l_, &optm_l_, &optm_r_, &env_optm_r_})
         for (plan& q : *v) q.autotune();
-      for (auto& kv : tm_) kv.second.autotune();
+      for (auto* t : {&tm_, &env_tm_})
+        for (auto& kv : *t) kv.second.autotune();
       for (plan& q : cct_) q.autotune();
+      for (plan& q : env_cct_)
+        if (q.get()) q.autotune();
     }
   }
 
@@ -410,6 +432,58 @@ class vumps {
           "TMDominantEig");
     gmres_iters += it;
     return V;
+  }
+  // the plans of the right-environment chain and the context they run on
+  struct chain_plans {
+    imps_ctx* ctx;
+    std::map<std::pair<int, int>, plan>* tm;  // (0, n) L, (1, n) R, (3, n) R1
+    std::vector<plan>* optm_r;
+    std::array<plan, 4>* cct;  // [2b]: C^T C on bond b
+  };
+  // its buffers, allocated (and y filled with the previous EHR of the site) on the legacy default
+  // stream before the chain starts
+  struct env_bufs {
+    dvec L, V, t, out, t2, y;
+  };
+  env_bufs env_buffers(int n) {
+    const int l = n, mm = 1 - n;
+    return env_bufs{z(LB_[l]), z(LB_[l]), z(LB_[mm]), z(LB_[l]), z(LB_[l]),
+                    have_ehr0_[mm] ? EHR0_[mm].clone() : z(LB_[l])};
+  }
+  // Right environment for site n+1 (VUMPS_main.cpp:241-247): L = C^T C on bond n (= bond n+2), its
+  // fixed point of [AR(n), AR(n+1)], GetHR, then EHR by InvertE_proj into b.y; returns the
+  // iterations of the two solves
+  int right_env(int n, double gtol, chain_plans P, env_bufs& b) {
+    const int l = n, mm = 1 - n;
+    int iters = 0, it = 0;
+    mul((*P.cct)[2 * l], C_[l], C_[l], b.L);
+    const dvec* L = &b.L;
+    auto bind_uc = [&](plan& q) { q.bind(2, AR_[n].get()); q.bind(3, AR_[mm].get()); return q.get(); };
+    if (o_.trueLR) {
+      double lam = 0.0;
+      check(imps_tm_dominant(bind_uc(P.tm->at({0, n})), b.L.get(), b.V.get(), IMPS_MEM_DEVICE, 1e-15, o_.gmres_maxit,
+                             &lam, &it),
+            "TMDominantEig");
+      iters += it;
+      L = &b.V;
+    }
+    // GetHR (VUMPS_helpers.hpp:20-36) of [AR(n), AR(n+1)] -> bond n, into b.out
+    auto optm_r = [&](int a, dvec& out) {
+      plan& q = (*P.optm_r)[a];
+      q.bind(0, AR_[a].get()); q.bind(1, AR_[1 - a].get()); q.bind(2, out.get());
+      q.run();
+    };
+    optm_r(mm, b.t);
+    plan& r1 = P.tm->at({3, n});
+    r1.bind(2, AR_[n].get()); r1.bind(0, b.t.get()); r1.bind(1, b.out.get());
+    r1.run();
+    optm_r(n, b.t2);
+    check(imps_axpby(P.ctx, 1.0, b.t2.get(), 1.0, b.out.get(), b.out.size()), "imps_axpby");
+    double rr = 0.0;
+    check(imps_invert_e_proj(bind_uc(P.tm->at({1, n})), b.out.get(), L->get(), eye_[l].get(), IMPS_DIR_RIGHT,
+                             b.y.get(), IMPS_MEM_DEVICE, gtol, o_.gmres_maxit, 0, &it, &rr),
+          "InvertE_proj");
+    return iters + it;
   }
   // eigs_rs "SA" with x0 = x; returns the number of applies
   int eigs(plan& p, dvec& x, double tol) const {
@@ -565,6 +639,54 @@ class vumps {
     C_[l] = std::move(CL);
     // left environment: R = CL CL^T, fixed point of [AL(n), AL(n+1)], EHL on bond n
     const double gtol = std::max(tol / o_.InvEfac, o_.InvETol);
+    // the right environment: with o_.concurrent on side_[1] (its own plans and a thread) beside
+    // the left chain
+    env_bufs eb = env_buffers(n);
+    int env_iters = 0;
+    std::exception_ptr env_err;
+    std::thread env_job;
+    if (o_.concurrent) {
+      cuda_check(cudaEventRecord(ev_main_, nullptr), "cudaEventRecord");
+      cuda_check(cudaStreamWaitEvent(side_[1].stream, ev_main_, 0), "cudaStreamWaitEvent");
+      env_job = std::thread([this, n, gtol, &eb, &env_iters, &env_err] {
+        try {
+          cuda_check(cudaSetDevice(side_[1].device), "cudaSetDevice");
+          env_iters = right_env(n, gtol, chain_plans{side_[1].ctx->get(), &env_tm_, &env_optm_r_, &env_cct_}, eb);
+        } catch (...) {
+          env_err = std::current_exception();
+        }
+      });
+    }
+    try {
+      left_env(n, gtol);
+    } catch (...) {
+      if (env_job.joinable()) env_job.join();
+      throw;
+    }
+    if (o_.concurrent) {
+      env_job.join();
+      if (env_err) std::rethrow_exception(env_err);
+      cuda_check(cudaEventRecord(side_[1].done, side_[1].stream), "cudaEventRecord");
+      cuda_check(cudaStreamWaitEvent(nullptr, side_[1].done, 0), "cudaStreamWaitEvent");
+    } else {
+      env_iters = right_env(n, gtol, chain_plans{c, &tm_, &optm_r_, &cct_}, eb);
+    }
+    gmres_iters += env_iters;
+    EHR_ = std::move(eb.y);
+    EHL_ = std::move(EHLtmp_);
+    dvec er = z(LB_[r]);
+    tm(3, mm, AR_, EHR_, er);
+    dvec er2 = z(LB_[r]);
+    optm(false, mm, AR_, er2);
+    axpby(1.0, er, 1.0, er2);
+    EHR1_ = std::move(er2);
+    redops(n);
+  }
+
+  // the left-environment chain of site n (VUMPS_main.cpp:236-240): EHL on bond n, EHL1, and EHL
+  // shifted to bond n+1 (kept in EHLtmp_ until the right chain has finished)
+  void left_env(int n, double gtol) {
+    const int l = n, r = 1 - n, mm = 1 - n;
     dvec R = cct(l, true);
     if (o_.trueLR) R = tm_dominant(1, n, AL_, R, 1e-15);
     dvec HAL = get_hl(n);
@@ -582,19 +704,7 @@ class vumps {
     tm(2, mm, AL_, EHLtmp, tt2);
     axpby(1.0, e1, 1.0, tt2);
     EHL1_ = std::move(tt2);
-    // right environment for site n+1: L = C^T C on bond n, [AR(n), AR(n+1)]
-    dvec Lm = cct(l, false);
-    if (o_.trueLR) Lm = tm_dominant(0, n, AR_, Lm, 1e-15);
-    dvec HAR = get_hr(n);
-    EHR_ = invert_e(1, n, AR_, HAR, Lm, eye_[l], 'r', have_ehr0_[mm] ? &EHR0_[mm] : nullptr, gtol);
-    EHL_ = std::move(EHLtmp);
-    dvec er = z(LB_[r]);
-    tm(3, mm, AR_, EHR_, er);
-    dvec er2 = z(LB_[r]);
-    optm(false, mm, AR_, er2);
-    axpby(1.0, er, 1.0, er2);
-    EHR1_ = std::move(er2);
-    redops(n);
+    EHLtmp_ = std::move(EHLtmp);
   }
 };
 
