@@ -151,19 +151,50 @@ static int max_splits(const Stage& S, int T) {
   return std::max(1, std::min(8, max_chunks / (T == 16 ? 4 : 2)));
 }
 
-// (re)build the stage's tiles for shape (T, splits) and upload them
+// (re)build the stage's tiles for shape (T, splits) and upload them.  Split-K in proportion to
+// the work: the tile with the most K chunks is split over `splits` CTAs, every other tile over
+// ceil(splits x its chunks / the most chunks), each share keeping at least one chunk per K group
+// of the kernel, so that the CTAs of a launch carry about equal work; the CTA entries are ordered
+// by decreasing work.
 static int install_stage(Stage& S, int T, int splits) {
   cudaFree(S.d_tiles); cudaFree(S.d_ws); cudaFree(S.d_cnt);
   S.d_tiles = nullptr; S.d_ws = nullptr; S.d_cnt = nullptr;
   finalize_tiles(S, T, T);
   S.splits = splits;
+  const int ks = T == 16 ? 4 : 2;  // K groups of the kernel for this tile size
+  const size_t ntiles = S.tiles.size();
+  std::vector<int> ch(ntiles, 0);
+  int cmax = 1;
+  for (size_t i = 0; i < ntiles; ++i) {
+    for (int t = S.tiles[i].t0; t < S.tiles[i].t1; ++t) ch[i] += (S.terms[t].k + 15) / 16;
+    cmax = std::max(cmax, ch[i]);
+  }
+  std::vector<Tile> units;
+  int nws = 0;
+  for (size_t i = 0; i < ntiles; ++i) {
+    Tile t = S.tiles[i];
+    int np = splits > 1 ? (int)(((int64_t)ch[i] * splits + cmax - 1) / cmax) : 1;
+    np = std::max(1, std::min(np, ch[i] / ks));
+    t.nparts = np;
+    t.cnt_idx = (int)i;
+    t.ws_unit = np > 1 ? nws : 0;
+    if (np > 1) nws += np;
+    for (int q = 0; q < np; ++q) {
+      t.part = q;
+      units.push_back(t);
+    }
+  }
+  std::stable_sort(units.begin(), units.end(), [&](const Tile& a, const Tile& b) {
+    return (int64_t)ch[a.cnt_idx] * b.nparts > (int64_t)ch[b.cnt_idx] * a.nparts;
+  });
+  S.tiles = std::move(units);
   if (!S.tiles.empty()) {
     CK(cudaMalloc(&S.d_tiles, S.tiles.size() * sizeof(Tile)));
     CK(cudaMemcpy(S.d_tiles, S.tiles.data(), S.tiles.size() * sizeof(Tile), cudaMemcpyHostToDevice));
     if (S.splits > 1) {
-      CK(cudaMalloc(&S.d_ws, S.tiles.size() * S.splits * (size_t)T * T * sizeof(double)));
-      CK(cudaMalloc(&S.d_cnt, S.tiles.size() * sizeof(int)));
-      CK(cudaMemset(S.d_cnt, 0, S.tiles.size() * sizeof(int)));
+      CK(cudaMalloc(&S.d_ws, (size_t)std::max(nws, 1) * T * T * sizeof(double)));
+      CK(cudaMalloc(&S.d_cnt, std::max<size_t>(ntiles, 1) * sizeof(int)));
+      CK(cudaMemset(S.d_cnt, 0, std::max<size_t>(ntiles, 1) * sizeof(int)));
     }
   }
   return IMPS_OK;

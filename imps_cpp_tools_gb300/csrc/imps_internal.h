@@ -66,8 +66,12 @@ struct Tile {
   int32_t t0, t1;
   int16_t c_slot;
   int16_t accumulate;  // 1: C += sum, 0: C = sum
+  // split-K: the CTA of this entry takes share `part` of `nparts` equal shares of the tile's K
+  // chunks; with nparts > 1 it stores its partial tile at workspace tile ws_unit + part, and the
+  // ticket counter cnt_idx picks the CTA that sums the tile's partials
+  int32_t part, nparts, ws_unit, cnt_idx;
 };
-static_assert(sizeof(Tile) == 40, "Tile layout");
+static_assert(sizeof(Tile) == 56, "Tile layout");
 
 // Logical output block with its terms (kept on the host for table export and for the
 // tensor-core packer).
@@ -152,5 +156,7 @@ void finalize_tiles(Stage& S, int tm, int tn);
 
 // ----- kernel launchers (kernels_f64.cu) -----
 struct imps_dslots { double* p[imps::kMaxSlots]; };
+// ntiles: table entries, one CTA each; splits: the largest share count of a tile (> 1 needs the
+// workspace ws and the ticket counters cnt)
 int imps_launch_grouped_f64(const void* d_tiles, int ntiles, const void* d_terms, imps_dslots slots,
                             int tile_m, int splits, double* ws, int* cnt, void* stream);

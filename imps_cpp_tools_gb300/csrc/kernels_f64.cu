@@ -1,13 +1,14 @@
 // FP64 kernels for the block-sparse hot path on sm_103a.
 //
-//  * grouped_gemm_f64: output-stationary grouped GEMM over the planner's tile/term tables.
-//    `splits` CTAs per output tile (split-K: each takes an equal share of the tile's K chunks,
-//    over all of its terms in order); inside a CTA the chunks are dealt to K groups whose
-//    partial tiles are summed in a fixed order.  With one split the tile is written directly;
-//    otherwise every CTA stores its partial tile and the last CTA of the tile to finish (an
-//    atomic ticket after a memory fence; nobody waits) sums the partials in split order and
-//    writes the tile.  Deterministic for a given plan; no separate zero-fill: the first write
-//    also performs the reference's memset of `out`, VUMPS_helpers.hpp:69.
+//  * grouped_gemm_f64: output-stationary grouped GEMM over the planner's tile/term tables, one
+//    CTA per table entry: an output tile, or one of `nparts` shares of its K chunks (split-K,
+//    over all of its terms in order; the share count is set per tile by the host); inside a CTA
+//    the chunks are dealt to K groups whose partial tiles are summed in a fixed order.  With one
+//    share the tile is written directly; otherwise every CTA stores its partial tile and the
+//    last CTA of the tile to finish (an atomic ticket after a memory fence; nobody waits) sums
+//    the partials in share order and writes the tile.  Deterministic for a given plan; no
+//    separate zero-fill: the first write also performs the reference's memset of `out`,
+//    VUMPS_helpers.hpp:69.
 //  * Krylov BLAS-1 (reductions without atomics: fixed-grid partials + one finishing block).
 #include <cuda_runtime.h>
 
@@ -35,7 +36,7 @@ __device__ __forceinline__ void group_sync(int id, int nthreads) {
 template <int TM, int TN, int RM, int RN, int KS>
 __global__ void __launch_bounds__((TM / RM) * (TN / RN) * KS)
 grouped_gemm_f64_kernel(const Tile* __restrict__ tiles, const Term* __restrict__ terms,
-                        imps_dslots slots, int splits, double* __restrict__ ws, int* __restrict__ cnt) {
+                        imps_dslots slots, double* __restrict__ ws, int* __restrict__ cnt) {
   constexpr int NT = (TM / RM) * (TN / RN);
   constexpr int TX = TN / RN;  // threads along n
   constexpr int AS = TK * (TM + 1), BS = TK * (TN + 1);
@@ -43,8 +44,8 @@ grouped_gemm_f64_kernel(const Tile* __restrict__ tiles, const Term* __restrict__
   constexpr int RED = (KS - 1) * NT * RM * RN;
   __shared__ double smem[STAGE > RED ? STAGE : RED];
   __shared__ int last;
-  const int tile_id = blockIdx.x / splits, part = blockIdx.x - tile_id * splits;
-  const Tile tl = tiles[tile_id];
+  const Tile tl = tiles[blockIdx.x];
+  const int splits = tl.nparts, part = tl.part;
   // this CTA's chunk range [c_lo, c_hi) of the tile's chunk sequence
   int c_lo = 0, c_hi = 1 << 30;
   if (splits > 1) {
@@ -131,14 +132,14 @@ grouped_gemm_f64_kernel(const Tile* __restrict__ tiles, const Term* __restrict__
   }
   if (splits > 1) {
     // partial tile -> workspace; the last CTA of the tile sums all partials in split order
-    double* wp = ws + ((int64_t)tile_id * splits + part) * (TM * TN);
+    double* wp = ws + ((int64_t)tl.ws_unit + part) * (TM * TN);
 #pragma unroll
     for (int i = 0; i < RM; ++i)
 #pragma unroll
       for (int j = 0; j < RN; ++j) wp[(ty + i * (TM / RM)) * TN + tx + j * TX] = acc[i][j];
     __threadfence();
     group_sync(1, NT);
-    if (tid == 0) last = atomicAdd(cnt + tile_id, 1) == splits - 1;
+    if (tid == 0) last = atomicAdd(cnt + tl.cnt_idx, 1) == splits - 1;
     group_sync(1, NT);
     if (!last) return;
     __threadfence();
@@ -148,10 +149,10 @@ grouped_gemm_f64_kernel(const Tile* __restrict__ tiles, const Term* __restrict__
       for (int j = 0; j < RN; ++j) {
         const int e = (ty + i * (TM / RM)) * TN + tx + j * TX;
         double sum = 0.0;
-        for (int q = 0; q < splits; ++q) sum += __ldcg(ws + ((int64_t)tile_id * splits + q) * (TM * TN) + e);
+        for (int q = 0; q < splits; ++q) sum += __ldcg(ws + ((int64_t)tl.ws_unit + q) * (TM * TN) + e);
         acc[i][j] = sum;
       }
-    if (tid == 0) cnt[tile_id] = 0;  // re-armed for the next launch of this stage
+    if (tid == 0) cnt[tl.cnt_idx] = 0;  // re-armed for the next launch of this stage
   }
   double* __restrict__ C = slots.p[tl.c_slot] + tl.c_off;
 #pragma unroll
@@ -175,14 +176,14 @@ int imps_launch_grouped_f64(const void* d_tiles, int ntiles, const void* d_terms
   if (ntiles <= 0) return IMPS_OK;
   if (splits < 1 || (splits > 1 && (!ws || !cnt))) return IMPS_ERR_BAD_ARG;
   cudaStream_t st = (cudaStream_t)stream;
-  const int grid = ntiles * splits;
+  const int grid = ntiles;  // one CTA per table entry (a tile or one K share of it)
   imps::count_launch();
   if (tile_m == 16) {
     grouped_gemm_f64_kernel<16, 16, 2, 2, 4><<<grid, 256, 0, st>>>((const Tile*)d_tiles, (const Term*)d_terms,
-                                                                  slots, splits, ws, cnt);
+                                                                  slots, ws, cnt);
   } else {
     grouped_gemm_f64_kernel<32, 32, 2, 4, 2><<<grid, 256, 0, st>>>((const Tile*)d_tiles, (const Term*)d_terms,
-                                                                   slots, splits, ws, cnt);
+                                                                   slots, ws, cnt);
   }
   return cudaGetLastError() == cudaSuccess ? IMPS_OK : IMPS_ERR_CUDA;
 }

@@ -103,6 +103,10 @@ void emit_tiles(StageOut& so, imps::Tile* tiles, int c_slot, int64_t c_off, int 
       t.t1 = t1;
       t.c_slot = (int16_t)c_slot;
       t.accumulate = 0;
+      t.part = 0;
+      t.nparts = 1;
+      t.ws_unit = 0;
+      t.cnt_idx = 0;
     }
 }
 

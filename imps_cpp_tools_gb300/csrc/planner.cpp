@@ -151,6 +151,7 @@ void finalize_tiles(Stage& S, int tm, int tn) {
         t.t1 = o.t1;
         t.c_slot = o.c_slot;
         t.accumulate = o.accumulate;
+        t.nparts = 1;
         S.tiles.push_back(t);
       }
   }
