@@ -17,6 +17,13 @@
  *    mem = IMPS_MEM_DEVICE: pointers are device memory on the context's device.
  *  - One context = one device + one CUDA stream; calls on one context are serialised on its
  *    stream, no call retains a caller pointer after it returns (except imps_plan_bind).
+ *  - Contexts share no mutable state (each has its own stream, Krylov workspace, scratch and
+ *    pinned staging; the launch-shape cache of imps_plan_autotune is locked): calls on plans of
+ *    different contexts may run at the same time from different host threads, the caller
+ *    ordering their streams (events).  Calls on one context, or on the plans of one context,
+ *    come from one thread at a time.  Plan creation uploads its tables by synchronous copies on
+ *    the legacy default stream: synchronise the device before a plan's first launch on a
+ *    non-blocking stream.
  */
 #ifndef IMPS_GB300_H
 #define IMPS_GB300_H
