@@ -28,6 +28,11 @@ class _PlanSet:
 
 
 class VumpsGPU:
+    """The VUMPS sweep of VUMPS_main.cpp:97-354 on the device for a two-site unit cell.  `ctx`
+    runs on torch's current stream (ctx.set_stream(torch.cuda.current_stream())): the driver's
+    torch operations and its C-ABI calls share that stream, and with concurrent=True the side
+    contexts are ordered against it."""
+
     def __init__(self, ctx, model, dims0=None, dimvec=None, seed=1, InvETol=5e-15, InvEfac=2.0,
                  fixed_tol=None, tolmin=5e-16, tolmax=1e-6, trueLR=True, svdthresh=5e-7, precision="fp64",
                  init_state=None, lanczos_maxit=300, gmres_maxit=4000, lanczos_ncv=126, eig_margin=0.1,
