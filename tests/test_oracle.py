@@ -272,3 +272,23 @@ def test_vumps_transient_is_chaotic():
     assert np.abs(a[1] - b[1]).max() > 1e-5
     a, b = _zn_run(*args, 5, 0.0, 3), _zn_run(*args, 5, 1e-13, 3)
     assert np.abs(a - b).max() < 1e-11
+
+
+@pytest.mark.parametrize("N", [3, 4])
+def test_oracle_vumps_longer_unit_cells(N):
+    """The reference's VUMPS takes any unit-cell length N >= 2 (VUMPS_main.cpp:31,55-56; its site
+    loop rotates the unit-cell arrays, :256-259); the oracle follows it for any N.  At N = 3 and 4
+    the quantum Ising chain (Z(2) charges, J = 1, h = 0.7) reaches the exact transverse-field
+    Ising energy on every bond."""
+    from scipy.integrate import quad
+    J, hf = 1.0, 0.7
+    Jp, hp = J / 4, hf / 2
+    e0 = -quad(lambda k: math.sqrt(Jp ** 2 + hp ** 2 - 2 * Jp * hp * math.cos(k)), -math.pi, math.pi,
+               epsabs=1e-14)[0] / (2 * math.pi)
+    with O.charge_group((2,)):
+        v = O.VUMPS(O.qim_h(J, hf), 2, O.qim_i2k(), {(0,): 8, (1,): 8}, N=N, seed=2)
+        for _ in range(60):
+            E, F, _ = v.sweep()
+            if F.max() < 1e-11:
+                break
+    assert len(E) == N and F.max() < 1e-10 and np.abs(E - e0).max() < 1e-11
