@@ -400,3 +400,62 @@ def test_batched_heff_tables_equal_per_momentum():
                 if k == EX.OPS:
                     continue
                 assert np.array_equal(big[k][j * S[k]:(j + 1) * S[k]], ref[j][k]), (which, j, k)
+
+
+def _cell_excitation_setup(model, N, dims, K, params):
+    """A random N-site state of the oracle (randMPS_LR), h shifted by its energy density, its
+    environments (HeffConstants), null spaces and the X structure for charge K."""
+    from imps_cpp_tools_gb300 import models
+    d, I2K, h = models.build_model(model, **params)
+    dimvec = models.make_dims(dims, N, I2K)
+    AL, AR, C = O.randMPS_LR(N, I2K, dimvec, np.random.default_rng(3))
+    C0 = C[-1]  # bond 0
+    R, L = O.bd_mul(C0, O.bd_t(C0)), O.bd_mul(O.bd_t(C0), C0)
+    hn = O.sparse_nnz(h)
+    E0 = O.bd_trace(O.bd_mul(O.GetHL(AL, hn), R)) / N
+    hs = O.sparse_nnz(h - E0 * np.eye(h.shape[0]))
+    HLtot, HRtot = O.HeffConstants(AL, AR, L, R, hs, tol=1e-13)
+    NL = [O.Nullspace(AL[n], "l") for n in range(N)]
+    return dict(AL=AL, AR=AR, NL=NL, d=d, h=hs, HLtot=HLtot, HRtot=HRtot, xdims=O.XDims(NL, AR, K))
+
+
+@pytest.mark.parametrize("model,N,dims,K,params,periods", [
+    ("qim", 3, {(0,): 4, (1,): 3}, (1,), dict(J=1.0, h=0.7), (2,)),
+    ("xxz", 4, {(-2,): 1, (0,): 3, (2,): 2}, (2,), dict(J=1.0, Delta=-1.0), None),
+])
+def test_heff_program_longer_unit_cells(model, N, dims, K, params, periods):
+    """Excitations_main.cpp runs any unit-cell length; the host compilation of ApplyHeff
+    (HeffProgram) takes the cell length from its inputs.  For a three-site quantum Ising cell
+    (Z(2), odd sector) and a four-site XXZ cell, its tables executed with numpy and the oracle's
+    two factored solves reproduce the oracle's ApplyHeff on every site."""
+    import contextlib
+    from imps_cpp_tools_gb300 import excitations as EX
+    with (O.charge_group(periods) if periods else contextlib.nullcontext()):
+        e = _cell_excitation_setup(model, N, dims, K, params)
+        kfac = np.exp(0.6j)
+        pr = EX.HeffProgram(e["AL"], e["AR"], e["NL"], e["HLtot"], e["HRtot"], e["h"], e["d"], e["xdims"], kfac)
+        bufs = {k: np.zeros(max(int(pr.sizes.get(k, 0)), 1)) for k in range(6)}
+        bufs[EX.OPS][:pr.ops_vec.size] = pr.ops_vec
+        X = rand_x(e["xdims"], np.random.default_rng(12))
+        for (xo, n), x in zip(pr.xoff, X):
+            v = O.bm_vec(x)
+            bufs[EX.XS][xo:xo + n], bufs[EX.XS][xo + n:xo + 2 * n] = v.real, v.imag
+        run_tables(pr.prog_a.stages, bufs)
+
+        def to_bm(t_re, t_im, slot):
+            return {k[1]: (qo, (bufs[slot][o1:o1 + r * c] + 1j * bufs[slot][t_im.blocks[k][3]:t_im.blocks[k][3] + r * c])
+                           .reshape(c, r).T) for k, (qo, r, c, o1) in t_re.blocks.items()}
+
+        yr, _ = O.InvertE_fac(e["AL"], e["AR"], to_bm(*pr.rhs_r, EX.RHS), "r", kfac, tol=1e-13)
+        yl, _ = O.InvertE_fac(e["AR"], e["AL"], to_bm(*pr.rhs_l, EX.RHS), "l", np.conj(kfac), tol=1e-13)
+        vr, vl = O.bm_vec(yr), O.bm_vec(yl)
+        nr, nl = pr.nr, pr.nl
+        bufs[EX.ES][:nr], bufs[EX.ES][nr:2 * nr] = vr.real, vr.imag
+        bufs[EX.ES][2 * nr:2 * nr + nl], bufs[EX.ES][2 * nr + nl:2 * nr + 2 * nl] = vl.real, vl.imag
+        run_tables(pr.prog_b.stages, bufs)
+        ref = O.ApplyHeff(X, kfac, e["AL"], e["AR"], e["NL"], e["h"], e["d"], e["HLtot"], e["HRtot"], tol=1e-13)
+    assert len(pr.xoff) == N
+    for n, ((xo, nn), dims_n) in enumerate(zip(pr.xoff, e["xdims"])):
+        got = bufs[EX.OUT][xo:xo + nn] + 1j * bufs[EX.OUT][xo + nn:xo + 2 * nn]
+        refv = np.concatenate([ref[n][qi][1].reshape(-1, order="F") for (qi, _, _, _) in dims_n])
+        assert np.linalg.norm(got - refv) / np.linalg.norm(refv) < 1e-9, n
