@@ -459,3 +459,54 @@ def test_heff_program_longer_unit_cells(model, N, dims, K, params, periods):
         got = bufs[EX.OUT][xo:xo + nn] + 1j * bufs[EX.OUT][xo + nn:xo + 2 * nn]
         refv = np.concatenate([ref[n][qi][1].reshape(-1, order="F") for (qi, _, _, _) in dims_n])
         assert np.linalg.norm(got - refv) / np.linalg.norm(refv) < 1e-9, n
+
+
+@pytest.mark.parametrize("N", [3, 4])
+def test_ising_dispersion_longer_unit_cells(N):
+    """The excitation ansatz of Excitations_main.cpp on an N-site cell of the transverse-field
+    Ising chain (Z(2), odd sector K = 1, D = 8 + 8 per bond): at cell momentum P the N lowest
+    H_eff eigenvalues are the exact quasiparticle energies eps((P + 2 pi m) / N), m = 0..N-1."""
+    import math
+    from scipy.sparse.linalg import LinearOperator, eigsh
+    J, h = 1.0, 1.0
+    Jp, hp = J / 4, h / 2
+    eps = lambda k: 2 * math.sqrt(Jp ** 2 + hp ** 2 - 2 * Jp * hp * math.cos(k))  # noqa: E731
+    with O.charge_group((2,)):
+        H = O.qim_h(J, h)
+        v = O.VUMPS(H, 2, O.qim_i2k(), {(0,): 8, (1,): 8}, N=N, seed=2)
+        for _ in range(80):
+            E, F, _ = v.sweep()
+            if F.max() < 1e-12:
+                break
+        AL, AR, C0 = v.AL, O.shift(v.AR, 1), v.C[-1]
+        R, L = O.bd_mul(C0, O.bd_t(C0)), O.bd_mul(O.bd_t(C0), C0)
+        hs = O.sparse_nnz(H - float(E.mean()) * np.eye(4))
+        K = (1,)
+        _, _, OL, _, _ = O.LRoverlaps(AL, AR, K, 2)
+        if OL < 0:  # Excitations_main.cpp:177-178
+            AR = [[{q: (qo, -M) for q, (qo, M) in bm.items()} for bm in AR[0]]] + list(AR[1:])
+        HL, HR = O.HeffConstants(AL, AR, L, R, hs, tol=1e-13)
+        NL = [O.Nullspace(AL[n], "l") for n in range(N)]
+        xd = O.XDims(NL, AR, K)
+        n = sum(ml * mr for dd in xd for (_, _, ml, mr) in dd)
+
+        def tox(vec):
+            out, pos = [], 0
+            for dd in xd:
+                bm = {}
+                for (qi, qo, ml, mr) in dd:
+                    bm[qi] = (qo, vec[pos:pos + ml * mr].reshape(mr, ml).T.copy())
+                    pos += ml * mr
+                out.append(bm)
+            return out
+
+        def fromx(X):
+            return np.concatenate([X[m][qi][1].T.reshape(-1) for m, dd in enumerate(xd) for (qi, _, _, _) in dd])
+
+        for P in (0.3, 2.0):
+            kfac = np.exp(1j * P)
+            op = LinearOperator((n, n), dtype=complex, matvec=lambda x: fromx(O.ApplyHeff(
+                tox(np.asarray(x, complex).ravel()), kfac, AL, AR, NL, hs, 2, HL, HR, tol=1e-13)))
+            w = np.sort(eigsh(op, k=N, which="SA", tol=1e-10)[0])
+            exact = sorted(eps((P + 2 * math.pi * m) / N) for m in range(N))
+            assert np.abs(w - exact).max() < 1e-10, (P, w, exact)
