@@ -552,7 +552,7 @@ def run_vumps(args):
             "vs_baseline": None, "dtype": "bf16x6->f32 applies, f64 Krylov/decompositions" if args.precision == "bf16x6"
             else "f64", "data": "synthetic",
             "config": {"workload": _workload_desc(), "precision": args.precision, "start_state": state_src,
-                       "lanczos_ncv": _NCV[0], "autotune": _AUTOTUNE[0], "concurrent_hc_solves": _CONCURRENT[0],
+                       "lanczos_ncv": _NCV[0], "autotune": _AUTOTUNE[0], "concurrent_solves": _CONCURRENT[0],
                        "l2": "working set (~40 MB) is L2-resident by design; H_AC timing flushes L2 (512 MB write)",
                        "parallelism": f"replicas x{ws}"},
             "fp64": {"sweeps_per_s": 1.0 / float(np.mean(r64["times"])), "ms_per_step": 1e3 * float(np.mean(r64["times"])),

@@ -178,10 +178,11 @@ def test_sweep_from_warm_state_matches_oracle_full_size(cuda_ctx):
 
 
 def test_concurrent_hc_solves_equal_serial(cuda_ctx):
-    """The H_C eigensolves run on their own contexts and host threads beside the H_AC eigensolve
-    (concurrent=True, the default) or after it on one stream: the sweeps are bit-identical (no
-    state is shared between the solves), from the committed warmed XXZ D=512 state at the
-    benchmark's tolerances."""
+    """The H_C eigensolves run on their own contexts and host threads beside the H_AC eigensolve,
+    and the right-environment chain beside the left one (concurrent=True, the default), or all of
+    them one after another on one stream: the sweeps are bit-identical (no state is shared
+    between the solves), from the committed warmed XXZ D=512 state at the benchmark's
+    tolerances."""
     import torch
     import bench
     from imps_cpp_tools_gb300 import configs
