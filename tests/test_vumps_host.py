@@ -139,6 +139,36 @@ def test_two_site_driver_host_logic(fake_device):
     assert fake_device == []
 
 
+def test_two_site_driver_host_logic_concurrent(fake_device, monkeypatch):
+    """The concurrent path (H_C eigensolves and the right-environment chain on side contexts from
+    worker threads, with their own transfer-matrix plans) binds every slot with the right size
+    too; the streams are stand-ins."""
+    import contextlib
+    from imps_cpp_tools_gb300 import models
+    from imps_cpp_tools_gb300.vumps import VumpsGPU
+
+    class _Stream:
+        cuda_stream = 0
+
+        def wait_stream(self, other):
+            pass
+
+    monkeypatch.setattr(torch.cuda, "Stream", _Stream)
+    monkeypatch.setattr(torch.cuda, "current_stream", lambda *a, **k: _Stream())
+    monkeypatch.setattr(torch.cuda, "stream", lambda s: contextlib.nullcontext())
+    monkeypatch.setattr(torch.Tensor, "record_stream", lambda self, s: None)
+    model, dimvec, params = CASES[2]
+    _, I2K, _ = models.build_model(model, **params)
+    LA = [B.Layout.mps(I2K, dimvec[n], dimvec[1 - n]) for n in range(2)]
+    LB = [B.Layout.blockdiag(dimvec[b]) for b in range(2)]
+    v = VumpsGPU(B.Context(-1), model, dimvec=dimvec, init_state=_init(dimvec, I2K, LA, LB), fixed_tol=1e-12,
+                 concurrent=True, **params)
+    assert v._env is not None and all(p.ctx is v._side_ctx[1] for p in v._env.tm.values())
+    assert all(p.ctx is v._side_ctx[0] for p in v.p_hcl) and all(p.ctx is v._side_ctx[1] for p in v.p_hcr)
+    _sweeps(v, 2, fake_device)
+    assert fake_device == []
+
+
 def test_host_logic_check_catches_a_wrong_bond(fake_device, monkeypatch):
     """The recorder is not blind: a GetHR that returns the source on the wrong bond is caught."""
     from imps_cpp_tools_gb300 import models
